@@ -1,0 +1,224 @@
+/*
+ * lidar_gb300.h — C ABI of the GB300 (sm_103a) LiDAR perception library.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns an lp_status and
+ * never throws. Host buffers are owned by the caller. Device buffers are owned by the context;
+ * a context is not thread-safe (one per host thread), mirroring the reference's stateful,
+ * single-threaded algorithm objects.
+ *
+ * Reference interfaces replaced (paths are inside YevgeniyEngineer/LiDAR-Processing-V2):
+ *   lp_add_ring_info        Dataloader::addRingInfo               src/dataloader/src/dataloader.cpp:68-137
+ *   lp_segment              Segmenter::segment<PointT>            lidar_processing_lib/src/segmenter.cpp:87-101
+ *                           (+ Segmenter::image(), segmenter.hpp:163-166, as image_bgr_out)
+ *   lp_noise_remove         NoiseRemover::filter                  lidar_processing_lib/src/noise_remover.cpp:38-68
+ *   lp_cluster              Clusterer::cluster<PointT>            lidar_processing_lib/src/clusterer.cpp:43-53
+ *   lp_convex_hull          Polygonizer::convexHull<PointXY>      lidar_processing_lib/src/polygonizer.cpp:33-91
+ *   lp_antipodal_pairs      Polygonizer::findAntipodalPairsOfConvexHull  polygonizer.cpp:93-163
+ *   lp_bounding_box_rotating_calipers  Polygonizer::boundingBoxRotatingCalipers  polygonizer.cpp:165-278
+ *   lp_bounding_box_pca     Polygonizer::boundingBoxPrincipalComponentAnalysis  polygonizer.cpp:280-362
+ *   lp_process_scan / lp_process_batch
+ *                           Processor::run (segment → obstacle split → cluster → per-cluster
+ *                           gather → convexHull), src/processor/src/processor.cpp:492-671
+ */
+#ifndef LIDAR_GB300_H
+#define LIDAR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t lp_status;
+
+enum
+{
+    LP_OK = 0,
+    LP_ERR_BAD_ARG = 1,   /* null pointer, zero capacity, malformed config */
+    LP_ERR_CAPACITY = 2,  /* a fixed capacity was exceeded (e.g. the 200,000-voxel map) */
+    LP_ERR_TIMEOUT = 3,   /* a bounded device-side wait ran out */
+    LP_ERR_CUDA = 4,      /* a CUDA runtime call failed; see lp_last_error */
+    LP_ERR_NO_DEVICE = 5, /* no CUDA device / library built without one */
+    LP_ERR_INTERNAL = 6   /* device-side consistency check failed (error word set) */
+};
+
+/* Segmentation labels, segmenter.hpp:69-74. */
+enum
+{
+    LP_LABEL_UNKNOWN = 0,
+    LP_LABEL_GROUND = 1,
+    LP_LABEL_OBSTACLE = 2
+};
+
+/* Noise labels, noise_remover.hpp:35-39. */
+enum
+{
+    LP_NOISE_VALID = 0,
+    LP_NOISE_NOISE = 1
+};
+
+#define LP_INVALID_CLUSTER (-1)
+
+/* Mirrors SegmenterConfiguration, segmenter.hpp:87-112 (bools widened to int32). */
+typedef struct lp_segmenter_config
+{
+    float elevation_up_deg;
+    float elevation_down_deg;
+    int32_t image_width;
+    int32_t image_height;
+    int32_t assume_unorganized_cloud;
+    float grid_radial_spacing_m;
+    float grid_slice_resolution_deg;
+    float ground_height_threshold_m;
+    float road_maximum_slope_m_per_m;
+    float min_distance_m;
+    float max_distance_m;
+    float sensor_height_m;
+    float kernel_threshold_distance_m;
+    float amplification_factor;
+    float z_min_m;
+    float z_max_m;
+} lp_segmenter_config;
+
+/* Mirrors NoiseRemoverConfiguration, noise_remover.hpp:41-54. */
+typedef struct lp_noise_remover_config
+{
+    float radius_multiplier_m_per_m;
+    float min_search_radius_m;
+    uint32_t min_neighbours;
+} lp_noise_remover_config;
+
+/* Mirrors ClustererConfiguration, clusterer.hpp:61-68. */
+typedef struct lp_clusterer_config
+{
+    float voxel_grid_range_resolution_m;
+    float voxel_grid_azimuth_resolution_deg;
+    float voxel_grid_elevation_resolution_deg;
+    uint32_t min_cluster_size;
+} lp_clusterer_config;
+
+/* Mirrors BoundingBox, polygonizer.hpp:75-81: corners[k] = {x, y}. */
+typedef struct lp_bounding_box
+{
+    double corners[4][2];
+    float area;
+    float angle_rad;
+    int32_t is_valid;
+} lp_bounding_box;
+
+/* Defaults equal to the reference structs' member initialisers. */
+void lp_segmenter_config_default(lp_segmenter_config* cfg);
+void lp_noise_remover_config_default(lp_noise_remover_config* cfg);
+void lp_clusterer_config_default(lp_clusterer_config* cfg);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Context                                                                                     */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct lp_context lp_context;
+
+lp_status lp_context_create(int32_t device, lp_context** out);
+void lp_context_destroy(lp_context* ctx);
+const char* lp_status_string(lp_status status);
+/* Text of the last failure on this context ("" if none). */
+const char* lp_last_error(const lp_context* ctx);
+/* Number of kernels this context launched since creation (instrumentation). */
+uint64_t lp_kernel_launch_count(const lp_context* ctx);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Single-scan entry points (the reference's per-call form). Inputs and outputs in host memory. */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Ring index per point from azimuth-quadrant transitions in input order; the first ring is
+ * `first_ring` (63 in the reference) and each FOURTH->FIRST quadrant change decrements it down
+ * to 0. xyzi: n x 4 floats. */
+lp_status lp_add_ring_info(lp_context* ctx, const float* xyzi, uint32_t n, uint16_t first_ring,
+                           uint16_t* ring_out);
+
+/* Ground segmentation. xyzi: n x 4 floats (x, y, z, intensity). ring: per-point ring index, or
+ * NULL for a cloud without a ring field (the height index then comes from the elevation angle,
+ * as for pcl::PointXYZ/XYZI). labels_out: n uint32 (LP_LABEL_*). image_bgr_out: optional
+ * image_height x image_width x 3 bytes, the jump-convolution colour image. */
+lp_status lp_segment(lp_context* ctx, const float* xyzi, const uint16_t* ring, uint32_t n,
+                     const lp_segmenter_config* cfg, uint32_t* labels_out, uint8_t* image_bgr_out);
+
+/* Dynamic-radius outlier removal. xyz: n points, `stride` floats apart (3 for
+ * std::array<float,3>, 4 for XYZI). labels_out: n bytes (LP_NOISE_*). */
+lp_status lp_noise_remove(lp_context* ctx, const float* xyz, uint32_t stride, uint32_t n,
+                          const lp_noise_remover_config* cfg, uint8_t* labels_out);
+
+/* Curved-voxel clustering. labels_out: n int32, cluster id or LP_INVALID_CLUSTER. */
+lp_status lp_cluster(lp_context* ctx, const float* xyz, uint32_t stride, uint32_t n,
+                     const lp_clusterer_config* cfg, int32_t* labels_out);
+
+/* Convex hull (Andrew's monotone chain). xy: n x 2 doubles. indices_out: capacity >= n + 1;
+ * *n_out receives the hull size. Counter-clockwise, starting at the lexicographic minimum. */
+lp_status lp_convex_hull(lp_context* ctx, const double* xy, uint32_t n, int32_t* indices_out,
+                         uint32_t* n_out);
+
+/* Antipodal pairs of a convex polygon (Shamos). pairs_out: capacity pairs x 2 int32. */
+lp_status lp_antipodal_pairs(lp_context* ctx, const double* hull_xy, uint32_t n,
+                             int32_t* pairs_out, uint32_t capacity, uint32_t* n_pairs);
+
+lp_status lp_bounding_box_rotating_calipers(lp_context* ctx, const double* hull_xy, uint32_t n,
+                                            lp_bounding_box* out);
+lp_status lp_bounding_box_pca(lp_context* ctx, const double* hull_xy, uint32_t n,
+                              lp_bounding_box* out);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Whole per-scan pipeline, one scan or a batch of scans in one launch sequence.              */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct lp_pipeline_config
+{
+    lp_clusterer_config cluster;
+    lp_noise_remover_config noise;
+    int32_t enable_noise_removal; /* 1: DROR on the input cloud, segment the VALID points */
+    int32_t compute_ring;         /* 1: derive ring indices on the device (lp_add_ring_info) */
+    uint16_t first_ring;          /* start ring for compute_ring (63 in the reference) */
+    uint16_t reserved0;
+    int32_t compute_obb;          /* 1: rotating-calipers and PCA boxes per cluster */
+} lp_pipeline_config;
+
+void lp_pipeline_config_default(lp_pipeline_config* cfg);
+
+typedef struct lp_scan_input
+{
+    const float* xyzi;    /* n x 4 floats */
+    const uint16_t* ring; /* n ring indices, or NULL (compute_ring, or unorganized cloud) */
+    uint32_t n;
+    lp_segmenter_config seg;
+} lp_scan_input;
+
+typedef struct lp_scan_output
+{
+    /* Per input point (n entries each). */
+    uint8_t* noise_labels;   /* optional; LP_NOISE_* (VALID everywhere when DROR is off) */
+    uint32_t* seg_labels;    /* optional; LP_LABEL_* (UNKNOWN for points removed as noise) */
+    int32_t* cluster_labels; /* optional; cluster id of obstacle points, else LP_INVALID_CLUSTER */
+    /* Per cluster. Hull indices are local to the cluster: they index the cluster's points in
+     * input order, exactly as the reference's per-cluster gather + convexHull produce them. */
+    uint32_t cluster_capacity;
+    uint32_t hull_capacity;
+    uint32_t* hull_offsets;       /* cluster_capacity + 1 */
+    int32_t* hull_indices;        /* hull_capacity */
+    float* z_min;                 /* optional, cluster_capacity */
+    float* z_max;                 /* optional, cluster_capacity */
+    lp_bounding_box* obb_calipers; /* optional, cluster_capacity */
+    lp_bounding_box* obb_pca;      /* optional, cluster_capacity */
+    /* Written by the library. */
+    uint32_t n_obstacles;
+    uint32_t n_clusters;
+    uint32_t n_hull_indices;
+    lp_status status;
+} lp_scan_output;
+
+lp_status lp_process_scan(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scan,
+                          lp_scan_output* out);
+lp_status lp_process_batch(lp_context* ctx, const lp_pipeline_config* cfg,
+                           const lp_scan_input* scans, lp_scan_output* outs, uint32_t nscans);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIDAR_GB300_H */

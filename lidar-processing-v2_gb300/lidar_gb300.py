@@ -1,0 +1,444 @@
+"""Python host API for the GB300 LiDAR perception library (ctypes over liblp_gpu.so).
+
+Mirrors the reference library's classes (lidar_processing_lib, YevgeniyEngineer/LiDAR-Processing-V2):
+
+    Segmenter.segment(cloud)            segmenter.cpp:87-101   -> uint32 labels (UNKNOWN/GROUND/OBSTACLE)
+    NoiseRemover.filter(points)         noise_remover.cpp:38-68 -> uint8 labels (VALID/NOISE)
+    Clusterer.cluster(cloud)            clusterer.cpp:43-53    -> int32 labels (-1 = none)
+    Polygonizer.convexHull(points)      polygonizer.cpp:33-91  -> int32 hull indices
+    Polygonizer.boundingBoxRotatingCalipers / boundingBoxPrincipalComponentAnalysis
+    add_ring_info(cloud)                dataloader.cpp:68-137  -> uint16 rings
+
+and the batched pipeline (process_batch). Errors raise the exception type the reference throws for
+the same condition (RuntimeError, OverflowError, ValueError). Every call runs CUDA kernels; the
+library refuses to load, rather than falling back to the CPU, when its shared object is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liblp_gpu.so")
+SYNTH_PATH = os.path.join(_HERE, "liblp_synth.so")
+
+LP_OK, LP_ERR_BAD_ARG, LP_ERR_CAPACITY, LP_ERR_TIMEOUT, LP_ERR_CUDA, LP_ERR_NO_DEVICE, LP_ERR_INTERNAL = range(7)
+UNKNOWN, GROUND, OBSTACLE = 0, 1, 2
+VALID, NOISE = 0, 1
+INVALID_CLUSTER = -1
+
+
+class SegmenterConfig(ctypes.Structure):
+    """lp_segmenter_config == SegmenterConfiguration (segmenter.hpp:87-112)."""
+
+    _fields_ = [
+        ("elevation_up_deg", ctypes.c_float),
+        ("elevation_down_deg", ctypes.c_float),
+        ("image_width", ctypes.c_int32),
+        ("image_height", ctypes.c_int32),
+        ("assume_unorganized_cloud", ctypes.c_int32),
+        ("grid_radial_spacing_m", ctypes.c_float),
+        ("grid_slice_resolution_deg", ctypes.c_float),
+        ("ground_height_threshold_m", ctypes.c_float),
+        ("road_maximum_slope_m_per_m", ctypes.c_float),
+        ("min_distance_m", ctypes.c_float),
+        ("max_distance_m", ctypes.c_float),
+        ("sensor_height_m", ctypes.c_float),
+        ("kernel_threshold_distance_m", ctypes.c_float),
+        ("amplification_factor", ctypes.c_float),
+        ("z_min_m", ctypes.c_float),
+        ("z_max_m", ctypes.c_float),
+    ]
+
+    @classmethod
+    def default(cls, **kw):
+        c = cls(2.0, -24.8, 2048, 64, 0, 2.0, 1.0, 0.2, 0.2, 2.0, 100.0, 1.73, 1.0, 5.0, -3.0, 4.0)
+        for k, v in kw.items():
+            setattr(c, k, v)
+        return c
+
+
+class NoiseRemoverConfig(ctypes.Structure):
+    """lp_noise_remover_config == NoiseRemoverConfiguration (noise_remover.hpp:41-54)."""
+
+    _fields_ = [
+        ("radius_multiplier_m_per_m", ctypes.c_float),
+        ("min_search_radius_m", ctypes.c_float),
+        ("min_neighbours", ctypes.c_uint32),
+    ]
+
+    @classmethod
+    def default(cls, **kw):
+        c = cls(0.02, 0.1, 4)
+        for k, v in kw.items():
+            setattr(c, k, v)
+        return c
+
+
+class ClustererConfig(ctypes.Structure):
+    """lp_clusterer_config == ClustererConfiguration (clusterer.hpp:61-68)."""
+
+    _fields_ = [
+        ("voxel_grid_range_resolution_m", ctypes.c_float),
+        ("voxel_grid_azimuth_resolution_deg", ctypes.c_float),
+        ("voxel_grid_elevation_resolution_deg", ctypes.c_float),
+        ("min_cluster_size", ctypes.c_uint32),
+    ]
+
+    @classmethod
+    def default(cls, **kw):
+        c = cls(0.4, 1.0, 1.5, 3)
+        for k, v in kw.items():
+            setattr(c, k, v)
+        return c
+
+    @classmethod
+    def processor(cls):
+        """The processor node's YAML values (processor.param.yaml:31-35): elevation 3.0 deg."""
+        return cls(0.4, 1.0, 3.0, 3)
+
+
+class BoundingBox(ctypes.Structure):
+    """lp_bounding_box == BoundingBox (polygonizer.hpp:75-81)."""
+
+    _fields_ = [
+        ("corners", (ctypes.c_double * 2) * 4),
+        ("area", ctypes.c_float),
+        ("angle_rad", ctypes.c_float),
+        ("is_valid", ctypes.c_int32),
+    ]
+
+    def corners_array(self):
+        return np.array([[self.corners[k][0], self.corners[k][1]] for k in range(4)])
+
+
+class PipelineConfig(ctypes.Structure):
+    _fields_ = [
+        ("cluster", ClustererConfig),
+        ("noise", NoiseRemoverConfig),
+        ("enable_noise_removal", ctypes.c_int32),
+        ("compute_ring", ctypes.c_int32),
+        ("first_ring", ctypes.c_uint16),
+        ("reserved0", ctypes.c_uint16),
+        ("compute_obb", ctypes.c_int32),
+    ]
+
+    @classmethod
+    def default(cls, **kw):
+        c = cls(ClustererConfig.processor(), NoiseRemoverConfig.default(), 0, 0, 63, 0, 1)
+        for k, v in kw.items():
+            setattr(c, k, v)
+        return c
+
+
+class ScanInput(ctypes.Structure):
+    _fields_ = [
+        ("xyzi", ctypes.c_void_p),
+        ("ring", ctypes.c_void_p),
+        ("n", ctypes.c_uint32),
+        ("seg", SegmenterConfig),
+    ]
+
+
+class ScanOutput(ctypes.Structure):
+    _fields_ = [
+        ("noise_labels", ctypes.c_void_p),
+        ("seg_labels", ctypes.c_void_p),
+        ("cluster_labels", ctypes.c_void_p),
+        ("cluster_capacity", ctypes.c_uint32),
+        ("hull_capacity", ctypes.c_uint32),
+        ("hull_offsets", ctypes.c_void_p),
+        ("hull_indices", ctypes.c_void_p),
+        ("z_min", ctypes.c_void_p),
+        ("z_max", ctypes.c_void_p),
+        ("obb_calipers", ctypes.c_void_p),
+        ("obb_pca", ctypes.c_void_p),
+        ("n_obstacles", ctypes.c_uint32),
+        ("n_clusters", ctypes.c_uint32),
+        ("n_hull_indices", ctypes.c_uint32),
+        ("status", ctypes.c_int32),
+    ]
+
+
+def ptr(a):
+    """ctypes void pointer of a contiguous numpy array (None passes NULL)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+@dataclass
+class ScanResult:
+    noise_labels: np.ndarray
+    seg_labels: np.ndarray
+    cluster_labels: np.ndarray
+    n_obstacles: int
+    n_clusters: int
+    hull_offsets: np.ndarray
+    hull_indices: np.ndarray
+    z_min: np.ndarray
+    z_max: np.ndarray
+    obb_calipers: list
+    obb_pca: list
+
+    def hull(self, k):
+        return self.hull_indices[self.hull_offsets[k]:self.hull_offsets[k + 1]]
+
+
+class ResultBuffers:
+    """Host result buffers for one scan, in the layout lp_scan_output points at."""
+
+    def __init__(self, n, cluster_capacity=None, hull_capacity=None):
+        cc = cluster_capacity if cluster_capacity is not None else max(64, n // 3 + 1)
+        hc = hull_capacity if hull_capacity is not None else max(256, n + cc)
+        self.noise = np.zeros(n, np.uint8)
+        self.seg = np.zeros(n, np.uint32)
+        self.cl = np.zeros(n, np.int32)
+        self.hoff = np.zeros(cc + 1, np.uint32)
+        self.hidx = np.zeros(hc, np.int32)
+        self.zmin = np.zeros(cc, np.float32)
+        self.zmax = np.zeros(cc, np.float32)
+        self.obb_c = (BoundingBox * cc)()
+        self.obb_p = (BoundingBox * cc)()
+        self.out = ScanOutput(ptr(self.noise), ptr(self.seg), ptr(self.cl), cc, hc, ptr(self.hoff),
+                              ptr(self.hidx), ptr(self.zmin), ptr(self.zmax),
+                              ctypes.cast(self.obb_c, ctypes.c_void_p), ctypes.cast(self.obb_p, ctypes.c_void_p),
+                              0, 0, 0, 0)
+
+    def result(self):
+        k = self.out.n_clusters
+        return ScanResult(self.noise.copy(), self.seg.copy(), self.cl.copy(), self.out.n_obstacles, k,
+                          self.hoff[:k + 1].copy(), self.hidx[:self.out.n_hull_indices].copy(),
+                          self.zmin[:k].copy(), self.zmax[:k].copy(),
+                          [self.obb_c[i] for i in range(k)], [self.obb_p[i] for i in range(k)])
+
+
+def _declare(lib):
+    c = ctypes
+    P = c.c_void_p
+    sig = {
+        "lp_context_create": (c.c_int32, [c.c_int32, c.POINTER(P)]),
+        "lp_context_destroy": (None, [P]),
+        "lp_status_string": (c.c_char_p, [c.c_int32]),
+        "lp_last_error": (c.c_char_p, [P]),
+        "lp_kernel_launch_count": (c.c_uint64, [P]),
+        "lp_add_ring_info": (c.c_int32, [P, P, c.c_uint32, c.c_uint16, P]),
+        "lp_segment": (c.c_int32, [P, P, P, c.c_uint32, P, P, P]),
+        "lp_noise_remove": (c.c_int32, [P, P, c.c_uint32, c.c_uint32, P, P]),
+        "lp_cluster": (c.c_int32, [P, P, c.c_uint32, c.c_uint32, P, P]),
+        "lp_convex_hull": (c.c_int32, [P, P, c.c_uint32, P, P]),
+        "lp_antipodal_pairs": (c.c_int32, [P, P, c.c_uint32, P, c.c_uint32, P]),
+        "lp_bounding_box_rotating_calipers": (c.c_int32, [P, P, c.c_uint32, P]),
+        "lp_bounding_box_pca": (c.c_int32, [P, P, c.c_uint32, P]),
+        "lp_process_scan": (c.c_int32, [P, P, P, P]),
+        "lp_process_batch": (c.c_int32, [P, P, P, P, c.c_uint32]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+_lib = None
+
+
+def library():
+    """Load liblp_gpu.so (built in-tree by __graft_entry__.build()). Raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"liblp_gpu.so not built at {LIB_PATH}; run __graft_entry__.build()")
+        _lib = _declare(ctypes.CDLL(LIB_PATH))
+    return _lib
+
+
+class LidarError(RuntimeError):
+    pass
+
+
+def check(status, ctx=None):
+    if status == LP_OK:
+        return
+    lib = library()
+    msg = lib.lp_status_string(status).decode()
+    if ctx is not None:
+        detail = lib.lp_last_error(ctx.handle)
+        if detail:
+            msg += ": " + detail.decode()
+    if status == LP_ERR_CAPACITY:
+        raise OverflowError(msg)
+    if status == LP_ERR_BAD_ARG:
+        raise ValueError(msg)
+    raise LidarError(msg)
+
+
+class Context:
+    """One device context (device buffers, stream). Not thread-safe, like the reference objects."""
+
+    def __init__(self, device=0):
+        lib = library()
+        h = ctypes.c_void_p()
+        check(lib.lp_context_create(device, ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            library().lp_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def launches(self):
+        return int(library().lp_kernel_launch_count(self.handle))
+
+
+def _xyzi(cloud):
+    a = np.ascontiguousarray(cloud, dtype=np.float32)
+    if a.ndim != 2 or a.shape[1] not in (3, 4):
+        raise ValueError("cloud must be N x 3 or N x 4 float32")
+    if a.shape[1] == 3:
+        a = np.ascontiguousarray(np.concatenate([a, np.zeros((len(a), 1), np.float32)], axis=1))
+    return a
+
+
+def add_ring_info(ctx, cloud, first_ring=63):
+    a = _xyzi(cloud)
+    out = np.zeros(len(a), np.uint16)
+    check(library().lp_add_ring_info(ctx.handle, ptr(a), len(a), first_ring, ptr(out)), ctx)
+    return out
+
+
+class Segmenter:
+    """Segmenter (segmenter.hpp:131-262): config() then segment(cloud[, ring]) -> labels."""
+
+    def __init__(self, ctx, config=None):
+        self.ctx = ctx
+        self._config = config or SegmenterConfig.default()
+        self._image = None
+
+    def config(self, cfg=None):
+        if cfg is not None:
+            self._config = cfg
+        return self._config
+
+    def segment(self, cloud, ring=None, want_image=False):
+        a = _xyzi(cloud)
+        labels = np.zeros(len(a), np.uint32)
+        img = np.zeros((self._config.image_height, self._config.image_width, 3), np.uint8) if want_image else None
+        r = None if ring is None else np.ascontiguousarray(ring, dtype=np.uint16)
+        check(library().lp_segment(self.ctx.handle, ptr(a), ptr(r), len(a), ctypes.byref(self._config),
+                                   ptr(labels), ptr(img)), self.ctx)
+        self._image = img
+        return labels
+
+    def image(self):
+        return self._image
+
+
+class NoiseRemover:
+    """NoiseRemover (noise_remover.hpp:56-86): filter(points) -> VALID/NOISE per point."""
+
+    def __init__(self, ctx, config=None):
+        self.ctx = ctx
+        self._config = config or NoiseRemoverConfig.default()
+
+    def config(self, cfg=None):
+        if cfg is not None:
+            self._config = cfg
+        return self._config
+
+    def filter(self, points):
+        a = np.ascontiguousarray(points, dtype=np.float32)
+        out = np.zeros(len(a), np.uint8)
+        check(library().lp_noise_remove(self.ctx.handle, ptr(a), a.shape[1], len(a), ctypes.byref(self._config),
+                                        ptr(out)), self.ctx)
+        return out
+
+
+class Clusterer:
+    """Clusterer (clusterer.hpp:70-175): cluster(cloud) -> int32 labels."""
+
+    def __init__(self, ctx, config=None):
+        self.ctx = ctx
+        self._config = config or ClustererConfig.default()
+
+    def config(self, cfg=None):
+        if cfg is not None:
+            self._config = cfg
+        return self._config
+
+    def cluster(self, cloud):
+        a = np.ascontiguousarray(cloud, dtype=np.float32)
+        out = np.zeros(len(a), np.int32)
+        check(library().lp_cluster(self.ctx.handle, ptr(a), a.shape[1], len(a), ctypes.byref(self._config),
+                                   ptr(out)), self.ctx)
+        return out
+
+
+class Polygonizer:
+    """Polygonizer (polygonizer.hpp:85-150)."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+
+    def convexHull(self, points):
+        a = np.ascontiguousarray(points, dtype=np.float64)
+        out = np.zeros(len(a) + 1, np.int32)
+        n = ctypes.c_uint32()
+        check(library().lp_convex_hull(self.ctx.handle, ptr(a), len(a), ptr(out), ctypes.byref(n)), self.ctx)
+        return out[: n.value].copy()
+
+    def findAntipodalPairsOfConvexHull(self, hull_points):
+        a = np.ascontiguousarray(hull_points, dtype=np.float64)
+        cap = 4 * len(a) + 8
+        out = np.zeros((cap, 2), np.int32)
+        n = ctypes.c_uint32()
+        check(library().lp_antipodal_pairs(self.ctx.handle, ptr(a), len(a), ptr(out), cap, ctypes.byref(n)), self.ctx)
+        return out[: n.value].copy()
+
+    def boundingBoxRotatingCalipers(self, hull_points):
+        a = np.ascontiguousarray(hull_points, dtype=np.float64)
+        b = BoundingBox()
+        check(library().lp_bounding_box_rotating_calipers(self.ctx.handle, ptr(a), len(a), ctypes.byref(b)), self.ctx)
+        return b
+
+    def boundingBoxPrincipalComponentAnalysis(self, hull_points):
+        a = np.ascontiguousarray(hull_points, dtype=np.float64)
+        b = BoundingBox()
+        check(library().lp_bounding_box_pca(self.ctx.handle, ptr(a), len(a), ctypes.byref(b)), self.ctx)
+        return b
+
+
+def process_batch(ctx, scans, pipeline=None, seg_configs=None, rings=None):
+    """Run the whole per-scan path on a batch of scans in one launch sequence.
+
+    scans: list of N_i x 4 float32 arrays; seg_configs: list of SegmenterConfig (default each);
+    rings: list of uint16 arrays or None. Returns a list of ScanResult.
+    """
+    pipeline = pipeline or PipelineConfig.default()
+    n = len(scans)
+    arrs = [_xyzi(s) for s in scans]
+    rr = [None if (rings is None or rings[i] is None) else np.ascontiguousarray(rings[i], np.uint16)
+          for i in range(n)]
+    cfgs = seg_configs or [SegmenterConfig.default() for _ in range(n)]
+    ins = (ScanInput * n)()
+    bufs = []
+    for i in range(n):
+        ins[i] = ScanInput(arrs[i].ctypes.data, None if rr[i] is None else rr[i].ctypes.data, len(arrs[i]), cfgs[i])
+        bufs.append(ResultBuffers(len(arrs[i])))
+    outs = (ScanOutput * n)(*[b.out for b in bufs])
+    st = library().lp_process_batch(ctx.handle, ctypes.byref(pipeline), ins, outs, n)
+    for i in range(n):
+        bufs[i].out = outs[i]
+    check(st, ctx)
+    return [b.result() for b in bufs]
