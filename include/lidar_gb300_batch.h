@@ -1,0 +1,49 @@
+/*
+ * lidar_gb300_batch.h — prepared batches: scans uploaded once into HBM and re-executed, for
+ * throughput measurement, CUDA-graph replay and the serving loop. These entry points have no
+ * counterpart in the reference library (it processes one scan per call on the CPU); they run the
+ * same launch sequence as lp_process_batch (lidar_gb300.h).
+ */
+#ifndef LIDAR_GB300_BATCH_H
+#define LIDAR_GB300_BATCH_H
+
+#include "lidar_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct lp_batch lp_batch;
+
+/* Plans the layout, allocates device memory and uploads the scans (host buffers must stay
+ * valid for lp_batch_upload). */
+lp_status lp_batch_create(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans,
+                          uint32_t nscans, lp_batch** out);
+void lp_batch_destroy(lp_context* ctx, lp_batch* batch);
+/* Copies the scans' host buffers to the device again (asynchronous on the context stream). */
+lp_status lp_batch_upload(lp_context* ctx, lp_batch* batch);
+/* Runs the whole pipeline on the device-resident inputs (asynchronous). */
+lp_status lp_batch_execute(lp_context* ctx, lp_batch* batch);
+/* Captures the launch sequence into a CUDA graph; later lp_batch_execute calls replay it. */
+lp_status lp_batch_capture_graph(lp_context* ctx, lp_batch* batch);
+/* Waits for the stream and copies every scan's results into outs[0..nscans). */
+lp_status lp_batch_download(lp_context* ctx, lp_batch* batch, lp_scan_output* outs);
+lp_status lp_context_synchronize(lp_context* ctx);
+uint32_t lp_batch_points(const lp_batch* batch);
+uint64_t lp_batch_device_bytes(const lp_batch* batch);
+/* Mean device time of one execution over `iters` runs (CUDA events on the context stream);
+ * flush_l2 writes a 512 MiB buffer before each run, outside the timed interval. */
+lp_status lp_batch_time(lp_context* ctx, lp_batch* batch, uint32_t iters, int32_t flush_l2, float* ms_per_iter);
+/* Per-kernel device times of one execution: names (name_len bytes each) and milliseconds for up
+ * to cap launches in launch order; *count receives the number of launches. */
+lp_status lp_batch_profile(lp_context* ctx, lp_batch* batch, char* names, uint32_t name_len, float* ms,
+                           uint32_t cap, uint32_t* count);
+/* Device evaluation of the library's correctly rounded binary32 functions (kind 0 atan2(a, b),
+ * 1 atan(a), 2 exp(a), 3 the reference's atan2 approximation); used by the parity tests. */
+lp_status lp_debug_math(lp_context* ctx, int32_t kind, const float* a, const float* b, uint32_t n, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIDAR_GB300_BATCH_H */

@@ -1,0 +1,1273 @@
+// lp_api.cu — context, batch planning/allocation and the C ABI of liblp_gpu.so.
+//
+// A context is one CUDA stream. A batch owns one device allocation holding every array of the
+// launch sequence (inputs stay resident, so a prepared batch can be re-executed or captured as
+// a CUDA graph). A one-shot call (lp_segment, lp_process_batch, ...) reuses a batch cached in
+// the context: plan on the host, upload, run the whole sequence without host syncs, read the
+// small per-scan state, then the results. All waits inside kernels are bounded.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "lidar_gb300.h"
+#include "lidar_gb300_batch.h"
+#include "lp_batch.cuh"
+#include "lp_common.cuh"
+#include "lp_stages.hpp"
+
+using namespace lpg;
+
+namespace
+{
+constexpr float kDegToRad = static_cast<float>(M_PI / 180.0); // segmenter.hpp:135, clusterer.hpp:78
+constexpr float kTwoPiF = static_cast<float>(2.0 * M_PI);     // segmenter.hpp:136
+
+enum Stage : uint32_t
+{
+    ST_RING = 1u << 0,    // ring partition (lp_add_ring_info)
+    ST_NOISE = 1u << 1,   // DROR on the input cloud
+    ST_SEG = 1u << 2,     // segmentation
+    ST_CLUSTER = 1u << 3, // cluster the obstacle points
+    ST_HULL = 1u << 4,
+    ST_OBB = 1u << 5,
+    ST_ALL_OBS = 1u << 6, // cluster the whole input (lp_cluster)
+    ST_IMAGE = 1u << 7,
+};
+
+struct ScanIn
+{
+    const float* xyzi = nullptr; // host
+    uint32_t stride = 4;         // floats between points
+    const uint16_t* ring = nullptr;
+    uint32_t n = 0;
+    lp_segmenter_config seg{};
+    int32_t compute_ring = 0;
+    int32_t first_ring = 0;
+};
+
+struct Run
+{
+    uint32_t stages = 0;
+    lp_clusterer_config cl{};
+    lp_noise_remover_config nr{};
+    std::vector<ScanIn> scans;
+};
+} // namespace
+
+struct lp_context
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t launches = 0;
+    std::string last_error;
+    std::vector<cudaEvent_t> events;
+    lp_batch* cached = nullptr;
+    void* flush = nullptr; // buffer larger than L2 for cache flushing between timed runs
+    size_t flush_bytes = 0;
+};
+
+struct lp_batch
+{
+    Run run;
+    BatchHost hb;
+    BatchDev b{};
+    char* mem = nullptr;
+    size_t cap = 0;
+    uint32_t* scan_sums = nullptr;
+    uint8_t* d_image = nullptr;
+    std::vector<ScanState> h_state;
+    std::vector<float4> staging; // host repack for stride-3 inputs
+    cudaGraphExec_t graph = nullptr;
+    std::vector<LaunchRecord> prof;
+    bool profiling = false;
+};
+
+namespace
+{
+lp_status fail(lp_context* ctx, lp_status st, const std::string& msg)
+{
+    if (ctx)
+        ctx->last_error = msg;
+    return st;
+}
+
+lp_status cuda_fail(lp_context* ctx, cudaError_t e, const char* where)
+{
+    cudaGetLastError();
+    return fail(ctx, LP_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define LP_CUDA(ctx, call)                                                                                  \
+    do                                                                                                      \
+    {                                                                                                       \
+        const cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                              \
+            return cuda_fail(ctx, e_, #call);                                                               \
+    } while (0)
+
+#define LP_TRY(call)                                                                                        \
+    do                                                                                                      \
+    {                                                                                                       \
+        const lp_status s_ = (call);                                                                        \
+        if (s_ != LP_OK)                                                                                    \
+            return s_;                                                                                      \
+    } while (0)
+
+struct Carver
+{
+    char* base;
+    size_t off = 0;
+    template <typename T>
+    T* take(size_t count)
+    {
+        off = (off + 255) & ~static_cast<size_t>(255);
+        T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+        off += count * sizeof(T) + 16;
+        return p;
+    }
+};
+
+bool seg_config_ok(const lp_segmenter_config& c)
+{
+    if (c.image_width <= 0 || c.image_height <= 0 || c.image_width > 65535 || c.image_height > 65535)
+        return false;
+    if (!(c.grid_radial_spacing_m > 0) || !(c.grid_slice_resolution_deg > 0) || !(c.max_distance_m > 0))
+        return false;
+    const float slice_res = c.grid_slice_resolution_deg * kDegToRad;
+    const int32_t nrad = static_cast<int32_t>(c.max_distance_m / c.grid_radial_spacing_m);
+    const int32_t nslice = static_cast<int32_t>(kTwoPiF / slice_res);
+    return nrad >= kRansacRadialBins && nslice >= 1 && static_cast<int64_t>(nrad) * nslice < (1 << 24) &&
+           static_cast<int64_t>(c.image_width) * c.image_height < (1 << 28);
+}
+
+// Host-side layout and the configuration constants of every scan (binary32 expressions
+// evaluated exactly as the reference writes them).
+lp_status plan(lp_context* ctx, lp_batch& B)
+{
+    const Run& R = B.run;
+    BatchHost& hb = B.hb;
+    hb = BatchHost{};
+    hb.nscan = static_cast<int>(R.scans.size());
+    hb.any_noise = (R.stages & ST_NOISE) != 0;
+    uint64_t pt = 0, pix = 0, row = 0, tile = 0, slice = 0, cell = 0, nearc = 0, hash = 0, cl = 0, dh = 0;
+    const bool seg = (R.stages & ST_SEG) != 0;
+    for (const ScanIn& in : R.scans)
+    {
+        ScanDev sd{};
+        sd.pt_off = static_cast<uint32_t>(pt);
+        sd.n = in.n;
+        sd.src_off = static_cast<uint32_t>(pt);
+        sd.n_src = in.n;
+        sd.tile_off = static_cast<uint32_t>(tile);
+        sd.compute_ring = in.compute_ring;
+        if (in.compute_ring)
+            hb.any_compute_ring = true;
+        sd.first_ring = in.first_ring;
+        if (seg)
+        {
+            const lp_segmenter_config& c = in.seg;
+            if (!seg_config_ok(c))
+                return fail(ctx, LP_ERR_BAD_ARG, "segmenter configuration out of the supported range");
+            sd.H = c.image_height;
+            sd.W = c.image_width;
+            sd.pix_off = static_cast<uint32_t>(pix);
+            sd.row_off = static_cast<uint32_t>(row);
+            sd.slice_res = c.grid_slice_resolution_deg * kDegToRad; // segmenter.cpp:42-46
+            sd.nrad = static_cast<int32_t>(c.max_distance_m / c.grid_radial_spacing_m);
+            sd.nslice = static_cast<int32_t>(kTwoPiF / sd.slice_res);
+            sd.cell_off = static_cast<uint32_t>(cell);
+            sd.slice_off = static_cast<uint32_t>(slice);
+            sd.nnear_per_slice = std::min(kRansacRadialBins, sd.nrad);
+            sd.near_off = static_cast<uint32_t>(nearc);
+            const float up = c.elevation_up_deg * kDegToRad; // segmenter.cpp:106-109
+            const float down = c.elevation_down_deg * kDegToRad;
+            const float vfov = up - down;
+            sd.rad_per_px = vfov / static_cast<float>(c.image_height);
+            sd.down_rad = down;
+            sd.zmin_adj = -c.sensor_height_m + c.z_min_m; // segmenter.cpp:121-122
+            sd.zmax_adj = -c.sensor_height_m + c.z_max_m;
+            sd.spacing = c.grid_radial_spacing_m;
+            sd.min_d = c.min_distance_m;
+            sd.max_d = c.max_distance_m;
+            sd.delta = std::min(c.grid_radial_spacing_m * std::tan(c.road_maximum_slope_m_per_m), // :209-211
+                                c.ground_height_threshold_m - std::numeric_limits<float>::epsilon());
+            sd.thr = c.ground_height_threshold_m;
+            sd.sensor_h = c.sensor_height_m;
+            sd.kthr2 = c.kernel_threshold_distance_m * c.kernel_threshold_distance_m; // :532-533
+            sd.amp = c.amplification_factor;
+            sd.max_cos = std::cos(std::tan(c.road_maximum_slope_m_per_m)); // :360
+            sd.use_ring = ((in.ring != nullptr) || in.compute_ring) && !c.assume_unorganized_cloud;
+            if (sd.compute_ring && sd.first_ring < 0)
+                sd.first_ring = c.image_height - 1;
+            pix += static_cast<uint64_t>(sd.H) * static_cast<uint64_t>(sd.W);
+            row += static_cast<uint64_t>(sd.H);
+            cell += static_cast<uint64_t>(sd.nslice) * static_cast<uint64_t>(sd.nrad);
+            slice += static_cast<uint64_t>(sd.nslice);
+            nearc += static_cast<uint64_t>(sd.nslice) * static_cast<uint64_t>(sd.nnear_per_slice);
+        }
+        else if (sd.compute_ring && sd.first_ring < 0)
+        {
+            sd.first_ring = 63; // dataloader.cpp:87
+        }
+        sd.res_r = R.cl.voxel_grid_range_resolution_m; // Clusterer::config, clusterer.hpp:76-84
+        sd.res_a = R.cl.voxel_grid_azimuth_resolution_deg * kDegToRad;
+        sd.res_e = R.cl.voxel_grid_elevation_resolution_deg * kDegToRad;
+        sd.min_cluster = R.cl.min_cluster_size;
+        sd.hash_off = static_cast<uint32_t>(hash);
+        sd.hash_cap = next_pow2(std::max(64u, 2u * in.n));
+        const uint32_t minc = std::max(1u, R.cl.min_cluster_size);
+        sd.cluster_cap = in.n / minc + 1;
+        sd.cl_off = static_cast<uint32_t>(cl);
+        sd.hull_cap = in.n;
+        sd.dror_s2 = std::pow(static_cast<double>(R.nr.radius_multiplier_m_per_m), 2.0); // noise_remover.cpp:49-52
+        sd.dror_rmin2 = R.nr.min_search_radius_m * R.nr.min_search_radius_m;
+        sd.dror_k = R.nr.min_neighbours;
+        sd.dhash_off = static_cast<uint32_t>(dh);
+        sd.dhash_cap = next_pow2(std::max(64u, 2u * in.n));
+        pt += in.n;
+        tile += div_up(std::max(in.n, 1u), 1024u);
+        hash += sd.hash_cap;
+        cl += sd.cluster_cap;
+        dh += sd.dhash_cap;
+        hb.scans.push_back(sd);
+    }
+    const uint64_t lim = 0x7fffffffull;
+    if (pt > lim / 4 || pix > lim / 8 || hash > lim || cell > lim || dh > lim || cl > lim)
+        return fail(ctx, LP_ERR_CAPACITY, "batch too large for 32-bit indexing; split it");
+    hb.ntiles = static_cast<uint32_t>(tile);
+    hb.nslices = static_cast<uint32_t>(slice);
+    BatchDev& b = B.b;
+    b = BatchDev{};
+    b.nscan = hb.nscan;
+    b.nsrc = static_cast<uint32_t>(pt);
+    b.npts = static_cast<uint32_t>(pt);
+    b.ntiles = static_cast<uint32_t>(tile);
+    b.ncell = static_cast<uint32_t>(cell);
+    b.nnear = static_cast<uint32_t>(nearc);
+    b.npix = static_cast<uint32_t>(pix);
+    b.nrows = static_cast<uint32_t>(row);
+    b.nhash = static_cast<uint32_t>(hash);
+    b.ncl = static_cast<uint32_t>(cl);
+    b.ndhash = static_cast<uint32_t>(dh);
+    return LP_OK;
+}
+
+// Lays out every array of the batch (pass 1 with base == nullptr measures the size).
+size_t carve(lp_batch& B, char* base)
+{
+    BatchDev& b = B.b;
+    const Run& R = B.run;
+    const uint32_t N = b.npts, S = static_cast<uint32_t>(b.nscan);
+    const bool seg = R.stages & ST_SEG;
+    const bool clu = R.stages & (ST_CLUSTER | ST_ALL_OBS);
+    const bool hull = R.stages & ST_HULL;
+    const bool noise = R.stages & ST_NOISE;
+    const bool ring_in = std::any_of(R.scans.begin(), R.scans.end(), [](const ScanIn& s) { return s.ring != nullptr; });
+    Carver c{base};
+    auto put = [&](auto*& field, size_t count) {
+        using T = std::remove_reference_t<decltype(*field)>;
+        field = c.take<std::remove_const_t<T>>(count);
+    };
+    ScanDev* scans;
+    put(scans, S);
+    b.scans = scans;
+    put(b.state, S);
+    put(b.d_scan_total, 4);
+    const uint32_t maxlen = std::max({N, b.npix, b.nhash, b.ncell, b.ndhash, b.ncl, b.ntiles, b.nnear}) + 2;
+    put(B.scan_sums, div_up(maxlen, static_cast<uint32_t>(kScanTile)) + 4);
+    float4* src;
+    put(src, N);
+    b.src = src;
+    b.ring_in = nullptr;
+    if (ring_in)
+    {
+        uint16_t* r;
+        put(r, N);
+        b.ring_in = r;
+    }
+    put(b.noise, N);
+    put(b.ring, N);
+    if (noise)
+    {
+        put(b.src_pos, N + 1);
+        put(b.pts, N);
+        put(b.pt_src, N);
+        put(b.dkey, b.ndhash);
+        put(b.dcnt, b.ndhash + 1);
+        put(b.dstart, b.ndhash + 1);
+        put(b.dslot, N);
+        put(b.drank, N);
+        put(b.dorder, N);
+        put(b.dr2, N);
+    }
+    else
+    {
+        b.pts = src;
+        b.pt_src = nullptr;
+    }
+    put(b.quad, N);
+    put(b.tile_cnt, b.ntiles + 1);
+    put(b.seg_label, N);
+    put(b.out_seg, N);
+    put(b.out_cl, N);
+    B.d_image = nullptr;
+    if (seg)
+    {
+        put(b.pt_cell, N);
+        put(b.pt_pix, N);
+        put(b.pt_slot, N);
+        put(b.cell_cnt, b.ncell + 1);
+        put(b.cell_start, b.ncell + 1);
+        put(b.csr_idx, N);
+        put(b.csr_z, N);
+        put(b.zlow, b.ncell);
+        put(b.elev, b.ncell);
+        put(b.large_list, b.ncell);
+        put(b.n_large, 1);
+        put(b.near_cnt, b.nnear + 1);
+        put(b.near_start, b.nnear + 1);
+        put(b.cand, N);
+        put(b.planes, S * kMaxRansacIters);
+        put(b.pvalid, S);
+        put(b.inliers, S * kMaxRansacIters);
+        put(b.pt_label, N);
+        put(b.pix_depth, b.npix);
+        put(b.pix_key, b.npix);
+        put(b.pix_map, b.npix);
+        put(b.pix_state, b.npix);
+        put(b.row_cols, b.npix);
+        put(b.row_cnt, b.nrows + 1);
+        put(b.jw, static_cast<size_t>(b.npix) * 26);
+        put(b.jmap, b.npix);
+        if (R.stages & ST_IMAGE)
+            put(B.d_image, static_cast<size_t>(b.npix) * 3);
+    }
+    if (clu)
+    {
+        put(b.obs_flag, N + 1);
+        put(b.obs_pts, N);
+        put(b.obs_pt, N);
+        put(b.obs_r, N);
+        put(b.obs_a, N);
+        put(b.obs_e, N);
+        put(b.obs_hslot, N);
+        put(b.hkey, b.nhash);
+        put(b.hmin, b.nhash);
+        put(b.hcnt, b.nhash);
+        put(b.hvid, b.nhash + 1);
+        put(b.vslot, b.nhash);
+        put(b.parent, b.nhash);
+        put(b.cmin, b.nhash);
+        put(b.ccnt, b.nhash);
+        put(b.kflag, N + 1);
+        put(b.obs_label, N);
+        put(b.cl_cnt, b.ncl + 1);
+        put(b.cl_start, b.ncl + 1);
+        put(b.cl_fill, b.ncl + 1);
+        put(b.members, N);
+    }
+    if (hull)
+    {
+        put(b.hull_cnt, b.ncl + 1);
+        put(b.hull_tmp, N);
+        put(b.hull_out, N);
+        put(b.cl_zmin, b.ncl);
+        put(b.cl_zmax, b.ncl);
+        put(b.obb_c, b.ncl);
+        put(b.obb_p, b.ncl);
+        uint8_t* cand;
+        put(cand, static_cast<size_t>(2) * N * 12 + 64);
+        b.hs_cand = cand;
+        put(b.hs_stack, static_cast<size_t>(2) * N + 2ull * b.ncl + 8);
+        put(b.hs_pts, static_cast<size_t>(N) + 8);
+        put(b.hs_pairs, static_cast<size_t>(4) * N + 16ull * b.ncl + 16);
+    }
+    return c.off + 4096;
+}
+
+lp_status build(lp_context* ctx, lp_batch& B)
+{
+    LP_TRY(plan(ctx, B));
+    const size_t bytes = carve(B, nullptr);
+    if (bytes > B.cap)
+    {
+        if (B.graph)
+        {
+            cudaGraphExecDestroy(B.graph);
+            B.graph = nullptr;
+        }
+        if (B.mem)
+        {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(B.mem);
+            B.mem = nullptr;
+            B.cap = 0;
+        }
+        const size_t cap = bytes + bytes / 8;
+        LP_CUDA(ctx, cudaMalloc(reinterpret_cast<void**>(&B.mem), cap));
+        B.cap = cap;
+    }
+    carve(B, B.mem);
+    B.h_state.assign(B.hb.nscan, ScanState{});
+    return LP_OK;
+}
+
+lp_status upload(lp_context* ctx, lp_batch& B)
+{
+    BatchDev& b = B.b;
+    const cudaStream_t st = ctx->stream;
+    LP_CUDA(ctx, cudaMemcpyAsync(const_cast<ScanDev*>(b.scans), B.hb.scans.data(),
+                                 B.hb.scans.size() * sizeof(ScanDev), cudaMemcpyHostToDevice, st));
+    for (size_t s = 0; s < B.run.scans.size(); ++s)
+    {
+        const ScanIn& in = B.run.scans[s];
+        const ScanDev& sd = B.hb.scans[s];
+        if (in.n == 0)
+            continue;
+        float4* dst = const_cast<float4*>(b.src) + sd.src_off;
+        if (in.stride == 4)
+        {
+            LP_CUDA(ctx, cudaMemcpyAsync(dst, in.xyzi, static_cast<size_t>(in.n) * 16, cudaMemcpyHostToDevice, st));
+        }
+        else
+        {
+            B.staging.resize(in.n);
+            for (uint32_t i = 0; i < in.n; ++i)
+                B.staging[i] = make_float4(in.xyzi[static_cast<size_t>(in.stride) * i],
+                                           in.xyzi[static_cast<size_t>(in.stride) * i + 1],
+                                           in.xyzi[static_cast<size_t>(in.stride) * i + 2], 0.0f);
+            LP_CUDA(ctx, cudaMemcpyAsync(dst, B.staging.data(), static_cast<size_t>(in.n) * 16, cudaMemcpyHostToDevice, st));
+            LP_CUDA(ctx, cudaStreamSynchronize(st)); // staging is reused by the next scan
+        }
+        if (in.ring && b.ring_in)
+            LP_CUDA(ctx, cudaMemcpyAsync(const_cast<uint16_t*>(b.ring_in) + sd.src_off, in.ring,
+                                         static_cast<size_t>(in.n) * 2, cudaMemcpyHostToDevice, st));
+    }
+    return LP_OK;
+}
+
+// The whole launch sequence of a batch (memsets + kernels), no host synchronisation.
+lp_status execute(lp_context* ctx, lp_batch& B)
+{
+    BatchDev& b = B.b;
+    const Run& R = B.run;
+    const cudaStream_t st = ctx->stream;
+    Launcher L;
+    L.stream = st;
+    L.launches = &ctx->launches;
+    L.scan_sums = B.scan_sums;
+    L.scan_total = b.d_scan_total;
+    L.event_pool = &ctx->events;
+    if (B.profiling)
+        L.prof = &B.prof;
+    const uint32_t N = b.npts, S = static_cast<uint32_t>(b.nscan);
+    LP_CUDA(ctx, cudaMemsetAsync(b.state, 0, S * sizeof(ScanState), st));
+    LP_CUDA(ctx, cudaMemsetAsync(b.seg_label, 0, static_cast<size_t>(N) * 4, st));
+    LP_CUDA(ctx, cudaMemsetAsync(b.out_seg, 0, static_cast<size_t>(N) * 4, st));
+    LP_CUDA(ctx, cudaMemsetAsync(b.out_cl, 0xff, static_cast<size_t>(N) * 4, st));
+    const bool noise = R.stages & ST_NOISE;
+    if (!noise)
+        LP_CUDA(ctx, cudaMemsetAsync(b.noise, 0, N, st));
+    if (b.ring_in && !noise)
+        LP_CUDA(ctx, cudaMemcpyAsync(b.ring, b.ring_in, static_cast<size_t>(N) * 2, cudaMemcpyDeviceToDevice, st));
+    launch_state_init(L, b, noise ? 1 : 0);
+    if (noise)
+    {
+        LP_CUDA(ctx, cudaMemsetAsync(b.dkey, 0xff, static_cast<size_t>(b.ndhash) * 8, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.dcnt, 0, (static_cast<size_t>(b.ndhash) + 1) * 4, st));
+        launch_noise(L, b, B.hb, R.nr);
+        if (R.stages & (ST_SEG | ST_CLUSTER | ST_ALL_OBS | ST_RING))
+            launch_noise_compaction(L, b, B.hb);
+    }
+    if (R.stages & (ST_RING | ST_SEG))
+    {
+        LP_CUDA(ctx, cudaMemsetAsync(b.tile_cnt, 0, (static_cast<size_t>(b.ntiles) + 1) * 4, st));
+    }
+    if ((R.stages & ST_RING) && !(R.stages & ST_SEG))
+        launch_ring_only(L, b, B.hb);
+    if (R.stages & ST_SEG)
+    {
+        LP_CUDA(ctx, cudaMemsetAsync(b.cell_cnt, 0, (static_cast<size_t>(b.ncell) + 1) * 4, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.n_large, 0, 4, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.near_cnt, 0, (static_cast<size_t>(b.nnear) + 1) * 4, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.pix_depth, 0xff, static_cast<size_t>(b.npix) * 4, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.pix_key, 0xff, static_cast<size_t>(b.npix) * 8, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.row_cnt, 0, (static_cast<size_t>(b.nrows) + 1) * 4, st));
+        launch_segmentation(L, b, B.hb, B.d_image);
+    }
+    if (R.stages & ST_ALL_OBS)
+        launch_mark_all_obstacles(L, b);
+    if (R.stages & (ST_CLUSTER | ST_ALL_OBS))
+    {
+        LP_CUDA(ctx, cudaMemsetAsync(b.hkey, 0xff, static_cast<size_t>(b.nhash) * 4, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.hmin, 0xff, static_cast<size_t>(b.nhash) * 4, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.hcnt, 0, static_cast<size_t>(b.nhash) * 4, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.kflag, 0, (static_cast<size_t>(N) + 1) * 4, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.cl_cnt, 0, (static_cast<size_t>(b.ncl) + 1) * 4, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.cl_fill, 0, (static_cast<size_t>(b.ncl) + 1) * 4, st));
+        launch_clustering(L, b, B.hb);
+    }
+    if (R.stages & ST_HULL)
+    {
+        LP_CUDA(ctx, cudaMemsetAsync(b.hull_cnt, 0, (static_cast<size_t>(b.ncl) + 1) * 4, st));
+        launch_polygons(L, b, B.hb, (R.stages & ST_OBB) ? 1 : 0);
+    }
+    if (R.stages & (ST_SEG | ST_CLUSTER | ST_ALL_OBS))
+        launch_outputs(L, b, (R.stages & (ST_CLUSTER | ST_ALL_OBS)) ? 1 : 0);
+    if (L.err != cudaSuccess)
+        return cuda_fail(ctx, L.err, "kernel launch");
+    return LP_OK;
+}
+
+lp_status fetch_state(lp_context* ctx, lp_batch& B)
+{
+    LP_CUDA(ctx, cudaMemcpyAsync(B.h_state.data(), B.b.state, B.h_state.size() * sizeof(ScanState),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    lp_status worst = LP_OK;
+    for (size_t s = 0; s < B.h_state.size(); ++s)
+    {
+        const uint32_t e = B.h_state[s].err;
+        if (!e)
+            continue;
+        lp_status st = LP_ERR_INTERNAL;
+        std::string what;
+        if (e & (ERR_VOXEL_CAPACITY | ERR_CLUSTER_CAPACITY | ERR_CELL_TOO_LARGE | ERR_HASH_FULL | ERR_HULL_CAPACITY))
+        {
+            st = LP_ERR_CAPACITY;
+            what = (e & ERR_VOXEL_CAPACITY) ? "more than 200000 occupied voxels (Exceeded reserved element capacity)"
+                                            : "a fixed capacity was exceeded";
+        }
+        else if (e & ERR_UF_TIMEOUT)
+        {
+            st = LP_ERR_TIMEOUT;
+            what = "union-find iteration limit reached";
+        }
+        else
+        {
+            what = "device consistency check failed";
+        }
+        ctx->last_error = "scan " + std::to_string(s) + ": " + what;
+        if (worst == LP_OK)
+            worst = st;
+    }
+    return worst;
+}
+
+lp_status ensure_device(lp_context* ctx)
+{
+    LP_CUDA(ctx, cudaSetDevice(ctx->device));
+    return LP_OK;
+}
+
+lp_batch& cached(lp_context* ctx)
+{
+    if (!ctx->cached)
+        ctx->cached = new lp_batch();
+    return *ctx->cached;
+}
+
+void destroy_batch(lp_batch* B)
+{
+    if (!B)
+        return;
+    if (B->graph)
+        cudaGraphExecDestroy(B->graph);
+    if (B->mem)
+        cudaFree(B->mem);
+    delete B;
+}
+
+lp_status run_once(lp_context* ctx, lp_batch& B)
+{
+    LP_TRY(build(ctx, B));
+    LP_TRY(upload(ctx, B));
+    LP_TRY(execute(ctx, B));
+    return fetch_state(ctx, B);
+}
+
+lp_status copy_d2h(lp_context* ctx, void* dst, const void* src, size_t bytes)
+{
+    if (!dst || bytes == 0)
+        return LP_OK;
+    LP_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return LP_OK;
+}
+
+// Per-scan results of a pipeline batch into the caller's lp_scan_output structs.
+lp_status download(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
+{
+    const BatchDev& b = B.b;
+    const bool hull = B.run.stages & ST_HULL;
+    std::vector<uint32_t> hoff;
+    lp_status worst = LP_OK;
+    for (size_t s = 0; s < B.run.scans.size(); ++s)
+    {
+        const ScanDev& sd = B.hb.scans[s];
+        const ScanState& st = B.h_state[s];
+        lp_scan_output& o = outs[s];
+        const size_t n = sd.n_src;
+        LP_TRY(copy_d2h(ctx, o.noise_labels, b.noise + sd.src_off, n));
+        LP_TRY(copy_d2h(ctx, o.seg_labels, b.out_seg + sd.src_off, n * 4));
+        LP_TRY(copy_d2h(ctx, o.cluster_labels, b.out_cl + sd.src_off, n * 4));
+        o.n_obstacles = st.n_obs;
+        o.n_clusters = st.n_clusters;
+        o.status = LP_OK;
+        if (!hull)
+            continue;
+        const uint32_t k = st.n_clusters;
+        if (k > o.cluster_capacity)
+        {
+            o.status = LP_ERR_CAPACITY;
+            if (worst == LP_OK)
+                worst = fail(ctx, LP_ERR_CAPACITY, "scan " + std::to_string(s) + ": cluster_capacity too small");
+            continue;
+        }
+        hoff.resize(k + 1);
+        LP_CUDA(ctx, cudaMemcpyAsync(hoff.data(), b.hull_cnt + sd.cl_off, (k + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        const uint32_t base = hoff[0];
+        const uint32_t nh = hoff[k] - base;
+        if (nh > o.hull_capacity)
+        {
+            o.status = LP_ERR_CAPACITY;
+            if (worst == LP_OK)
+                worst = fail(ctx, LP_ERR_CAPACITY, "scan " + std::to_string(s) + ": hull_capacity too small");
+            continue;
+        }
+        if (o.hull_offsets)
+            for (uint32_t i = 0; i <= k; ++i)
+                o.hull_offsets[i] = hoff[i] - base;
+        o.n_hull_indices = nh;
+        LP_TRY(copy_d2h(ctx, o.hull_indices, b.hull_out + base, static_cast<size_t>(nh) * 4));
+        LP_TRY(copy_d2h(ctx, o.z_min, b.cl_zmin + sd.cl_off, static_cast<size_t>(k) * 4));
+        LP_TRY(copy_d2h(ctx, o.z_max, b.cl_zmax + sd.cl_off, static_cast<size_t>(k) * 4));
+        if (B.run.stages & ST_OBB)
+        {
+            LP_TRY(copy_d2h(ctx, o.obb_calipers, b.obb_c + sd.cl_off, static_cast<size_t>(k) * sizeof(lp_bounding_box)));
+            LP_TRY(copy_d2h(ctx, o.obb_pca, b.obb_p + sd.cl_off, static_cast<size_t>(k) * sizeof(lp_bounding_box)));
+        }
+    }
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return worst;
+}
+
+lp_status fill_pipeline(lp_context* ctx, lp_batch& B, const lp_pipeline_config* cfg, const lp_scan_input* scans,
+                        uint32_t nscans)
+{
+    if (!cfg || (!scans && nscans))
+        return fail(ctx, LP_ERR_BAD_ARG, "null pipeline configuration or scans");
+    Run& R = B.run;
+    R = Run{};
+    R.stages = ST_SEG | ST_CLUSTER | ST_HULL | (cfg->compute_obb ? ST_OBB : 0u) |
+               (cfg->enable_noise_removal ? ST_NOISE : 0u);
+    R.cl = cfg->cluster;
+    R.nr = cfg->noise;
+    for (uint32_t i = 0; i < nscans; ++i)
+    {
+        if (scans[i].n && !scans[i].xyzi)
+            return fail(ctx, LP_ERR_BAD_ARG, "scan with points but no xyzi pointer");
+        ScanIn in;
+        in.xyzi = scans[i].xyzi;
+        in.ring = cfg->compute_ring ? nullptr : scans[i].ring;
+        in.n = scans[i].n;
+        in.seg = scans[i].seg;
+        in.compute_ring = cfg->compute_ring;
+        in.first_ring = cfg->first_ring ? static_cast<int32_t>(cfg->first_ring) : -1; // 0: image_height - 1
+        R.scans.push_back(in);
+    }
+    return LP_OK;
+}
+} // namespace
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+extern "C" {
+
+void lp_segmenter_config_default(lp_segmenter_config* c)
+{
+    // SegmenterConfiguration member initialisers, segmenter.hpp:91-108
+    c->elevation_up_deg = 2.0F;
+    c->elevation_down_deg = -24.8F;
+    c->image_width = 2048;
+    c->image_height = 64;
+    c->assume_unorganized_cloud = 0;
+    c->grid_radial_spacing_m = 2.0F;
+    c->grid_slice_resolution_deg = 1.0F;
+    c->ground_height_threshold_m = 0.2F;
+    c->road_maximum_slope_m_per_m = 0.2F;
+    c->min_distance_m = 2.0F;
+    c->max_distance_m = 100.0F;
+    c->sensor_height_m = 1.73F;
+    c->kernel_threshold_distance_m = 1.0F;
+    c->amplification_factor = 5.0F;
+    c->z_min_m = -3.0F;
+    c->z_max_m = 4.0F;
+}
+
+void lp_noise_remover_config_default(lp_noise_remover_config* c)
+{
+    // noise_remover.hpp:41-54
+    c->radius_multiplier_m_per_m = 0.02F;
+    c->min_search_radius_m = 0.1F;
+    c->min_neighbours = 4U;
+}
+
+void lp_clusterer_config_default(lp_clusterer_config* c)
+{
+    // clusterer.hpp:61-68
+    c->voxel_grid_range_resolution_m = 0.4F;
+    c->voxel_grid_azimuth_resolution_deg = 1.0F;
+    c->voxel_grid_elevation_resolution_deg = 1.5F;
+    c->min_cluster_size = 3;
+}
+
+void lp_pipeline_config_default(lp_pipeline_config* c)
+{
+    lp_clusterer_config_default(&c->cluster);
+    c->cluster.voxel_grid_elevation_resolution_deg = 3.0F; // processor.param.yaml:34
+    lp_noise_remover_config_default(&c->noise);
+    c->enable_noise_removal = 0;
+    c->compute_ring = 0;
+    c->first_ring = 0;
+    c->reserved0 = 0;
+    c->compute_obb = 1;
+}
+
+const char* lp_status_string(lp_status s)
+{
+    switch (s)
+    {
+    case LP_OK:
+        return "ok";
+    case LP_ERR_BAD_ARG:
+        return "bad argument";
+    case LP_ERR_CAPACITY:
+        return "capacity exceeded";
+    case LP_ERR_TIMEOUT:
+        return "bounded device wait timed out";
+    case LP_ERR_CUDA:
+        return "CUDA error";
+    case LP_ERR_NO_DEVICE:
+        return "no CUDA device";
+    case LP_ERR_INTERNAL:
+        return "internal consistency check failed";
+    default:
+        return "unknown status";
+    }
+}
+
+lp_status lp_context_create(int32_t device, lp_context** out)
+{
+    if (!out)
+        return LP_ERR_BAD_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+    {
+        cudaGetLastError();
+        return LP_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count)
+        return LP_ERR_BAD_ARG;
+    lp_context* ctx = new lp_context();
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        cudaGetLastError();
+        delete ctx;
+        return LP_ERR_CUDA;
+    }
+    *out = ctx;
+    return LP_OK;
+}
+
+void lp_context_destroy(lp_context* ctx)
+{
+    if (!ctx)
+        return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    destroy_batch(ctx->cached);
+    for (cudaEvent_t e : ctx->events)
+        cudaEventDestroy(e);
+    if (ctx->flush)
+        cudaFree(ctx->flush);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* lp_last_error(const lp_context* ctx)
+{
+    return ctx ? ctx->last_error.c_str() : "";
+}
+
+uint64_t lp_kernel_launch_count(const lp_context* ctx)
+{
+    return ctx ? ctx->launches : 0;
+}
+
+lp_status lp_add_ring_info(lp_context* ctx, const float* xyzi, uint32_t n, uint16_t first_ring, uint16_t* ring_out)
+{
+    if (!ctx || (n && (!xyzi || !ring_out)))
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument");
+    if (n == 0)
+        return LP_OK;
+    LP_TRY(ensure_device(ctx));
+    lp_batch& B = cached(ctx);
+    B.run = Run{};
+    B.run.stages = ST_RING;
+    ScanIn in;
+    in.xyzi = xyzi;
+    in.n = n;
+    in.compute_ring = 1;
+    in.first_ring = first_ring;
+    B.run.scans.push_back(in);
+    LP_TRY(run_once(ctx, B));
+    LP_CUDA(ctx, cudaMemcpyAsync(ring_out, B.b.ring, static_cast<size_t>(n) * 2, cudaMemcpyDeviceToHost, ctx->stream));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LP_OK;
+}
+
+lp_status lp_segment(lp_context* ctx, const float* xyzi, const uint16_t* ring, uint32_t n,
+                     const lp_segmenter_config* cfg, uint32_t* labels_out, uint8_t* image_bgr_out)
+{
+    if (!ctx || !cfg || (n && (!xyzi || !labels_out)))
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument");
+    if (!seg_config_ok(*cfg))
+        return fail(ctx, LP_ERR_BAD_ARG, "segmenter configuration out of the supported range");
+    if (n == 0 && !image_bgr_out)
+        return LP_OK;
+    LP_TRY(ensure_device(ctx));
+    lp_batch& B = cached(ctx);
+    B.run = Run{};
+    B.run.stages = ST_SEG | (image_bgr_out ? ST_IMAGE : 0u);
+    ScanIn in;
+    in.xyzi = xyzi;
+    in.ring = ring;
+    in.n = n;
+    in.seg = *cfg;
+    B.run.scans.push_back(in);
+    LP_TRY(run_once(ctx, B));
+    LP_TRY(copy_d2h(ctx, labels_out, B.b.out_seg, static_cast<size_t>(n) * 4));
+    if (image_bgr_out)
+        LP_TRY(copy_d2h(ctx, image_bgr_out, B.d_image, static_cast<size_t>(B.b.npix) * 3));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LP_OK;
+}
+
+lp_status lp_noise_remove(lp_context* ctx, const float* xyz, uint32_t stride, uint32_t n,
+                          const lp_noise_remover_config* cfg, uint8_t* labels_out)
+{
+    if (!ctx || !cfg || (n && (!xyz || !labels_out)) || stride < 3)
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument or stride < 3");
+    if (n == 0)
+        return LP_OK;
+    LP_TRY(ensure_device(ctx));
+    lp_batch& B = cached(ctx);
+    B.run = Run{};
+    B.run.stages = ST_NOISE;
+    B.run.nr = *cfg;
+    ScanIn in;
+    in.xyzi = xyz;
+    in.stride = stride;
+    in.n = n;
+    B.run.scans.push_back(in);
+    LP_TRY(run_once(ctx, B));
+    LP_TRY(copy_d2h(ctx, labels_out, B.b.noise, n));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LP_OK;
+}
+
+lp_status lp_cluster(lp_context* ctx, const float* xyz, uint32_t stride, uint32_t n, const lp_clusterer_config* cfg,
+                     int32_t* labels_out)
+{
+    if (!ctx || !cfg || (n && (!xyz || !labels_out)) || stride < 3)
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument or stride < 3");
+    if (n == 0)
+        return LP_OK;
+    if (!(cfg->voxel_grid_range_resolution_m > 0) || !(cfg->voxel_grid_azimuth_resolution_deg > 0) ||
+        !(cfg->voxel_grid_elevation_resolution_deg > 0))
+        return fail(ctx, LP_ERR_BAD_ARG, "voxel resolution must be positive");
+    LP_TRY(ensure_device(ctx));
+    lp_batch& B = cached(ctx);
+    B.run = Run{};
+    B.run.stages = ST_ALL_OBS;
+    B.run.cl = *cfg;
+    ScanIn in;
+    in.xyzi = xyz;
+    in.stride = stride;
+    in.n = n;
+    B.run.scans.push_back(in);
+    LP_TRY(run_once(ctx, B));
+    LP_TRY(copy_d2h(ctx, labels_out, B.b.out_cl, static_cast<size_t>(n) * 4));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LP_OK;
+}
+
+// Single-polygon entry points use a small scratch allocation of their own.
+static lp_status poly_scratch(lp_context* ctx, size_t bytes, char** out)
+{
+    lp_batch& B = cached(ctx);
+    if (B.cap < bytes)
+    {
+        if (B.graph)
+        {
+            cudaGraphExecDestroy(B.graph);
+            B.graph = nullptr;
+        }
+        if (B.mem)
+        {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(B.mem);
+        }
+        B.mem = nullptr;
+        B.cap = 0;
+        LP_CUDA(ctx, cudaMalloc(reinterpret_cast<void**>(&B.mem), bytes));
+        B.cap = bytes;
+    }
+    *out = B.mem;
+    return LP_OK;
+}
+
+lp_status lp_convex_hull(lp_context* ctx, const double* xy, uint32_t n, int32_t* indices_out, uint32_t* n_out)
+{
+    if (!ctx || !n_out || (n && (!xy || !indices_out)))
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument");
+    if (n < 3)
+    {
+        // polygonizer.cpp:36-41
+        for (uint32_t i = 0; i < n; ++i)
+            indices_out[i] = static_cast<int32_t>(i);
+        *n_out = n;
+        return LP_OK;
+    }
+    LP_TRY(ensure_device(ctx));
+    const size_t np2 = next_pow2(n);
+    const size_t bytes = 4096 + n * 16 + np2 * 24 + (2 * n + 8) * 4 + (n + 8) * 4 + 64;
+    char* m;
+    LP_TRY(poly_scratch(ctx, bytes, &m));
+    Carver c{m};
+    double2* pts = c.take<double2>(n);
+    char* scratch = c.take<char>(np2 * 24);
+    int* stack = c.take<int>(2 * n + 8);
+    int32_t* out = c.take<int32_t>(n + 8);
+    uint32_t* nout = c.take<uint32_t>(4);
+    LP_CUDA(ctx, cudaMemcpyAsync(pts, xy, static_cast<size_t>(n) * 16, cudaMemcpyHostToDevice, ctx->stream));
+    Launcher L;
+    L.stream = ctx->stream;
+    L.launches = &ctx->launches;
+    launch_hull_single(L, pts, n, scratch, stack, out, nout);
+    if (L.err != cudaSuccess)
+        return cuda_fail(ctx, L.err, "lp_convex_hull launch");
+    uint32_t h = 0;
+    LP_CUDA(ctx, cudaMemcpyAsync(&h, nout, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    LP_CUDA(ctx, cudaMemcpyAsync(indices_out, out, static_cast<size_t>(h) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *n_out = h;
+    return LP_OK;
+}
+
+static lp_status boxes_single(lp_context* ctx, const double* hull_xy, uint32_t n, int kind, lp_bounding_box* out,
+                              int32_t* pairs_out, uint32_t capacity, uint32_t* n_pairs)
+{
+    LP_TRY(ensure_device(ctx));
+    const int cap = static_cast<int>(4 * n + 16);
+    const size_t bytes = 4096 + static_cast<size_t>(n) * 16 + static_cast<size_t>(cap) * 8 + sizeof(lp_bounding_box) + 64;
+    char* m;
+    LP_TRY(poly_scratch(ctx, bytes, &m));
+    Carver c{m};
+    double2* P = c.take<double2>(n + 1);
+    int2* pairs = c.take<int2>(cap);
+    lp_bounding_box* box = c.take<lp_bounding_box>(1);
+    int* np = c.take<int>(4);
+    if (n)
+        LP_CUDA(ctx, cudaMemcpyAsync(P, hull_xy, static_cast<size_t>(n) * 16, cudaMemcpyHostToDevice, ctx->stream));
+    Launcher L;
+    L.stream = ctx->stream;
+    L.launches = &ctx->launches;
+    launch_boxes_single(L, P, n, pairs, cap, kind, box, np);
+    if (L.err != cudaSuccess)
+        return cuda_fail(ctx, L.err, "bounding box launch");
+    int hnp = 0;
+    LP_CUDA(ctx, cudaMemcpyAsync(&hnp, np, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (out)
+        LP_CUDA(ctx, cudaMemcpyAsync(out, box, sizeof(lp_bounding_box), cudaMemcpyDeviceToHost, ctx->stream));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (n_pairs)
+        *n_pairs = static_cast<uint32_t>(hnp);
+    if (pairs_out)
+    {
+        if (static_cast<uint32_t>(hnp) > capacity || hnp > cap)
+            return fail(ctx, LP_ERR_CAPACITY, "antipodal pair capacity too small");
+        LP_CUDA(ctx, cudaMemcpyAsync(pairs_out, pairs, static_cast<size_t>(hnp) * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return LP_OK;
+}
+
+lp_status lp_antipodal_pairs(lp_context* ctx, const double* hull_xy, uint32_t n, int32_t* pairs_out, uint32_t capacity,
+                             uint32_t* n_pairs)
+{
+    if (!ctx || !n_pairs || (n && (!hull_xy || !pairs_out)))
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument");
+    if (n < 2)
+    {
+        *n_pairs = 0;
+        return LP_OK;
+    }
+    return boxes_single(ctx, hull_xy, n, 2, nullptr, pairs_out, capacity, n_pairs);
+}
+
+lp_status lp_bounding_box_rotating_calipers(lp_context* ctx, const double* hull_xy, uint32_t n, lp_bounding_box* out)
+{
+    if (!ctx || !out || (n && !hull_xy))
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    if (n < 3)
+        return LP_OK;
+    return boxes_single(ctx, hull_xy, n, 0, out, nullptr, 0, nullptr);
+}
+
+lp_status lp_bounding_box_pca(lp_context* ctx, const double* hull_xy, uint32_t n, lp_bounding_box* out)
+{
+    if (!ctx || !out || (n && !hull_xy))
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    if (n < 3)
+        return LP_OK;
+    return boxes_single(ctx, hull_xy, n, 1, out, nullptr, 0, nullptr);
+}
+
+lp_status lp_process_batch(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans,
+                           lp_scan_output* outs, uint32_t nscans)
+{
+    if (!ctx || !outs)
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument");
+    if (nscans == 0)
+        return LP_OK;
+    LP_TRY(ensure_device(ctx));
+    lp_batch& B = cached(ctx);
+    LP_TRY(fill_pipeline(ctx, B, cfg, scans, nscans));
+    const lp_status st = run_once(ctx, B);
+    if (st != LP_OK && st != LP_ERR_CAPACITY)
+        return st;
+    const lp_status dl = download(ctx, B, outs);
+    return st != LP_OK ? st : dl;
+}
+
+lp_status lp_process_scan(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scan,
+                          lp_scan_output* out)
+{
+    return lp_process_batch(ctx, cfg, scan, out, 1);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Prepared batches (lidar_gb300_batch.h)
+// ---------------------------------------------------------------------------------------------
+lp_status lp_batch_create(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans, uint32_t nscans,
+                          lp_batch** out)
+{
+    if (!ctx || !out || nscans == 0)
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument or empty batch");
+    *out = nullptr;
+    LP_TRY(ensure_device(ctx));
+    lp_batch* B = new lp_batch();
+    lp_status st = fill_pipeline(ctx, *B, cfg, scans, nscans);
+    if (st == LP_OK)
+        st = build(ctx, *B);
+    if (st == LP_OK)
+        st = upload(ctx, *B);
+    if (st != LP_OK)
+    {
+        destroy_batch(B);
+        return st;
+    }
+    *out = B;
+    return LP_OK;
+}
+
+void lp_batch_destroy(lp_context* ctx, lp_batch* batch)
+{
+    if (ctx)
+    {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    destroy_batch(batch);
+}
+
+lp_status lp_batch_upload(lp_context* ctx, lp_batch* B)
+{
+    if (!ctx || !B)
+        return LP_ERR_BAD_ARG;
+    return upload(ctx, *B);
+}
+
+lp_status lp_batch_execute(lp_context* ctx, lp_batch* B)
+{
+    if (!ctx || !B)
+        return LP_ERR_BAD_ARG;
+    if (B->graph)
+    {
+        LP_CUDA(ctx, cudaGraphLaunch(B->graph, ctx->stream));
+        ctx->launches += 1;
+        return LP_OK;
+    }
+    return execute(ctx, *B);
+}
+
+lp_status lp_batch_capture_graph(lp_context* ctx, lp_batch* B)
+{
+    if (!ctx || !B)
+        return LP_ERR_BAD_ARG;
+    if (B->graph)
+        return LP_OK;
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaGraph_t g;
+    LP_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const uint64_t before = ctx->launches;
+    const lp_status st = execute(ctx, *B);
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->launches = before;
+    if (st != LP_OK)
+        return st;
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "cudaStreamEndCapture");
+    const cudaError_t ie = cudaGraphInstantiate(&B->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess)
+        return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+    return LP_OK;
+}
+
+lp_status lp_batch_download(lp_context* ctx, lp_batch* B, lp_scan_output* outs)
+{
+    if (!ctx || !B || !outs)
+        return LP_ERR_BAD_ARG;
+    const lp_status st = fetch_state(ctx, *B);
+    if (st != LP_OK && st != LP_ERR_CAPACITY)
+        return st;
+    const lp_status dl = download(ctx, *B, outs);
+    return st != LP_OK ? st : dl;
+}
+
+lp_status lp_context_synchronize(lp_context* ctx)
+{
+    if (!ctx)
+        return LP_ERR_BAD_ARG;
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LP_OK;
+}
+
+uint32_t lp_batch_points(const lp_batch* B)
+{
+    return B ? B->b.nsrc : 0;
+}
+
+uint64_t lp_batch_device_bytes(const lp_batch* B)
+{
+    return B ? B->cap : 0;
+}
+
+// Device time of `iters` executions with CUDA events on the context stream. flush_l2: write a
+// buffer larger than L2 before each execution (outside the timed interval).
+lp_status lp_batch_time(lp_context* ctx, lp_batch* B, uint32_t iters, int32_t flush_l2, float* ms_per_iter)
+{
+    if (!ctx || !B || !ms_per_iter || iters == 0)
+        return LP_ERR_BAD_ARG;
+    if (flush_l2 && !ctx->flush)
+    {
+        ctx->flush_bytes = 512ull << 20;
+        LP_CUDA(ctx, cudaMalloc(&ctx->flush, ctx->flush_bytes));
+    }
+    cudaEvent_t e0, e1;
+    LP_CUDA(ctx, cudaEventCreate(&e0));
+    LP_CUDA(ctx, cudaEventCreate(&e1));
+    float total = 0.0f;
+    for (uint32_t it = 0; it < iters; ++it)
+    {
+        if (flush_l2)
+            LP_CUDA(ctx, cudaMemsetAsync(ctx->flush, static_cast<int>(it & 0xff), ctx->flush_bytes, ctx->stream));
+        LP_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        const lp_status st = lp_batch_execute(ctx, B);
+        if (st != LP_OK)
+            return st;
+        LP_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        LP_CUDA(ctx, cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        LP_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+        total += ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_per_iter = total / static_cast<float>(iters);
+    return LP_OK;
+}
+
+// Per-kernel device time of one (non-graph) execution: every launch bracketed by events on the
+// context stream. Writes up to `cap` (name, milliseconds) records; *count receives the total.
+lp_status lp_batch_profile(lp_context* ctx, lp_batch* B, char* names, uint32_t name_len, float* ms, uint32_t cap,
+                           uint32_t* count)
+{
+    if (!ctx || !B || !count)
+        return LP_ERR_BAD_ARG;
+    B->prof.clear();
+    B->profiling = true;
+    const lp_status st = execute(ctx, *B);
+    B->profiling = false;
+    if (st != LP_OK)
+        return st;
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *count = static_cast<uint32_t>(B->prof.size());
+    for (uint32_t i = 0; i < B->prof.size() && i < cap; ++i)
+    {
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, B->prof[i].start, B->prof[i].stop);
+        if (ms)
+            ms[i] = t;
+        if (names && name_len)
+        {
+            std::strncpy(names + static_cast<size_t>(i) * name_len, B->prof[i].name, name_len - 1);
+            names[static_cast<size_t>(i) * name_len + name_len - 1] = 0;
+        }
+    }
+    return LP_OK;
+}
+
+// Evaluates the device's correctly rounded binary32 functions (kind 0 atan2, 1 atan, 2 exp,
+// 3 the reference's atan2 approximation) on host arrays; used by the parity tests.
+lp_status lp_debug_math(lp_context* ctx, int32_t kind, const float* a, const float* b, uint32_t n, float* out)
+{
+    if (!ctx || !a || !out)
+        return LP_ERR_BAD_ARG;
+    if (n == 0)
+        return LP_OK;
+    LP_TRY(ensure_device(ctx));
+    char* m;
+    LP_TRY(poly_scratch(ctx, static_cast<size_t>(n) * 12 + 1024, &m));
+    Carver c{m};
+    float* da = c.take<float>(n);
+    float* db = c.take<float>(n);
+    float* dout = c.take<float>(n);
+    LP_CUDA(ctx, cudaMemcpyAsync(da, a, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, ctx->stream));
+    LP_CUDA(ctx, cudaMemcpyAsync(db, b ? b : a, static_cast<size_t>(n) * 4, cudaMemcpyHostToDevice, ctx->stream));
+    Launcher L;
+    L.stream = ctx->stream;
+    L.launches = &ctx->launches;
+    launch_debug_math(L, kind, da, db, n, dout);
+    if (L.err != cudaSuccess)
+        return cuda_fail(ctx, L.err, "lp_debug_math launch");
+    LP_CUDA(ctx, cudaMemcpyAsync(out, dout, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LP_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,160 @@
+// lp_batch.cuh — device pointers of one batch (passed by value to every kernel).
+//
+// HBM layout: each array is flat over the batch; scan s owns [ScanDev::*_off, + count).
+//   points       float4 xyzi (16 B)            npts      (after optional noise compaction)
+//   pixels       state u8, map i32, keys u64    npix      = sum H*W
+//   polar cells  counts/starts/elevation        ncell     = sum nslice*nrad
+//   near cells   RANSAC candidate counts        nnear     = sum nslice*4
+//   obstacles    float4 + src index             <= npts
+//   voxel hash   key/min/count                  nhash     = sum pow2 >= 2*n
+//   clusters     counts/starts/boxes            ncl       = sum (n/min_size + 1)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lp_internal.cuh"
+
+namespace lpg
+{
+// Pixel states of the range image (the reference's BGR colours, segmenter.hpp:144-148).
+enum : uint8_t
+{
+    PX_EMPTY = 0,     // (0,0,0)
+    PX_GROUND = 1,    // (0,255,0)
+    PX_OBSTACLE = 2,  // (0,0,255)
+    PX_INTERSECT = 4, // (255,0,0)   queued, not (yet) resolved by the vote
+    PX_EMPTY_RED = 6, // (0,0,255)   empty pixel whose red channel was dilated
+    PX_RES_G = 7,     // (0,255,0)   queued pixel the vote resolved to ground
+    PX_RES_O = 8      // (0,0,255)   queued pixel the vote resolved to obstacle
+};
+
+// Vote outcomes / labels seen by a neighbour: 0 unknown, 1 ground, 2 obstacle.
+enum : uint8_t
+{
+    V_U = 0,
+    V_G = 1,
+    V_O = 2
+};
+
+struct BatchDev
+{
+    int nscan;
+    const ScanDev* scans;
+    ScanState* state;
+    uint32_t* d_scan_total; // scratch for device-wide scan grand totals
+
+    // ---- input / points --------------------------------------------------------------------
+    uint32_t nsrc;            // input points (before noise compaction)
+    const float4* src;        // input points
+    uint8_t* noise;           // per input point: LP_NOISE_*
+    uint32_t* src_pos;        // per input point: compacted position (scan of VALID flags)
+    uint32_t npts;            // points entering segmentation
+    float4* pts;              // compacted points (== src when noise removal is off)
+    int32_t* pt_src;          // compacted point -> input point (global)
+    uint16_t* ring;           // per compacted point
+    const uint16_t* ring_in;  // per input point, or null
+
+    // ---- ring partition ---------------------------------------------------------------------
+    uint8_t* quad;            // per point quadrant
+    uint32_t ntiles;
+    uint32_t* tile_cnt;       // transitions per 1024-point tile -> exclusive scan in place
+
+    // ---- polar grid --------------------------------------------------------------------------
+    int32_t* pt_cell;  // global cell or -1
+    int32_t* pt_pix;   // local pixel h*W+w
+    uint32_t* pt_slot; // arrival slot in the cell
+    uint32_t ncell;
+    uint32_t* cell_cnt;
+    uint32_t* cell_start;
+    int32_t* csr_idx;  // local point index per grid entry
+    float* csr_z;
+    float* zlow;       // per cell
+    float* elev;       // per cell
+    uint32_t* large_list;
+    uint32_t* n_large;
+
+    // ---- RANSAC ------------------------------------------------------------------------------
+    uint32_t nnear;
+    uint32_t* near_cnt;
+    uint32_t* near_start;
+    float4* cand;
+    float4* planes;            // nscan * 60
+    unsigned long long* pvalid; // nscan: bit it = hypothesis it usable
+    uint32_t* inliers;         // nscan * 60
+
+    // ---- projection / range image ------------------------------------------------------------
+    uint8_t* pt_label; // per point after RECM + RANSAC
+    uint32_t npix;
+    uint32_t* pix_depth;
+    unsigned long long* pix_key;
+    int32_t* pix_map;
+    uint8_t* pix_state;
+
+    // ---- jump convolution -------------------------------------------------------------------
+    uint32_t nrows;
+    uint16_t* row_cols;        // per pixel slot: intersection columns of the row in order
+    uint32_t* row_cnt;         // per global row
+    float* jw;                 // per entry: 24 fresh weights + sum (stride 26)
+    unsigned long long* jmap;  // per entry: 9-state transition map
+
+    // ---- segmentation output -----------------------------------------------------------------
+    uint32_t* seg_label; // per compacted point
+
+    // ---- clustering --------------------------------------------------------------------------
+    uint32_t* obs_flag;   // per point: 1 if obstacle -> exclusive scan in place (obstacle slot)
+    float4* obs_pts;      // per obstacle: x, y, z, (float)local index
+    int32_t* obs_pt;      // per obstacle: compacted point index (global)
+    float* obs_r;
+    float* obs_a;
+    float* obs_e;
+    uint32_t* obs_hslot;  // per obstacle: hash slot
+    uint32_t nhash;
+    uint32_t* hkey;       // per slot: voxel flat key or 0xffffffff
+    uint32_t* hmin;       // per slot: min local obstacle index
+    uint32_t* hcnt;       // per slot: points in voxel
+    uint32_t* hvid;       // per slot: 1 if occupied -> exclusive scan in place (voxel id)
+    uint32_t* vslot;      // per voxel id: hash slot
+    uint32_t* parent;     // per voxel id
+    uint32_t* cmin;       // per voxel id (valid at roots)
+    uint32_t* ccnt;
+    uint32_t* kflag;      // per obstacle: 1 at the min point of a kept component -> scan
+    int32_t* obs_label;   // per obstacle: cluster label or -1
+
+    // ---- per-cluster ---------------------------------------------------------------------------
+    uint32_t ncl;
+    uint32_t* cl_cnt;     // members per cluster
+    uint32_t* cl_start;   // exclusive scan of cl_cnt
+    uint32_t* cl_fill;
+    uint32_t* members;    // obstacle indices grouped by cluster (unordered within)
+    uint32_t* hull_cnt;   // hull vertices per cluster -> exclusive scan in place
+    int32_t* hull_tmp;    // per member slot: hull local indices at cl_start
+    int32_t* hull_out;    // dense hull local indices (batch)
+    float* cl_zmin;
+    float* cl_zmax;
+    lp_bounding_box* obb_c;
+    lp_bounding_box* obb_p;
+    void* hs_cand;        // hull candidates (12 B each), 2 per member slot, at 2 * cl_start
+    int32_t* hs_stack;    // monotone-chain stack, at 2 * cl_start + 2 * cluster
+    double2* hs_pts;      // hull vertices as FP64, at cl_start
+    int2* hs_pairs;       // antipodal pairs, at 4 * cl_start + 16 * cluster
+
+    // ---- DROR --------------------------------------------------------------------------------
+    uint32_t ndhash;           // grid-cell hash slots
+    unsigned long long* dkey;  // per slot: packed cell coordinates or ~0
+    uint32_t* dcnt;            // per slot: points in the cell (ndhash + 1)
+    uint32_t* dstart;          // exclusive scan of dcnt
+    uint32_t* dslot;           // per input point: hash slot
+    uint32_t* drank;           // per input point: arrival rank in its cell
+    uint32_t* dorder;          // input points grouped by cell
+    float* dr2;                // per input point: squared search radius
+
+    // ---- outputs per input point ---------------------------------------------------------------
+    uint32_t* out_seg;
+    int32_t* out_cl;
+};
+
+__device__ __forceinline__ int scan_of_point(const BatchDev& b, uint32_t i)
+{
+    return find_scan(b.nscan, i, [&](int s) { return b.scans[s].pt_off; });
+}
+} // namespace lpg

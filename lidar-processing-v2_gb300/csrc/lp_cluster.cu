@@ -1,0 +1,401 @@
+// lp_cluster.cu — curved-voxel clustering of the obstacle points.
+//
+// Reference: lidar_processing_lib/src/clusterer.cpp. The reference labels 26-connected
+// components of occupied (range, azimuth, elevation) voxels by a BFS seeded in point order, so
+// a component's label is the rank of its smallest point index; components smaller than
+// min_cluster_size are dropped and the rest renumbered in the same order (clusterer.cpp:
+// 122-239). Here: a per-scan open-addressing hash of occupied voxels, lock-free union-find over
+// the 26-neighbour graph (the azimuth index wraps modulo num_azimuth as in clusterer.cpp:
+// 161-169), and the canonical labels from a prefix scan of "component minimum" flags. Labels
+// are identical to the reference's, not only the partition.
+#include "lp_batch.cuh"
+#include "lp_common.cuh"
+#include "lp_math.cuh"
+#include "lp_stages.hpp"
+
+namespace lpg
+{
+namespace
+{
+constexpr float kTwoPiF = 6.28318548202514648438f; // Clusterer::TWO_M_PIf
+constexpr float kPi2F = 1.57079637050628662109f;   // M_PI_2f
+constexpr uint32_t kEmpty = 0xffffffffu;
+constexpr int kMaxIters = 1 << 22;
+
+__device__ __forceinline__ int scan_of_obs(const BatchDev& b, uint32_t o)
+{
+    return find_scan(b.nscan, o, [&](int s) { return b.state[s].obs_off; });
+}
+__device__ __forceinline__ int scan_of_hash(const BatchDev& b, uint32_t h)
+{
+    return find_scan(b.nscan, h, [&](int s) { return b.scans[s].hash_off; });
+}
+__device__ __forceinline__ uint32_t hash_mix(uint32_t k)
+{
+    k *= 0x9E3779B1u;
+    k ^= k >> 15;
+    k *= 0x85EBCA77u;
+    k ^= k >> 13;
+    return k;
+}
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p)
+{
+    return *reinterpret_cast<const volatile uint32_t*>(p);
+}
+
+__global__ void k_obs_flag(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > b.npts)
+        return;
+    b.obs_flag[i] = (i < b.npts && b.seg_label[i] == LP_LABEL_OBSTACLE) ? 1u : 0u;
+}
+
+__global__ void k_obs_state(BatchDev b)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= b.nscan)
+        return;
+    const ScanDev& sd = b.scans[s];
+    ScanState& st = b.state[s];
+    st.obs_off = b.obs_flag[sd.pt_off];
+    st.n_obs = b.obs_flag[sd.pt_off + sd.n] - st.obs_off;
+    st.max_r_bits = 0u;
+    st.max_a_bits = 0u;
+    st.max_e_bits = 0u;
+}
+
+// Obstacle cloud in input order (processor.cpp:562-579) with the spherical coordinates of
+// Clusterer::cartesianToSpherical (clusterer.cpp:55-100).
+__global__ void k_obs_gather(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.npts || b.seg_label[i] != LP_LABEL_OBSTACLE)
+        return;
+    const uint32_t o = b.obs_flag[i];
+    const int s = scan_of_point(b, i);
+    ScanState& st = b.state[s];
+    const float4 p = b.pts[i];
+    b.obs_pts[o] = p;
+    b.obs_pt[o] = static_cast<int32_t>(i);
+    float az = lpm::cr_atan2f(p.y, p.x);
+    az = (az < 0) ? (az + kTwoPiF) : az;
+    const float d2 = p.x * p.x + p.y * p.y;
+    const float d = sqrtf(d2);
+    const float r = sqrtf(d2 + p.z * p.z);
+    const float el = lpm::cr_atanf(p.z / d) + kPi2F;
+    b.obs_r[o] = r;
+    b.obs_a[o] = az;
+    b.obs_e[o] = el;
+    atomicMax(&st.max_r_bits, r > 0.0f ? __float_as_uint(r) : 0u);
+    atomicMax(&st.max_a_bits, az > 0.0f ? __float_as_uint(az) : 0u);
+    atomicMax(&st.max_e_bits, el > 0.0f ? __float_as_uint(el) : 0u);
+}
+
+__global__ void k_dims(BatchDev b)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= b.nscan)
+        return;
+    const ScanDev& sd = b.scans[s];
+    ScanState& st = b.state[s];
+    if (st.n_obs == 0)
+    {
+        st.nr = st.na = st.ne = 0;
+        return;
+    }
+    st.nr = static_cast<int32_t>(ceilf(__uint_as_float(st.max_r_bits) / sd.res_r) + 1.0f);
+    st.na = static_cast<int32_t>(ceilf(__uint_as_float(st.max_a_bits) / sd.res_a) + 1.0f);
+    st.ne = static_cast<int32_t>(ceilf(__uint_as_float(st.max_e_bits) / sd.res_e) + 1.0f);
+    const long long cells = static_cast<long long>(st.nr) * st.na * st.ne;
+    if (cells > 0x7fffffffLL)
+        raise_err(&st, ERR_INTERNAL);
+}
+
+__device__ __forceinline__ int32_t flat_voxel(int32_t nr, int32_t na, int32_t r, int32_t a, int32_t e)
+{
+    return nr * (na * e + a) + r; // Clusterer::flatVoxelIndex, clusterer.hpp:136-142
+}
+
+__global__ void k_vox_insert(BatchDev b)
+{
+    const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= b.obs_flag[b.npts])
+        return;
+    const int s = scan_of_obs(b, o);
+    const ScanDev& sd = b.scans[s];
+    ScanState& st = b.state[s];
+    const int32_t vr = static_cast<int32_t>(b.obs_r[o] / sd.res_r);
+    const int32_t va = static_cast<int32_t>(b.obs_a[o] / sd.res_a);
+    const int32_t ve = static_cast<int32_t>(b.obs_e[o] / sd.res_e);
+    const uint32_t key = static_cast<uint32_t>(flat_voxel(st.nr, st.na, vr, va, ve));
+    const uint32_t mask = sd.hash_cap - 1u;
+    uint32_t h = hash_mix(key) & mask;
+    for (uint32_t probe = 0; probe < sd.hash_cap; ++probe)
+    {
+        const uint32_t slot = sd.hash_off + h;
+        const uint32_t prev = atomicCAS(&b.hkey[slot], kEmpty, key);
+        if (prev == kEmpty || prev == key)
+        {
+            b.obs_hslot[o] = slot;
+            atomicMin(&b.hmin[slot], o - st.obs_off);
+            atomicAdd(&b.hcnt[slot], 1u);
+            return;
+        }
+        h = (h + 1u) & mask;
+    }
+    raise_err(&st, ERR_HASH_FULL);
+    b.obs_hslot[o] = kEmpty;
+}
+
+__global__ void k_hash_flag(BatchDev b)
+{
+    const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h > b.nhash)
+        return;
+    b.hvid[h] = (h < b.nhash && b.hkey[h] != kEmpty) ? 1u : 0u;
+}
+
+// hvid now holds voxel ids (exclusive scan of the occupancy flags).
+__global__ void k_vox_init(BatchDev b)
+{
+    const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= b.nhash || b.hkey[h] == kEmpty)
+        return;
+    const uint32_t v = b.hvid[h];
+    b.vslot[v] = h;
+    b.parent[v] = v;
+    b.cmin[v] = kEmpty;
+    b.ccnt[v] = 0u;
+}
+
+__global__ void k_vox_count(BatchDev b)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= b.nscan)
+        return;
+    const ScanDev& sd = b.scans[s];
+    ScanState& st = b.state[s];
+    st.n_vox = b.hvid[sd.hash_off + sd.hash_cap] - b.hvid[sd.hash_off];
+    if (st.n_vox > kVoxelCapacity)
+        raise_err(&st, ERR_VOXEL_CAPACITY); // StaticUnorderedMap::insert throws (static_unordered_map.hpp:81)
+}
+
+__device__ uint32_t uf_find(uint32_t* parent, uint32_t x, ScanState* st)
+{
+    for (int it = 0; it < kMaxIters; ++it)
+    {
+        const uint32_t p = ld_volatile(&parent[x]);
+        if (p == x)
+            return x;
+        const uint32_t gp = ld_volatile(&parent[p]);
+        if (gp != p)
+            atomicCAS(&parent[x], p, gp); // path halving; parents only ever decrease
+        x = gp;
+    }
+    raise_err(st, ERR_UF_TIMEOUT);
+    return x;
+}
+
+__device__ void uf_union(uint32_t* parent, uint32_t a, uint32_t c, ScanState* st)
+{
+    for (int it = 0; it < kMaxIters; ++it)
+    {
+        a = uf_find(parent, a, st);
+        c = uf_find(parent, c, st);
+        if (a == c)
+            return;
+        if (a > c)
+        {
+            const uint32_t t = a;
+            a = c;
+            c = t;
+        }
+        // link the larger root below the smaller one
+        const uint32_t old = atomicCAS(&parent[c], c, a);
+        if (old == c)
+            return;
+        c = old;
+    }
+    raise_err(st, ERR_UF_TIMEOUT);
+}
+
+__device__ __forceinline__ uint32_t hash_lookup(const BatchDev& b, const ScanDev& sd, uint32_t key)
+{
+    const uint32_t mask = sd.hash_cap - 1u;
+    uint32_t h = hash_mix(key) & mask;
+    for (uint32_t probe = 0; probe < sd.hash_cap; ++probe)
+    {
+        const uint32_t k = b.hkey[sd.hash_off + h];
+        if (k == key)
+            return sd.hash_off + h;
+        if (k == kEmpty)
+            return kEmpty;
+        h = (h + 1u) & mask;
+    }
+    return kEmpty;
+}
+
+// Neighbour offsets (clusterer.hpp:101-105): all 26 (dr, da, de) != (0, 0, 0).
+__global__ void k_uf_hook(BatchDev b)
+{
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= b.hvid[b.nhash])
+        return;
+    const uint32_t slot = b.vslot[v];
+    const int s = scan_of_hash(b, slot);
+    const ScanDev& sd = b.scans[s];
+    ScanState* st = &b.state[s];
+    const int32_t nr = st->nr, na = st->na, ne = st->ne;
+    const int32_t key = static_cast<int32_t>(b.hkey[slot]);
+    const int32_t r = key % nr;
+    const int32_t a = (key / nr) % na;
+    const int32_t e = key / (nr * na);
+    for (int de = -1; de <= 1; ++de)
+        for (int da = -1; da <= 1; ++da)
+            for (int dr = -1; dr <= 1; ++dr)
+            {
+                if (dr == 0 && da == 0 && de == 0)
+                    continue;
+                const int32_t rr = r + dr, ee = e + de;
+                if (rr < 0 || rr >= nr || ee < 0 || ee >= ne)
+                    continue;
+                int32_t aa = a + da;
+                if (aa < 0)
+                    aa += na;
+                else if (aa >= na)
+                    aa -= na;
+                const uint32_t nslot = hash_lookup(b, sd, static_cast<uint32_t>(flat_voxel(nr, na, rr, aa, ee)));
+                if (nslot == kEmpty)
+                    continue;
+                const uint32_t u = b.hvid[nslot];
+                if (u > v)
+                    uf_union(b.parent, v, u, st);
+            }
+}
+
+__global__ void k_uf_flatten(BatchDev b)
+{
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= b.hvid[b.nhash])
+        return;
+    const uint32_t slot = b.vslot[v];
+    const int s = scan_of_hash(b, slot);
+    const uint32_t root = uf_find(b.parent, v, &b.state[s]);
+    __syncwarp();
+    b.parent[v] = root;
+}
+
+__global__ void k_comp_stats(BatchDev b)
+{
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= b.hvid[b.nhash])
+        return;
+    const uint32_t root = b.parent[v];
+    const uint32_t slot = b.vslot[v];
+    atomicMin(&b.cmin[root], b.hmin[slot]);
+    atomicAdd(&b.ccnt[root], b.hcnt[slot]);
+}
+
+__global__ void k_keep(BatchDev b)
+{
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= b.hvid[b.nhash] || b.parent[v] != v)
+        return;
+    const uint32_t slot = b.vslot[v];
+    const int s = scan_of_hash(b, slot);
+    if (b.ccnt[v] >= b.scans[s].min_cluster)
+        b.kflag[b.state[s].obs_off + b.cmin[v]] = 1u;
+}
+
+// kflag now holds the exclusive scan: rank of each kept component among the scan's kept
+// components ordered by smallest point index == the reference's final label.
+__global__ void k_obs_label(BatchDev b)
+{
+    const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= b.obs_flag[b.npts])
+        return;
+    const int s = scan_of_obs(b, o);
+    const ScanDev& sd = b.scans[s];
+    const ScanState& st = b.state[s];
+    const uint32_t slot = b.obs_hslot[o];
+    int32_t label = LP_INVALID_CLUSTER;
+    if (slot != kEmpty)
+    {
+        const uint32_t root = b.parent[b.hvid[slot]];
+        if (b.ccnt[root] >= sd.min_cluster)
+            label = static_cast<int32_t>(b.kflag[st.obs_off + b.cmin[root]] - b.kflag[st.obs_off]);
+    }
+    b.obs_label[o] = label;
+    if (label >= 0)
+        atomicAdd(&b.cl_cnt[sd.cl_off + static_cast<uint32_t>(label)], 1u);
+}
+
+__global__ void k_cl_state(BatchDev b)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= b.nscan)
+        return;
+    const ScanDev& sd = b.scans[s];
+    ScanState& st = b.state[s];
+    st.n_clusters = b.kflag[st.obs_off + st.n_obs] - b.kflag[st.obs_off];
+    if (st.n_clusters > sd.cluster_cap)
+        raise_err(&st, ERR_CLUSTER_CAPACITY);
+}
+
+__global__ void k_cl_scatter(BatchDev b)
+{
+    const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= b.obs_flag[b.npts])
+        return;
+    const int32_t label = b.obs_label[o];
+    if (label < 0)
+        return;
+    const int s = scan_of_obs(b, o);
+    const uint32_t g = b.scans[s].cl_off + static_cast<uint32_t>(label);
+    const uint32_t pos = b.cl_start[g] + atomicAdd(&b.cl_fill[g], 1u);
+    b.members[pos] = o;
+}
+} // namespace
+
+// Clusterer::cluster on a caller-supplied cloud: every point is a member of the cloud to cluster.
+__global__ void k_mark_all(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.npts)
+        return;
+    const int s = scan_of_point(b, i);
+    b.seg_label[i] = (i - b.scans[s].pt_off < b.state[s].n_pts) ? LP_LABEL_OBSTACLE : LP_LABEL_UNKNOWN;
+}
+
+void launch_mark_all_obstacles(Launcher& L, const BatchDev& b)
+{
+    LP_LAUNCH(L, k_mark_all, div_up(b.npts, 256u), 256, b);
+}
+
+void launch_clustering(Launcher& L, const BatchDev& b, const BatchHost& hb)
+{
+    const uint32_t T = 256;
+    const uint32_t ns = static_cast<uint32_t>(b.nscan);
+    LP_LAUNCH(L, k_obs_flag, div_up(b.npts + 1, T), T, b);
+    L.scan(b.obs_flag, b.obs_flag, b.npts + 1);
+    LP_LAUNCH(L, k_obs_state, div_up(ns, 64u), 64, b);
+    LP_LAUNCH(L, k_obs_gather, div_up(b.npts, T), T, b);
+    LP_LAUNCH(L, k_dims, div_up(ns, 64u), 64, b);
+    LP_LAUNCH(L, k_vox_insert, div_up(b.npts, T), T, b);
+    LP_LAUNCH(L, k_hash_flag, div_up(b.nhash + 1, T), T, b);
+    L.scan(b.hvid, b.hvid, b.nhash + 1);
+    LP_LAUNCH(L, k_vox_init, div_up(b.nhash, T), T, b);
+    LP_LAUNCH(L, k_vox_count, div_up(ns, 64u), 64, b);
+    LP_LAUNCH(L, k_uf_hook, div_up(b.nhash, T), T, b);
+    LP_LAUNCH(L, k_uf_flatten, div_up(b.nhash, T), T, b);
+    LP_LAUNCH(L, k_comp_stats, div_up(b.nhash, T), T, b);
+    LP_LAUNCH(L, k_keep, div_up(b.nhash, T), T, b);
+    L.scan(b.kflag, b.kflag, b.npts + 1);
+    LP_LAUNCH(L, k_obs_label, div_up(b.npts, T), T, b);
+    LP_LAUNCH(L, k_cl_state, div_up(ns, 64u), 64, b);
+    L.scan(b.cl_cnt, b.cl_start, b.ncl + 1);
+    LP_LAUNCH(L, k_cl_scatter, div_up(b.npts, T), T, b);
+    (void)hb;
+}
+} // namespace lpg

@@ -1,0 +1,131 @@
+// lp_common.cuh — device primitives shared by the stages: block/warp scans, device-wide
+// exclusive scan, bitonic sorts in shared memory, bounded-wait helpers.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lp_internal.cuh"
+
+namespace lpg
+{
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems; // 2048 elements per block
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane_id() >= static_cast<uint32_t>(o))
+            v += t;
+    }
+    return v;
+}
+
+__device__ __forceinline__ uint32_t warp_sum(uint32_t v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Exclusive scan across the block (blockDim.x == kScanThreads); returns the exclusive prefix of
+// v and writes the block total to *total. smem: kScanThreads / 32 + 1 words.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* smem, uint32_t* total)
+{
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    const uint32_t nw = blockDim.x >> 5;
+    const uint32_t incl = warp_incl_scan(v);
+    if (lane == 31)
+        smem[warp] = incl;
+    __syncthreads();
+    if (warp == 0)
+    {
+        const uint32_t w = (lane < nw) ? smem[lane] : 0u;
+        const uint32_t wi = warp_incl_scan(w);
+        if (lane < nw)
+            smem[lane] = wi - w;
+        if (lane == nw - 1)
+            smem[32] = wi;
+    }
+    __syncthreads();
+    const uint32_t res = smem[warp] + incl - v;
+    *total = smem[32];
+    __syncthreads();
+    return res;
+}
+
+__global__ void k_scan_reduce(const uint32_t* __restrict__ in, uint32_t n, uint32_t* __restrict__ sums);
+__global__ void k_scan_sums(uint32_t* sums, uint32_t nb, uint32_t* grand_total);
+__global__ void k_scan_down(const uint32_t* in, uint32_t* out, uint32_t n, const uint32_t* __restrict__ sums);
+
+// Bitonic sort of `n` (power of two) keys in shared memory by the whole block.
+template <typename T, typename Less>
+__device__ void block_bitonic_sort(T* s, uint32_t n, Less less)
+{
+    for (uint32_t k = 2; k <= n; k <<= 1)
+    {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1)
+        {
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+            {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i)
+                {
+                    const bool up = ((i & k) == 0);
+                    T a = s[i], b = s[ixj];
+                    const bool swap = up ? less(b, a) : less(a, b);
+                    if (swap)
+                    {
+                        s[i] = b;
+                        s[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Bitonic sort of 32 values held one per lane (ascending by lane).
+template <typename T, typename Less>
+__device__ __forceinline__ T warp_bitonic_sort(T v, Less less)
+{
+    const uint32_t lane = lane_id();
+#pragma unroll
+    for (uint32_t k = 2; k <= 32; k <<= 1)
+    {
+#pragma unroll
+        for (uint32_t j = k >> 1; j > 0; j >>= 1)
+        {
+            const T o = __shfl_xor_sync(0xffffffffu, v, j);
+            const bool up = ((lane & k) == 0);
+            const bool lower = ((lane & j) == 0);
+            // lower lane keeps min when ascending
+            const bool take_o = (lower == up) ? less(o, v) : less(v, o);
+            if (take_o)
+                v = o;
+        }
+    }
+    return v;
+}
+
+__host__ __device__ inline uint32_t next_pow2(uint32_t v)
+{
+    v--;
+    v |= v >> 1;
+    v |= v >> 2;
+    v |= v >> 4;
+    v |= v >> 8;
+    v |= v >> 16;
+    return v + 1;
+}
+
+__host__ __device__ inline uint32_t div_up(uint32_t a, uint32_t b)
+{
+    return (a + b - 1) / b;
+}
+} // namespace lpg

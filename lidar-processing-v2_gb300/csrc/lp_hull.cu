@@ -1,0 +1,625 @@
+// lp_hull.cu — per-cluster convex hull and oriented bounding boxes.
+//
+// Reference: lidar_processing_lib/src/polygonizer.cpp and Processor::run's per-cluster gather
+// (src/processor/src/processor.cpp:627-671). One CTA per cluster:
+//   1. z range and the four extreme points of the cluster's members,
+//   2. Akl-Toussaint prefilter: members strictly inside the extreme quadrilateral (by a
+//      relative margin far above double rounding) cannot be hull vertices and are dropped,
+//   3. bitonic sort of the candidates by (x, y, member order), Andrew's monotone chain with the
+//      reference's FP64 orientation predicate (polygonizer.cpp:45-50, 62-85),
+//   4. local hull indices = rank of each hull vertex among the cluster's members in input
+//      order (the reference gathers a cluster's points in obstacle order, processor.cpp:640),
+//   5. rotating-calipers box (Shamos antipodal pairs, FP64, best area kept as a float exactly
+//      like BoundingBox::area) and the PCA box, by one warp.
+#include <cfloat>
+
+#include "lp_batch.cuh"
+#include "lp_common.cuh"
+#include "lp_math.cuh"
+#include "lp_stages.hpp"
+
+namespace lpg
+{
+namespace
+{
+constexpr int kHullThreads = 256;
+constexpr int kHullSmem = 1024; // candidates sorted in shared memory; larger sets use global scratch
+
+template <typename T>
+struct HPt
+{
+    T x, y;
+    uint32_t key; // tie-break and identity: member input order
+};
+
+template <typename T>
+__device__ __forceinline__ bool hpt_less(const HPt<T>& a, const HPt<T>& b)
+{
+    if (a.x < b.x)
+        return true;
+    if (b.x < a.x)
+        return false;
+    if (a.y < b.y)
+        return true;
+    if (b.y < a.y)
+        return false;
+    return a.key < b.key;
+}
+
+// polygonizer.cpp:45-50: counter-clockwise or collinear, evaluated in FP64 exactly as written
+__device__ __forceinline__ bool ccw_or_colinear(double ax, double ay, double bx, double by, double cx, double cy)
+{
+    return (bx - ax) * (cy - ay) - (by - ay) * (cx - ax) <= 0;
+}
+
+__device__ __forceinline__ uint32_t ford(float f)
+{
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float funord(uint32_t u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__device__ __forceinline__ unsigned long long warp_min64(unsigned long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+        v = t < v ? t : v;
+    }
+    return v;
+}
+__device__ __forceinline__ unsigned long long warp_max64(unsigned long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+        v = t > v ? t : v;
+    }
+    return v;
+}
+__device__ __forceinline__ double warp_min_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Strictly inside the quadrilateral a->b->c->d (counter-clockwise), with a relative margin.
+__device__ __forceinline__ bool left_strict(double ax, double ay, double bx, double by, double px, double py)
+{
+    const double ex = bx - ax, ey = by - ay, qx = px - ax, qy = py - ay;
+    const double cr = ex * qy - ey * qx;
+    const double scale = (fabs(ex) + fabs(ey)) * (fabs(qx) + fabs(qy));
+    return cr > 1e-9 * scale + 1e-300;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Shamos antipodal pairs (polygonizer.cpp:93-163) for the hull P[0..n), written to `pairs`.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ double tri_area(double ax, double ay, double bx, double by, double cx, double cy)
+{
+    // areaOfTriangle, polygonizer.hpp:227-231
+    return fabs((ax * (by - cy) + bx * (cy - ay) + cx * (ay - by)) * 0.5);
+}
+
+__device__ int antipodal_pairs(const double2* P, int n, int2* pairs, int cap)
+{
+    int np = 0;
+    if (n < 2)
+        return 0;
+    auto nx = [n](int i) { return (i + 1 == n) ? 0 : i + 1; };
+    auto ar = [P](int a, int b, int c) { return tri_area(P[a].x, P[a].y, P[b].x, P[b].y, P[c].x, P[c].y); };
+    auto push = [&](int a, int b) {
+        if (np < cap)
+            pairs[np] = make_int2(a, b);
+        ++np;
+    };
+    const int i0 = n - 1;
+    int i = 0, j = 1;
+    int guard = 0;
+    while (ar(i, nx(i), nx(j)) > ar(i, nx(i), j) && guard++ < 4 * n + 8)
+        j = nx(j);
+    const int j0 = j;
+    guard = 0;
+    while (i != j0 && guard++ < 4 * n + 8)
+    {
+        i = nx(i);
+        push(i, j);
+        int g2 = 0;
+        while (ar(i, nx(i), nx(j)) > ar(i, nx(i), j) && g2++ < 4 * n + 8)
+        {
+            j = nx(j);
+            if (!(i == j0 && j == i0))
+                push(i, j);
+            else
+                return np;
+        }
+        if (ar(j, nx(i), nx(j)) == ar(i, nx(i), j))
+        {
+            if (!(i == j0 && j == i0))
+                push(i, nx(j));
+            else
+                push(nx(i), j);
+        }
+    }
+    return np;
+}
+
+// Rotating calipers (polygonizer.cpp:165-278) by one warp: all lanes return the same box.
+__device__ void calipers_warp(const double2* P, int n, const int2* pairs, int npairs, lp_bounding_box* out)
+{
+    const uint32_t lane = lane_id();
+    lp_bounding_box box;
+    for (int k = 0; k < 4; ++k)
+        box.corners[k][0] = box.corners[k][1] = 0.0;
+    box.area = 0.0f;
+    box.angle_rad = 0.0f;
+    box.is_valid = 0;
+    if (n < 3)
+    {
+        if (lane == 0)
+            *out = box;
+        return;
+    }
+    double cx = 0.0, cy = 0.0;
+    for (int k = 0; k < n; ++k)
+    {
+        cx += P[k].x;
+        cy += P[k].y;
+    }
+    cx /= n;
+    cy /= n;
+    float best = __double2float_rn(DBL_MAX); // BoundingBox::area is a float: DBL_MAX -> +inf
+    for (int pi = 0; pi < npairs; ++pi)
+    {
+        const int2 pr = pairs[pi];
+        for (int e = 0; e < 2; ++e)
+        {
+            const int index = e == 0 ? pr.x : pr.y;
+            for (int o = 0; o < 2; ++o)
+            {
+                int nb = index + (o == 0 ? -1 : 1);
+                if (nb < 0)
+                    nb += n;
+                else if (nb >= n)
+                    nb -= n;
+                const double ex = P[nb].x - P[index].x;
+                const double ey = P[nb].y - P[index].y;
+                const double len = sqrt(ex * ex + ey * ey);
+                if (len < 1.0e-6)
+                    continue;
+                const double ux = ex / len, uy = ey / len;
+                double mnx = DBL_MAX, mxx = -DBL_MAX, mny = DBL_MAX, mxy = -DBL_MAX;
+                for (int k = static_cast<int>(lane); k < n; k += 32)
+                {
+                    const double tx = P[k].x - cx, ty = P[k].y - cy;
+                    const double rx = tx * ux + ty * uy;
+                    const double ry = -tx * uy + ty * ux;
+                    mnx = fmin(mnx, rx);
+                    mxx = fmax(mxx, rx);
+                    mny = fmin(mny, ry);
+                    mxy = fmax(mxy, ry);
+                }
+                mnx = warp_min_d(mnx);
+                mxx = warp_max_d(mxx);
+                mny = warp_min_d(mny);
+                mxy = warp_max_d(mxy);
+                const double area = (mxx - mnx) * (mxy - mny);
+                if (area < static_cast<double>(best))
+                {
+                    best = __double2float_rn(area);
+                    box.area = best;
+                    box.corners[0][0] = mnx * ux - mny * uy + cx;
+                    box.corners[0][1] = mnx * uy + mny * ux + cy;
+                    box.corners[1][0] = mxx * ux - mny * uy + cx;
+                    box.corners[1][1] = mxx * uy + mny * ux + cy;
+                    box.corners[2][0] = mxx * ux - mxy * uy + cx;
+                    box.corners[2][1] = mxx * uy + mxy * ux + cy;
+                    box.corners[3][0] = mnx * ux - mxy * uy + cx;
+                    box.corners[3][1] = mnx * uy + mxy * ux + cy;
+                    box.angle_rad = lpm::atan2_approx(__double2float_rn(uy), __double2float_rn(ux));
+                    box.is_valid = 1;
+                }
+            }
+        }
+    }
+    if (lane == 0)
+        *out = box;
+}
+
+// PCA box (polygonizer.cpp:280-362) in FP64: mean, centred X^T X / (n - 1), principal axis
+// angle of the 2x2 covariance, rotate, min/max, corners back to the original frame.
+__device__ void pca_box(const double2* P, int n, lp_bounding_box* out)
+{
+    lp_bounding_box box;
+    for (int k = 0; k < 4; ++k)
+        box.corners[k][0] = box.corners[k][1] = 0.0;
+    box.area = 0.0f;
+    box.angle_rad = 0.0f;
+    box.is_valid = 0;
+    if (n >= 3)
+    {
+        double mx = 0.0, my = 0.0;
+        for (int i = 0; i < n; ++i)
+        {
+            mx += P[i].x;
+            my += P[i].y;
+        }
+        mx /= n;
+        my /= n;
+        double sxx = 0.0, sxy = 0.0, syy = 0.0;
+        for (int i = 0; i < n; ++i)
+        {
+            const double dx = P[i].x - mx, dy = P[i].y - my;
+            sxx += dx * dx;
+            sxy += dx * dy;
+            syy += dy * dy;
+        }
+        sxx /= (n - 1);
+        sxy /= (n - 1);
+        syy /= (n - 1);
+        const double theta = 0.5 * atan2(2.0 * sxy, sxx - syy);
+        const double v00 = cos(theta), v10 = sin(theta);
+        const double v01 = -v10, v11 = v00;
+        double mnx = DBL_MAX, mxx = -DBL_MAX, mny = DBL_MAX, mxy = -DBL_MAX;
+        for (int i = 0; i < n; ++i)
+        {
+            const double dx = P[i].x - mx, dy = P[i].y - my;
+            const double rx = dx * v00 + dy * v10;
+            const double ry = dx * v01 + dy * v11;
+            mnx = fmin(mnx, rx);
+            mxx = fmax(mxx, rx);
+            mny = fmin(mny, ry);
+            mxy = fmax(mxy, ry);
+        }
+        const double xs[4] = {mnx, mxx, mxx, mnx};
+        const double ys[4] = {mny, mny, mxy, mxy};
+        for (int k = 0; k < 4; ++k)
+        {
+            box.corners[k][0] = xs[k] * v00 + ys[k] * v01 + mx;
+            box.corners[k][1] = xs[k] * v10 + ys[k] * v11 + my;
+        }
+        box.area = __double2float_rn((mxx - mnx) * (mxy - mny));
+        box.angle_rad = __double2float_rn(atan2(v10, v00));
+        box.is_valid = 1;
+    }
+    *out = box;
+}
+
+// Monotone chain over sorted candidates C[0..m) (polygonizer.cpp:62-88) by one thread.
+// Writes candidate positions of the hull to H (capacity 2m) and returns the hull size.
+template <typename T>
+__device__ int monotone_chain(const HPt<T>* C, int m, int* H)
+{
+    int k = 0;
+    for (int i = 0; i < m; ++i)
+    {
+        while (k > 1 && ccw_or_colinear(C[H[k - 2]].x, C[H[k - 2]].y, C[H[k - 1]].x, C[H[k - 1]].y, C[i].x, C[i].y))
+            --k;
+        H[k++] = i;
+    }
+    for (int i = m - 2, t = k + 1; i >= 0; --i)
+    {
+        while (k >= t && ccw_or_colinear(C[H[k - 2]].x, C[H[k - 2]].y, C[H[k - 1]].x, C[H[k - 1]].y, C[i].x, C[i].y))
+            --k;
+        H[k++] = i;
+    }
+    return k - 1;
+}
+
+// Bitonic sort of n candidates (capacity next_pow2(n)) in global memory by one block.
+template <typename T>
+__device__ void block_sort_global(HPt<T>* a, uint32_t n)
+{
+    const uint32_t np2 = next_pow2(n);
+    for (uint32_t k = n + threadIdx.x; k < np2; k += blockDim.x)
+        a[k] = HPt<T>{static_cast<T>(INFINITY), static_cast<T>(INFINITY), 0xffffffffu};
+    __syncthreads();
+    for (uint32_t k = 2; k <= np2; k <<= 1)
+        for (uint32_t j = k >> 1; j > 0; j >>= 1)
+        {
+            for (uint32_t i = threadIdx.x; i < np2; i += blockDim.x)
+            {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i)
+                {
+                    const bool up = ((i & k) == 0);
+                    const HPt<T> x = a[i], y = a[ixj];
+                    if (up ? hpt_less(y, x) : hpt_less(x, y))
+                    {
+                        a[i] = y;
+                        a[ixj] = x;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+}
+
+struct HullSmem
+{
+    HPt<float> cand[kHullSmem];
+    int stack[2 * kHullSmem + 2];
+    double2 hp[kHullSmem];
+    unsigned long long ext[4][kHullThreads / 32];
+    float zr[2][kHullThreads / 32];
+    int ncand;
+    int nhull;
+};
+
+// One CTA per cluster of the batch.
+__global__ void __launch_bounds__(kHullThreads) k_hull(BatchDev b, int compute_obb)
+{
+    __shared__ HullSmem sm;
+    const uint32_t g = blockIdx.x;
+    const int s = find_scan(b.nscan, g, [&](int q) { return b.scans[q].cl_off; });
+    const ScanDev& sd = b.scans[s];
+    ScanState* st = &b.state[s];
+    const uint32_t k = g - sd.cl_off;
+    if (k >= st->n_clusters)
+        return;
+    const uint32_t n = b.cl_cnt[g];
+    const uint32_t start = b.cl_start[g];
+    const uint32_t* mem = b.members + start;
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+
+    // 1. z range and extreme points
+    float zmn = INFINITY, zmx = -INFINITY;
+    unsigned long long eL = ~0ull, eR = 0ull, eB = ~0ull, eT = 0ull;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+    {
+        const float4 p = b.obs_pts[mem[i]];
+        zmn = fminf(zmn, p.z);
+        zmx = fmaxf(zmx, p.z);
+        const unsigned long long kxy = (static_cast<unsigned long long>(ford(p.x)) << 32) | ford(p.y);
+        const unsigned long long kyx = (static_cast<unsigned long long>(ford(p.y)) << 32) | ford(p.x);
+        eL = kxy < eL ? kxy : eL;
+        eR = kxy > eR ? kxy : eR;
+        eB = kyx < eB ? kyx : eB;
+        eT = kyx > eT ? kyx : eT;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        zmn = fminf(zmn, __shfl_xor_sync(0xffffffffu, zmn, o));
+        zmx = fmaxf(zmx, __shfl_xor_sync(0xffffffffu, zmx, o));
+    }
+    eL = warp_min64(eL);
+    eR = warp_max64(eR);
+    eB = warp_min64(eB);
+    eT = warp_max64(eT);
+    if (lane == 0)
+    {
+        sm.ext[0][warp] = eL;
+        sm.ext[1][warp] = eR;
+        sm.ext[2][warp] = eB;
+        sm.ext[3][warp] = eT;
+        sm.zr[0][warp] = zmn;
+        sm.zr[1][warp] = zmx;
+    }
+    if (threadIdx.x == 0)
+        sm.ncand = 0;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        for (int w = 1; w < kHullThreads / 32; ++w)
+        {
+            sm.ext[0][0] = sm.ext[0][w] < sm.ext[0][0] ? sm.ext[0][w] : sm.ext[0][0];
+            sm.ext[1][0] = sm.ext[1][w] > sm.ext[1][0] ? sm.ext[1][w] : sm.ext[1][0];
+            sm.ext[2][0] = sm.ext[2][w] < sm.ext[2][0] ? sm.ext[2][w] : sm.ext[2][0];
+            sm.ext[3][0] = sm.ext[3][w] > sm.ext[3][0] ? sm.ext[3][w] : sm.ext[3][0];
+            sm.zr[0][0] = fminf(sm.zr[0][0], sm.zr[0][w]);
+            sm.zr[1][0] = fmaxf(sm.zr[1][0], sm.zr[1][w]);
+        }
+        b.cl_zmin[g] = sm.zr[0][0];
+        b.cl_zmax[g] = sm.zr[1][0];
+    }
+    __syncthreads();
+
+    int32_t* hull_dst = b.hull_tmp + start;
+    if (n < 3)
+    {
+        // convexHull with fewer than 3 points returns 0..n-1 (polygonizer.cpp:36-41)
+        if (threadIdx.x == 0)
+        {
+            for (uint32_t i = 0; i < n; ++i)
+                hull_dst[i] = static_cast<int32_t>(i);
+            b.hull_cnt[g] = n;
+            if (compute_obb)
+            {
+                lp_bounding_box z;
+                memset(&z, 0, sizeof(z));
+                b.obb_c[g] = z;
+                b.obb_p[g] = z;
+            }
+        }
+        return;
+    }
+
+    // 2. Akl-Toussaint prefilter against the quadrilateral L -> B -> R -> T
+    const double Lx = funord(static_cast<uint32_t>(sm.ext[0][0] >> 32)), Ly = funord(static_cast<uint32_t>(sm.ext[0][0]));
+    const double Rx = funord(static_cast<uint32_t>(sm.ext[1][0] >> 32)), Ry = funord(static_cast<uint32_t>(sm.ext[1][0]));
+    const double By = funord(static_cast<uint32_t>(sm.ext[2][0] >> 32)), Bx = funord(static_cast<uint32_t>(sm.ext[2][0]));
+    const double Ty = funord(static_cast<uint32_t>(sm.ext[3][0] >> 32)), Tx = funord(static_cast<uint32_t>(sm.ext[3][0]));
+    HPt<float>* gs = reinterpret_cast<HPt<float>*>(b.hs_cand) + 2ull * start; // capacity 2n >= next_pow2(n)
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+    {
+        const uint32_t o = mem[i];
+        const float4 p = b.obs_pts[o];
+        const double px = p.x, py = p.y;
+        const bool inside = left_strict(Lx, Ly, Bx, By, px, py) && left_strict(Bx, By, Rx, Ry, px, py) &&
+                            left_strict(Rx, Ry, Tx, Ty, px, py) && left_strict(Tx, Ty, Lx, Ly, px, py);
+        if (!inside)
+        {
+            const int pos = atomicAdd(&sm.ncand, 1);
+            const HPt<float> c{p.x, p.y, o};
+            if (pos < kHullSmem)
+                sm.cand[pos] = c;
+            gs[pos] = c;
+        }
+    }
+    __syncthreads();
+    const int m = sm.ncand;
+    const bool small = m <= kHullSmem;
+    const HPt<float>* C;
+    int* H;
+    if (small)
+    {
+        // m <= kHullSmem (a power of two), so the padded size fits the shared array
+        const uint32_t np2 = next_pow2(static_cast<uint32_t>(m));
+        for (uint32_t i = m + threadIdx.x; i < np2; i += blockDim.x)
+            sm.cand[i] = HPt<float>{INFINITY, INFINITY, 0xffffffffu};
+        __syncthreads();
+        block_bitonic_sort(sm.cand, np2, [](const HPt<float>& a, const HPt<float>& c) { return hpt_less(a, c); });
+        C = sm.cand;
+        H = sm.stack;
+    }
+    else
+    {
+        block_sort_global(gs, static_cast<uint32_t>(m));
+        C = gs;
+        H = b.hs_stack + 2ull * start + 2ull * g; // capacity 2n + 2 >= 2m + 2
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        sm.nhull = monotone_chain(C, m, H);
+    __syncthreads();
+    const int h = sm.nhull;
+
+    // 4. local index of each hull vertex = rank among the members by input order
+    for (int j = static_cast<int>(warp); j < h; j += kHullThreads / 32)
+    {
+        const uint32_t key = C[H[j]].key;
+        uint32_t cnt = 0;
+        for (uint32_t base = 0; base < n; base += 32)
+        {
+            const uint32_t i = base + lane;
+            const bool lt = (i < n) && (mem[i] < key);
+            cnt += __popc(__ballot_sync(0xffffffffu, lt));
+        }
+        if (lane == 0)
+            hull_dst[j] = static_cast<int32_t>(cnt);
+    }
+    if (threadIdx.x == 0)
+        b.hull_cnt[g] = static_cast<uint32_t>(h);
+
+    // 5. boxes on the hull vertices (the hull is small; one warp)
+    if (!compute_obb)
+        return;
+    double2* P = (h <= kHullSmem) ? sm.hp : (b.hs_pts + start);
+    for (int j = threadIdx.x; j < h; j += blockDim.x)
+        P[j] = make_double2(static_cast<double>(C[H[j]].x), static_cast<double>(C[H[j]].y));
+    __syncthreads();
+    if (warp == 0)
+    {
+        int2* pairs = b.hs_pairs + 4ull * start + 16ull * g;
+        const int cap = 4 * h + 16;
+        int npairs = 0;
+        if (lane == 0)
+            npairs = antipodal_pairs(P, h, pairs, cap);
+        npairs = __shfl_sync(0xffffffffu, npairs, 0);
+        if (npairs > cap)
+        {
+            if (lane == 0)
+                raise_err(st, ERR_INTERNAL);
+            npairs = cap;
+        }
+        __syncwarp();
+        calipers_warp(P, h, pairs, npairs, &b.obb_c[g]);
+        if (lane == 0)
+            pca_box(P, h, &b.obb_p[g]);
+    }
+}
+
+// Dense hull output: hull_cnt holds the exclusive scan (hull offsets over the batch).
+__global__ void k_hull_compact(BatchDev b)
+{
+    const uint32_t g = blockIdx.x;
+    const int s = find_scan(b.nscan, g, [&](int q) { return b.scans[q].cl_off; });
+    const ScanDev& sd = b.scans[s];
+    if (g - sd.cl_off >= b.state[s].n_clusters)
+        return;
+    const uint32_t off = b.hull_cnt[g];
+    const uint32_t cnt = b.hull_cnt[g + 1] - off;
+    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x)
+        b.hull_out[off + i] = b.hull_tmp[b.cl_start[g] + i];
+}
+
+// ---------------------------------------------------------------------------------------------
+// Standalone single-polygon entry points (double inputs): one CTA.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kHullThreads) k_hull_single(const double2* pts, uint32_t n, HPt<double>* scratch,
+                                                            int* stack, int32_t* out, uint32_t* n_out)
+{
+    // the sort runs in global scratch (capacity next_pow2(n)); no prefilter (the polygon is
+    // the caller's whole input)
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        scratch[i] = HPt<double>{pts[i].x, pts[i].y, i};
+    __syncthreads();
+    block_sort_global(scratch, n);
+    __syncthreads();
+    __shared__ int hn;
+    if (threadIdx.x == 0)
+        hn = monotone_chain(scratch, static_cast<int>(n), stack);
+    __syncthreads();
+    for (int j = threadIdx.x; j < hn; j += blockDim.x)
+        out[j] = static_cast<int32_t>(scratch[stack[j]].key);
+    if (threadIdx.x == 0)
+        *n_out = static_cast<uint32_t>(hn);
+}
+
+__global__ void k_boxes_single(const double2* P, uint32_t n, int2* pairs, int cap, int kind, lp_bounding_box* out,
+                               int* npairs_out)
+{
+    if (threadIdx.x >= 32)
+        return;
+    const uint32_t lane = lane_id();
+    int np = 0;
+    if (lane == 0)
+        np = antipodal_pairs(P, static_cast<int>(n), pairs, cap);
+    np = __shfl_sync(0xffffffffu, np, 0);
+    if (lane == 0 && npairs_out)
+        *npairs_out = np;
+    if (np > cap)
+        np = cap;
+    __syncwarp();
+    if (kind == 0)
+        calipers_warp(P, static_cast<int>(n), pairs, np, out);
+    else if (kind == 1 && lane == 0)
+        pca_box(P, static_cast<int>(n), out);
+}
+} // namespace
+
+void launch_polygons(Launcher& L, const BatchDev& b, const BatchHost& hb, int compute_obb)
+{
+    (void)hb;
+    LP_LAUNCH(L, k_hull, b.ncl, kHullThreads, b, compute_obb);
+    L.scan(b.hull_cnt, b.hull_cnt, b.ncl + 1);
+    LP_LAUNCH(L, k_hull_compact, b.ncl, 128, b);
+}
+
+void launch_hull_single(Launcher& L, const double2* pts, uint32_t n, void* scratch, int* stack, int32_t* out,
+                        uint32_t* n_out)
+{
+    LP_LAUNCH(L, k_hull_single, 1, kHullThreads, pts, n, reinterpret_cast<HPt<double>*>(scratch), stack, out, n_out);
+}
+
+void launch_boxes_single(Launcher& L, const double2* P, uint32_t n, int2* pairs, int cap, int kind, lp_bounding_box* out,
+                         int* npairs_out)
+{
+    LP_LAUNCH(L, k_boxes_single, 1, 32, P, n, pairs, cap, kind, out, npairs_out);
+}
+} // namespace lpg

@@ -1,0 +1,1133 @@
+// lp_segment.cu — ground segmentation kernels (ring partition, polar grid, RECM, RANSAC,
+// range-image projection, dilation, jump convolution, label population).
+//
+// Reference: lidar_processing_lib/src/segmenter.cpp (Segmenter::segment and helpers) and
+// src/dataloader/src/dataloader.cpp:68-137 (ring partition). Every binary32 expression keeps
+// the reference's operation order; the library is compiled with --fmad=false so that no
+// multiply-add is contracted.
+#include <cfloat>
+
+#include "lp_batch.cuh"
+#include "lp_common.cuh"
+#include "lp_math.cuh"
+#include "lp_stages.hpp"
+
+namespace lpg
+{
+namespace
+{
+constexpr float kPiF = 3.14159274101257324219f;       // M_PIf
+constexpr float kPi2F = 1.57079637050628662109f;      // M_PI_2f
+constexpr float kPi15F = 4.71238899230957031250f;     // 1.5F * M_PIf (dataloader.cpp:108)
+constexpr float kTwoPiF = 6.28318548202514648438f;    // 2.0F * M_PIf == (float)(2*M_PI)
+constexpr int kRingTile = 1024;
+constexpr int kSmallCell = 32;
+constexpr uint32_t kLargeCellMax = 8192;
+
+__device__ __forceinline__ int scan_of_cell(const BatchDev& b, uint32_t c)
+{
+    return find_scan(b.nscan, c, [&](int s) { return b.scans[s].cell_off; });
+}
+__device__ __forceinline__ int scan_of_near(const BatchDev& b, uint32_t g)
+{
+    return find_scan(b.nscan, g, [&](int s) { return b.scans[s].near_off; });
+}
+__device__ __forceinline__ int scan_of_pix(const BatchDev& b, uint32_t p)
+{
+    return find_scan(b.nscan, p, [&](int s) { return b.scans[s].pix_off; });
+}
+__device__ __forceinline__ int scan_of_row(const BatchDev& b, uint32_t r)
+{
+    return find_scan(b.nscan, r, [&](int s) { return b.scans[s].row_off; });
+}
+__device__ __forceinline__ int scan_of_tile(const BatchDev& b, uint32_t t)
+{
+    return find_scan(b.nscan, t, [&](int s) { return b.scans[s].tile_off; });
+}
+__device__ __forceinline__ int scan_of_slice(const BatchDev& b, uint32_t t)
+{
+    return find_scan(b.nscan, t, [&](int s) { return b.scans[s].slice_off; });
+}
+
+// ------------------------------------------------------------------------------------------
+// Ring partition (dataloader.cpp:68-137): quadrant of the wrapped azimuth, FOURTH->FIRST
+// transitions counted by a prefix scan, ring = first_ring - min(first_ring, count).
+// ------------------------------------------------------------------------------------------
+__global__ void k_quadrant(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.npts)
+        return;
+    const float4 p = b.pts[i];
+    float az = lpm::cr_atan2f(p.y, p.x);
+    az = (az < 0) ? (az + kTwoPiF) : az;
+    uint8_t q;
+    if (az < kPi2F)
+        q = 0;
+    else if (az < kPiF)
+        q = 1;
+    else if (az < kPi15F)
+        q = 2;
+    else
+        q = 3;
+    b.quad[i] = q;
+}
+
+__device__ __forceinline__ uint32_t ring_flag(const BatchDev& b, const ScanDev& sd, uint32_t i)
+{
+    // point i (global) starts a new ring: FIRST after FOURTH, not the scan's first point
+    return (i > sd.pt_off && b.quad[i] == 0 && b.quad[i - 1] == 3) ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(256) k_ring_count(BatchDev b)
+{
+    const uint32_t t = blockIdx.x;
+    const int s = scan_of_tile(b, t);
+    const ScanDev& sd = b.scans[s];
+    const uint32_t first = sd.pt_off + (t - sd.tile_off) * kRingTile;
+    const uint32_t end = sd.pt_off + b.state[s].n_pts;
+    uint32_t c = 0;
+    for (uint32_t k = threadIdx.x; k < kRingTile; k += blockDim.x)
+    {
+        const uint32_t i = first + k;
+        if (i < end)
+            c += ring_flag(b, sd, i);
+    }
+    c = warp_sum(c);
+    __shared__ uint32_t sm[8];
+    if (lane_id() == 0)
+        sm[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        uint32_t tot = 0;
+        for (int w = 0; w < 8; ++w)
+            tot += sm[w];
+        b.tile_cnt[t] = tot;
+    }
+}
+
+// tile_cnt holds the exclusive scan of the per-tile counts over the whole batch.
+__global__ void __launch_bounds__(256) k_ring_apply(BatchDev b)
+{
+    __shared__ uint32_t sm[33];
+    const uint32_t t = blockIdx.x;
+    const int s = scan_of_tile(b, t);
+    const ScanDev& sd = b.scans[s];
+    const uint32_t first = sd.pt_off + (t - sd.tile_off) * kRingTile;
+    const uint32_t end = sd.pt_off + b.state[s].n_pts;
+    const uint32_t base = b.tile_cnt[t] - b.tile_cnt[sd.tile_off];
+    // 4 consecutive points per thread keep the scan in point order
+    const uint32_t i0 = first + threadIdx.x * 4;
+    uint32_t f[4];
+    uint32_t loc = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        f[k] = (i0 + k < end) ? ring_flag(b, sd, i0 + k) : 0u;
+        loc += f[k];
+    }
+    uint32_t total;
+    uint32_t pre = block_excl_scan(loc, sm, &total) + base;
+    const uint32_t fr = static_cast<uint32_t>(sd.first_ring);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        pre += f[k];
+        if (i0 + k < end)
+            b.ring[i0 + k] = static_cast<uint16_t>(fr - min(fr, pre));
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Polar grid (constructPolarGrid, segmenter.cpp:103-204).
+// ------------------------------------------------------------------------------------------
+__global__ void k_bin(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.npts)
+        return;
+    const int s = scan_of_point(b, i);
+    const ScanDev& sd = b.scans[s];
+    b.pt_cell[i] = -1;
+    if (i - sd.pt_off >= b.state[s].n_pts)
+        return; // slot left empty by noise removal
+    const float4 p = b.pts[i];
+    if (p.z < sd.zmin_adj || p.z > sd.zmax_adj)
+        return;
+    const float d = sqrtf(p.x * p.x + p.y * p.y);
+    const int32_t radial = static_cast<int32_t>(d / sd.spacing);
+    if (d < sd.min_d || d > sd.max_d || radial >= sd.nrad)
+        return;
+    float az = lpm::atan2_approx(p.y, p.x);
+    az = (az < 0) ? (az + kTwoPiF) : az;
+    const int32_t slice = min(static_cast<int32_t>(az / sd.slice_res), sd.nslice - 1);
+    int32_t h;
+    if (sd.use_ring)
+    {
+        h = b.ring[i];
+        if (h >= sd.H)
+            return;
+    }
+    else
+    {
+        const float el = lpm::cr_atanf(p.z / d);
+        h = static_cast<int32_t>((el - sd.down_rad) / sd.rad_per_px);
+        if (h < 0 || h >= sd.H)
+            return;
+    }
+    const int32_t w = static_cast<int32_t>(static_cast<uint16_t>(static_cast<float>(sd.W - 1) * az / kTwoPiF));
+    const uint32_t cell = sd.cell_off + static_cast<uint32_t>(slice * sd.nrad + radial);
+    b.pt_cell[i] = static_cast<int32_t>(cell);
+    b.pt_pix[i] = h * sd.W + w;
+    b.pt_slot[i] = atomicAdd(&b.cell_cnt[cell], 1u);
+}
+
+__global__ void k_scatter(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.npts)
+        return;
+    const int32_t c = b.pt_cell[i];
+    if (c < 0)
+        return;
+    const int s = scan_of_point(b, i);
+    const uint32_t pos = b.cell_start[c] + b.pt_slot[i];
+    b.csr_idx[pos] = static_cast<int32_t>(i - b.scans[s].pt_off);
+    b.csr_z[pos] = b.pts[i].z;
+}
+
+// zlow of a sorted cell (segmenter.cpp:249-260): z[k*] for the largest k in [1, n/2] with
+// z[k] - z[k-1] > 0.5, else z[0].
+__global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
+{
+    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= b.ncell)
+        return;
+    const uint32_t lane = lane_id();
+    const uint32_t n = b.cell_cnt[c];
+    if (n == 0)
+        return;
+    const int s = scan_of_cell(b, c);
+    const ScanDev& sd = b.scans[s];
+    const bool near = static_cast<int32_t>((c - sd.cell_off) % static_cast<uint32_t>(sd.nrad)) < kRansacRadialBins;
+    if (n > kSmallCell)
+    {
+        if (lane == 0)
+        {
+            const uint32_t k = atomicAdd(b.n_large, 1u);
+            b.large_list[k] = c;
+        }
+        return;
+    }
+    const uint32_t start = b.cell_start[c];
+    float z = (lane < n) ? b.csr_z[start + lane] : INFINITY;
+    z = warp_bitonic_sort(z, [](float a, float bb) { return a < bb; });
+    const float zp = __shfl_up_sync(0xffffffffu, z, 1);
+    const bool gap = (lane >= 1 && lane <= n / 2 && (z - zp) > 0.5F);
+    const uint32_t mask = __ballot_sync(0xffffffffu, gap);
+    const int ks = mask ? (31 - __clz(mask)) : 0;
+    const float zl = __shfl_sync(0xffffffffu, z, ks);
+    if (lane == 0)
+        b.zlow[c] = zl;
+    if (near)
+    {
+        int32_t idx = (lane < n) ? b.csr_idx[start + lane] : INT32_MAX;
+        idx = warp_bitonic_sort(idx, [](int32_t a, int32_t bb) { return a < bb; });
+        if (lane < n)
+            b.csr_idx[start + lane] = idx;
+    }
+}
+
+__global__ void __launch_bounds__(512) k_cell_large(BatchDev b)
+{
+    __shared__ float sz[kLargeCellMax];
+    __shared__ int32_t sk;
+    const uint32_t nl = *b.n_large;
+    for (uint32_t li = blockIdx.x; li < nl; li += gridDim.x)
+    {
+        const uint32_t c = b.large_list[li];
+        const uint32_t n = b.cell_cnt[c];
+        const uint32_t start = b.cell_start[c];
+        const int s = scan_of_cell(b, c);
+        const ScanDev& sd = b.scans[s];
+        if (n > kLargeCellMax)
+        {
+            if (threadIdx.x == 0)
+            {
+                raise_err(&b.state[s], ERR_CELL_TOO_LARGE);
+                b.zlow[c] = b.csr_z[start];
+            }
+            continue;
+        }
+        const uint32_t np2 = next_pow2(n);
+        for (uint32_t k = threadIdx.x; k < np2; k += blockDim.x)
+            sz[k] = (k < n) ? b.csr_z[start + k] : INFINITY;
+        if (threadIdx.x == 0)
+            sk = 0;
+        __syncthreads();
+        block_bitonic_sort(sz, np2, [](float a, float bb) { return a < bb; });
+        for (uint32_t k = 1 + threadIdx.x; k <= n / 2; k += blockDim.x)
+            if (sz[k] - sz[k - 1] > 0.5F)
+                atomicMax(&sk, static_cast<int32_t>(k));
+        __syncthreads();
+        if (threadIdx.x == 0)
+            b.zlow[c] = sz[sk];
+        __syncthreads();
+        const bool near = static_cast<int32_t>((c - sd.cell_off) % static_cast<uint32_t>(sd.nrad)) < kRansacRadialBins;
+        if (near)
+        {
+            int32_t* si = reinterpret_cast<int32_t*>(sz);
+            for (uint32_t k = threadIdx.x; k < np2; k += blockDim.x)
+                si[k] = (k < n) ? b.csr_idx[start + k] : INT32_MAX;
+            __syncthreads();
+            block_bitonic_sort(si, np2, [](int32_t a, int32_t bb) { return a < bb; });
+            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+                b.csr_idx[start + k] = si[k];
+        }
+        __syncthreads();
+    }
+}
+
+// RECM elevation chain per azimuth slice (segmenter.cpp:215-267).
+__global__ void k_chain(BatchDev b, uint32_t nslices_total)
+{
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nslices_total)
+        return;
+    const int s = scan_of_slice(b, g);
+    const ScanDev& sd = b.scans[s];
+    const uint32_t slice = g - sd.slice_off;
+    const uint32_t off = sd.cell_off + slice * static_cast<uint32_t>(sd.nrad);
+    float prev = -sd.sensor_h + sd.thr;
+    b.elev[off] = prev;
+    for (int32_t r = 1; r < sd.nrad; ++r)
+    {
+        const uint32_t c = off + static_cast<uint32_t>(r);
+        float e;
+        if (b.cell_cnt[c] == 0)
+        {
+            e = prev + sd.delta;
+        }
+        else
+        {
+            const float lim = prev + sd.delta;
+            const float zl = b.zlow[c];
+            e = (lim < zl) ? lim : zl; // std::min(curr_z_min, prev + delta)
+        }
+        b.elev[c] = e;
+        prev = e;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// RANSAC near-field correction (correctCloseRangeFalsePositivesRANSAC, segmenter.cpp:321-479).
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t near_cell(const ScanDev& sd, uint32_t k)
+{
+    const uint32_t slice = k / static_cast<uint32_t>(sd.nnear_per_slice);
+    const uint32_t radial = k % static_cast<uint32_t>(sd.nnear_per_slice);
+    return sd.cell_off + slice * static_cast<uint32_t>(sd.nrad) + radial;
+}
+
+__global__ void __launch_bounds__(256) k_near(BatchDev b, int write)
+{
+    const uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (g >= b.nnear)
+        return;
+    const uint32_t lane = lane_id();
+    const int s = scan_of_near(b, g);
+    const ScanDev& sd = b.scans[s];
+    const uint32_t c = near_cell(sd, g - sd.near_off);
+    const uint32_t n = b.cell_cnt[c];
+    const uint32_t start = b.cell_start[c];
+    const float e = b.elev[c];
+    const float lim = 2.0F * sd.thr;
+    uint32_t pos = write ? b.near_start[g] : 0u;
+    for (uint32_t base = 0; base < n; base += 32)
+    {
+        const uint32_t k = base + lane;
+        bool pred = false;
+        float4 p = make_float4(0, 0, 0, 0);
+        if (k < n)
+        {
+            p = b.pts[sd.pt_off + static_cast<uint32_t>(b.csr_idx[start + k])];
+            pred = fabsf(e - p.z) < lim;
+        }
+        const uint32_t m = __ballot_sync(0xffffffffu, pred);
+        if (write && pred)
+            b.cand[pos + __popc(m & ((1u << lane) - 1u))] = make_float4(p.x, p.y, p.z, 0.0f);
+        pos += __popc(m);
+    }
+    if (!write && lane == 0)
+        b.near_cnt[g] = pos;
+}
+
+// MT19937 (Matsumoto & Nishimura, 1998) and Lemire's nearly divisionless bounded draw
+// (Lemire, "Fast Random Integer Generation in an Interval", 2019), which is how
+// std::uniform_int_distribution<uint32_t> maps a 32-bit engine onto [0, n-1].
+struct Mt19937
+{
+    uint32_t mt[624];
+    int idx;
+    __device__ explicit Mt19937(uint32_t seed)
+    {
+        mt[0] = seed;
+        for (int i = 1; i < 624; ++i)
+            mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + static_cast<uint32_t>(i);
+        idx = 624;
+    }
+    __device__ void twist()
+    {
+        for (int i = 0; i < 624; ++i)
+        {
+            const uint32_t y = (mt[i] & 0x80000000u) | (mt[(i + 1) % 624] & 0x7fffffffu);
+            mt[i] = mt[(i + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+        }
+        idx = 0;
+    }
+    __device__ uint32_t next()
+    {
+        if (idx >= 624)
+            twist();
+        uint32_t y = mt[idx++];
+        y ^= y >> 11;
+        y ^= (y << 7) & 0x9d2c5680u;
+        y ^= (y << 15) & 0xefc60000u;
+        y ^= y >> 18;
+        return y;
+    }
+    __device__ uint32_t bounded(uint32_t range) // uniform in [0, range)
+    {
+        uint64_t m = static_cast<uint64_t>(next()) * range;
+        uint32_t l = static_cast<uint32_t>(m);
+        if (l < range)
+        {
+            const uint32_t t = (0u - range) % range;
+            while (l < t)
+            {
+                m = static_cast<uint64_t>(next()) * range;
+                l = static_cast<uint32_t>(m);
+            }
+        }
+        return static_cast<uint32_t>(m >> 32);
+    }
+};
+
+__global__ void k_ransac_draw(BatchDev b)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= b.nscan)
+        return;
+    const ScanDev& sd = b.scans[s];
+    ScanState& st = b.state[s];
+    const uint32_t first = b.near_start[sd.near_off];
+    const uint32_t nnear_s = static_cast<uint32_t>(sd.nslice * sd.nnear_per_slice);
+    const uint32_t last = b.near_start[sd.near_off + nnear_s]; // near_start has nnear + 1 entries
+    const uint32_t N = last - first;
+    st.cand_off = first;
+    st.n_cand = N;
+    st.ransac_ok = 0;
+    b.pvalid[s] = 0ull;
+    if (N < 2)
+        return; // the reference never ends its p3 draw for N == 1 (segmenter.cpp:382-386)
+    Mt19937 gen(42u);
+    const float p1x = 0.0F, p1y = 0.0F, p1z = -sd.sensor_h;
+    unsigned long long valid = 0ull;
+    for (int it = 0; it < kMaxRansacIters; ++it)
+    {
+        const uint32_t i2 = gen.bounded(N);
+        uint32_t i3 = gen.bounded(N);
+        int guard = 0;
+        while (i3 == i2 && guard < (1 << 20))
+        {
+            i3 = gen.bounded(N);
+            ++guard;
+        }
+        if (guard >= (1 << 20))
+        {
+            raise_err(&st, ERR_INTERNAL);
+            return;
+        }
+        const float4 p2 = b.cand[first + i2];
+        const float4 p3 = b.cand[first + i3];
+        float nx = ((p2.y - p1y) * (p3.z - p1z)) - ((p2.z - p1z) * (p3.y - p1y));
+        float ny = ((p2.z - p1z) * (p3.x - p1x)) - ((p2.x - p1x) * (p3.z - p1z));
+        float nz = ((p2.x - p1x) * (p3.y - p1y)) - ((p2.y - p1y) * (p3.x - p1x));
+        const float den = (nx * nx) + (ny * ny) + (nz * nz);
+        float4 pl = make_float4(0, 0, 0, 0);
+        if (!(den < 1.0e-5F))
+        {
+            const float norm = 1.0F / sqrtf(den);
+            nz *= norm;
+            if (!(fabsf(nz) < sd.max_cos))
+            {
+                nx *= norm;
+                ny *= norm;
+                const float pd = (nx * p1x) + (ny * p1y) + (nz * p1z);
+                pl = make_float4(nx, ny, nz, pd);
+                valid |= (1ull << it);
+            }
+        }
+        b.planes[s * kMaxRansacIters + it] = pl;
+        b.inliers[s * kMaxRansacIters + it] = 0u;
+    }
+    b.pvalid[s] = valid;
+}
+
+__global__ void __launch_bounds__(256) k_ransac_inliers(BatchDev b)
+{
+    __shared__ float4 pl[kMaxRansacIters];
+    __shared__ uint32_t cnt[kMaxRansacIters];
+    const int s = blockIdx.y;
+    const ScanDev& sd = b.scans[s];
+    const ScanState& st = b.state[s];
+    const unsigned long long valid = b.pvalid[s];
+    if (threadIdx.x < kMaxRansacIters)
+    {
+        pl[threadIdx.x] = b.planes[s * kMaxRansacIters + threadIdx.x];
+        cnt[threadIdx.x] = 0u;
+    }
+    __syncthreads();
+    const uint32_t N = st.n_cand;
+    if (valid != 0ull)
+    {
+        const uint32_t lane = lane_id();
+        const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+        for (uint32_t base = warp_global * 32; base < N; base += nwarps * 32)
+        {
+            const uint32_t j = base + lane;
+            float4 p = make_float4(0, 0, 0, 0);
+            if (j < N)
+                p = b.cand[st.cand_off + j];
+            for (int it = 0; it < kMaxRansacIters; ++it)
+            {
+                if (!((valid >> it) & 1ull))
+                    continue;
+                const float4 q = pl[it];
+                const bool in = (j < N) && (fabsf((q.x * p.x) + (q.y * p.y) + (q.z * p.z) - q.w) < sd.thr);
+                const uint32_t m = __ballot_sync(0xffffffffu, in);
+                if (lane == 0 && m)
+                    atomicAdd(&cnt[it], static_cast<uint32_t>(__popc(m)));
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < kMaxRansacIters && cnt[threadIdx.x])
+        atomicAdd(&b.inliers[s * kMaxRansacIters + threadIdx.x], cnt[threadIdx.x]);
+}
+
+__global__ void k_ransac_select(BatchDev b)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= b.nscan)
+        return;
+    ScanState& st = b.state[s];
+    const unsigned long long valid = b.pvalid[s];
+    uint32_t best = 0;
+    int bi = -1;
+    for (int it = 0; it < kMaxRansacIters; ++it)
+    {
+        if (!((valid >> it) & 1ull))
+            continue;
+        const uint32_t c = b.inliers[s * kMaxRansacIters + it];
+        if (c > best)
+        {
+            best = c;
+            bi = it;
+        }
+    }
+    if (best > 0)
+    {
+        float4 q = b.planes[s * kMaxRansacIters + bi];
+        if (q.z < 0)
+        {
+            q.x = -q.x;
+            q.y = -q.y;
+            q.z = -q.z;
+            q.w = -q.w;
+        }
+        st.plane[0] = q.x;
+        st.plane[1] = q.y;
+        st.plane[2] = q.z;
+        st.plane[3] = q.w;
+        st.ransac_ok = 1;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Labels and range-image projection (segmenter.cpp:269-318 + the RANSAC relabel :445-478).
+// Per pixel the winner is the lexicographic minimum of (x^2+y^2, cell, cloud index), the
+// order in which the reference's strict '<' visits candidates.
+// ------------------------------------------------------------------------------------------
+__global__ void k_label_depth(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.npts)
+        return;
+    const int32_t c = b.pt_cell[i];
+    if (c < 0)
+        return;
+    const int s = scan_of_point(b, i);
+    const ScanDev& sd = b.scans[s];
+    const ScanState& st = b.state[s];
+    const float4 p = b.pts[i];
+    uint8_t lbl = (p.z >= b.elev[c] + sd.thr) ? LP_LABEL_OBSTACLE : LP_LABEL_GROUND;
+    const int32_t radial = static_cast<int32_t>((static_cast<uint32_t>(c) - sd.cell_off) % static_cast<uint32_t>(sd.nrad));
+    if (radial < kRansacRadialBins && st.ransac_ok)
+    {
+        const float sdist = (st.plane[0] * p.x) + (st.plane[1] * p.y) + (st.plane[2] * p.z) - st.plane[3];
+        if (sdist < sd.thr)
+            lbl = LP_LABEL_GROUND;
+    }
+    b.pt_label[i] = lbl;
+    const float d2 = (p.x * p.x) + (p.y * p.y);
+    atomicMin(&b.pix_depth[sd.pix_off + static_cast<uint32_t>(b.pt_pix[i])], __float_as_uint(d2));
+}
+
+__global__ void k_project_key(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.npts)
+        return;
+    const int32_t c = b.pt_cell[i];
+    if (c < 0)
+        return;
+    const int s = scan_of_point(b, i);
+    const ScanDev& sd = b.scans[s];
+    const float4 p = b.pts[i];
+    const float d2 = (p.x * p.x) + (p.y * p.y);
+    const uint32_t pix = sd.pix_off + static_cast<uint32_t>(b.pt_pix[i]);
+    if (__float_as_uint(d2) != b.pix_depth[pix])
+        return;
+    const unsigned long long key = (static_cast<unsigned long long>(static_cast<uint32_t>(c) - sd.cell_off) << 32) |
+                                   static_cast<unsigned long long>(i - sd.pt_off);
+    atomicMin(&b.pix_key[pix], key);
+}
+
+__global__ void k_pixel(BatchDev b)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= b.npix)
+        return;
+    const unsigned long long key = b.pix_key[p];
+    if (key == ~0ull)
+    {
+        b.pix_map[p] = -1;
+        b.pix_state[p] = PX_EMPTY;
+        return;
+    }
+    const int s = scan_of_pix(b, p);
+    const uint32_t li = static_cast<uint32_t>(key & 0xffffffffull);
+    b.pix_map[p] = static_cast<int32_t>(li);
+    b.pix_state[p] = (b.pt_label[b.scans[s].pt_off + li] == LP_LABEL_GROUND) ? PX_GROUND : PX_OBSTACLE;
+}
+
+// ------------------------------------------------------------------------------------------
+// Dilation of the obstacle channel by a 5x5 rectangle clipped at the image border, and the
+// row-major intersection queue (segmenter.cpp:486-514): one block per image row.
+// ------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_dilate_rows(BatchDev b)
+{
+    __shared__ uint32_t sm[33];
+    const uint32_t r = blockIdx.x;
+    const int s = scan_of_row(b, r);
+    const ScanDev& sd = b.scans[s];
+    const int32_t h = static_cast<int32_t>(r - sd.row_off);
+    const int32_t H = sd.H, W = sd.W;
+    uint8_t* st = b.pix_state + sd.pix_off;
+    const uint32_t row_base = sd.pix_off + static_cast<uint32_t>(h * W);
+    uint32_t count = 0;
+    for (int32_t base = 0; base < W; base += blockDim.x)
+    {
+        const int32_t w = base + static_cast<int32_t>(threadIdx.x);
+        bool inter = false;
+        if (w < W)
+        {
+            const uint8_t cur = st[h * W + w];
+            bool dil = false;
+            for (int32_t dh = -2; dh <= 2 && !dil; ++dh)
+            {
+                const int32_t hh = h + dh;
+                if (hh < 0 || hh >= H)
+                    continue;
+                for (int32_t dw = -2; dw <= 2; ++dw)
+                {
+                    const int32_t ww = w + dw;
+                    if (ww >= 0 && ww < W && st[hh * W + ww] == PX_OBSTACLE)
+                    {
+                        dil = true;
+                        break;
+                    }
+                }
+            }
+            if (dil)
+            {
+                if (cur == PX_GROUND)
+                {
+                    inter = true; // valid index is implied by a ground colour
+                    st[h * W + w] = PX_INTERSECT;
+                }
+                else if (cur == PX_EMPTY)
+                {
+                    st[h * W + w] = PX_EMPTY_RED;
+                }
+            }
+        }
+        uint32_t tot;
+        const uint32_t pre = block_excl_scan(inter ? 1u : 0u, sm, &tot);
+        if (inter)
+            b.row_cols[row_base + count + pre] = static_cast<uint16_t>(w);
+        count += tot;
+    }
+    if (threadIdx.x == 0)
+        b.row_cnt[r] = count;
+}
+
+// Offsets of the 24-neighbour kernel, segmenter.cpp:527-530.
+__constant__ int8_t kOffH[24] = {-2, -2, -2, -2, -2, -1, -1, -1, -1, -1, 0, 0, 0, 0, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2};
+__constant__ int8_t kOffW[24] = {-2, -1, 0, 1, 2, -2, -1, 0, 1, 2, -2, -1, 1, 2, -2, -1, 0, 1, 2, -2, -1, 0, 1, 2};
+
+// Fresh (not stale) weight of every in-bounds neighbour slot of every queued pixel: 0 for an
+// empty neighbour or one farther than the kernel threshold, else expf(-amp * dist)
+// (segmenter.cpp:545-607). These depend on geometry only, so they are computed in parallel
+// before the ordered vote.
+__global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
+{
+    const uint32_t r = blockIdx.x;
+    const int s = scan_of_row(b, r);
+    const ScanDev& sd = b.scans[s];
+    const int32_t h = static_cast<int32_t>(r - sd.row_off);
+    const int32_t H = sd.H, W = sd.W;
+    const uint32_t row_base = sd.pix_off + static_cast<uint32_t>(h * W);
+    const uint32_t m = b.row_cnt[r];
+    const int32_t* map = b.pix_map + sd.pix_off;
+    const float4* pts = b.pts + sd.pt_off;
+    for (uint32_t j = threadIdx.x; j < m; j += blockDim.x)
+    {
+        const int32_t w = b.row_cols[row_base + j];
+        const float4 cp = pts[map[h * W + w]];
+        float* out = b.jw + static_cast<size_t>(row_base + j) * 26;
+        float sum = 0.0F;
+        for (int k = 0; k < 24; ++k)
+        {
+            const int32_t hh = h + kOffH[k], ww = w + kOffW[k];
+            float wt = 0.0F;
+            if (hh >= 0 && hh < H && ww >= 0 && ww < W)
+            {
+                const int32_t ni = map[hh * W + ww];
+                if (ni >= 0)
+                {
+                    const float4 np = pts[ni];
+                    const float dx = cp.x - np.x;
+                    const float dy = cp.y - np.y;
+                    const float dz = cp.z - np.z;
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (!(d2 > sd.kthr2))
+                    {
+                        const float dist = sqrtf(d2);
+                        wt = lpm::cr_expf(-sd.amp * dist);
+                        sum += wt;
+                    }
+                }
+            }
+            out[k] = wt;
+        }
+        out[24] = sum;
+    }
+}
+
+__device__ __forceinline__ uint8_t final_view(uint8_t st)
+{
+    return (st == PX_GROUND || st == PX_RES_G) ? V_G : ((st == PX_OBSTACLE || st == PX_RES_O) ? V_O : V_U);
+}
+__device__ __forceinline__ uint8_t pre_view(uint8_t st)
+{
+    return (st == PX_GROUND) ? V_G : ((st == PX_OBSTACLE) ? V_O : V_U);
+}
+
+__device__ __forceinline__ unsigned long long map_compose(unsigned long long later, unsigned long long earlier)
+{
+    unsigned long long r = 0ull;
+#pragma unroll
+    for (int s = 0; s < 9; ++s)
+    {
+        const uint32_t mid = static_cast<uint32_t>((earlier >> (4 * s)) & 0xfull);
+        r |= ((later >> (4 * mid)) & 0xfull) << (4 * s);
+    }
+    return r;
+}
+__device__ __forceinline__ unsigned long long map_identity()
+{
+    unsigned long long r = 0ull;
+#pragma unroll
+    for (int s = 0; s < 9; ++s)
+        r |= static_cast<unsigned long long>(s) << (4 * s);
+    return r;
+}
+
+// The ordered vote (segmenter.cpp:535-637), one block per scan, image rows in order.
+//
+// Within a row, the queued pixel at column c reads the vote outcomes of the queued pixels at
+// c-1 and c-2 (already written in the reference's FIFO); everything else it reads is fixed:
+// rows above are final, rows below and columns to the right still hold their pre-vote colour.
+// Each queued pixel therefore has a vote table f(a, b) over the outcomes a (column c-1) and
+// b (column c-2), each in {unknown, ground, obstacle}; the row is a chain of 9-state
+// transitions composed by a block-wide prefix scan, which reproduces the FIFO exactly.
+//
+// Slots outside the image keep the weight and label the previous queued pixel wrote to that
+// slot (segmenter.cpp:552-556). That pixel is the last earlier queued pixel for which the slot
+// was inside the image: for a right-border pixel it can be an earlier pixel of the same row
+// (columns <= W-1-dw); otherwise it lies in an earlier row, tracked as a running value per
+// slot across rows.
+__global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
+{
+    __shared__ float run_w[24];
+    __shared__ uint8_t run_l[24];
+    __shared__ int32_t lastq[3]; // entry index of the last queued pixel with col <= W-1-d
+    __shared__ unsigned long long wmaps[8];
+    const int s = blockIdx.x;
+    const ScanDev& sd = b.scans[s];
+    const int32_t H = sd.H, W = sd.W;
+    uint8_t* st = b.pix_state + sd.pix_off;
+    const int32_t* map = b.pix_map + sd.pix_off;
+    if (threadIdx.x < 24)
+    {
+        run_w[threadIdx.x] = 0.0F;
+        run_l[threadIdx.x] = V_U;
+    }
+    __syncthreads();
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    for (int32_t h = 0; h < H; ++h)
+    {
+        const uint32_t r = sd.row_off + static_cast<uint32_t>(h);
+        const uint32_t m = b.row_cnt[r];
+        if (m == 0)
+            continue;
+        const uint32_t row_base = sd.pix_off + static_cast<uint32_t>(h * W);
+        const uint16_t* cols = b.row_cols + row_base;
+        if (threadIdx.x < 3)
+        {
+            const int32_t d = static_cast<int32_t>(threadIdx.x);
+            int32_t q = -1;
+            for (int32_t j = static_cast<int32_t>(m) - 1; j >= 0 && j >= static_cast<int32_t>(m) - 3; --j)
+                if (cols[j] <= W - 1 - d)
+                {
+                    q = j;
+                    break;
+                }
+            lastq[d] = q;
+        }
+        __syncthreads();
+
+        // ---- per queued pixel: vote table -> 9-state transition map --------------------------
+        const uint32_t chunk = (m + blockDim.x - 1) / blockDim.x;
+        const uint32_t j0 = threadIdx.x * chunk;
+        const uint32_t j1 = min(m, j0 + chunk);
+        unsigned long long agg = map_identity();
+        for (uint32_t j = j0; j < j1; ++j)
+        {
+            const int32_t c = cols[j];
+            const float* wj = b.jw + static_cast<size_t>(row_base + j) * 26;
+            const float sum = wj[24];
+            uint8_t outc[9];
+            if (fabsf(sum) > FLT_EPSILON)
+            {
+                float wv[24];
+                uint8_t lb[24];
+                bool sym_a = false, sym_b = false;
+                for (int k = 0; k < 24; ++k)
+                {
+                    const int32_t dh = kOffH[k], dw = kOffW[k];
+                    const int32_t hh = h + dh, ww = c + dw;
+                    if (hh < 0 || hh >= H || ww < 0 || ww >= W)
+                    {
+                        // stale slot
+                        const int32_t qd = dw > 0 ? dw : 0;
+                        const int32_t q = (dw > 0 && hh >= 0 && hh < H) ? lastq[qd] : -1;
+                        if (q >= 0)
+                        {
+                            const float qw = b.jw[static_cast<size_t>(row_base + q) * 26 + k];
+                            wv[k] = qw;
+                            if (qw == 0.0F)
+                                lb[k] = V_U;
+                            else
+                            {
+                                const uint8_t ns = st[hh * W + cols[q] + dw];
+                                lb[k] = (dh < 0) ? final_view(ns) : pre_view(ns);
+                            }
+                        }
+                        else
+                        {
+                            wv[k] = run_w[k];
+                            lb[k] = run_l[k];
+                        }
+                        continue;
+                    }
+                    const float wt = wj[k];
+                    wv[k] = wt;
+                    if (wt == 0.0F)
+                    {
+                        lb[k] = V_U;
+                        continue;
+                    }
+                    const uint8_t ns = st[hh * W + ww];
+                    if (dh < 0)
+                        lb[k] = final_view(ns);
+                    else if (dh > 0 || dw > 0)
+                        lb[k] = pre_view(ns);
+                    else
+                    {
+                        // same row, left of c: symbolic when queued (vote outcome), else fixed
+                        if (ns == PX_INTERSECT)
+                        {
+                            lb[k] = V_U;
+                            if (dw == -1)
+                                sym_a = true;
+                            else
+                                sym_b = true;
+                        }
+                        else
+                            lb[k] = final_view(ns);
+                    }
+                }
+                float wn[24];
+                for (int k = 0; k < 24; ++k)
+                    wn[k] = wv[k] / sum;
+                float g9 = 0.0F, o9 = 0.0F;
+                for (int k = 0; k < 10; ++k)
+                {
+                    if (lb[k] == V_G)
+                        g9 += wn[k];
+                    else if (lb[k] == V_O)
+                        o9 += wn[k];
+                }
+                for (int a = 0; a < 3; ++a)
+                    for (int bb = 0; bb < 3; ++bb)
+                    {
+                        float g = g9, o = o9;
+                        const uint8_t l10 = sym_b ? static_cast<uint8_t>(bb) : lb[10];
+                        const uint8_t l11 = sym_a ? static_cast<uint8_t>(a) : lb[11];
+                        if (l10 == V_G)
+                            g += wn[10];
+                        else if (l10 == V_O)
+                            o += wn[10];
+                        if (l11 == V_G)
+                            g += wn[11];
+                        else if (l11 == V_O)
+                            o += wn[11];
+                        for (int k = 12; k < 24; ++k)
+                        {
+                            if (lb[k] == V_G)
+                                g += wn[k];
+                            else if (lb[k] == V_O)
+                                o += wn[k];
+                        }
+                        outc[3 * a + bb] = (o > g) ? V_O : V_G;
+                    }
+            }
+            else
+            {
+                for (int k = 0; k < 9; ++k)
+                    outc[k] = V_U;
+            }
+            const int32_t gap = (j > 0) ? (c - static_cast<int32_t>(cols[j - 1])) : 1000;
+            unsigned long long t = 0ull;
+            for (int sidx = 0; sidx < 9; ++sidx)
+            {
+                const int a = sidx / 3, bb = sidx % 3;
+                int ap, bp, an;
+                if (gap == 1)
+                {
+                    ap = a;
+                    bp = bb;
+                    an = a;
+                }
+                else if (gap == 2)
+                {
+                    ap = V_U;
+                    bp = a;
+                    an = V_U;
+                }
+                else
+                {
+                    ap = V_U;
+                    bp = V_U;
+                    an = V_U;
+                }
+                const int x = outc[3 * ap + bp];
+                t |= static_cast<unsigned long long>(3 * x + an) << (4 * sidx);
+            }
+            b.jmap[row_base + j] = t;
+            agg = map_compose(t, agg);
+        }
+
+        // ---- block-wide exclusive scan of the thread aggregates (composition order) -----------
+        unsigned long long incl = agg;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const unsigned long long other = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= static_cast<uint32_t>(o))
+                incl = map_compose(incl, other);
+        }
+        if (lane == 31)
+            wmaps[warp] = incl;
+        __syncthreads();
+        unsigned long long wpre = map_identity();
+        for (uint32_t w2 = 0; w2 < warp; ++w2)
+            wpre = map_compose(wmaps[w2], wpre);
+        unsigned long long excl = __shfl_up_sync(0xffffffffu, incl, 1);
+        if (lane == 0)
+            excl = map_identity();
+        excl = map_compose(excl, wpre);
+        // state before this thread's chunk, starting from (unknown, unknown)
+        uint32_t state = static_cast<uint32_t>(excl & 0xfull);
+        for (uint32_t j = j0; j < j1; ++j)
+        {
+            state = static_cast<uint32_t>((b.jmap[row_base + j] >> (4 * state)) & 0xfull);
+            const uint32_t x = state / 3;
+            if (x != V_U)
+                st[h * W + cols[j]] = (x == V_O) ? PX_RES_O : PX_RES_G;
+        }
+        __syncthreads();
+
+        // ---- running stale values: last queued pixel of this row with the slot in bounds ------
+        if (threadIdx.x < 24)
+        {
+            const int k = threadIdx.x;
+            const int32_t dh = kOffH[k], dw = kOffW[k];
+            const int32_t hh = h + dh;
+            if (hh >= 0 && hh < H)
+            {
+                const int32_t q = lastq[dw > 0 ? dw : 0];
+                if (q >= 0 && static_cast<int32_t>(cols[q]) >= (dw < 0 ? -dw : 0))
+                {
+                    const float qw = b.jw[static_cast<size_t>(row_base + q) * 26 + k];
+                    uint8_t l = V_U;
+                    if (qw != 0.0F)
+                    {
+                        const uint8_t ns = st[hh * W + cols[q] + dw];
+                        const bool before = (dh < 0) || (dh == 0 && dw < 0);
+                        l = before ? final_view(ns) : pre_view(ns);
+                    }
+                    run_w[k] = qw;
+                    run_l[k] = l;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    (void)map;
+}
+
+// populateLabels (segmenter.cpp:640-669) and the colour image of Segmenter::image().
+__global__ void k_populate(BatchDev b, uint8_t* image)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= b.npix)
+        return;
+    const uint8_t stv = b.pix_state[p];
+    const int32_t li = b.pix_map[p];
+    if (li >= 0)
+    {
+        const int s = scan_of_pix(b, p);
+        const uint8_t v = final_view(stv);
+        if (v != V_U)
+            b.seg_label[b.scans[s].pt_off + static_cast<uint32_t>(li)] = (v == V_G) ? LP_LABEL_GROUND : LP_LABEL_OBSTACLE;
+    }
+    if (image)
+    {
+        uint8_t bgr[3] = {0, 0, 0};
+        switch (stv)
+        {
+        case PX_GROUND:
+        case PX_RES_G:
+            bgr[1] = 255;
+            break;
+        case PX_OBSTACLE:
+        case PX_RES_O:
+        case PX_EMPTY_RED:
+            bgr[2] = 255;
+            break;
+        case PX_INTERSECT:
+            bgr[0] = 255;
+            break;
+        default:
+            break;
+        }
+        image[3 * p] = bgr[0];
+        image[3 * p + 1] = bgr[1];
+        image[3 * p + 2] = bgr[2];
+    }
+}
+} // namespace
+
+// ------------------------------------------------------------------------------------------
+// Host launch sequence for the segmentation stage (all launches on one stream, no host sync).
+// ------------------------------------------------------------------------------------------
+void launch_ring_only(Launcher& L, const BatchDev& b, const BatchHost& hb)
+{
+    const uint32_t T = 256;
+    LP_LAUNCH(L, k_quadrant, div_up(b.npts, T), T, b);
+    LP_LAUNCH(L, k_ring_count, hb.ntiles, 256, b);
+    L.scan(b.tile_cnt, b.tile_cnt, hb.ntiles + 1);
+    LP_LAUNCH(L, k_ring_apply, hb.ntiles, 256, b);
+}
+
+__global__ void k_debug_math(int kind, const float* a, const float* bb, uint32_t n, float* out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    float r;
+    switch (kind)
+    {
+    case 0:
+        r = lpm::cr_atan2f(a[i], bb[i]);
+        break;
+    case 1:
+        r = lpm::cr_atanf(a[i]);
+        break;
+    case 2:
+        r = lpm::cr_expf(a[i]);
+        break;
+    default:
+        r = lpm::atan2_approx(a[i], bb[i]);
+        break;
+    }
+    out[i] = r;
+}
+
+void launch_debug_math(Launcher& L, int kind, const float* a, const float* bb, uint32_t n, float* out)
+{
+    LP_LAUNCH(L, k_debug_math, div_up(n, 256u), 256, kind, a, bb, n, out);
+}
+
+void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, uint8_t* d_image)
+{
+    const uint32_t T = 256;
+    if (hb.any_compute_ring)
+        launch_ring_only(L, b, hb);
+    LP_LAUNCH(L, k_bin, div_up(b.npts, T), T, b);
+    L.scan(b.cell_cnt, b.cell_start, b.ncell + 1);
+    LP_LAUNCH(L, k_scatter, div_up(b.npts, T), T, b);
+    LP_LAUNCH(L, k_cell_small, div_up(b.ncell * 32u, 256u), 256, b);
+    LP_LAUNCH(L, k_cell_large, 152u * 2u, 512, b);
+    LP_LAUNCH(L, k_chain, div_up(hb.nslices, 128u), 128, b, hb.nslices);
+    LP_LAUNCH(L, k_near, div_up(b.nnear * 32u, 256u), 256, b, 0);
+    L.scan(b.near_cnt, b.near_start, b.nnear + 1); // near_cnt[nnear] == 0: last entry is the total
+    LP_LAUNCH(L, k_near, div_up(b.nnear * 32u, 256u), 256, b, 1);
+    LP_LAUNCH(L, k_ransac_draw, div_up(static_cast<uint32_t>(b.nscan), 64u), 64, b);
+    LP_LAUNCH2D(L, k_ransac_inliers, dim3(16, static_cast<uint32_t>(b.nscan)), 256, b);
+    LP_LAUNCH(L, k_ransac_select, div_up(static_cast<uint32_t>(b.nscan), 64u), 64, b);
+    LP_LAUNCH(L, k_label_depth, div_up(b.npts, T), T, b);
+    LP_LAUNCH(L, k_project_key, div_up(b.npts, T), T, b);
+    LP_LAUNCH(L, k_pixel, div_up(b.npix, T), T, b);
+    LP_LAUNCH(L, k_dilate_rows, b.nrows, 256, b);
+    LP_LAUNCH(L, k_jcp_weights, b.nrows, 256, b);
+    LP_LAUNCH(L, k_jcp_rows, static_cast<uint32_t>(b.nscan), 256, b);
+    LP_LAUNCH(L, k_populate, div_up(b.npix, T), T, b, d_image);
+}
+} // namespace lpg

@@ -1,0 +1,130 @@
+// lp_stages.hpp — host-side launch helpers and the stage entry points of liblp_gpu.so.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "lp_batch.cuh"
+
+namespace lpg
+{
+void scan_exclusive(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* sums,
+                    uint32_t* grand_total, uint64_t& launches);
+
+// One timed launch (profiling mode only).
+struct LaunchRecord
+{
+    const char* name;
+    cudaEvent_t start, stop;
+};
+
+// Issues kernel launches on one stream, counts them and remembers the first launch error. In
+// profiling mode every launch is bracketed by CUDA events on the same stream.
+struct Launcher
+{
+    cudaStream_t stream = nullptr;
+    uint64_t* launches = nullptr;
+    uint32_t* scan_sums = nullptr; // scratch for device-wide scans
+    uint32_t* scan_total = nullptr;
+    cudaError_t err = cudaSuccess;
+    std::vector<LaunchRecord>* prof = nullptr;
+    std::vector<cudaEvent_t>* event_pool = nullptr;
+    size_t pool_next = 0;
+
+    cudaEvent_t next_event()
+    {
+        if (pool_next >= event_pool->size())
+        {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            event_pool->push_back(e);
+        }
+        return (*event_pool)[pool_next++];
+    }
+    void begin(const char* name)
+    {
+        if (prof)
+        {
+            LaunchRecord r{name, next_event(), next_event()};
+            cudaEventRecord(r.start, stream);
+            prof->push_back(r);
+        }
+    }
+    void end()
+    {
+        if (prof)
+            cudaEventRecord(prof->back().stop, stream);
+    }
+
+    template <typename K, typename... Args>
+    void launch(const char* name, K kernel, uint32_t grid, uint32_t block, Args... args)
+    {
+        if (grid == 0)
+            return;
+        begin(name);
+        kernel<<<grid, block, 0, stream>>>(args...);
+        end();
+        note();
+    }
+    template <typename K, typename... Args>
+    void launch2d(const char* name, K kernel, dim3 grid, uint32_t block, Args... args)
+    {
+        if (grid.x == 0 || grid.y == 0)
+            return;
+        begin(name);
+        kernel<<<grid, block, 0, stream>>>(args...);
+        end();
+        note();
+    }
+    void scan(const uint32_t* in, uint32_t* out, uint32_t n)
+    {
+        if (n == 0)
+            return;
+        begin("k_scan");
+        scan_exclusive(stream, in, out, n, scan_sums, scan_total, *launches);
+        end();
+        note_only();
+    }
+    void note()
+    {
+        ++(*launches);
+        note_only();
+    }
+    void note_only()
+    {
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess && err == cudaSuccess)
+            err = e;
+    }
+};
+
+#define LP_LAUNCH(L, k, grid, block, ...) (L).launch(#k, k, grid, block, __VA_ARGS__)
+#define LP_LAUNCH2D(L, k, grid, block, ...) (L).launch2d(#k, k, grid, block, __VA_ARGS__)
+
+// Host-side sizes of a batch (what the kernels' grids are sized by).
+struct BatchHost
+{
+    int nscan = 0;
+    bool any_compute_ring = false;
+    bool any_noise = false;
+    uint32_t ntiles = 0;
+    uint32_t nslices = 0;
+    std::vector<ScanDev> scans;
+};
+
+void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, uint8_t* d_image);
+void launch_ring_only(Launcher& L, const BatchDev& b, const BatchHost& hb);
+void launch_clustering(Launcher& L, const BatchDev& b, const BatchHost& hb);
+void launch_polygons(Launcher& L, const BatchDev& b, const BatchHost& hb, int compute_obb);
+void launch_noise(Launcher& L, const BatchDev& b, const BatchHost& hb, const lp_noise_remover_config& cfg);
+void launch_noise_compaction(Launcher& L, const BatchDev& b, const BatchHost& hb);
+void launch_state_init(Launcher& L, const BatchDev& b, int noise);
+void launch_outputs(Launcher& L, const BatchDev& b, int with_clusters);
+void launch_mark_all_obstacles(Launcher& L, const BatchDev& b);
+void launch_hull_single(Launcher& L, const double2* pts, uint32_t n, void* scratch, int* stack, int32_t* out,
+                        uint32_t* n_out);
+void launch_boxes_single(Launcher& L, const double2* P, uint32_t n, int2* pairs, int cap, int kind,
+                         lp_bounding_box* out, int* npairs_out);
+void launch_debug_math(Launcher& L, int kind, const float* a, const float* b, uint32_t n, float* out);
+} // namespace lpg

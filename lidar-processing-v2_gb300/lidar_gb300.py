@@ -236,6 +236,18 @@ def _declare(lib):
         "lp_bounding_box_pca": (c.c_int32, [P, P, c.c_uint32, P]),
         "lp_process_scan": (c.c_int32, [P, P, P, P]),
         "lp_process_batch": (c.c_int32, [P, P, P, P, c.c_uint32]),
+        "lp_batch_create": (c.c_int32, [P, P, P, c.c_uint32, c.POINTER(P)]),
+        "lp_batch_destroy": (None, [P, P]),
+        "lp_batch_upload": (c.c_int32, [P, P]),
+        "lp_batch_execute": (c.c_int32, [P, P]),
+        "lp_batch_capture_graph": (c.c_int32, [P, P]),
+        "lp_batch_download": (c.c_int32, [P, P, P]),
+        "lp_context_synchronize": (c.c_int32, [P]),
+        "lp_batch_points": (c.c_uint32, [P]),
+        "lp_batch_device_bytes": (c.c_uint64, [P]),
+        "lp_batch_time": (c.c_int32, [P, P, c.c_uint32, c.c_int32, c.POINTER(c.c_float)]),
+        "lp_batch_profile": (c.c_int32, [P, P, P, c.c_uint32, P, c.c_uint32, c.POINTER(c.c_uint32)]),
+        "lp_debug_math": (c.c_int32, [P, c.c_int32, P, P, c.c_uint32, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -417,6 +429,86 @@ class Polygonizer:
         b = BoundingBox()
         check(library().lp_bounding_box_pca(self.ctx.handle, ptr(a), len(a), ctypes.byref(b)), self.ctx)
         return b
+
+
+class PreparedBatch:
+    """Scans uploaded once to HBM; execute() re-runs the pipeline on the device-resident inputs
+    (optionally as a captured CUDA graph), download() returns ScanResults, upload() re-copies the
+    host inputs (end-to-end measurement)."""
+
+    def __init__(self, ctx, scans, pipeline=None, seg_configs=None, rings=None):
+        self.ctx = ctx
+        self.pipeline = pipeline or PipelineConfig.default()
+        n = len(scans)
+        self._arrs = [_xyzi(s) for s in scans]
+        self._rings = [None if (rings is None or rings[i] is None) else np.ascontiguousarray(rings[i], np.uint16)
+                       for i in range(n)]
+        cfgs = seg_configs or [SegmenterConfig.default() for _ in range(n)]
+        self._ins = (ScanInput * n)()
+        for i in range(n):
+            self._ins[i] = ScanInput(self._arrs[i].ctypes.data,
+                                     None if self._rings[i] is None else self._rings[i].ctypes.data,
+                                     len(self._arrs[i]), cfgs[i])
+        self._bufs = [ResultBuffers(len(a)) for a in self._arrs]
+        h = ctypes.c_void_p()
+        check(library().lp_batch_create(ctx.handle, ctypes.byref(self.pipeline), self._ins, n, ctypes.byref(h)), ctx)
+        self.handle = h
+        self.n = n
+
+    @property
+    def points(self):
+        return int(library().lp_batch_points(self.handle))
+
+    @property
+    def device_bytes(self):
+        return int(library().lp_batch_device_bytes(self.handle))
+
+    def upload(self):
+        check(library().lp_batch_upload(self.ctx.handle, self.handle), self.ctx)
+
+    def execute(self):
+        check(library().lp_batch_execute(self.ctx.handle, self.handle), self.ctx)
+
+    def capture_graph(self):
+        check(library().lp_batch_capture_graph(self.ctx.handle, self.handle), self.ctx)
+
+    def synchronize(self):
+        check(library().lp_context_synchronize(self.ctx.handle), self.ctx)
+
+    def download(self):
+        outs = (ScanOutput * self.n)(*[b.out for b in self._bufs])
+        st = library().lp_batch_download(self.ctx.handle, self.handle, outs)
+        for i in range(self.n):
+            self._bufs[i].out = outs[i]
+        check(st, self.ctx)
+        return [b.result() for b in self._bufs]
+
+    def time(self, iters, flush_l2=True):
+        ms = ctypes.c_float()
+        check(library().lp_batch_time(self.ctx.handle, self.handle, iters, 1 if flush_l2 else 0, ctypes.byref(ms)),
+              self.ctx)
+        return ms.value
+
+    def profile(self, cap=256, name_len=48):
+        names = ctypes.create_string_buffer(cap * name_len)
+        ms = np.zeros(cap, np.float32)
+        cnt = ctypes.c_uint32()
+        check(library().lp_batch_profile(self.ctx.handle, self.handle, names, name_len, ptr(ms), cap,
+                                         ctypes.byref(cnt)), self.ctx)
+        k = min(cnt.value, cap)
+        raw = names.raw
+        return [(raw[i * name_len:(i + 1) * name_len].split(b"\0")[0].decode(), float(ms[i])) for i in range(k)]
+
+    def close(self):
+        if self.handle:
+            library().lp_batch_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def process_batch(ctx, scans, pipeline=None, seg_configs=None, rings=None):

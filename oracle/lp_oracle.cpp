@@ -532,7 +532,7 @@ lp_status lpo_segment(const float* xyzi, const uint16_t* ring, uint32_t n, const
 
 // ---------------------------------------------------------------------------------------------
 // DROR — NoiseRemover::filter, lidar_processing_lib/src/noise_remover.cpp:38-68.
-// Radius per point: s2 = pow(double(mult), 2); rho2 = double(x*x) + double(y*y) (float products);
+// Radius per point: s2 = pow(double(mult), 2); rho2 = double(x*x + y*y) (float products and sum);
 // r2 = max(float(s2 * rho2), rmin*rmin). Neighbour test: d0 + (d1 + d2) <= r2 with dk = (q_k -
 // p_k)^2 in float, query first (kdtree.hpp:131-143, :363).
 //
@@ -555,7 +555,8 @@ inline float drorDist(const float* q, const float* p)
 
 inline float drorRadius2(const float* p, double s2, float rmin2)
 {
-    const double rho2 = static_cast<double>(p[0] * p[0]) + static_cast<double>(p[1] * p[1]);
+    // (point[0] * point[0]) + (point[1] * point[1]) is a float sum, then widened (noise_remover.cpp:55)
+    const double rho2 = static_cast<double>((p[0] * p[0]) + (p[1] * p[1]));
     return std::max(static_cast<float>(s2 * rho2), rmin2);
 }
 } // namespace
@@ -1165,3 +1166,22 @@ lp_status lpo_process_scan(const lp_pipeline_config* cfg, const lp_scan_input* s
 }
 
 } // extern "C"
+
+extern "C" {
+// RANSAC index stream exactly as segmenter.cpp:369-386 draws it: std::mt19937{42} and
+// std::uniform_int_distribution<uint32_t>{0, n - 1}; out receives 2 * iters indices (p2, p3).
+void lpo_ransac_draws(uint32_t n, uint32_t iters, uint32_t* out)
+{
+    std::mt19937 gen{42};
+    std::uniform_int_distribution<uint32_t> dist{0, n - 1U};
+    for (uint32_t it = 0; it < iters; ++it)
+    {
+        const uint32_t a = dist(gen);
+        uint32_t b = dist(gen);
+        while (b == a && n > 1)
+            b = dist(gen);
+        out[2 * it] = a;
+        out[2 * it + 1] = b;
+    }
+}
+}

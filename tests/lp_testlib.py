@@ -81,6 +81,39 @@ def ref():
     return _ref
 
 
+# ---------------------------------------------------------------------------- synthetic scans
+def synth():
+    global _synth
+    if _synth is None:
+        s = ctypes.CDLL(lp.SYNTH_PATH)
+        P, c = ctypes.c_void_p, ctypes
+        s.lp_synth_capacity.restype = c.c_uint32
+        s.lp_synth_capacity.argtypes = [c.c_int32, c.c_int32]
+        s.lp_synth_scan.restype = c.c_uint32
+        s.lp_synth_scan.argtypes = [c.c_int32, c.c_int32, P, P, c.c_uint32]
+        s.lp_synth_shape.restype = None
+        s.lp_synth_shape.argtypes = [c.c_int32, c.c_int32, P, P, P, P]
+        _synth = s
+    return _synth
+
+
+def synth_shape(workload, scan):
+    r, w, up, dn = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_float(), ctypes.c_float()
+    synth().lp_synth_shape(workload, scan, ctypes.byref(r), ctypes.byref(w), ctypes.byref(up), ctypes.byref(dn))
+    return r.value, w.value, up.value, dn.value
+
+
+def synth_scan(workload, scan):
+    """(xyzi float32 N x 4, true ring uint16, SegmenterConfig) of a seeded synthetic scan."""
+    cap = synth().lp_synth_capacity(workload, scan)
+    x = np.zeros((cap, 4), np.float32)
+    r = np.zeros(cap, np.uint16)
+    n = synth().lp_synth_scan(workload, scan, ptr(x), ptr(r), cap)
+    rings, bins, up, dn = synth_shape(workload, scan)
+    cfg = lp.SegmenterConfig.default(image_height=rings, image_width=bins, elevation_up_deg=up, elevation_down_deg=dn)
+    return np.ascontiguousarray(x[:n]), np.ascontiguousarray(r[:n]), cfg
+
+
 # ------------------------------------------------------------------------------------------ I/O
 def read_pcd(path):
     """Binary PCD v0.7 with FIELDS x y z intensity (the reference's data/*.pcd)."""

@@ -1,0 +1,230 @@
+"""GPU parity: every stage through the C ABI against the CPU oracle (correctly rounded libm mode)
+on seeded synthetic scans and the committed reference fixtures. Integer outputs (labels,
+partitions, hull index sequences, masks) must be identical; calipers boxes identical; PCA box
+corners within 1e-4 m as a set."""
+import ctypes
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import lp_testlib as T
+
+lp = T.lp
+pytestmark = pytest.mark.gpu
+
+
+# ------------------------------------------------------------------------------- correctly rounded
+def gpu_math(ctx, kind, a, b=None):
+    a = np.ascontiguousarray(a, np.float32)
+    bb = np.ascontiguousarray(b if b is not None else a, np.float32)
+    out = np.zeros(len(a), np.float32)
+    lib = lp.library()
+    lib.lp_debug_math.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                  ctypes.c_void_p]
+    lp.check(lib.lp_debug_math(ctx.handle, kind, T.ptr(a), T.ptr(bb), len(a), T.ptr(out)), ctx)
+    return out
+
+
+def oracle_math(kind, a, b=None):
+    T.oracle().lpo_set_libm_mode(T.LIBM_CR)
+    b = a if b is None else b
+    return np.array([T.oracle().lpo_math(kind, float(x), float(y)) for x, y in zip(a, b)], np.float32)
+
+
+def test_correctly_rounded_math(ctx):
+    rng = np.random.default_rng(5)
+    n = 20000
+    y = rng.uniform(-80, 80, n).astype(np.float32)
+    x = rng.uniform(-80, 80, n).astype(np.float32)
+    specials = np.array([0.0, -0.0, 1e-30, -1e-30, 1.0, -1.0, 3e-8, -3e-8, 80.0], np.float32)
+    y = np.concatenate([y, specials, specials * 0 + 1.0, specials])
+    x = np.concatenate([x, specials * 0 + 1.0, specials, -specials])
+    assert np.array_equal(gpu_math(ctx, 0, y, x).view(np.uint32), oracle_math(0, y, x).view(np.uint32))
+    t = rng.uniform(-4, 4, n).astype(np.float32)
+    assert np.array_equal(gpu_math(ctx, 1, t).view(np.uint32), oracle_math(1, t).view(np.uint32))
+    e = -5.0 * np.sqrt(rng.uniform(0, 1, n)).astype(np.float32)
+    assert np.array_equal(gpu_math(ctx, 2, e).view(np.uint32), oracle_math(2, e).view(np.uint32))
+    assert np.array_equal(gpu_math(ctx, 3, y, x).view(np.uint32), oracle_math(3, y, x).view(np.uint32))
+
+
+# ------------------------------------------------------------------------------------ per stage
+def scans(spec):
+    return [T.synth_scan(w, s) for w, s in spec]
+
+
+@pytest.mark.parametrize("w,s", [(1, 0), (3, 0), (3, 1), (3, 2)])
+def test_ring_partition(ctx, w, s):
+    x, _, cfg = T.synth_scan(w, s)
+    first = cfg.image_height - 1
+    assert np.array_equal(lp.add_ring_info(ctx, x, first), T.o_ring(x, first))
+
+
+@pytest.mark.parametrize("w,s", [(1, 0), (1, 1), (2, 0), (3, 0), (3, 3), (3, 5)])
+def test_segment_organized(ctx, w, s):
+    x, ring, cfg = T.synth_scan(w, s)
+    seg = lp.Segmenter(ctx, cfg)
+    got = seg.segment(x, ring, want_image=True)
+    want, img = T.o_segment(x, ring, cfg, image=True)
+    assert np.array_equal(got, want)
+    assert np.array_equal(seg.image(), img)
+
+
+@pytest.mark.parametrize("w,s", [(1, 0), (2, 1)])
+def test_segment_unorganized(ctx, w, s):
+    x, _, cfg = T.synth_scan(w, s)
+    got = lp.Segmenter(ctx, cfg).segment(x, None)
+    assert np.array_equal(got, T.o_segment(x, None, cfg))
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(T.GOLDEN, "*_sector.npz"))),
+                         ids=lambda p: os.path.basename(p))
+def test_segment_reference_fixtures(ctx, path):
+    """Against the reference's own outputs (the organised path uses no libm function)."""
+    g = dict(np.load(path))
+    cfg = lp.SegmenterConfig(*[float(v) if t is not ctypes.c_int32 else int(v)
+                               for v, (_, t) in zip(g["seg_cfg"], lp.SegmenterConfig._fields_)])
+    seg = lp.Segmenter(ctx, cfg)
+    assert np.array_equal(seg.segment(g["xyzi"], g["ring"], want_image=True), g["seg_labels"])
+    assert np.array_equal(seg.image(), g["seg_image"])
+
+
+@pytest.mark.parametrize("w,s", [(1, 0), (2, 0), (3, 4)])
+def test_cluster(ctx, w, s):
+    x, ring, cfg = T.synth_scan(w, s)
+    lab = T.o_segment(x, ring, cfg)
+    obs = np.ascontiguousarray(x[lab == lp.OBSTACLE][:, :3])
+    c = lp.ClustererConfig.processor()
+    got = lp.Clusterer(ctx, c).cluster(obs)
+    want = T.o_cluster(obs, c)
+    assert np.array_equal(got, want)
+
+
+def test_cluster_voxel_capacity(ctx):
+    """More than 200,000 occupied voxels: the reference throws std::overflow_error
+    (static_unordered_map.hpp:81); the library reports LP_ERR_CAPACITY (OverflowError)."""
+    rng = np.random.default_rng(0)
+    pts = rng.uniform(-80, 80, size=(260000, 3)).astype(np.float32)
+    with pytest.raises(OverflowError):
+        lp.Clusterer(ctx, lp.ClustererConfig(0.05, 0.25, 0.25, 3)).cluster(pts)
+    with pytest.raises(OverflowError):
+        T.o_cluster(pts, lp.ClustererConfig(0.05, 0.25, 0.25, 3))
+
+
+@pytest.mark.parametrize("cfg", [lp.NoiseRemoverConfig.default(), lp.NoiseRemoverConfig(3 * 0.17 * np.pi / 180, 0.1, 3)],
+                         ids=["default", "dense"])
+def test_noise_removal_exact(ctx, cfg):
+    x, _, _ = T.synth_scan(1, 0)
+    rng = np.random.default_rng(3)
+    clutter = rng.normal(size=(3000, 3)) * 6.0
+    pts = np.ascontiguousarray(np.concatenate([x[:, :3], clutter]).astype(np.float32))
+    pts = np.ascontiguousarray(pts[rng.permutation(len(pts))])
+    got = lp.NoiseRemover(ctx, cfg).filter(pts)
+    assert np.array_equal(got, T.o_noise(pts, cfg, T.DROR_EXACT))
+    assert got.sum() > 0
+
+
+def test_polygons(ctx):
+    rng = np.random.default_rng(11)
+    poly = lp.Polygonizer(ctx)
+    for t in range(30):
+        m = int(rng.integers(3, 400))
+        pts = (rng.normal(size=(m, 2)) * rng.uniform(0.2, 15.0)).astype(np.float32).astype(np.float64)
+        if t % 3 == 0:
+            pts = np.round(pts, 1)
+        h = poly.convexHull(pts)
+        assert np.array_equal(h, T.o_hull(pts))
+        hp = np.ascontiguousarray(pts[h])
+        if len(hp) >= 2:
+            assert np.array_equal(poly.findAntipodalPairsOfConvexHull(hp), T.o_antipodal(hp))
+        assert T.boxes_identical(poly.boundingBoxRotatingCalipers(hp), T.o_calipers(hp))
+        assert T.box_corner_set_close(poly.boundingBoxPrincipalComponentAnalysis(hp), T.o_pca(hp)[0], 1e-4)
+
+
+# ------------------------------------------------------------------------------------- pipeline
+def compare_scan(got, want, label=""):
+    assert np.array_equal(got.seg_labels, want.seg_labels), label
+    assert np.array_equal(got.cluster_labels, want.cluster_labels), label
+    assert got.n_clusters == want.n_clusters, label
+    assert np.array_equal(got.hull_offsets, want.hull_offsets), label
+    assert np.array_equal(got.hull_indices, want.hull_indices), label
+    assert np.array_equal(got.z_min, want.z_min) and np.array_equal(got.z_max, want.z_max), label
+    for a, b in zip(got.obb_calipers, want.obb_calipers):
+        assert T.boxes_identical(a, b), label
+    for a, b in zip(got.obb_pca, want.obb_pca):
+        assert T.box_corner_set_close(a, b, 1e-4), label
+
+
+def test_pipeline_batch_mixed(ctx):
+    spec = [(3, i) for i in range(8)]
+    data = scans(spec)
+    pipe = lp.PipelineConfig.default()
+    res = lp.process_batch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
+    for (x, ring, cfg), r, sp in zip(data, res, spec):
+        compare_scan(r, T.o_process(x, ring, cfg, pipe), str(sp))
+
+
+def test_pipeline_computed_rings(ctx):
+    data = scans([(1, 2), (3, 6)])
+    pipe = lp.PipelineConfig.default(compute_ring=1)
+    res = lp.process_batch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], None)
+    for (x, _, cfg), r in zip(data, res):
+        rings = T.o_ring(x, cfg.image_height - 1)
+        compare_scan(r, T.o_process(x, rings, cfg, lp.PipelineConfig.default()))
+
+
+def test_pipeline_with_noise_removal(ctx):
+    data = scans([(1, 3), (3, 7)])
+    pipe = lp.PipelineConfig.default(enable_noise_removal=1,
+                                     noise=lp.NoiseRemoverConfig(3 * 0.17 * np.pi / 180, 0.1, 3))
+    res = lp.process_batch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
+    for (x, ring, cfg), r in zip(data, res):
+        want = T.o_process(x, ring, cfg, pipe, dror_mode=T.DROR_EXACT)
+        assert np.array_equal(r.noise_labels, want.noise_labels)
+        compare_scan(r, want)
+
+
+def test_batch_equals_alone(ctx):
+    data = scans([(3, 8), (3, 9), (3, 10)])
+    pipe = lp.PipelineConfig.default()
+    batched = lp.process_batch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
+    for d, b in zip(data, batched):
+        alone = lp.process_batch(ctx, [d[0]], pipe, [d[2]], [d[1]])[0]
+        compare_scan(b, alone)
+
+
+def test_edge_cases(ctx):
+    x, ring, cfg = T.synth_scan(1, 0)
+    pipe = lp.PipelineConfig.default()
+    far = x[np.hypot(x[:, 0], x[:, 1]) > 30.0]
+    cases = [
+        (x[:0], ring[:0]),                     # empty scan
+        (x[:1], ring[:1]),                     # one point
+        (x[:2], ring[:2]),                     # two points
+        (far, ring[np.hypot(x[:, 0], x[:, 1]) > 30.0]),  # no near-field RANSAC candidates
+        (x[x[:, 2] < -1.5], ring[x[:, 2] < -1.5]),        # ground only
+    ]
+    xs = [np.ascontiguousarray(c[0]) for c in cases]
+    rs = [np.ascontiguousarray(c[1]) for c in cases]
+    res = lp.process_batch(ctx, xs, pipe, [cfg] * len(xs), rs)
+    for xx, rr, r in zip(xs, rs, res):
+        compare_scan(r, T.o_process(xx, rr, cfg, pipe), f"n={len(xx)}")
+
+
+def test_prepared_batch_and_graph(ctx):
+    """lp_batch_create / execute / capture_graph give the same results as lp_process_batch."""
+    data = scans([(3, 11), (1, 4)])
+    pipe = lp.PipelineConfig.default()
+    ref = lp.process_batch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
+    b = lp.PreparedBatch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
+    b.execute()
+    got = b.download()
+    b.capture_graph()
+    b.execute()
+    b.execute()
+    got2 = b.download()
+    for r, g1, g2 in zip(ref, got, got2):
+        compare_scan(g1, r)
+        compare_scan(g2, r)
+    b.close()

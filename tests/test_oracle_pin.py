@@ -1,0 +1,153 @@
+"""Pins the CPU oracle (oracle/lp_oracle.cpp) against fixtures produced by the reference library's
+own code (tests/golden/make_golden.py over oracle/_ref). The oracle runs with the host libm, as
+the reference does; all comparisons are exact except the PCA box (Eigen's JacobiSVD is restated),
+whose corners are compared as a set within 1e-9 m."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import lp_testlib as T
+
+lp = T.lp
+CASES = sorted(glob.glob(os.path.join(T.GOLDEN, "*_sector.npz")))
+
+
+def load(path):
+    return dict(np.load(path))
+
+
+def seg_cfg(g):
+    return lp.SegmenterConfig(*[float(v) if t is not lp.ctypes.c_int32 else int(v)
+                                for v, (_, t) in zip(g["seg_cfg"], lp.SegmenterConfig._fields_)])
+
+
+def box_from(row):
+    b = lp.BoundingBox()
+    for k in range(4):
+        b.corners[k][0], b.corners[k][1] = row[2 * k], row[2 * k + 1]
+    b.area, b.angle_rad, b.is_valid = row[8], row[9], int(row[10])
+    return b
+
+
+@pytest.mark.parametrize("path", CASES, ids=lambda p: os.path.basename(p))
+def test_segmentation_pinned(built, path):
+    g = load(path)
+    cfg = seg_cfg(g)
+    lab, img = T.o_segment(g["xyzi"], g["ring"], cfg, libm=T.LIBM_HOST, image=True)
+    assert np.array_equal(lab, g["seg_labels"])
+    assert np.array_equal(img, g["seg_image"])
+    assert np.array_equal(T.o_segment(g["xyzi"], None, cfg, libm=T.LIBM_HOST), g["seg_labels_unorganized"])
+
+
+@pytest.mark.parametrize("path", CASES, ids=lambda p: os.path.basename(p))
+def test_clustering_pinned(built, path):
+    g = load(path)
+    obs = np.ascontiguousarray(g["xyzi"][g["seg_labels"] == lp.OBSTACLE][:, :3])
+    assert np.array_equal(T.o_cluster(obs, lp.ClustererConfig.processor(), libm=T.LIBM_HOST), g["cluster_labels"])
+
+
+@pytest.mark.parametrize("path", CASES, ids=lambda p: os.path.basename(p))
+def test_pipeline_pinned(built, path):
+    g = load(path)
+    r = T.o_process(g["xyzi"], g["ring"], seg_cfg(g), lp.PipelineConfig.default(), libm=T.LIBM_HOST)
+    assert np.array_equal(r.seg_labels, g["pipe_seg"])
+    assert np.array_equal(r.cluster_labels, g["pipe_cluster"])
+    assert np.array_equal(r.hull_offsets, g["pipe_hull_offsets"])
+    assert np.array_equal(r.hull_indices, g["pipe_hull_indices"])
+    assert np.array_equal(r.z_min, g["pipe_zmin"]) and np.array_equal(r.z_max, g["pipe_zmax"])
+    for b, row in zip(r.obb_calipers, g["pipe_calipers"]):
+        assert T.boxes_identical(b, box_from(row))
+    for b, row in zip(r.obb_pca, g["pipe_pca"]):
+        assert T.box_corner_set_close(b, box_from(row), 1e-9)
+
+
+@pytest.mark.parametrize("path", CASES, ids=lambda p: os.path.basename(p))
+def test_dror_kdtree_pinned(built, path):
+    """The reference kd-tree search keeps its traversal stack across queries (kdtree.hpp:339-397);
+    the oracle's kd-tree mode reproduces that exactly, in input order and shuffled."""
+    g = load(path)
+    x = np.ascontiguousarray(g["xyzi"][:, :3])
+    perm = g["dror_perm"]
+    for tag, c in (("default", lp.NoiseRemoverConfig.default()),
+                   ("dense", lp.NoiseRemoverConfig(3 * 0.17 * np.pi / 180.0, 0.1, 3))):
+        assert np.array_equal(T.o_noise(x, c, T.DROR_KDTREE), g["dror_" + tag])
+        assert np.array_equal(T.o_noise(np.ascontiguousarray(x[perm]), c, T.DROR_KDTREE), g["dror_shuffled_" + tag])
+
+
+def test_polygons_pinned(built):
+    g = load(os.path.join(T.GOLDEN, "polygons.npz"))
+    off = np.concatenate([[0], np.cumsum(g["sizes"])])
+    hoff = np.concatenate([[0], np.cumsum(g["hull_sizes"])])
+    poff = np.concatenate([[0], np.cumsum(g["pair_sizes"])])
+    for t in range(len(g["sizes"])):
+        pts = g["points"][off[t]:off[t + 1]]
+        h = T.o_hull(pts)
+        want = g["hulls"][hoff[t]:hoff[t + 1]]
+        # identical hull point sequences; indices identical where no duplicate points exist
+        assert np.array_equal(pts[h], pts[want])
+        if len(np.unique(pts, axis=0)) == len(pts):
+            assert np.array_equal(h, want)
+        hp = pts[want]
+        if len(hp) >= 2:
+            assert np.array_equal(T.o_antipodal(hp), g["pairs"][poff[t]:poff[t + 1]])
+        assert T.boxes_identical(T.o_calipers(hp), box_from(g["calipers"][t]))
+        assert T.box_corner_set_close(T.o_pca(hp)[0], box_from(g["pca"][t]), 1e-9)
+
+
+# ------------------------------------------------------------------ RANSAC index stream restatement
+class Mt19937:
+    """MT19937 (Matsumoto & Nishimura 1998), as restated in the device kernel."""
+
+    def __init__(self, seed):
+        self.mt = [0] * 624
+        self.mt[0] = seed
+        for i in range(1, 624):
+            self.mt[i] = (1812433253 * (self.mt[i - 1] ^ (self.mt[i - 1] >> 30)) + i) & 0xFFFFFFFF
+        self.idx = 624
+
+    def next(self):
+        if self.idx >= 624:
+            for i in range(624):
+                y = (self.mt[i] & 0x80000000) | (self.mt[(i + 1) % 624] & 0x7FFFFFFF)
+                self.mt[i] = self.mt[(i + 397) % 624] ^ (y >> 1) ^ (0x9908B0DF if y & 1 else 0)
+            self.idx = 0
+        y = self.mt[self.idx]
+        self.idx += 1
+        y ^= y >> 11
+        y ^= (y << 7) & 0x9D2C5680
+        y ^= (y << 15) & 0xEFC60000
+        y ^= y >> 18
+        return y & 0xFFFFFFFF
+
+    def bounded(self, rng):
+        """Lemire's nearly divisionless draw in [0, rng)."""
+        m = self.next() * rng
+        low = m & 0xFFFFFFFF
+        if low < rng:
+            t = ((1 << 32) - rng) % rng
+            while low < t:
+                m = self.next() * rng
+                low = m & 0xFFFFFFFF
+        return m >> 32
+
+
+def test_ransac_index_stream_matches_libstdcxx():
+    """The device RANSAC draws (MT19937 + Lemire bounded draw) equal std::mt19937{42} with
+    std::uniform_int_distribution<uint32_t>{0, n-1} (segmenter.cpp:369-386) as recorded from the
+    reference toolchain."""
+    g = load(os.path.join(T.GOLDEN, "ransac_stream.npz"))
+    for n, want in zip(g["n"], g["draws"]):
+        n = int(n)
+        if n > 0xFFFFFFFF:
+            continue
+        gen = Mt19937(42)
+        got = []
+        for _ in range(60):
+            a = gen.bounded(n)
+            b = gen.bounded(n)
+            while b == a:
+                b = gen.bounded(n)
+            got += [a, b]
+        assert got == want.tolist(), n
