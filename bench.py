@@ -1,0 +1,318 @@
+"""Benchmark of the per-scan perception path (segmentation -> clustering -> hull + OBB).
+
+Workload "batch64_mixed": 64 seeded synthetic scans of uneven size in one launch sequence (ring
+count {32,64,128}, azimuth bins {1024,2048,4096}, return rate U[0.3,1], 10-200 obstacles, flat /
+sloped / undulating ground), ~8.3M float32 XYZI points; one step = the whole pipeline over the
+batch. `value` is device-resident scans/s of the batched form (captured CUDA graph), `e2e` the same
+metric through the C ABI with host buffers (H2D + D2H inside the timed region). The plain form (one
+scan per launch sequence) is timed on the same scans for the batched/plain ratio, and the CPU
+oracle (a restatement of the reference path) on a bounded sample of the same workload.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Multi-GPU (torchrun): replicas, one independent batch per rank (scans do not shard a step).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "lidar-processing-v2_gb300"))
+sys.path.insert(0, os.path.join(REPO, "tests"))
+
+WORKLOAD = 3
+NSCANS = 64
+METRIC = "scans/s (batched, 64 mixed scans, exact labels)"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def dist_init(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def dist_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_workload():
+    import lp_testlib as T
+
+    data = [T.synth_scan(WORKLOAD, i) for i in range(NSCANS)]
+    return data
+
+
+def cpu_baseline(data, budget_s=20.0, threads=None):
+    """The oracle (CPU restatement of the reference path) over scans of the same workload, one
+    scan per thread (the reference objects are not thread-safe, so each thread runs its own)."""
+    import lp_testlib as T
+    import lidar_gb300 as lp
+    from concurrent.futures import ThreadPoolExecutor
+
+    threads = threads or (os.cpu_count() or 1)
+    pipe = lp.PipelineConfig.default()
+    T.oracle()
+    done = []
+    t0 = time.perf_counter()
+
+    def work(k):
+        x, ring, cfg = data[k % len(data)]
+        T.o_process(x, ring, cfg, pipe)
+        return len(x)
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        k = 0
+        while time.perf_counter() - t0 < budget_s and k < 4 * len(data):
+            batch = list(range(k, k + threads))
+            done += list(ex.map(work, batch))
+            k += threads
+    dt = time.perf_counter() - t0
+    return {"value": len(done) / dt, "unit": "scans/s", "cores": threads, "kind": "port",
+            "sample": f"{len(done)} scans of the batch64_mixed workload ({sum(done)} points) through the CPU oracle "
+                      f"restatement of the reference path, {threads} threads, {dt:.1f} s"}
+
+
+def kernel_profile(batch):
+    prof = batch.profile()
+    agg = {}
+    for name, ms in prof:
+        a = agg.setdefault(name, [0, 0.0])
+        a[0] += 1
+        a[1] += ms
+    return prof, agg
+
+
+def run_reference_arm(args, rank, world):
+    data = make_workload()
+    if rank != 0:
+        return
+    budget = max(10.0, min(120.0, 5.0 * args.steps))
+    cb = cpu_baseline(data, budget_s=budget)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "scans/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch64_mixed", "scans": NSCANS, "generator_seed": "1000*3+scan"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "scans/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    dist = dist_init(world)
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        barrier(dist)
+        return
+
+    import lidar_gb300 as lp
+
+    ctx = lp.Context(local)
+    data = make_workload()
+    xs, rings, cfgs = [d[0] for d in data], [d[1] for d in data], [d[2] for d in data]
+    pipe = lp.PipelineConfig.default()
+    npts = sum(len(x) for x in xs)
+    batch = lp.PreparedBatch(ctx, xs, pipe, cfgs, rings)
+
+    # per-kernel profile of one un-captured execution (dominant kernel for the roofline)
+    batch.execute()
+    batch.synchronize()
+    prof, agg = kernel_profile(batch)
+    kernels_per_step = sum(1 for n, _ in prof if n != "k_scan") + 3 * sum(1 for n, _ in prof if n == "k_scan")
+    top = max(agg.items(), key=lambda kv: kv[1][1])
+    res = batch.download()
+    n_obs = sum(r.n_obstacles for r in res)
+    n_clusters = sum(r.n_clusters for r in res)
+    n_clustered = sum(int((r.cluster_labels >= 0).sum()) for r in res)
+    n_hull = sum(len(r.hull_indices) for r in res)
+
+    batch.capture_graph()
+    for _ in range(args.warmup):
+        batch.execute()
+    batch.synchronize()
+    barrier(dist)
+    with ClockSampler(local) as clocks:
+        step_ms = []
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step_ms.append(batch.time(1, flush_l2=False))
+        wall = time.perf_counter() - t0
+    barrier(dist)
+    dev_ms = sum(step_ms)
+    dev_ms_max = dist_max(dist, dev_ms)
+    value = world * NSCANS * args.steps / (dev_ms_max / 1e3)
+
+    # the dominant kernel's launches timed with events on the context stream (roofline)
+    top_name = top[0]
+    prof2, agg2 = kernel_profile(batch)
+    top_ms = agg2[top_name][1] / agg2[top_name][0]
+    alg = {
+        "k_hull": 8 * n_clustered + 4 * n_hull + 64 * n_clusters,
+        "k_jcp_rows": 20 * npts,
+        "k_obs_gather": 20 * n_obs,
+    }
+    alg_bytes = alg.get(top_name, 20 * npts)
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (top_ms / 1e3) / 1e9
+
+    # plain form: one scan per launch sequence, device-resident, no graph
+    plain = []
+    for i in range(min(NSCANS, 32)):
+        pb = lp.PreparedBatch(ctx, [xs[i]], pipe, [cfgs[i]], [rings[i]])
+        pb.execute()
+        pb.synchronize()
+        plain.append(pb.time(3, flush_l2=True))
+        pb.close()
+    plain_ms = float(np.mean(plain))
+
+    # end to end through the C ABI with host buffers
+    e2e_times = []
+    res_e2e = None
+    for it in range(max(2, args.steps // 4) + 1):
+        t1 = time.perf_counter()
+        res_e2e = lp.process_batch(ctx, xs, pipe, cfgs, rings)
+        dt = time.perf_counter() - t1
+        if it > 0:
+            e2e_times.append(dt)
+    e2e_s = dist_max(dist, float(np.mean(e2e_times)))
+    h2d = sum(x.nbytes + r.nbytes for x, r in zip(xs, rings))
+    d2h = sum(len(r.seg_labels) * 9 + 4 * (len(r.hull_offsets) + len(r.hull_indices)) + 8 * r.n_clusters
+              + 2 * 72 * r.n_clusters for r in res_e2e)
+
+    cb = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_baseline(data, budget_s=15.0)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "scans/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch64_mixed", "scans": NSCANS, "points": npts, "obstacles": n_obs,
+                       "clusters": n_clusters, "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2 (133 MB XYZI, multi-GB working set)",
+                       "graph": "captured CUDA graph per batch"},
+            "points_per_s": world * npts * args.steps / (dev_ms_max / 1e3),
+            "plain": {"ms_per_scan": plain_ms, "scans_per_s": 1e3 / plain_ms,
+                      "p50_ms": float(np.percentile(plain, 50)), "p99_ms": float(np.percentile(plain, 99)),
+                      "scans": len(plain)},
+            "batched_over_plain": (value / world) / (1e3 / plain_ms),
+            "batch_latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+            "e2e": {"value": world * NSCANS / e2e_s, "unit": "scans/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(kernels_per_step * args.steps),
+            "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": top_ms},
+            "kernel_share": {k: round(v[1] / sum(a[1] for a in agg2.values()), 4)
+                             for k, v in sorted(agg2.items(), key=lambda kv: -kv[1][1])[:8]},
+            "clocks": clocks.summary(),
+            "cpu_baseline": cb,
+            "wall_s": wall,
+        }
+        print(json.dumps(line))
+    batch.close()
+    ctx.close()
+    barrier(dist)
+
+
+if __name__ == "__main__":
+    main()

@@ -386,6 +386,7 @@ size_t carve(lp_batch& B, char* base)
         put(b.hs_stack, static_cast<size_t>(2) * N + 2ull * b.ncl + 8);
         put(b.hs_pts, static_cast<size_t>(N) + 8);
         put(b.hs_pairs, static_cast<size_t>(4) * N + 16ull * b.ncl + 16);
+        put(b.queue, 8);
     }
     return c.off + 4096;
 }
@@ -515,6 +516,7 @@ lp_status execute(lp_context* ctx, lp_batch& B)
     if (R.stages & ST_HULL)
     {
         LP_CUDA(ctx, cudaMemsetAsync(b.hull_cnt, 0, (static_cast<size_t>(b.ncl) + 1) * 4, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.queue, 0, 8 * 4, st));
         launch_polygons(L, b, B.hb, (R.stages & ST_OBB) ? 1 : 0);
     }
     if (R.stages & (ST_SEG | ST_CLUSTER | ST_ALL_OBS))
@@ -784,6 +786,7 @@ lp_status lp_context_create(int32_t device, lp_context** out)
         delete ctx;
         return LP_ERR_CUDA;
     }
+    init_kernel_attributes();
     *out = ctx;
     return LP_OK;
 }

@@ -137,6 +137,7 @@ struct BatchDev
     int32_t* hs_stack;    // monotone-chain stack, at 2 * cl_start + 2 * cluster
     double2* hs_pts;      // hull vertices as FP64, at cl_start
     int2* hs_pairs;       // antipodal pairs, at 4 * cl_start + 16 * cluster
+    uint32_t* queue;      // [0] clusters in the batch, [1] hull work-queue head
 
     // ---- DROR --------------------------------------------------------------------------------
     uint32_t ndhash;           // grid-cell hash slots

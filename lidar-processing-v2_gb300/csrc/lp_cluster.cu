@@ -70,26 +70,50 @@ __global__ void k_obs_state(BatchDev b)
 __global__ void k_obs_gather(BatchDev b)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.npts || b.seg_label[i] != LP_LABEL_OBSTACLE)
-        return;
-    const uint32_t o = b.obs_flag[i];
-    const int s = scan_of_point(b, i);
-    ScanState& st = b.state[s];
-    const float4 p = b.pts[i];
-    b.obs_pts[o] = p;
-    b.obs_pt[o] = static_cast<int32_t>(i);
-    float az = lpm::cr_atan2f(p.y, p.x);
-    az = (az < 0) ? (az + kTwoPiF) : az;
-    const float d2 = p.x * p.x + p.y * p.y;
-    const float d = sqrtf(d2);
-    const float r = sqrtf(d2 + p.z * p.z);
-    const float el = lpm::cr_atanf(p.z / d) + kPi2F;
-    b.obs_r[o] = r;
-    b.obs_a[o] = az;
-    b.obs_e[o] = el;
-    atomicMax(&st.max_r_bits, r > 0.0f ? __float_as_uint(r) : 0u);
-    atomicMax(&st.max_a_bits, az > 0.0f ? __float_as_uint(az) : 0u);
-    atomicMax(&st.max_e_bits, el > 0.0f ? __float_as_uint(el) : 0u);
+    const bool valid = i < b.npts && b.seg_label[i] == LP_LABEL_OBSTACLE;
+    const int s = valid ? scan_of_point(b, i) : -1;
+    uint32_t rb = 0u, ab = 0u, eb = 0u;
+    if (valid)
+    {
+        const uint32_t o = b.obs_flag[i];
+        const float4 p = b.pts[i];
+        b.obs_pts[o] = p;
+        b.obs_pt[o] = static_cast<int32_t>(i);
+        float az = lpm::cr_atan2f(p.y, p.x);
+        az = (az < 0) ? (az + kTwoPiF) : az;
+        const float d2 = p.x * p.x + p.y * p.y;
+        const float d = sqrtf(d2);
+        const float r = sqrtf(d2 + p.z * p.z);
+        const float el = lpm::cr_atanf(p.z / d) + kPi2F;
+        b.obs_r[o] = r;
+        b.obs_a[o] = az;
+        b.obs_e[o] = el;
+        rb = r > 0.0f ? __float_as_uint(r) : 0u; // non-negative floats order like their bits
+        ab = az > 0.0f ? __float_as_uint(az) : 0u;
+        eb = el > 0.0f ? __float_as_uint(el) : 0u;
+    }
+    // one atomic per warp when the warp's obstacle points belong to a single scan
+    const int smax = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(s + 1))) - 1;
+    if (__all_sync(0xffffffffu, s == smax || s < 0))
+    {
+        rb = __reduce_max_sync(0xffffffffu, rb);
+        ab = __reduce_max_sync(0xffffffffu, ab);
+        eb = __reduce_max_sync(0xffffffffu, eb);
+        if (lane_id() == 0 && smax >= 0)
+        {
+            ScanState& st = b.state[smax];
+            atomicMax(&st.max_r_bits, rb);
+            atomicMax(&st.max_a_bits, ab);
+            atomicMax(&st.max_e_bits, eb);
+        }
+    }
+    else if (valid)
+    {
+        ScanState& st = b.state[s];
+        atomicMax(&st.max_r_bits, rb);
+        atomicMax(&st.max_a_bits, ab);
+        atomicMax(&st.max_e_bits, eb);
+    }
 }
 
 __global__ void k_dims(BatchDev b)
@@ -181,9 +205,12 @@ __global__ void k_vox_count(BatchDev b)
         raise_err(&st, ERR_VOXEL_CAPACITY); // StaticUnorderedMap::insert throws (static_unordered_map.hpp:81)
 }
 
-__device__ uint32_t uf_find(uint32_t* parent, uint32_t x, ScanState* st)
+// Every parent pointer is strictly smaller than its index except at roots (links go from the
+// larger root to the smaller; path halving only shortens), so a find ends within x steps. The
+// per-thread budget bounds the total work anyway: exhausting it raises ERR_UF_TIMEOUT.
+__device__ uint32_t uf_find(uint32_t* parent, uint32_t x, ScanState* st, int& budget)
 {
-    for (int it = 0; it < kMaxIters; ++it)
+    while (budget-- > 0)
     {
         const uint32_t p = ld_volatile(&parent[x]);
         if (p == x)
@@ -197,12 +224,14 @@ __device__ uint32_t uf_find(uint32_t* parent, uint32_t x, ScanState* st)
     return x;
 }
 
-__device__ void uf_union(uint32_t* parent, uint32_t a, uint32_t c, ScanState* st)
+__device__ void uf_union(uint32_t* parent, uint32_t a, uint32_t c, ScanState* st, int& budget)
 {
-    for (int it = 0; it < kMaxIters; ++it)
+    while (budget > 0)
     {
-        a = uf_find(parent, a, st);
-        c = uf_find(parent, c, st);
+        a = uf_find(parent, a, st, budget);
+        c = uf_find(parent, c, st, budget);
+        if (budget <= 0)
+            return;
         if (a == c)
             return;
         if (a > c)
@@ -251,6 +280,7 @@ __global__ void k_uf_hook(BatchDev b)
     const int32_t r = key % nr;
     const int32_t a = (key / nr) % na;
     const int32_t e = key / (nr * na);
+    int budget = kMaxIters;
     for (int de = -1; de <= 1; ++de)
         for (int da = -1; da <= 1; ++da)
             for (int dr = -1; dr <= 1; ++dr)
@@ -270,7 +300,7 @@ __global__ void k_uf_hook(BatchDev b)
                     continue;
                 const uint32_t u = b.hvid[nslot];
                 if (u > v)
-                    uf_union(b.parent, v, u, st);
+                    uf_union(b.parent, v, u, st, budget);
             }
 }
 
@@ -281,8 +311,8 @@ __global__ void k_uf_flatten(BatchDev b)
         return;
     const uint32_t slot = b.vslot[v];
     const int s = scan_of_hash(b, slot);
-    const uint32_t root = uf_find(b.parent, v, &b.state[s]);
-    __syncwarp();
+    int budget = kMaxIters;
+    const uint32_t root = uf_find(b.parent, v, &b.state[s], budget);
     b.parent[v] = root;
 }
 

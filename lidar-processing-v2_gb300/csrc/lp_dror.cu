@@ -53,15 +53,29 @@ __global__ void k_state_init(BatchDev b, int noise)
 __global__ void k_dror_r2(BatchDev b)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.nsrc)
-        return;
-    const int s = scan_of_src(b, i);
-    const ScanDev& sd = b.scans[s];
-    const float4 p = b.src[i];
-    const double rho2 = static_cast<double>((p.x * p.x) + (p.y * p.y));
-    const float r2 = fmaxf(__double2float_rn(sd.dror_s2 * rho2), sd.dror_rmin2);
-    b.dr2[i] = r2;
-    atomicMax(&b.state[s].dmax_r2_bits, __float_as_uint(r2));
+    const bool valid = i < b.nsrc;
+    const int s = valid ? scan_of_src(b, i) : -1;
+    uint32_t bits = 0u;
+    if (valid)
+    {
+        const ScanDev& sd = b.scans[s];
+        const float4 p = b.src[i];
+        const double rho2 = static_cast<double>((p.x * p.x) + (p.y * p.y));
+        const float r2 = fmaxf(__double2float_rn(sd.dror_s2 * rho2), sd.dror_rmin2);
+        b.dr2[i] = r2;
+        bits = __float_as_uint(r2);
+    }
+    const int smax = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(s + 1))) - 1;
+    if (__all_sync(0xffffffffu, s == smax || s < 0))
+    {
+        bits = __reduce_max_sync(0xffffffffu, bits);
+        if (lane_id() == 0 && smax >= 0)
+            atomicMax(&b.state[smax].dmax_r2_bits, bits);
+    }
+    else if (valid)
+    {
+        atomicMax(&b.state[s].dmax_r2_bits, bits);
+    }
 }
 
 __global__ void k_dror_cell(BatchDev b)

@@ -349,47 +349,65 @@ __device__ void block_sort_global(HPt<T>* a, uint32_t n)
         }
 }
 
+constexpr int kDirs = 16;         // extreme-point directions of the initial polygon
+constexpr int kPolyCap = 256;     // refined polygon capacity
+constexpr int kRefineRounds = 12; // farthest-point insertion rounds
+constexpr uint32_t kBigCluster = 2048;
+
 struct HullSmem
 {
     HPt<float> cand[kHullSmem];
     int stack[2 * kHullSmem + 2];
     double2 hp[kHullSmem];
-    unsigned long long ext[4][kHullThreads / 32];
+    uint32_t hkey[kHullSmem]; // hull vertex member keys, sorted
+    int32_t diff[kHullSmem + 1];
+    float2 poly[kPolyCap];
+    float2 poly2[kPolyCap];
+    unsigned long long pkey[kPolyCap];
+    unsigned long long ext[kDirs][kHullThreads / 32];
+    float2 dirs[kDirs];
     float zr[2][kHullThreads / 32];
+    int npoly;
+    int grew;
     int ncand;
     int nhull;
+    uint32_t work;
 };
 
-// One CTA per cluster of the batch.
-__global__ void __launch_bounds__(kHullThreads) k_hull(BatchDev b, int compute_obb)
+__device__ __forceinline__ unsigned long long fkey_payload(float v, uint32_t i)
 {
-    __shared__ HullSmem sm;
-    const uint32_t g = blockIdx.x;
-    const int s = find_scan(b.nscan, g, [&](int q) { return b.scans[q].cl_off; });
-    const ScanDev& sd = b.scans[s];
+    return (static_cast<unsigned long long>(ford(v)) << 32) | i;
+}
+
+// Cluster g of scan s: z range, hull (local indices into hull_tmp at cl_start), boxes.
+__device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int compute_obb)
+{
     ScanState* st = &b.state[s];
-    const uint32_t k = g - sd.cl_off;
-    if (k >= st->n_clusters)
-        return;
     const uint32_t n = b.cl_cnt[g];
     const uint32_t start = b.cl_start[g];
     const uint32_t* mem = b.members + start;
     const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0)
+        sm.ncand = 0;
 
-    // 1. z range and extreme points
+    // 1. z range and the extreme member in each of kDirs directions (float projections: any
+    //    member is a valid polygon vertex, exactness is not needed here)
     float zmn = INFINITY, zmx = -INFINITY;
-    unsigned long long eL = ~0ull, eR = 0ull, eB = ~0ull, eT = 0ull;
+    unsigned long long ext[kDirs];
+#pragma unroll
+    for (int d = 0; d < kDirs; ++d)
+        ext[d] = 0ull;
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
     {
         const float4 p = b.obs_pts[mem[i]];
         zmn = fminf(zmn, p.z);
         zmx = fmaxf(zmx, p.z);
-        const unsigned long long kxy = (static_cast<unsigned long long>(ford(p.x)) << 32) | ford(p.y);
-        const unsigned long long kyx = (static_cast<unsigned long long>(ford(p.y)) << 32) | ford(p.x);
-        eL = kxy < eL ? kxy : eL;
-        eR = kxy > eR ? kxy : eR;
-        eB = kyx < eB ? kyx : eB;
-        eT = kyx > eT ? kyx : eT;
+#pragma unroll
+        for (int d = 0; d < kDirs; ++d)
+        {
+            const unsigned long long key = fkey_payload(p.x * sm.dirs[d].x + p.y * sm.dirs[d].y, i);
+            ext[d] = key > ext[d] ? key : ext[d];
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
@@ -397,35 +415,47 @@ __global__ void __launch_bounds__(kHullThreads) k_hull(BatchDev b, int compute_o
         zmn = fminf(zmn, __shfl_xor_sync(0xffffffffu, zmn, o));
         zmx = fmaxf(zmx, __shfl_xor_sync(0xffffffffu, zmx, o));
     }
-    eL = warp_min64(eL);
-    eR = warp_max64(eR);
-    eB = warp_min64(eB);
-    eT = warp_max64(eT);
+#pragma unroll
+    for (int d = 0; d < kDirs; ++d)
+        ext[d] = warp_max64(ext[d]);
     if (lane == 0)
     {
-        sm.ext[0][warp] = eL;
-        sm.ext[1][warp] = eR;
-        sm.ext[2][warp] = eB;
-        sm.ext[3][warp] = eT;
+#pragma unroll
+        for (int d = 0; d < kDirs; ++d)
+            sm.ext[d][warp] = ext[d];
         sm.zr[0][warp] = zmn;
         sm.zr[1][warp] = zmx;
     }
-    if (threadIdx.x == 0)
-        sm.ncand = 0;
     __syncthreads();
     if (threadIdx.x == 0)
     {
+        float a = sm.zr[0][0], c = sm.zr[1][0];
         for (int w = 1; w < kHullThreads / 32; ++w)
         {
-            sm.ext[0][0] = sm.ext[0][w] < sm.ext[0][0] ? sm.ext[0][w] : sm.ext[0][0];
-            sm.ext[1][0] = sm.ext[1][w] > sm.ext[1][0] ? sm.ext[1][w] : sm.ext[1][0];
-            sm.ext[2][0] = sm.ext[2][w] < sm.ext[2][0] ? sm.ext[2][w] : sm.ext[2][0];
-            sm.ext[3][0] = sm.ext[3][w] > sm.ext[3][0] ? sm.ext[3][w] : sm.ext[3][0];
-            sm.zr[0][0] = fminf(sm.zr[0][0], sm.zr[0][w]);
-            sm.zr[1][0] = fmaxf(sm.zr[1][0], sm.zr[1][w]);
+            a = fminf(a, sm.zr[0][w]);
+            c = fmaxf(c, sm.zr[1][w]);
         }
-        b.cl_zmin[g] = sm.zr[0][0];
-        b.cl_zmax[g] = sm.zr[1][0];
+        b.cl_zmin[g] = a;
+        b.cl_zmax[g] = c;
+        // initial polygon: extreme members in direction order (counter-clockwise), repeats dropped
+        int np = 0;
+        uint32_t prev = 0xffffffffu;
+        for (int d = 0; d < kDirs; ++d)
+        {
+            unsigned long long best = sm.ext[d][0];
+            for (int w = 1; w < kHullThreads / 32; ++w)
+                best = sm.ext[d][w] > best ? sm.ext[d][w] : best;
+            const uint32_t i = static_cast<uint32_t>(best & 0xffffffffull);
+            if (n > 0 && i != prev)
+            {
+                const float4 p = b.obs_pts[mem[i]];
+                sm.poly[np++] = make_float2(p.x, p.y);
+                prev = i;
+            }
+        }
+        if (np > 1 && sm.poly[np - 1].x == sm.poly[0].x && sm.poly[np - 1].y == sm.poly[0].y)
+            --np;
+        sm.npoly = np;
     }
     __syncthreads();
 
@@ -446,39 +476,117 @@ __global__ void __launch_bounds__(kHullThreads) k_hull(BatchDev b, int compute_o
                 b.obb_p[g] = z;
             }
         }
+        __syncthreads();
         return;
     }
 
-    // 2. Akl-Toussaint prefilter against the quadrilateral L -> B -> R -> T
-    const double Lx = funord(static_cast<uint32_t>(sm.ext[0][0] >> 32)), Ly = funord(static_cast<uint32_t>(sm.ext[0][0]));
-    const double Rx = funord(static_cast<uint32_t>(sm.ext[1][0] >> 32)), Ry = funord(static_cast<uint32_t>(sm.ext[1][0]));
-    const double By = funord(static_cast<uint32_t>(sm.ext[2][0] >> 32)), Bx = funord(static_cast<uint32_t>(sm.ext[2][0]));
-    const double Ty = funord(static_cast<uint32_t>(sm.ext[3][0] >> 32)), Tx = funord(static_cast<uint32_t>(sm.ext[3][0]));
+    // 2. refine the polygon: insert the member farthest outside each edge (Quickhull step),
+    //    while it grows and fits. Every vertex is a member, so the polygon stays inside the hull.
+    for (int round = 0; round < kRefineRounds; ++round)
+    {
+        const int np = sm.npoly;
+        if (np < 3)
+            break;
+        for (int e = threadIdx.x; e < np; e += blockDim.x)
+            sm.pkey[e] = 0ull;
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        {
+            const float4 p = b.obs_pts[mem[i]];
+            for (int e = 0; e < np; ++e)
+            {
+                const float2 a = sm.poly[e], c = sm.poly[(e + 1 == np) ? 0 : e + 1];
+                const float ex = c.x - a.x, ey = c.y - a.y, qx = p.x - a.x, qy = p.y - a.y;
+                const float cr = ex * qy - ey * qx; // < 0: right of the edge, outside
+                const float tol = 1e-6f * (fabsf(ex) + fabsf(ey)) * (fabsf(qx) + fabsf(qy));
+                if (cr < -tol)
+                {
+                    const unsigned long long key = fkey_payload(-cr, i);
+                    if (key > sm.pkey[e])
+                        atomicMax(&sm.pkey[e], key);
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            int add = 0;
+            for (int e = 0; e < np; ++e)
+                add += (sm.pkey[e] != 0ull);
+            sm.grew = 0;
+            if (add > 0 && np + add <= kPolyCap)
+            {
+                int w = 0;
+                for (int e = 0; e < np; ++e)
+                {
+                    sm.poly2[w++] = sm.poly[e];
+                    if (sm.pkey[e] != 0ull)
+                    {
+                        const float4 p = b.obs_pts[mem[static_cast<uint32_t>(sm.pkey[e] & 0xffffffffull)]];
+                        sm.poly2[w++] = make_float2(p.x, p.y);
+                    }
+                }
+                for (int e = 0; e < w; ++e)
+                    sm.poly[e] = sm.poly2[e];
+                sm.npoly = w;
+                sm.grew = 1;
+            }
+        }
+        __syncthreads();
+        if (!sm.grew)
+            break;
+    }
+
+    // 3. candidates: members not strictly inside the polygon by a relative margin far above
+    //    double rounding (a hull vertex is never strictly inside a polygon of members)
+    const int npf = sm.npoly;
     HPt<float>* gs = reinterpret_cast<HPt<float>*>(b.hs_cand) + 2ull * start; // capacity 2n >= next_pow2(n)
+    auto inside = [&](double px, double py) {
+        if (npf < 3)
+            return false;
+        for (int d = 0; d < npf; ++d)
+        {
+            const float2 a = sm.poly[d], c = sm.poly[(d + 1 == npf) ? 0 : d + 1];
+            if (!left_strict(a.x, a.y, c.x, c.y, px, py))
+                return false;
+        }
+        return true;
+    };
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
     {
         const uint32_t o = mem[i];
         const float4 p = b.obs_pts[o];
-        const double px = p.x, py = p.y;
-        const bool inside = left_strict(Lx, Ly, Bx, By, px, py) && left_strict(Bx, By, Rx, Ry, px, py) &&
-                            left_strict(Rx, Ry, Tx, Ty, px, py) && left_strict(Tx, Ty, Lx, Ly, px, py);
-        if (!inside)
+        if (!inside(p.x, p.y))
         {
             const int pos = atomicAdd(&sm.ncand, 1);
-            const HPt<float> c{p.x, p.y, o};
             if (pos < kHullSmem)
-                sm.cand[pos] = c;
-            gs[pos] = c;
+                sm.cand[pos] = HPt<float>{p.x, p.y, o};
         }
     }
     __syncthreads();
     const int m = sm.ncand;
     const bool small = m <= kHullSmem;
+    if (!small)
+    {
+        __syncthreads();
+        if (threadIdx.x == 0)
+            sm.ncand = 0;
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        {
+            const uint32_t o = mem[i];
+            const float4 p = b.obs_pts[o];
+            if (!inside(p.x, p.y))
+                gs[atomicAdd(&sm.ncand, 1)] = HPt<float>{p.x, p.y, o};
+        }
+        __syncthreads();
+    }
+
+    // 4. sort by (x, y, input order) and the monotone chain
     const HPt<float>* C;
     int* H;
     if (small)
     {
-        // m <= kHullSmem (a power of two), so the padded size fits the shared array
         const uint32_t np2 = next_pow2(static_cast<uint32_t>(m));
         for (uint32_t i = m + threadIdx.x; i < np2; i += blockDim.x)
             sm.cand[i] = HPt<float>{INFINITY, INFINITY, 0xffffffffu};
@@ -499,63 +607,169 @@ __global__ void __launch_bounds__(kHullThreads) k_hull(BatchDev b, int compute_o
     __syncthreads();
     const int h = sm.nhull;
 
-    // 4. local index of each hull vertex = rank among the members by input order
-    for (int j = static_cast<int>(warp); j < h; j += kHullThreads / 32)
+    // 5. local index of each hull vertex = number of members before it in input order
+    if (h <= kHullSmem)
     {
-        const uint32_t key = C[H[j]].key;
-        uint32_t cnt = 0;
-        for (uint32_t base = 0; base < n; base += 32)
+        for (int j = threadIdx.x; j < h; j += blockDim.x)
+            sm.hkey[j] = C[H[j]].key;
+        const uint32_t np2 = next_pow2(static_cast<uint32_t>(h));
+        for (uint32_t j = h + threadIdx.x; j < np2; j += blockDim.x)
+            sm.hkey[j] = 0xffffffffu;
+        for (int j = threadIdx.x; j <= h; j += blockDim.x)
+            sm.diff[j] = 0;
+        __syncthreads();
+        block_bitonic_sort(sm.hkey, np2, [](uint32_t a, uint32_t c) { return a < c; });
+        // member o adds 1 to every hull vertex with a larger key: diff[upper_bound(o)] += 1
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
         {
-            const uint32_t i = base + lane;
-            const bool lt = (i < n) && (mem[i] < key);
-            cnt += __popc(__ballot_sync(0xffffffffu, lt));
+            const uint32_t o = mem[i];
+            int lo = 0, hi = h;
+            while (lo < hi)
+            {
+                const int mid = (lo + hi) >> 1;
+                if (sm.hkey[mid] > o)
+                    hi = mid;
+                else
+                    lo = mid + 1;
+            }
+            if (lo < h)
+                atomicAdd(&sm.diff[lo], 1);
         }
-        if (lane == 0)
-            hull_dst[j] = static_cast<int32_t>(cnt);
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            int run = 0;
+            for (int t = 0; t < h; ++t)
+            {
+                run += sm.diff[t];
+                sm.diff[t] = run; // members with a smaller key than hkey[t]
+            }
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < h; j += blockDim.x)
+        {
+            const uint32_t key = C[H[j]].key;
+            int lo = 0, hi = h - 1;
+            while (lo < hi)
+            {
+                const int mid = (lo + hi) >> 1;
+                if (sm.hkey[mid] < key)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            hull_dst[j] = sm.diff[lo];
+        }
+    }
+    else
+    {
+        for (int j = static_cast<int>(warp); j < h; j += kHullThreads / 32)
+        {
+            const uint32_t key = C[H[j]].key;
+            uint32_t cnt = 0;
+            for (uint32_t base = 0; base < n; base += 32)
+            {
+                const uint32_t i = base + lane;
+                const bool lt = (i < n) && (mem[i] < key);
+                cnt += __popc(__ballot_sync(0xffffffffu, lt));
+            }
+            if (lane == 0)
+                hull_dst[j] = static_cast<int32_t>(cnt);
+        }
     }
     if (threadIdx.x == 0)
         b.hull_cnt[g] = static_cast<uint32_t>(h);
 
-    // 5. boxes on the hull vertices (the hull is small; one warp)
-    if (!compute_obb)
-        return;
-    double2* P = (h <= kHullSmem) ? sm.hp : (b.hs_pts + start);
-    for (int j = threadIdx.x; j < h; j += blockDim.x)
-        P[j] = make_double2(static_cast<double>(C[H[j]].x), static_cast<double>(C[H[j]].y));
-    __syncthreads();
-    if (warp == 0)
+    // 6. boxes on the hull vertices (one warp)
+    if (compute_obb)
     {
-        int2* pairs = b.hs_pairs + 4ull * start + 16ull * g;
-        const int cap = 4 * h + 16;
-        int npairs = 0;
-        if (lane == 0)
-            npairs = antipodal_pairs(P, h, pairs, cap);
-        npairs = __shfl_sync(0xffffffffu, npairs, 0);
-        if (npairs > cap)
+        double2* P = (h <= kHullSmem) ? sm.hp : (b.hs_pts + start);
+        for (int j = threadIdx.x; j < h; j += blockDim.x)
+            P[j] = make_double2(static_cast<double>(C[H[j]].x), static_cast<double>(C[H[j]].y));
+        __syncthreads();
+        if (warp == 0)
         {
+            int2* pairs = b.hs_pairs + 4ull * start + 16ull * g;
+            const int cap = 4 * h + 16;
+            int npairs = 0;
             if (lane == 0)
-                raise_err(st, ERR_INTERNAL);
-            npairs = cap;
+                npairs = antipodal_pairs(P, h, pairs, cap);
+            npairs = __shfl_sync(0xffffffffu, npairs, 0);
+            if (npairs > cap)
+            {
+                if (lane == 0)
+                    raise_err(st, ERR_INTERNAL);
+                npairs = cap;
+            }
+            __syncwarp();
+            calipers_warp(P, h, pairs, npairs, &b.obb_c[g]);
+            if (lane == 0)
+                pca_box(P, h, &b.obb_p[g]);
         }
-        __syncwarp();
-        calipers_warp(P, h, pairs, npairs, &b.obb_c[g]);
-        if (lane == 0)
-            pca_box(P, h, &b.obb_p[g]);
+    }
+    __syncthreads();
+}
+
+// Work items: every cluster of the batch, big ones first (they bound the kernel's tail).
+// queue[2] counts big clusters listed from the front of `work`, queue[3] small ones from the back.
+__global__ void k_hull_worklist(BatchDev b, uint32_t* work)
+{
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= b.ncl)
+        return;
+    const int s = find_scan(b.nscan, g, [&](int q) { return b.scans[q].cl_off; });
+    if (g - b.scans[s].cl_off >= b.state[s].n_clusters)
+        return;
+    if (b.cl_cnt[g] > kBigCluster)
+        work[atomicAdd(&b.queue[2], 1u)] = g;
+    else
+        work[b.ncl - 1u - atomicAdd(&b.queue[3], 1u)] = g;
+}
+
+__device__ __forceinline__ uint32_t work_item(const BatchDev& b, const uint32_t* work, uint32_t w)
+{
+    const uint32_t nbig = b.queue[2];
+    return (w < nbig) ? work[w] : work[b.ncl - 1u - (w - nbig)];
+}
+
+// Persistent CTAs pull clusters from the work queue until it is empty.
+__global__ void __launch_bounds__(kHullThreads) k_hull(BatchDev b, int compute_obb, const uint32_t* work)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    HullSmem& sm = *reinterpret_cast<HullSmem*>(smraw);
+    if (threadIdx.x < kDirs)
+    {
+        const float a = 6.28318530717958647692f * static_cast<float>(threadIdx.x) / kDirs;
+        sm.dirs[threadIdx.x] = make_float2(cosf(a), sinf(a));
+    }
+    const uint32_t total = b.queue[2] + b.queue[3];
+    for (;;)
+    {
+        __syncthreads();
+        if (threadIdx.x == 0)
+            sm.work = atomicAdd(&b.queue[1], 1u);
+        __syncthreads();
+        const uint32_t w = sm.work;
+        if (w >= total)
+            break;
+        const uint32_t g = work_item(b, work, w);
+        const int s = find_scan(b.nscan, g, [&](int q) { return b.scans[q].cl_off; });
+        hull_one(b, sm, g, s, compute_obb);
     }
 }
 
 // Dense hull output: hull_cnt holds the exclusive scan (hull offsets over the batch).
-__global__ void k_hull_compact(BatchDev b)
+__global__ void k_hull_compact(BatchDev b, const uint32_t* work)
 {
-    const uint32_t g = blockIdx.x;
-    const int s = find_scan(b.nscan, g, [&](int q) { return b.scans[q].cl_off; });
-    const ScanDev& sd = b.scans[s];
-    if (g - sd.cl_off >= b.state[s].n_clusters)
-        return;
-    const uint32_t off = b.hull_cnt[g];
-    const uint32_t cnt = b.hull_cnt[g + 1] - off;
-    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x)
-        b.hull_out[off + i] = b.hull_tmp[b.cl_start[g] + i];
+    const uint32_t total = b.queue[2] + b.queue[3];
+    for (uint32_t w = blockIdx.x; w < total; w += gridDim.x)
+    {
+        const uint32_t g = work_item(b, work, w);
+        const uint32_t off = b.hull_cnt[g];
+        const uint32_t cnt = b.hull_cnt[g + 1] - off;
+        for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x)
+            b.hull_out[off + i] = b.hull_tmp[b.cl_start[g] + i];
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -606,9 +820,27 @@ __global__ void k_boxes_single(const double2* P, uint32_t n, int2* pairs, int ca
 void launch_polygons(Launcher& L, const BatchDev& b, const BatchHost& hb, int compute_obb)
 {
     (void)hb;
-    LP_LAUNCH(L, k_hull, b.ncl, kHullThreads, b, compute_obb);
+    // the work list reuses the cluster fill counters' scratch (cl_fill, ncl + 1 entries)
+    uint32_t* work = b.cl_fill;
+    LP_LAUNCH(L, k_hull_worklist, div_up(b.ncl, 256u), 256, b, work);
+    const int sms = sm_count();
+    LP_LAUNCH_SMEM(L, k_hull, static_cast<uint32_t>(sms * 2), kHullThreads, sizeof(HullSmem), b, compute_obb,
+                   static_cast<const uint32_t*>(work));
     L.scan(b.hull_cnt, b.hull_cnt, b.ncl + 1);
-    LP_LAUNCH(L, k_hull_compact, b.ncl, 128, b);
+    LP_LAUNCH(L, k_hull_compact, static_cast<uint32_t>(sms * 8), 128, b, static_cast<const uint32_t*>(work));
+}
+
+void init_kernel_attributes()
+{
+    cudaFuncSetAttribute(k_hull, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sizeof(HullSmem)));
+}
+
+int sm_count()
+{
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
 }
 
 void launch_hull_single(Launcher& L, const double2* pts, uint32_t n, void* scratch, int* stack, int32_t* out,

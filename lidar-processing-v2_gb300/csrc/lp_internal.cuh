@@ -86,6 +86,7 @@ struct ScanState
     uint32_t n_vox;
     uint32_t n_comp;
     uint32_t n_clusters;
+    uint32_t cl_base; // clusters of earlier scans (work-queue numbering)
     uint32_t n_hull;
     uint32_t pad[4];
 };

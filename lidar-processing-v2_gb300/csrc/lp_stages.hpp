@@ -77,6 +77,16 @@ struct Launcher
         end();
         note();
     }
+    template <typename K, typename... Args>
+    void launch_smem(const char* name, K kernel, uint32_t grid, uint32_t block, size_t smem, Args... args)
+    {
+        if (grid == 0)
+            return;
+        begin(name);
+        kernel<<<grid, block, smem, stream>>>(args...);
+        end();
+        note();
+    }
     void scan(const uint32_t* in, uint32_t* out, uint32_t n)
     {
         if (n == 0)
@@ -101,6 +111,12 @@ struct Launcher
 
 #define LP_LAUNCH(L, k, grid, block, ...) (L).launch(#k, k, grid, block, __VA_ARGS__)
 #define LP_LAUNCH2D(L, k, grid, block, ...) (L).launch2d(#k, k, grid, block, __VA_ARGS__)
+#define LP_LAUNCH_SMEM(L, k, grid, block, smem, ...) (L).launch_smem(#k, k, grid, block, smem, __VA_ARGS__)
+
+// One-time kernel attributes (dynamic shared memory opt-in); called when a context is created.
+void init_kernel_attributes();
+// Streaming multiprocessors of the current device (persistent grids are sized by it).
+int sm_count();
 
 // Host-side sizes of a batch (what the kernels' grids are sized by).
 struct BatchHost

@@ -128,7 +128,9 @@ class PipelineConfig(ctypes.Structure):
 
     @classmethod
     def default(cls, **kw):
-        c = cls(ClustererConfig.processor(), NoiseRemoverConfig.default(), 0, 0, 63, 0, 1)
+        """Processor settings; first_ring 0 means image_height - 1 (63 for the 64-ring sensor,
+        the reference's hard-coded start ring, dataloader.cpp:87)."""
+        c = cls(ClustererConfig.processor(), NoiseRemoverConfig.default(), 0, 0, 0, 0, 1)
         for k, v in kw.items():
             setattr(c, k, v)
         return c
