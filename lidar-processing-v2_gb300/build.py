@@ -74,6 +74,18 @@ def build_gpu(verbose=False, ptxas_info=False):
     return lib
 
 
+def build_example():
+    """C++ drop-in example (cpp/example_processor.cpp) linked against liblp_gpu.so."""
+    src = os.path.join(HERE, "cpp", "example_processor.cpp")
+    hdr = os.path.join(HERE, "cpp", "lidar_processing_gpu.hpp")
+    exe = os.path.join(HERE, "example_processor")
+    lib = os.path.join(HERE, "liblp_gpu.so")
+    if _stale(exe, [src, hdr, lib]):
+        _run(["g++", "-std=c++17", "-O2", "-I" + INCLUDE, "-I" + os.path.join(HERE, "cpp"), src, "-o", exe,
+              "-L" + HERE, "-llp_gpu", "-Wl,-rpath," + HERE])
+    return exe
+
+
 def build_synth():
     src = os.path.join(CSRC, "lp_synth.cpp")
     lib = os.path.join(HERE, "liblp_synth.so")
@@ -100,7 +112,9 @@ def build_oracle():
 def build_all(verbose=False):
     with ThreadPoolExecutor(max_workers=3) as ex:
         futs = [ex.submit(build_gpu, verbose), ex.submit(build_synth), ex.submit(build_oracle)]
-        return [f.result() for f in futs]
+        out = [f.result() for f in futs]
+    out.append(build_example())
+    return out
 
 
 if __name__ == "__main__":

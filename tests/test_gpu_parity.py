@@ -215,6 +215,36 @@ def test_edge_cases(ctx):
         compare_scan(r, T.o_process(xx, rr, cfg, pipe), f"n={len(xx)}")
 
 
+def test_cpp_dropin_example(ctx, tmp_path):
+    """The C++ drop-in classes (cpp/lidar_processing_gpu.hpp) reproduce the pipeline's labels and
+    hull indices: the example's checksum equals one computed from lp_process_batch."""
+    import subprocess
+
+    x, ring, cfg = T.synth_scan(1, 5)
+    (tmp_path / "x.bin").write_bytes(x.tobytes())
+    (tmp_path / "r.bin").write_bytes(ring.tobytes())
+    exe = os.path.join(T.PKG, "example_processor")
+    out = subprocess.run([exe, str(tmp_path / "x.bin"), str(tmp_path / "r.bin"), str(cfg.image_height),
+                          str(cfg.image_width)], capture_output=True, text=True, check=True).stdout
+    r = lp.process_batch(ctx, [x], lp.PipelineConfig.default(compute_obb=0), [cfg], [ring])[0]
+    h = 1469598103934665603
+    mask = (1 << 64) - 1
+
+    def mix(v):
+        nonlocal h
+        h = ((h ^ (int(v) & 0xFFFFFFFF)) * 1099511628211) & mask
+
+    for v in r.seg_labels:
+        mix(v)
+    for v in r.cluster_labels[r.seg_labels == lp.OBSTACLE]:
+        mix(v)
+    for k in range(r.n_clusters):
+        for v in r.hull(k):
+            mix(v)
+    assert f"clusters {r.n_clusters} " in out
+    assert out.strip().endswith(f"checksum {h:016x}"), out
+
+
 def test_prepared_batch_and_graph(ctx):
     """lp_batch_create / execute / capture_graph give the same results as lp_process_batch."""
     data = scans([(3, 11), (1, 4)])
