@@ -156,6 +156,24 @@ lp_status lp_cluster(lp_context* ctx, const float* xyz, uint32_t stride, uint32_
 lp_status lp_convex_hull(lp_context* ctx, const double* xy, uint32_t n, int32_t* indices_out,
                          uint32_t* n_out);
 
+/* Convex hull without any device allocation. This entry point has no counterpart in the
+ * reference library. It is for callers that cannot call cudaMalloc: real-time loops that reserve
+ * all memory up front (an allocation can synchronise the device and stall other work), plugin
+ * hosts whose allocation policy forbids it, and paths where an allocation failure cannot be
+ * handled. Inputs and outputs are DEVICE buffers owned by the caller: d_xy holds n x 2 doubles,
+ * d_indices_out at least n + 1 int32, d_n_out one uint32 (the hull size). Results equal
+ * lp_convex_hull's. The kernel's working memory is a static device array of 2.1 MiB that every
+ * GPU which loads the library keeps until the process exits; n above LP_NOALLOC_HULL_MAX_POINTS
+ * is rejected with LP_ERR_CAPACITY before anything runs. The first call on a device looks up that
+ * array's device address (once per device, with the device current), so make that first call
+ * before any stream capture. The work is enqueued on `stream` (a cudaStream_t, NULL for the
+ * default stream) and the call returns without waiting. All calls share the one array: calls
+ * whose kernels overlap on the GPU (other threads, other streams) race and must be serialised
+ * by the caller. */
+#define LP_NOALLOC_HULL_MAX_POINTS 65536u
+lp_status lp_convex_hull_noalloc(const double* d_xy, uint32_t n, int32_t* d_indices_out, uint32_t* d_n_out,
+                                 void* stream);
+
 /* Antipodal pairs of a convex polygon (Shamos). pairs_out: capacity pairs x 2 int32. */
 lp_status lp_antipodal_pairs(lp_context* ctx, const double* hull_xy, uint32_t n,
                              int32_t* pairs_out, uint32_t capacity, uint32_t* n_pairs);

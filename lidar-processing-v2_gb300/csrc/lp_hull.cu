@@ -12,6 +12,7 @@
 //   5. rotating-calipers box (Shamos antipodal pairs, FP64, best area kept as a float exactly
 //      like BoundingBox::area) and the PCA box, by one warp.
 #include <cfloat>
+#include <mutex>
 
 #include "lp_batch.cuh"
 #include "lp_common.cuh"
@@ -855,3 +856,83 @@ void launch_boxes_single(Launcher& L, const double2* P, uint32_t n, int2* pairs,
     LP_LAUNCH(L, k_boxes_single, 1, 32, P, n, pairs, cap, kind, out, npairs_out);
 }
 } // namespace lpg
+
+// =============================================================================================
+// Convex hull without any allocation (lp_convex_hull_noalloc, lidar_gb300.h).
+//
+// For callers that must not allocate device memory: code that runs inside a real-time loop
+// whose memory is reserved up front (cudaMalloc can synchronise the device and stall other
+// work), plugin hosts whose allocator policy forbids it, or code paths where an allocation
+// failure cannot be handled. The caller passes device buffers for the input and the output; the
+// kernel's working memory is the file-scope array below, which every GPU that loads this library
+// holds (2.1 MiB) until the process exits.
+// =============================================================================================
+namespace
+{
+constexpr uint32_t kNoallocMaxPoints = LP_NOALLOC_HULL_MAX_POINTS;
+// sort buffer: next_pow2(n) points of 24 bytes; chain stack: 2n + 8 ints
+constexpr size_t kNoallocSortBytes = static_cast<size_t>(kNoallocMaxPoints) * 24;
+constexpr size_t kNoallocStackBytes = (2 * static_cast<size_t>(kNoallocMaxPoints) + 8) * 4;
+
+static __device__ __align__(256) unsigned char g_noalloc_hull_scratch[kNoallocSortBytes + kNoallocStackBytes];
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+__global__ void k_hull_noalloc_small(uint32_t n, int32_t* out, uint32_t* n_out)
+{
+    // fewer than 3 points: indices 0..n-1 (polygonizer.cpp:36-41)
+    if (threadIdx.x < n)
+        out[threadIdx.x] = static_cast<int32_t>(threadIdx.x);
+    if (threadIdx.x == 0)
+        *n_out = n;
+}
+} // namespace
+
+extern "C" lp_status lp_convex_hull_noalloc(const double* d_xy, uint32_t n, int32_t* d_indices_out, uint32_t* d_n_out,
+                                            void* stream)
+{
+    if (!d_n_out || (n && (!d_xy || !d_indices_out)))
+        return LP_ERR_BAD_ARG;
+    if (n > kNoallocMaxPoints)
+        return LP_ERR_CAPACITY; // more points than the static working array holds
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices)
+    {
+        cudaGetLastError();
+        return LP_ERR_NO_DEVICE;
+    }
+    void* scratch = nullptr;
+    {
+        // once per device, with that device current: the device address of the static array
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_ptr[dev])
+        {
+            void* p = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_hull_scratch);
+            if (e != cudaSuccess || !p)
+            {
+                cudaGetLastError();
+                return LP_ERR_CUDA;
+            }
+            g_noalloc_ptr[dev] = p;
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    const cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (n < 3)
+    {
+        k_hull_noalloc_small<<<1, 32, 0, st>>>(n, d_indices_out, d_n_out);
+    }
+    else
+    {
+        // every scratch element the kernel reads is written earlier in the same launch, so the
+        // previous call's contents never leak into this one
+        auto* sort_buf = reinterpret_cast<lpg::HPt<double>*>(scratch);
+        int* stack = reinterpret_cast<int*>(static_cast<unsigned char*>(scratch) + kNoallocSortBytes);
+        lpg::k_hull_single<<<1, lpg::kHullThreads, 0, st>>>(reinterpret_cast<const double2*>(d_xy), n, sort_buf, stack,
+                                                          d_indices_out, d_n_out);
+    }
+    return cudaGetLastError() == cudaSuccess ? LP_OK : LP_ERR_CUDA;
+}
