@@ -9,6 +9,7 @@ scan per launch sequence) is timed on the same scans for the batched/plain ratio
 oracle (a restatement of the reference path) on a bounded sample of the same workload.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  small profiling case: python bench.py --steps 2 --warmup 1 --scans 16 --no-cpu --no-plain --no-e2e
 Multi-GPU (torchrun): replicas, one independent batch per rank (scans do not shard a step).
 """
 import argparse
@@ -27,7 +28,6 @@ sys.path.insert(0, os.path.join(REPO, "lidar-processing-v2_gb300"))
 sys.path.insert(0, os.path.join(REPO, "tests"))
 
 WORKLOAD = 3
-NSCANS = 64
 METRIC = "scans/s (batched, 64 mixed scans, exact labels)"
 
 
@@ -82,6 +82,7 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            time.sleep(0.3)
         except Exception:
             self.proc = None
         return self
@@ -126,11 +127,10 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def make_workload():
+def make_workload(nscans):
     import lp_testlib as T
 
-    data = [T.synth_scan(WORKLOAD, i) for i in range(NSCANS)]
-    return data
+    return [T.synth_scan(WORKLOAD, i) for i in range(nscans)]
 
 
 def cpu_baseline(data, budget_s=20.0, threads=None):
@@ -174,15 +174,15 @@ def kernel_profile(batch):
 
 
 def run_reference_arm(args, rank, world):
-    data = make_workload()
     if rank != 0:
         return
+    data = make_workload(args.scans)
     budget = max(10.0, min(120.0, 5.0 * args.steps))
     cb = cpu_baseline(data, budget_s=budget)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "scans/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batch64_mixed", "scans": NSCANS, "generator_seed": "1000*3+scan"},
+            "config": {"workload": "batch64_mixed", "scans": args.scans, "generator_seed": "1000*3+scan"},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "scans/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -194,7 +194,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--scans", type=int, default=64, help="scans per batch (64 for the headline workload)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
+    ap.add_argument("--no-plain", action="store_true", help="skip the one-scan-per-launch form")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end run")
     args = ap.parse_args()
     rank, world, local = dist_env()
     dist = dist_init(world)
@@ -205,8 +208,9 @@ def main():
 
     import lidar_gb300 as lp
 
+    ns = args.scans
     ctx = lp.Context(local)
-    data = make_workload()
+    data = make_workload(ns)
     xs, rings, cfgs = [d[0] for d in data], [d[1] for d in data], [d[2] for d in data]
     pipe = lp.PipelineConfig.default()
     npts = sum(len(x) for x in xs)
@@ -217,7 +221,7 @@ def main():
     batch.synchronize()
     prof, agg = kernel_profile(batch)
     kernels_per_step = sum(1 for n, _ in prof if n != "k_scan") + 3 * sum(1 for n, _ in prof if n == "k_scan")
-    top = max(agg.items(), key=lambda kv: kv[1][1])
+    top_name = max(agg.items(), key=lambda kv: kv[1][1])[0]
     res = batch.download()
     n_obs = sum(r.n_obstacles for r in res)
     n_clusters = sum(r.n_clusters for r in res)
@@ -238,11 +242,10 @@ def main():
     barrier(dist)
     dev_ms = sum(step_ms)
     dev_ms_max = dist_max(dist, dev_ms)
-    value = world * NSCANS * args.steps / (dev_ms_max / 1e3)
+    value = world * ns * args.steps / (dev_ms_max / 1e3)
 
-    # the dominant kernel's launches timed with events on the context stream (roofline)
-    top_name = top[0]
-    prof2, agg2 = kernel_profile(batch)
+    # the dominant kernel's launch timed with events on the context stream (roofline)
+    _, agg2 = kernel_profile(batch)
     top_ms = agg2[top_name][1] / agg2[top_name][0]
     alg = {
         "k_hull": 8 * n_clustered + 4 * n_hull + 64 * n_clusters,
@@ -252,30 +255,36 @@ def main():
     alg_bytes = alg.get(top_name, 20 * npts)
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (top_ms / 1e3) / 1e9
+    total_ms = sum(a[1] for a in agg2.values())
 
-    # plain form: one scan per launch sequence, device-resident, no graph
     plain = []
-    for i in range(min(NSCANS, 32)):
-        pb = lp.PreparedBatch(ctx, [xs[i]], pipe, [cfgs[i]], [rings[i]])
-        pb.execute()
-        pb.synchronize()
-        plain.append(pb.time(3, flush_l2=True))
-        pb.close()
-    plain_ms = float(np.mean(plain))
+    if not args.no_plain:
+        # plain form: one scan per launch sequence, device-resident, no graph
+        for i in range(min(ns, 32)):
+            pb = lp.PreparedBatch(ctx, [xs[i]], pipe, [cfgs[i]], [rings[i]])
+            pb.execute()
+            pb.synchronize()
+            plain.append(pb.time(3, flush_l2=True))
+            pb.close()
+    plain_ms = float(np.mean(plain)) if plain else None
 
-    # end to end through the C ABI with host buffers
-    e2e_times = []
-    res_e2e = None
-    for it in range(max(2, args.steps // 4) + 1):
-        t1 = time.perf_counter()
-        res_e2e = lp.process_batch(ctx, xs, pipe, cfgs, rings)
-        dt = time.perf_counter() - t1
-        if it > 0:
-            e2e_times.append(dt)
-    e2e_s = dist_max(dist, float(np.mean(e2e_times)))
-    h2d = sum(x.nbytes + r.nbytes for x, r in zip(xs, rings))
-    d2h = sum(len(r.seg_labels) * 9 + 4 * (len(r.hull_offsets) + len(r.hull_indices)) + 8 * r.n_clusters
-              + 2 * 72 * r.n_clusters for r in res_e2e)
+    e2e = None
+    if not args.no_e2e:
+        # end to end through the C ABI with host buffers
+        e2e_times = []
+        res_e2e = None
+        for it in range(max(2, args.steps // 4) + 1):
+            t1 = time.perf_counter()
+            res_e2e = lp.process_batch(ctx, xs, pipe, cfgs, rings)
+            dt = time.perf_counter() - t1
+            if it > 0:
+                e2e_times.append(dt)
+        e2e_s = dist_max(dist, float(np.mean(e2e_times)))
+        h2d = sum(x.nbytes + r.nbytes for x, r in zip(xs, rings))
+        d2h = sum(len(r.seg_labels) * 9 + 4 * (len(r.hull_offsets) + len(r.hull_indices)) + 8 * r.n_clusters
+                  + 2 * 72 * r.n_clusters for r in res_e2e)
+        e2e = {"value": world * ns / e2e_s, "unit": "scans/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
 
     cb = None
     if rank == 0 and not args.no_cpu:
@@ -286,24 +295,22 @@ def main():
             "metric": METRIC, "value": value, "unit": "scans/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batch64_mixed", "scans": NSCANS, "points": npts, "obstacles": n_obs,
-                       "clusters": n_clusters, "parallelism": f"replicas{world}",
+            "config": {"workload": "batch64_mixed" if ns == 64 else f"batch{ns}_mixed", "scans": ns, "points": npts,
+                       "obstacles": n_obs, "clusters": n_clusters, "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (133 MB XYZI, multi-GB working set)",
                        "graph": "captured CUDA graph per batch"},
             "points_per_s": world * npts * args.steps / (dev_ms_max / 1e3),
-            "plain": {"ms_per_scan": plain_ms, "scans_per_s": 1e3 / plain_ms,
-                      "p50_ms": float(np.percentile(plain, 50)), "p99_ms": float(np.percentile(plain, 99)),
-                      "scans": len(plain)},
-            "batched_over_plain": (value / world) / (1e3 / plain_ms),
+            "plain": None if not plain else {
+                "ms_per_scan": plain_ms, "scans_per_s": 1e3 / plain_ms, "p50_ms": float(np.percentile(plain, 50)),
+                "p99_ms": float(np.percentile(plain, 99)), "scans": len(plain)},
+            "batched_over_plain": None if not plain else (value / world) / (1e3 / plain_ms),
             "batch_latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
-            "e2e": {"value": world * NSCANS / e2e_s, "unit": "scans/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h)},
+            "e2e": e2e,
             "gpu_launches": int(kernels_per_step * args.steps),
             "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": top_ms},
-            "kernel_share": {k: round(v[1] / sum(a[1] for a in agg2.values()), 4)
-                             for k, v in sorted(agg2.items(), key=lambda kv: -kv[1][1])[:8]},
+            "kernel_share": {k: round(v[1] / total_ms, 4) for k, v in sorted(agg2.items(), key=lambda kv: -kv[1][1])[:10]},
             "clocks": clocks.summary(),
             "cpu_baseline": cb,
             "wall_s": wall,

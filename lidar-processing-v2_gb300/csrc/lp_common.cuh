@@ -90,6 +90,33 @@ __device__ void block_bitonic_sort(T* s, uint32_t n, Less less)
     }
 }
 
+// Bitonic sort of `n` (power of two) keys in shared memory by one full warp.
+template <typename T, typename Less>
+__device__ void warp_bitonic_smem(T* s, uint32_t n, Less less)
+{
+    for (uint32_t k = 2; k <= n; k <<= 1)
+    {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1)
+        {
+            for (uint32_t i = lane_id(); i < n; i += 32)
+            {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i)
+                {
+                    const bool up = ((i & k) == 0);
+                    T a = s[i], b = s[ixj];
+                    if (up ? less(b, a) : less(a, b))
+                    {
+                        s[i] = b;
+                        s[ixj] = a;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
 // Bitonic sort of 32 values held one per lane (ascending by lane).
 template <typename T, typename Less>
 __device__ __forceinline__ T warp_bitonic_sort(T v, Less less)

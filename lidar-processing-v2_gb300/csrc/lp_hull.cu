@@ -1,12 +1,16 @@
 // lp_hull.cu — per-cluster convex hull and oriented bounding boxes.
 //
 // Reference: lidar_processing_lib/src/polygonizer.cpp and Processor::run's per-cluster gather
-// (src/processor/src/processor.cpp:627-671). One CTA per cluster:
-//   1. z range and the four extreme points of the cluster's members,
-//   2. Akl-Toussaint prefilter: members strictly inside the extreme quadrilateral (by a
-//      relative margin far above double rounding) cannot be hull vertices and are dropped,
-//   3. bitonic sort of the candidates by (x, y, member order), Andrew's monotone chain with the
-//      reference's FP64 orientation predicate (polygonizer.cpp:45-50, 62-85),
+// (src/processor/src/processor.cpp:627-671). Persistent CTAs take clusters from a work queue
+// (largest first); per cluster:
+//   1. z range and the members extreme in 16 directions (an inscribed polygon of members),
+//   2. Quickhull refinement: the member farthest outside each polygon edge is inserted, for a
+//      few rounds; members proven strictly inside leave the active set. Every polygon vertex is a
+//      member, so a member strictly inside the polygon (checked in FP64 with a relative margin
+//      far above rounding) cannot be a hull vertex,
+//   3. bitonic sort of the remaining candidates by (x, y, member order), Andrew's monotone chain
+//      with the reference's FP64 orientation predicate (polygonizer.cpp:45-50, 62-85): the same
+//      output as the reference's chain over all members,
 //   4. local hull indices = rank of each hull vertex among the cluster's members in input
 //      order (the reference gathers a cluster's points in obstacle order, processor.cpp:640),
 //   5. rotating-calipers box (Shamos antipodal pairs, FP64, best area kept as a float exactly
@@ -483,6 +487,12 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
 
     // 2. refine the polygon: insert the member farthest outside each edge (Quickhull step),
     //    while it grows and fits. Every vertex is a member, so the polygon stays inside the hull.
+    //    Members proven strictly inside the current polygon leave the active set: the float test
+    //    keeps a 1e-5 relative margin, far above its rounding error, so no hull vertex is dropped.
+    uint32_t* act[2] = {reinterpret_cast<uint32_t*>(b.hs_stack + 2ull * start + 2ull * g), nullptr};
+    act[1] = act[0] + n; // two member lists of n entries in the chain-stack scratch (2n + 2)
+    int cur = -1;        // -1: the active set is all members
+    uint32_t nact = n;
     for (int round = 0; round < kRefineRounds; ++round)
     {
         const int np = sm.npoly;
@@ -490,25 +500,36 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
             break;
         for (int e = threadIdx.x; e < np; e += blockDim.x)
             sm.pkey[e] = 0ull;
+        if (threadIdx.x == 0)
+            sm.ncand = 0;
         __syncthreads();
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        const int nxt = (cur == 0) ? 1 : 0;
+        for (uint32_t t = threadIdx.x; t < nact; t += blockDim.x)
         {
+            const uint32_t i = (cur < 0) ? t : act[cur][t];
             const float4 p = b.obs_pts[mem[i]];
+            bool in = true;
             for (int e = 0; e < np; ++e)
             {
                 const float2 a = sm.poly[e], c = sm.poly[(e + 1 == np) ? 0 : e + 1];
                 const float ex = c.x - a.x, ey = c.y - a.y, qx = p.x - a.x, qy = p.y - a.y;
                 const float cr = ex * qy - ey * qx; // < 0: right of the edge, outside
-                const float tol = 1e-6f * (fabsf(ex) + fabsf(ey)) * (fabsf(qx) + fabsf(qy));
-                if (cr < -tol)
+                const float scale = (fabsf(ex) + fabsf(ey)) * (fabsf(qx) + fabsf(qy));
+                if (!(cr > 1e-5f * scale))
+                    in = false;
+                if (cr < -1e-6f * scale)
                 {
                     const unsigned long long key = fkey_payload(-cr, i);
                     if (key > sm.pkey[e])
                         atomicMax(&sm.pkey[e], key);
                 }
             }
+            if (!in)
+                act[nxt][atomicAdd(&sm.ncand, 1)] = i;
         }
         __syncthreads();
+        cur = nxt;
+        nact = static_cast<uint32_t>(sm.ncand);
         if (threadIdx.x == 0)
         {
             int add = 0;
@@ -538,8 +559,8 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
             break;
     }
 
-    // 3. candidates: members not strictly inside the polygon by a relative margin far above
-    //    double rounding (a hull vertex is never strictly inside a polygon of members)
+    // 3. candidates: active members not strictly inside the polygon by a relative margin far
+    //    above double rounding (a hull vertex is never strictly inside a polygon of members)
     const int npf = sm.npoly;
     HPt<float>* gs = reinterpret_cast<HPt<float>*>(b.hs_cand) + 2ull * start; // capacity 2n >= next_pow2(n)
     auto inside = [&](double px, double py) {
@@ -553,35 +574,24 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
         }
         return true;
     };
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+    if (threadIdx.x == 0)
+        sm.ncand = 0;
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < nact; t += blockDim.x)
     {
-        const uint32_t o = mem[i];
+        const uint32_t o = mem[(cur < 0) ? t : act[cur][t]];
         const float4 p = b.obs_pts[o];
         if (!inside(p.x, p.y))
         {
             const int pos = atomicAdd(&sm.ncand, 1);
             if (pos < kHullSmem)
                 sm.cand[pos] = HPt<float>{p.x, p.y, o};
+            gs[pos] = HPt<float>{p.x, p.y, o};
         }
     }
     __syncthreads();
     const int m = sm.ncand;
     const bool small = m <= kHullSmem;
-    if (!small)
-    {
-        __syncthreads();
-        if (threadIdx.x == 0)
-            sm.ncand = 0;
-        __syncthreads();
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
-        {
-            const uint32_t o = mem[i];
-            const float4 p = b.obs_pts[o];
-            if (!inside(p.x, p.y))
-                gs[atomicAdd(&sm.ncand, 1)] = HPt<float>{p.x, p.y, o};
-        }
-        __syncthreads();
-    }
 
     // 4. sort by (x, y, input order) and the monotone chain
     const HPt<float>* C;

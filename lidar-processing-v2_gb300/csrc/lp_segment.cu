@@ -21,7 +21,8 @@ constexpr float kPi2F = 1.57079637050628662109f;      // M_PI_2f
 constexpr float kPi15F = 4.71238899230957031250f;     // 1.5F * M_PIf (dataloader.cpp:108)
 constexpr float kTwoPiF = 6.28318548202514648438f;    // 2.0F * M_PIf == (float)(2*M_PI)
 constexpr int kRingTile = 1024;
-constexpr int kSmallCell = 32;
+constexpr int kSmallCell = 32;   // sorted in registers by one warp
+constexpr int kMediumCell = 256; // sorted in shared memory by one warp
 constexpr uint32_t kLargeCellMax = 8192;
 
 __device__ __forceinline__ int scan_of_cell(const BatchDev& b, uint32_t c)
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
     const int s = scan_of_cell(b, c);
     const ScanDev& sd = b.scans[s];
     const bool near = static_cast<int32_t>((c - sd.cell_off) % static_cast<uint32_t>(sd.nrad)) < kRansacRadialBins;
-    if (n > kSmallCell)
+    if (n > kMediumCell)
     {
         if (lane == 0)
         {
@@ -221,6 +222,37 @@ __global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
         return;
     }
     const uint32_t start = b.cell_start[c];
+    if (n > kSmallCell)
+    {
+        // one warp sorts the cell in its slice of shared memory (bitonic, __syncwarp per stage)
+        __shared__ float wz[8][kMediumCell];
+        __shared__ int32_t wi[8][kMediumCell];
+        const uint32_t warp = threadIdx.x >> 5;
+        float* zs = wz[warp];
+        const uint32_t np2 = next_pow2(n);
+        for (uint32_t k = lane; k < np2; k += 32)
+            zs[k] = (k < n) ? b.csr_z[start + k] : INFINITY;
+        __syncwarp();
+        warp_bitonic_smem(zs, np2, [](float a, float bb) { return a < bb; });
+        int kbest = 0;
+        for (uint32_t k = 1 + lane; k <= n / 2; k += 32)
+            if (zs[k] - zs[k - 1] > 0.5F)
+                kbest = static_cast<int>(k); // lanes visit k in increasing order
+        kbest = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(kbest)));
+        if (lane == 0)
+            b.zlow[c] = zs[kbest];
+        if (near)
+        {
+            int32_t* is = wi[warp];
+            for (uint32_t k = lane; k < np2; k += 32)
+                is[k] = (k < n) ? b.csr_idx[start + k] : INT32_MAX;
+            __syncwarp();
+            warp_bitonic_smem(is, np2, [](int32_t a, int32_t bb) { return a < bb; });
+            for (uint32_t k = lane; k < n; k += 32)
+                b.csr_idx[start + k] = is[k];
+        }
+        return;
+    }
     float z = (lane < n) ? b.csr_z[start + lane] : INFINITY;
     z = warp_bitonic_sort(z, [](float a, float bb) { return a < bb; });
     const float zp = __shfl_up_sync(0xffffffffu, z, 1);
