@@ -188,8 +188,88 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line))
 
 
+def run_serve(args):
+    """Serving workload: six sensors at 10 Hz (periods ~ N(100 ms, 10 ms)), the rate doubled
+    during the first second of every 5 s, scans of 32/64/128 rings x 1024-4096 bins (synthetic
+    workload 5), a 20 GB admission budget. Latency = submission -> results in host buffers."""
+    import lp_testlib as T
+    import lidar_gb300 as lp
+
+    sensors, per_sensor = 6, 8
+    pool = [[T.synth_scan(5, s * per_sensor + k) for k in range(per_sensor)] for s in range(sensors)]
+    pipe = lp.PipelineConfig.default()
+    server = lp.Server(0, pipe, memory_budget_bytes=20 << 30, max_batch_scans=16, slots=3)
+    rng = np.random.default_rng(5000)
+    events = []
+    for s in range(sensors):
+        t = float(rng.uniform(0.0, 0.1))
+        k = 0
+        while t < args.duration:
+            events.append((t, s, k))
+            k += 1
+            period = float(rng.normal(0.100, 0.010))
+            if (t % 5.0) < 1.0:
+                period *= 0.5
+            t += max(period, 0.005)
+    events.sort()
+    done = {}
+    stop = threading.Event()
+
+    def poller():
+        while not stop.is_set() or len(done) < len(events) + warm:
+            for d, _ in server.poll(wait_us=2000):
+                done[int(d.tag)] = (d.latency_ms, d.queue_ms, d.batch_scans, d.status)
+            if stop.is_set() and time.perf_counter() - t_end > 30:
+                break
+
+    # warm-up: every pool scan once
+    warm = 0
+    for s in range(sensors):
+        for k in range(per_sensor):
+            x, ring, cfg = pool[s][k]
+            server.submit(x, ring, cfg, 1_000_000 + warm)
+            warm += 1
+    t_end = time.perf_counter() + 1e9
+    th = threading.Thread(target=poller, daemon=True)
+    th.start()
+    while sum(1 for t in done if t >= 1_000_000) < warm:
+        time.sleep(0.01)
+    t0 = time.perf_counter()
+    for i, (t, s, k) in enumerate(events):
+        dt = t0 + t - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        x, ring, cfg = pool[s][k % per_sensor]
+        server.submit(x, ring, cfg, i)
+    t_end = time.perf_counter()
+    stop.set()
+    th.join(timeout=60)
+    stats = server.stats()
+    server.close()
+    lat = np.array([done[i][0] for i in range(len(events)) if i in done])
+    bs = np.array([done[i][2] for i in range(len(events)) if i in done])
+    ok = sum(1 for i in range(len(events)) if i in done and done[i][3] == 0)
+    pts = [len(pool[s][k % per_sensor][0]) for _, s, k in events]
+    line = {"metric": "serving latency p99 ms/scan (6 sensors x 10 Hz, continuous batching)",
+            "value": float(np.percentile(lat, 99)), "unit": "ms", "higher_is_better": False, "n_gpus": 1,
+            "data": "synthetic", "dtype": "f32",
+            "config": {"workload": "serve_6x10Hz_mixed", "sensors": sensors, "duration_s": args.duration,
+                       "burst": "rate x2 during the first 1 s of every 5 s", "memory_budget_gb": 20,
+                       "slots": 3, "max_batch_scans": 16},
+            "scans": int(len(lat)), "ok": int(ok), "offered_scans_per_s": len(events) / args.duration,
+            "achieved_scans_per_s": len(lat) / max(t_end - t0, 1e-9),
+            "points_per_scan": {"min": int(min(pts)), "max": int(max(pts)), "mean": float(np.mean(pts))},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "p99.9": float(np.percentile(lat, 99.9)), "max": float(lat.max())},
+            "batch_scans": {"mean": float(bs.mean()), "max": int(bs.max())},
+            "server": stats}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--serve", action="store_true", help="multi-sensor serving workload instead of the batch bench")
+    ap.add_argument("--duration", type=float, default=60.0, help="seconds of simulated sensor stream (--serve)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -203,6 +283,11 @@ def main():
     dist = dist_init(world)
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
+        barrier(dist)
+        return
+    if args.serve:
+        if rank == 0:
+            run_serve(args)
         barrier(dist)
         return
 

@@ -42,6 +42,47 @@ lp_status lp_batch_profile(lp_context* ctx, lp_batch* batch, char* names, uint32
  * 1 atan(a), 2 exp(a), 3 the reference's atan2 approximation); used by the parity tests. */
 lp_status lp_debug_math(lp_context* ctx, int32_t kind, const float* a, const float* b, uint32_t n, float* out);
 
+/* ------------------------------------------------------------------------------------------ */
+/* Serving: scans from several sensors submitted as they arrive, continuous batching.          */
+/* No counterpart in the reference (its processor node handles one scan per callback).         */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct lp_server lp_server;
+
+typedef struct lp_server_config
+{
+    uint64_t memory_budget_bytes; /* device memory reserved for in-flight batches (split over slots) */
+    uint32_t max_batch_scans;     /* most scans one batch admits */
+    uint32_t slots;               /* batches that can be on the GPU at once (each has its own stream) */
+} lp_server_config;
+
+typedef struct lp_server_done
+{
+    uint64_t tag;
+    lp_status status;
+    uint32_t batch_scans; /* scans in the batch this one ran in */
+    double latency_ms;    /* submission -> results in the caller's buffers */
+    double queue_ms;      /* submission -> its batch started */
+} lp_server_done;
+
+typedef struct lp_server_stats
+{
+    uint64_t submitted, completed, failed, batches, scans_in_batches, max_batch_seen, pending;
+    uint64_t device_bytes;
+} lp_server_stats;
+
+void lp_server_config_default(lp_server_config* cfg);
+lp_status lp_server_create(int32_t device, const lp_pipeline_config* cfg, const lp_server_config* scfg,
+                           lp_server** out);
+/* Queues one scan. The input buffers and `out` (with its buffers) must stay valid until the scan
+ * is reported by lp_server_poll; results are written there exactly as lp_process_scan would. */
+lp_status lp_server_submit(lp_server* server, const lp_scan_input* scan, lp_scan_output* out, uint64_t tag);
+/* Finished scans since the last poll (up to capacity); waits up to wait_us for at least one. */
+lp_status lp_server_poll(lp_server* server, lp_server_done* done, uint32_t capacity, uint32_t* n_done,
+                         uint32_t wait_us);
+lp_status lp_server_stats_get(lp_server* server, lp_server_stats* out);
+/* Drains the queue, waits for in-flight batches and releases the server. */
+void lp_server_destroy(lp_server* server);
+
 #ifdef __cplusplus
 }
 #endif

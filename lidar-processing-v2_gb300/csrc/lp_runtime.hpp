@@ -1,0 +1,91 @@
+// lp_runtime.hpp — host runtime shared by the C ABI (lp_api.cu) and the serving loop
+// (lp_serve.cu): contexts, batches and the plan/upload/execute/download steps of a batch.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "lidar_gb300.h"
+#include "lidar_gb300_batch.h"
+#include "lp_batch.cuh"
+#include "lp_stages.hpp"
+
+namespace lprt
+{
+enum Stage : uint32_t
+{
+    ST_RING = 1u << 0,    // ring partition (lp_add_ring_info)
+    ST_NOISE = 1u << 1,   // DROR on the input cloud
+    ST_SEG = 1u << 2,     // segmentation
+    ST_CLUSTER = 1u << 3, // cluster the obstacle points
+    ST_HULL = 1u << 4,
+    ST_OBB = 1u << 5,
+    ST_ALL_OBS = 1u << 6, // cluster the whole input (lp_cluster)
+    ST_IMAGE = 1u << 7,
+};
+
+struct ScanIn
+{
+    const float* xyzi = nullptr; // host
+    uint32_t stride = 4;         // floats between points
+    const uint16_t* ring = nullptr;
+    uint32_t n = 0;
+    lp_segmenter_config seg{};
+    int32_t compute_ring = 0;
+    int32_t first_ring = 0;
+};
+
+struct Run
+{
+    uint32_t stages = 0;
+    lp_clusterer_config cl{};
+    lp_noise_remover_config nr{};
+    std::vector<ScanIn> scans;
+};
+} // namespace lprt
+
+struct lp_context
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t launches = 0;
+    std::string last_error;
+    std::vector<cudaEvent_t> events;
+    lp_batch* cached = nullptr;
+    void* flush = nullptr; // buffer larger than L2 for cache flushing between timed runs
+    size_t flush_bytes = 0;
+};
+
+struct lp_batch
+{
+    lprt::Run run;
+    lpg::BatchHost hb;
+    lpg::BatchDev b{};
+    char* mem = nullptr;
+    size_t cap = 0;
+    uint32_t* scan_sums = nullptr;
+    uint8_t* d_image = nullptr;
+    std::vector<lpg::ScanState> h_state;
+    std::vector<float4> staging; // host repack for stride-3 inputs
+    cudaGraphExec_t graph = nullptr;
+    std::vector<lpg::LaunchRecord> prof;
+    bool profiling = false;
+};
+
+namespace lprt
+{
+lp_status fail(lp_context* ctx, lp_status st, const std::string& msg);
+// Layout of the batch on the host (no device work).
+lp_status plan(lp_context* ctx, lp_batch& B);
+// Device bytes a planned batch needs (carve with a null base).
+size_t measure(lp_batch& B);
+// plan + (re)allocate + carve.
+lp_status build(lp_context* ctx, lp_batch& B);
+lp_status upload(lp_context* ctx, lp_batch& B);
+lp_status execute(lp_context* ctx, lp_batch& B);
+lp_status fetch_state(lp_context* ctx, lp_batch& B);
+lp_status download(lp_context* ctx, lp_batch& B, lp_scan_output* outs);
+lp_status fill_pipeline(lp_context* ctx, lp_batch& B, const lp_pipeline_config* cfg, const lp_scan_input* scans,
+                        uint32_t nscans);
+void destroy_batch(lp_batch* B);
+} // namespace lprt

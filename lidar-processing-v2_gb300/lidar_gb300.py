@@ -250,6 +250,12 @@ def _declare(lib):
         "lp_batch_time": (c.c_int32, [P, P, c.c_uint32, c.c_int32, c.POINTER(c.c_float)]),
         "lp_batch_profile": (c.c_int32, [P, P, P, c.c_uint32, P, c.c_uint32, c.POINTER(c.c_uint32)]),
         "lp_debug_math": (c.c_int32, [P, c.c_int32, P, P, c.c_uint32, P]),
+        "lp_server_config_default": (None, [P]),
+        "lp_server_create": (c.c_int32, [c.c_int32, P, P, c.POINTER(P)]),
+        "lp_server_submit": (c.c_int32, [P, P, P, c.c_uint64]),
+        "lp_server_poll": (c.c_int32, [P, P, c.c_uint32, c.POINTER(c.c_uint32), c.c_uint32]),
+        "lp_server_stats_get": (c.c_int32, [P, P]),
+        "lp_server_destroy": (None, [P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -504,6 +510,70 @@ class PreparedBatch:
     def close(self):
         if self.handle:
             library().lp_batch_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("memory_budget_bytes", ctypes.c_uint64), ("max_batch_scans", ctypes.c_uint32),
+                ("slots", ctypes.c_uint32)]
+
+
+class ServerDone(ctypes.Structure):
+    _fields_ = [("tag", ctypes.c_uint64), ("status", ctypes.c_int32), ("batch_scans", ctypes.c_uint32),
+                ("latency_ms", ctypes.c_double), ("queue_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "batches", "scans_in_batches",
+                                               "max_batch_seen", "pending", "device_bytes")]
+
+
+class Server:
+    """Continuous-batching request loop (lp_server_*): submit scans as they arrive, poll results.
+    Inputs and result buffers of a scan are kept alive here until it is polled."""
+
+    def __init__(self, device=0, pipeline=None, memory_budget_bytes=20 << 30, max_batch_scans=16, slots=3):
+        self.pipeline = pipeline or PipelineConfig.default()
+        cfg = ServerConfig(memory_budget_bytes, max_batch_scans, slots)
+        h = ctypes.c_void_p()
+        check(library().lp_server_create(device, ctypes.byref(self.pipeline), ctypes.byref(cfg), ctypes.byref(h)))
+        self.handle = h
+        self._live = {}
+
+    def submit(self, xyzi, ring, seg_config, tag):
+        a = _xyzi(xyzi)
+        r = None if ring is None else np.ascontiguousarray(ring, np.uint16)
+        inp = ScanInput(a.ctypes.data, None if r is None else r.ctypes.data, len(a), seg_config)
+        buf = ResultBuffers(len(a))
+        self._live[int(tag)] = (a, r, inp, buf)
+        check(library().lp_server_submit(self.handle, ctypes.byref(inp), ctypes.byref(buf.out), int(tag)))
+
+    def poll(self, wait_us=1000, capacity=256):
+        """[(ServerDone, ScanResult or None)] of scans finished since the last poll."""
+        done = (ServerDone * capacity)()
+        n = ctypes.c_uint32()
+        check(library().lp_server_poll(self.handle, done, capacity, ctypes.byref(n), wait_us))
+        out = []
+        for i in range(n.value):
+            d = done[i]
+            _, _, _, buf = self._live.pop(int(d.tag))
+            out.append((d, buf.result() if d.status == LP_OK else None))
+        return out
+
+    def stats(self):
+        s = ServerStats()
+        check(library().lp_server_stats_get(self.handle, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in ServerStats._fields_}
+
+    def close(self):
+        if self.handle:
+            library().lp_server_destroy(self.handle)
             self.handle = None
 
     def __del__(self):
