@@ -266,9 +266,69 @@ def run_serve(args):
     print(json.dumps(line))
 
 
+def run_dror(args):
+    """Outlier-filter workload: 32 unorganised scans of 1.0 M points (128-ring geometry at 16384
+    bins, 950k returns + 50k clutter within 15 m, shuffled; synthetic workload 4) per launch. DROR
+    with multiplier 3 x 0.17 deg (rad), min neighbours 3, min radius 0.1 m on the input, then the
+    unorganised segmentation, clustering and hulls. Distinct scans: --dror-unique (each repeated)."""
+    import lp_testlib as T
+    import lidar_gb300 as lp
+
+    uniq = [T.synth_scan(4, i) for i in range(args.dror_unique)]
+    ns = 32
+    data = [uniq[i % len(uniq)] for i in range(ns)]
+    xs = [d[0] for d in data]
+    cfgs = []
+    for d in data:
+        c = d[2]
+        c.assume_unorganized_cloud = 1
+        cfgs.append(c)
+    noise = lp.NoiseRemoverConfig(3 * 0.17 * np.pi / 180.0, 0.1, 3)
+    pipe = lp.PipelineConfig.default(enable_noise_removal=1, noise=noise)
+    ctx = lp.Context(0)
+    npts = sum(len(x) for x in xs)
+    batch = lp.PreparedBatch(ctx, xs, pipe, cfgs, None)
+    batch.execute()
+    batch.synchronize()
+    res = batch.download()
+    noise_pts = int(sum(int(r.noise_labels.sum()) for r in res))
+    _, agg = kernel_profile(batch)
+    dror_kernels = [k for k in agg if k.startswith("k_dror")]
+    dror_ms = sum(agg[k][1] for k in dror_kernels)
+    total_ms = sum(a[1] for a in agg.values())
+    batch.capture_graph()
+    for _ in range(args.warmup):
+        batch.execute()
+    batch.synchronize()
+    with ClockSampler(0) as clocks:
+        step_ms = [batch.time(1, flush_l2=False) for _ in range(args.steps)]
+    ms = float(np.mean(step_ms))
+    peak, peak_kind = measured_peaks()
+    dror_gbs = 17.0 * npts / (dror_ms / 1e3) / 1e9
+    top = max(agg.items(), key=lambda kv: kv[1][1])
+    line = {"metric": "scans/s (32 x 1.0M-point unorganised scans, DROR + pipeline)", "value": ns / (ms / 1e3),
+            "unit": "scans/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "dror32x1M", "scans": ns, "distinct_scans": len(uniq), "points": npts,
+                       "dror": "multiplier 3*0.17deg, min_neighbours 3, min radius 0.1 m"},
+            "ms_per_step": ms, "points_per_s": npts / (ms / 1e3), "noise_points": noise_pts,
+            "dror_stage": {"ms": dror_ms, "kernels": dror_kernels, "points_per_s": npts / (dror_ms / 1e3),
+                           "roofline": {"bound": "hbm", "achieved": dror_gbs, "peak": peak, "unit": "GB/s",
+                                        "frac": dror_gbs / peak, "algorithmic_bytes_per_point": 17,
+                                        "peak_source": peak_kind},
+                           "share_of_step": dror_ms / total_ms},
+            "top_kernel": {"name": top[0], "share": top[1][1] / total_ms},
+            "clocks": clocks.summary()}
+    print(json.dumps(line))
+    batch.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--serve", action="store_true", help="multi-sensor serving workload instead of the batch bench")
+    ap.add_argument("--dror", action="store_true", help="32 x 1M-point outlier-filter workload")
+    ap.add_argument("--dror-unique", type=int, default=4, help="distinct generated scans in --dror (repeated to 32)")
     ap.add_argument("--duration", type=float, default=60.0, help="seconds of simulated sensor stream (--serve)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -288,6 +348,11 @@ def main():
     if args.serve:
         if rank == 0:
             run_serve(args)
+        barrier(dist)
+        return
+    if args.dror:
+        if rank == 0:
+            run_dror(args)
         barrier(dist)
         return
 

@@ -170,7 +170,7 @@ lp_status plan(lp_context* ctx, lp_batch& B)
         sd.dror_rmin2 = R.nr.min_search_radius_m * R.nr.min_search_radius_m;
         sd.dror_k = R.nr.min_neighbours;
         sd.dhash_off = static_cast<uint32_t>(dh);
-        sd.dhash_cap = next_pow2(std::max(64u, 2u * in.n));
+        sd.dhash_cap = next_pow2(std::max(64u, 4u * in.n)); // cells <= 3n band insertions
         pt += in.n;
         tile += div_up(std::max(in.n, 1u), 1024u);
         hash += sd.hash_cap;
@@ -242,9 +242,9 @@ size_t carve(lp_batch& B, char* base)
         put(b.dkey, b.ndhash);
         put(b.dcnt, b.ndhash + 1);
         put(b.dstart, b.ndhash + 1);
-        put(b.dslot, N);
-        put(b.drank, N);
-        put(b.dorder, N);
+        put(b.dslot, 3ull * N); // up to three band insertions per point
+        put(b.drank, 3ull * N);
+        put(b.dorder, 3ull * N);
         put(b.dr2, N);
     }
     else

@@ -5,9 +5,9 @@
 // squared search radius is r2 = max(float(s2 * double(x*x + y*y)), rmin^2) with s2 =
 // pow(double(multiplier), 2) (computed on the host); a point is NOISE when fewer than
 // min_neighbours points, itself included, satisfy d0 + (d1 + d2) <= r2 with dk = (q_k - p_k)^2
-// in binary32, query first (kdtree.hpp:131-143, :363). Counting runs over a uniform grid
-// whose cell edge is the scan's largest radius, so the 27 cells around a point hold every
-// candidate; the count stops at min_neighbours.
+// in binary32, query first (kdtree.hpp:131-143, :363). Counting runs over range-banded grids
+// (below) so that the 27 cells around a point hold every candidate; the count stops at
+// min_neighbours.
 #include "lp_batch.cuh"
 #include "lp_common.cuh"
 #include "lp_stages.hpp"
@@ -33,14 +33,6 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long k)
     return k;
 }
 
-__device__ __forceinline__ unsigned long long cell_key(int32_t ix, int32_t iy, int32_t iz)
-{
-    const unsigned long long ux = static_cast<uint32_t>(ix + (1 << 20)) & 0x1fffffu;
-    const unsigned long long uy = static_cast<uint32_t>(iy + (1 << 20)) & 0x1fffffu;
-    const unsigned long long uz = static_cast<uint32_t>(iz + (1 << 20)) & 0x1fffffu;
-    return (ux << 42) | (uy << 21) | uz;
-}
-
 __global__ void k_state_init(BatchDev b, int noise)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -50,42 +42,57 @@ __global__ void k_state_init(BatchDev b, int noise)
     st.n_pts = noise ? 0u : b.scans[s].n;
 }
 
+// Range bands. The radius grows with the horizontal range rho: r = rmin for rho below
+// rho_c = rmin / sqrt(s2), then proportional to rho. Band 0 is [0, rho_c); band b >= 1 is
+// [rho_c q^(b-1), rho_c q^b) with q = 1.25. Each band has its own grid whose cell edge bounds
+// every radius in the band, and every point is also inserted into the neighbouring bands whose
+// range it lies within one of their cells of, so the 27 cells around a query in its own band
+// hold all its neighbours.
+constexpr int kBands = 48;
+constexpr float kBandQ = 1.25f;
+
+__device__ __forceinline__ float band_rho_c(const ScanDev& sd)
+{
+    if (!(sd.dror_s2 > 0.0))
+        return INFINITY;
+    return fmaxf(static_cast<float>(sqrt(static_cast<double>(sd.dror_rmin2) / sd.dror_s2)), 1e-3f);
+}
+
+__device__ __forceinline__ int band_of(float rho, float rho_c)
+{
+    if (!(rho >= rho_c))
+        return 0;
+    const int bnd = 1 + static_cast<int>(floorf(log2f(rho / rho_c) / log2f(kBandQ)));
+    return min(max(bnd, 1), kBands - 1);
+}
+
+__device__ __forceinline__ float band_cell(const ScanDev& sd, int bnd, float rho_c)
+{
+    double r2 = static_cast<double>(sd.dror_rmin2);
+    if (bnd > 0 && isfinite(rho_c))
+    {
+        const double hi = static_cast<double>(rho_c) * pow(static_cast<double>(kBandQ), bnd);
+        r2 = fmax(sd.dror_s2 * hi * hi, r2);
+    }
+    return static_cast<float>(sqrt(r2)) * 1.001f + 1e-5f;
+}
+
+__device__ __forceinline__ float horiz(const float4& p)
+{
+    return sqrtf(p.x * p.x + p.y * p.y);
+}
+
 __global__ void k_dror_r2(BatchDev b)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < b.nsrc;
-    const int s = valid ? scan_of_src(b, i) : -1;
-    uint32_t bits = 0u;
-    if (valid)
-    {
-        const ScanDev& sd = b.scans[s];
-        const float4 p = b.src[i];
-        const double rho2 = static_cast<double>((p.x * p.x) + (p.y * p.y));
-        const float r2 = fmaxf(__double2float_rn(sd.dror_s2 * rho2), sd.dror_rmin2);
-        b.dr2[i] = r2;
-        bits = __float_as_uint(r2);
-    }
-    const int smax = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(s + 1))) - 1;
-    if (__all_sync(0xffffffffu, s == smax || s < 0))
-    {
-        bits = __reduce_max_sync(0xffffffffu, bits);
-        if (lane_id() == 0 && smax >= 0)
-            atomicMax(&b.state[smax].dmax_r2_bits, bits);
-    }
-    else if (valid)
-    {
-        atomicMax(&b.state[s].dmax_r2_bits, bits);
-    }
-}
-
-__global__ void k_dror_cell(BatchDev b)
-{
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= b.nscan)
+    if (i >= b.nsrc)
         return;
-    ScanState& st = b.state[s];
-    const float rmax = sqrtf(__uint_as_float(st.dmax_r2_bits));
-    st.dcell = fmaxf(rmax * 1.0001f + 1e-6f, 1e-3f);
+    const int s = scan_of_src(b, i);
+    const ScanDev& sd = b.scans[s];
+    const float4 p = b.src[i];
+    // noise_remover.cpp:55-57: float products and sum, widened, scaled, narrowed, floored
+    const double rho2 = static_cast<double>((p.x * p.x) + (p.y * p.y));
+    b.dr2[i] = fmaxf(__double2float_rn(sd.dror_s2 * rho2), sd.dror_rmin2);
 }
 
 __device__ __forceinline__ void cell_of(const float4& p, float c, int32_t& ix, int32_t& iy, int32_t& iz)
@@ -95,6 +102,16 @@ __device__ __forceinline__ void cell_of(const float4& p, float c, int32_t& ix, i
     iz = static_cast<int32_t>(floorf(p.z / c));
 }
 
+__device__ __forceinline__ unsigned long long band_key(int bnd, int32_t ix, int32_t iy, int32_t iz)
+{
+    const unsigned long long ux = static_cast<uint32_t>(ix + (1 << 18)) & 0x7ffffu;
+    const unsigned long long uy = static_cast<uint32_t>(iy + (1 << 18)) & 0x7ffffu;
+    const unsigned long long uz = static_cast<uint32_t>(iz + (1 << 18)) & 0x7ffffu;
+    return (static_cast<unsigned long long>(bnd) << 57) | (ux << 38) | (uy << 19) | uz;
+}
+
+// Each point goes into its own band's grid and into neighbouring bands within one cell; entry
+// 3 * i + j holds the j-th insertion of point i.
 __global__ void k_dror_insert(BatchDev b)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -103,33 +120,50 @@ __global__ void k_dror_insert(BatchDev b)
     const int s = scan_of_src(b, i);
     const ScanDev& sd = b.scans[s];
     ScanState& st = b.state[s];
-    int32_t ix, iy, iz;
-    cell_of(b.src[i], st.dcell, ix, iy, iz);
-    const unsigned long long key = cell_key(ix, iy, iz);
+    const float4 p = b.src[i];
+    const float rho_c = band_rho_c(sd);
+    const float rho = horiz(p);
+    const int own = band_of(rho, rho_c);
+    const float margin = band_cell(sd, min(own + 1, kBands - 1), rho_c) * 1.01f;
+    const int lo = band_of(fmaxf(rho - margin, 0.0f), rho_c);
+    const int hi = min(band_of(rho + margin, rho_c), lo + 2);
     const uint32_t mask = sd.dhash_cap - 1u;
-    uint32_t h = static_cast<uint32_t>(mix64(key)) & mask;
-    for (uint32_t probe = 0; probe < sd.dhash_cap; ++probe)
+    for (int j = 0; j < 3; ++j)
     {
-        const uint32_t slot = sd.dhash_off + h;
-        const unsigned long long prev = atomicCAS(&b.dkey[slot], kDEmpty, key);
-        if (prev == kDEmpty || prev == key)
+        const uint32_t e = 3u * i + static_cast<uint32_t>(j);
+        b.dslot[e] = 0xffffffffu;
+        const int bnd = lo + j;
+        if (bnd > hi)
+            continue;
+        int32_t ix, iy, iz;
+        cell_of(p, band_cell(sd, bnd, rho_c), ix, iy, iz);
+        const unsigned long long key = band_key(bnd, ix, iy, iz);
+        uint32_t h = static_cast<uint32_t>(mix64(key)) & mask;
+        bool placed = false;
+        for (uint32_t probe = 0; probe < sd.dhash_cap; ++probe)
         {
-            b.dslot[i] = slot;
-            b.drank[i] = atomicAdd(&b.dcnt[slot], 1u);
-            return;
+            const uint32_t slot = sd.dhash_off + h;
+            const unsigned long long prev = atomicCAS(&b.dkey[slot], kDEmpty, key);
+            if (prev == kDEmpty || prev == key)
+            {
+                b.dslot[e] = slot;
+                b.drank[e] = atomicAdd(&b.dcnt[slot], 1u);
+                placed = true;
+                break;
+            }
+            h = (h + 1u) & mask;
         }
-        h = (h + 1u) & mask;
+        if (!placed)
+            raise_err(&st, ERR_HASH_FULL);
     }
-    raise_err(&st, ERR_HASH_FULL);
-    b.dslot[i] = 0xffffffffu;
 }
 
 __global__ void k_dror_scatter(BatchDev b)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.nsrc || b.dslot[i] == 0xffffffffu)
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 3u * b.nsrc || b.dslot[e] == 0xffffffffu)
         return;
-    b.dorder[b.dstart[b.dslot[i]] + b.drank[i]] = i;
+    b.dorder[b.dstart[b.dslot[e]] + b.drank[e]] = e / 3u;
 }
 
 __device__ __forceinline__ uint32_t dlookup(const BatchDev& b, const ScanDev& sd, unsigned long long key)
@@ -155,18 +189,19 @@ __global__ void k_dror_query(BatchDev b)
         return;
     const int s = scan_of_src(b, i);
     const ScanDev& sd = b.scans[s];
-    const ScanState& st = b.state[s];
     const float4 q = b.src[i];
     const float r2 = b.dr2[i];
+    const float rho_c = band_rho_c(sd);
+    const int bnd = band_of(horiz(q), rho_c);
     int32_t ix, iy, iz;
-    cell_of(q, st.dcell, ix, iy, iz);
+    cell_of(q, band_cell(sd, bnd, rho_c), ix, iy, iz);
     uint32_t cnt = 0;
     const uint32_t k = sd.dror_k;
     for (int dz = -1; dz <= 1 && cnt < k; ++dz)
         for (int dy = -1; dy <= 1 && cnt < k; ++dy)
             for (int dx = -1; dx <= 1 && cnt < k; ++dx)
             {
-                const uint32_t slot = dlookup(b, sd, cell_key(ix + dx, iy + dy, iz + dz));
+                const uint32_t slot = dlookup(b, sd, band_key(bnd, ix + dx, iy + dy, iz + dz));
                 if (slot == 0xffffffffu)
                     continue;
                 const uint32_t a = b.dstart[slot], e = b.dstart[slot + 1];
@@ -243,10 +278,9 @@ void launch_noise(Launcher& L, const BatchDev& b, const BatchHost& hb, const lp_
     (void)cfg;
     const uint32_t T = 256;
     LP_LAUNCH(L, k_dror_r2, div_up(b.nsrc, T), T, b);
-    LP_LAUNCH(L, k_dror_cell, div_up(static_cast<uint32_t>(b.nscan), 64u), 64, b);
     LP_LAUNCH(L, k_dror_insert, div_up(b.nsrc, T), T, b);
     L.scan(b.dcnt, b.dstart, b.ndhash + 1);
-    LP_LAUNCH(L, k_dror_scatter, div_up(b.nsrc, T), T, b);
+    LP_LAUNCH(L, k_dror_scatter, div_up(3u * b.nsrc, T), T, b);
     LP_LAUNCH(L, k_dror_query, div_up(b.nsrc, T), T, b);
 }
 
