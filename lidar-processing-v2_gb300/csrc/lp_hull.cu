@@ -357,7 +357,7 @@ __device__ void block_sort_global(HPt<T>* a, uint32_t n)
 constexpr int kDirs = 16;         // extreme-point directions of the initial polygon
 constexpr int kPolyCap = 256;     // refined polygon capacity
 constexpr int kRefineRounds = 12; // farthest-point insertion rounds
-constexpr uint32_t kBigCluster = 2048;
+constexpr uint32_t kBigCluster = 512; // larger clusters take a whole CTA; smaller ones one warp
 
 struct HullSmem
 {
@@ -721,8 +721,188 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
     __syncthreads();
 }
 
-// Work items: every cluster of the batch, big ones first (they bound the kernel's tail).
-// queue[2] counts big clusters listed from the front of `work`, queue[3] small ones from the back.
+// ---------------------------------------------------------------------------------------------
+// Warp path for clusters of at most kBigCluster members: the same steps as hull_one without CTA
+// barriers (the 16-direction polygon is the prefilter; candidates rarely exceed a warp's buffer,
+// and then the sort and the chain stack move to global scratch).
+// ---------------------------------------------------------------------------------------------
+constexpr int kWarpCand = 256;
+
+struct WarpSmem
+{
+    HPt<float> cand[kWarpCand];
+    int stack[2 * kWarpCand + 2];
+    double2 hp[kWarpCand];
+    float2 poly[kDirs];
+    int npoly;
+};
+
+__device__ void hull_one_warp(const BatchDev& b, WarpSmem& ws, const float2* dirs, uint32_t g, int s, int compute_obb)
+{
+    ScanState* st = &b.state[s];
+    const uint32_t n = b.cl_cnt[g];
+    const uint32_t start = b.cl_start[g];
+    const uint32_t* mem = b.members + start;
+    const uint32_t lane = lane_id();
+    float zmn = INFINITY, zmx = -INFINITY;
+    unsigned long long ext[kDirs];
+#pragma unroll
+    for (int d = 0; d < kDirs; ++d)
+        ext[d] = 0ull;
+    for (uint32_t i = lane; i < n; i += 32)
+    {
+        const float4 p = b.obs_pts[mem[i]];
+        zmn = fminf(zmn, p.z);
+        zmx = fmaxf(zmx, p.z);
+#pragma unroll
+        for (int d = 0; d < kDirs; ++d)
+        {
+            const unsigned long long key = fkey_payload(p.x * dirs[d].x + p.y * dirs[d].y, i);
+            ext[d] = key > ext[d] ? key : ext[d];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        zmn = fminf(zmn, __shfl_xor_sync(0xffffffffu, zmn, o));
+        zmx = fmaxf(zmx, __shfl_xor_sync(0xffffffffu, zmx, o));
+    }
+#pragma unroll
+    for (int d = 0; d < kDirs; ++d)
+        ext[d] = warp_max64(ext[d]);
+    if (lane == 0)
+    {
+        b.cl_zmin[g] = zmn;
+        b.cl_zmax[g] = zmx;
+        int np = 0;
+        uint32_t prev = 0xffffffffu;
+        for (int d = 0; d < kDirs; ++d)
+        {
+            const uint32_t i = static_cast<uint32_t>(ext[d] & 0xffffffffull);
+            if (n > 0 && i != prev)
+            {
+                const float4 p = b.obs_pts[mem[i]];
+                ws.poly[np++] = make_float2(p.x, p.y);
+                prev = i;
+            }
+        }
+        if (np > 1 && ws.poly[np - 1].x == ws.poly[0].x && ws.poly[np - 1].y == ws.poly[0].y)
+            --np;
+        ws.npoly = np;
+    }
+    __syncwarp();
+    int32_t* hull_dst = b.hull_tmp + start;
+    if (n < 3)
+    {
+        if (lane == 0)
+        {
+            for (uint32_t i = 0; i < n; ++i)
+                hull_dst[i] = static_cast<int32_t>(i);
+            b.hull_cnt[g] = n;
+            if (compute_obb)
+            {
+                lp_bounding_box z;
+                memset(&z, 0, sizeof(z));
+                b.obb_c[g] = z;
+                b.obb_p[g] = z;
+            }
+        }
+        __syncwarp();
+        return;
+    }
+    const int npf = ws.npoly;
+    auto inside = [&](double px, double py) {
+        if (npf < 3)
+            return false;
+        for (int d = 0; d < npf; ++d)
+        {
+            const float2 a = ws.poly[d], c = ws.poly[(d + 1 == npf) ? 0 : d + 1];
+            if (!left_strict(a.x, a.y, c.x, c.y, px, py))
+                return false;
+        }
+        return true;
+    };
+    HPt<float>* gs = reinterpret_cast<HPt<float>*>(b.hs_cand) + 2ull * start; // capacity 2n >= next_pow2(n)
+    uint32_t m = 0;
+    for (uint32_t base = 0; base < n; base += 32)
+    {
+        const uint32_t i = base + lane;
+        bool keep = false;
+        HPt<float> c{0.0f, 0.0f, 0u};
+        if (i < n)
+        {
+            const uint32_t o = mem[i];
+            const float4 p = b.obs_pts[o];
+            keep = !inside(p.x, p.y);
+            c = HPt<float>{p.x, p.y, o};
+        }
+        const uint32_t mask = __ballot_sync(0xffffffffu, keep);
+        if (keep)
+        {
+            const uint32_t pos = m + __popc(mask & ((1u << lane) - 1u));
+            if (pos < static_cast<uint32_t>(kWarpCand))
+                ws.cand[pos] = c;
+            gs[pos] = c;
+        }
+        m += __popc(mask);
+    }
+    __syncwarp();
+    const bool small = m <= static_cast<uint32_t>(kWarpCand);
+    HPt<float>* C = small ? ws.cand : gs;
+    int* H = small ? ws.stack : (b.hs_stack + 2ull * start + 2ull * g);
+    const uint32_t np2 = next_pow2(m);
+    for (uint32_t i = m + lane; i < np2; i += 32)
+        C[i] = HPt<float>{INFINITY, INFINITY, 0xffffffffu};
+    __syncwarp();
+    warp_bitonic_smem(C, np2, [](const HPt<float>& x, const HPt<float>& y) { return hpt_less(x, y); });
+    int h = 0;
+    if (lane == 0)
+        h = monotone_chain(C, static_cast<int>(m), H);
+    h = __shfl_sync(0xffffffffu, h, 0);
+    __syncwarp();
+    for (int j = 0; j < h; ++j)
+    {
+        const uint32_t key = C[H[j]].key;
+        uint32_t cnt = 0;
+        for (uint32_t base = 0; base < n; base += 32)
+        {
+            const uint32_t i = base + lane;
+            cnt += __popc(__ballot_sync(0xffffffffu, (i < n) && (mem[i] < key)));
+        }
+        if (lane == 0)
+            hull_dst[j] = static_cast<int32_t>(cnt);
+    }
+    if (lane == 0)
+        b.hull_cnt[g] = static_cast<uint32_t>(h);
+    if (compute_obb)
+    {
+        double2* P = (h <= kWarpCand) ? ws.hp : (b.hs_pts + start);
+        for (int j = static_cast<int>(lane); j < h; j += 32)
+            P[j] = make_double2(static_cast<double>(C[H[j]].x), static_cast<double>(C[H[j]].y));
+        __syncwarp();
+        int2* pairs = b.hs_pairs + 4ull * start + 16ull * g;
+        const int cap = 4 * h + 16;
+        int npairs = 0;
+        if (lane == 0)
+            npairs = antipodal_pairs(P, h, pairs, cap);
+        npairs = __shfl_sync(0xffffffffu, npairs, 0);
+        if (npairs > cap)
+        {
+            if (lane == 0)
+                raise_err(st, ERR_INTERNAL);
+            npairs = cap;
+        }
+        __syncwarp();
+        calipers_warp(P, h, pairs, npairs, &b.obb_c[g]);
+        if (lane == 0)
+            pca_box(P, h, &b.obb_p[g]);
+    }
+    __syncwarp();
+}
+
+// Work items: every cluster of the batch. queue[2] counts clusters of more than kBigCluster
+// members (listed from the front of `work`, taken by whole CTAs first), queue[3] the others
+// (listed from the back, taken one warp each).
 __global__ void k_hull_worklist(BatchDev b, uint32_t* work)
 {
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -743,17 +923,25 @@ __device__ __forceinline__ uint32_t work_item(const BatchDev& b, const uint32_t*
     return (w < nbig) ? work[w] : work[b.ncl - 1u - (w - nbig)];
 }
 
-// Persistent CTAs pull clusters from the work queue until it is empty.
+constexpr size_t kHullDynSmem = sizeof(HullSmem) > (kHullThreads / 32) * sizeof(WarpSmem)
+                                    ? sizeof(HullSmem)
+                                    : (kHullThreads / 32) * sizeof(WarpSmem);
+
+// Persistent CTAs: first every large cluster (one CTA each, queue[1] is the head), then every
+// small cluster (one warp each, queue[4] is the head).
 __global__ void __launch_bounds__(kHullThreads) k_hull(BatchDev b, int compute_obb, const uint32_t* work)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ float2 dirs[kDirs];
     HullSmem& sm = *reinterpret_cast<HullSmem*>(smraw);
     if (threadIdx.x < kDirs)
     {
         const float a = 6.28318530717958647692f * static_cast<float>(threadIdx.x) / kDirs;
-        sm.dirs[threadIdx.x] = make_float2(cosf(a), sinf(a));
+        dirs[threadIdx.x] = make_float2(cosf(a), sinf(a));
+        sm.dirs[threadIdx.x] = dirs[threadIdx.x];
     }
-    const uint32_t total = b.queue[2] + b.queue[3];
+    const uint32_t nbig = b.queue[2];
+    const uint32_t nsmall = b.queue[3];
     for (;;)
     {
         __syncthreads();
@@ -761,11 +949,25 @@ __global__ void __launch_bounds__(kHullThreads) k_hull(BatchDev b, int compute_o
             sm.work = atomicAdd(&b.queue[1], 1u);
         __syncthreads();
         const uint32_t w = sm.work;
-        if (w >= total)
+        if (w >= nbig)
             break;
-        const uint32_t g = work_item(b, work, w);
+        const uint32_t g = work[w];
         const int s = find_scan(b.nscan, g, [&](int q) { return b.scans[q].cl_off; });
         hull_one(b, sm, g, s, compute_obb);
+    }
+    __syncthreads(); // the CTA's shared memory now becomes eight per-warp regions
+    WarpSmem& ws = reinterpret_cast<WarpSmem*>(smraw)[threadIdx.x >> 5];
+    for (;;)
+    {
+        uint32_t w = 0;
+        if (lane_id() == 0)
+            w = atomicAdd(&b.queue[4], 1u);
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (w >= nsmall)
+            break;
+        const uint32_t g = work[b.ncl - 1u - w];
+        const int s = find_scan(b.nscan, g, [&](int q) { return b.scans[q].cl_off; });
+        hull_one_warp(b, ws, dirs, g, s, compute_obb);
     }
 }
 
@@ -835,7 +1037,7 @@ void launch_polygons(Launcher& L, const BatchDev& b, const BatchHost& hb, int co
     uint32_t* work = b.cl_fill;
     LP_LAUNCH(L, k_hull_worklist, div_up(b.ncl, 256u), 256, b, work);
     const int sms = sm_count();
-    LP_LAUNCH_SMEM(L, k_hull, static_cast<uint32_t>(sms * 2), kHullThreads, sizeof(HullSmem), b, compute_obb,
+    LP_LAUNCH_SMEM(L, k_hull, static_cast<uint32_t>(sms * 2), kHullThreads, kHullDynSmem, b, compute_obb,
                    static_cast<const uint32_t*>(work));
     L.scan(b.hull_cnt, b.hull_cnt, b.ncl + 1);
     LP_LAUNCH(L, k_hull_compact, static_cast<uint32_t>(sms * 8), 128, b, static_cast<const uint32_t*>(work));
@@ -843,7 +1045,7 @@ void launch_polygons(Launcher& L, const BatchDev& b, const BatchHost& hb, int co
 
 void init_kernel_attributes()
 {
-    cudaFuncSetAttribute(k_hull, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sizeof(HullSmem)));
+    cudaFuncSetAttribute(k_hull, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kHullDynSmem));
 }
 
 int sm_count()
