@@ -62,21 +62,7 @@ __device__ __forceinline__ uint32_t ford(float f)
     const uint32_t u = __float_as_uint(f);
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
-__device__ __forceinline__ float funord(uint32_t u)
-{
-    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
-}
 
-__device__ __forceinline__ unsigned long long warp_min64(unsigned long long v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        const unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
-        v = t < v ? t : v;
-    }
-    return v;
-}
 __device__ __forceinline__ unsigned long long warp_max64(unsigned long long v)
 {
 #pragma unroll
@@ -102,15 +88,6 @@ __device__ __forceinline__ double warp_max_d(double v)
     return v;
 }
 
-// Strictly inside the quadrilateral a->b->c->d (counter-clockwise), with a relative margin.
-__device__ __forceinline__ bool left_strict(double ax, double ay, double bx, double by, double px, double py)
-{
-    const double ex = bx - ax, ey = by - ay, qx = px - ax, qy = py - ay;
-    const double cr = ex * qy - ey * qx;
-    const double scale = (fabs(ex) + fabs(ey)) * (fabs(qx) + fabs(qy));
-    return cr > 1e-9 * scale + 1e-300;
-}
-
 // ---------------------------------------------------------------------------------------------
 // Shamos antipodal pairs (polygonizer.cpp:93-163) for the hull P[0..n), written to `pairs`.
 // ---------------------------------------------------------------------------------------------
@@ -120,13 +97,69 @@ __device__ __forceinline__ double tri_area(double ax, double ay, double bx, doub
     return fabs((ax * (by - cy) + bx * (cy - ay) + cx * (ay - by)) * 0.5);
 }
 
-__device__ int antipodal_pairs(const double2* P, int n, int2* pairs, int cap)
+// Triangle-area comparisons of the pair walk, evaluated in FP64 exactly as the reference does.
+struct AreaCmpFp64
+{
+    const double2* P;
+    __device__ __forceinline__ double ad(int a, int b, int c) const
+    {
+        return tri_area(P[a].x, P[a].y, P[b].x, P[b].y, P[c].x, P[c].y);
+    }
+    __device__ __forceinline__ bool gt(int a1, int b1, int c1, int a2, int b2, int c2) const
+    {
+        return ad(a1, b1, c1) > ad(a2, b2, c2);
+    }
+    __device__ __forceinline__ bool eq(int a1, int b1, int c1, int a2, int b2, int c2) const
+    {
+        return ad(a1, b1, c1) == ad(a2, b2, c2);
+    }
+};
+
+// The same comparisons decided in FP32 where the float areas differ by more than `tol`, else in
+// FP64. Float areas use coordinates relative to (ox, oy): with every |local vertex| <= R the
+// float area is within 1.02e-6 R^2 of the exact area of the (float-valued) vertices, and the FP64
+// area of the reference within 1e-14 M R (M the largest |coordinate|). tol is at least twice the
+// sum of both bounds, so a decision taken in FP32 is the one FP64 takes.
+struct AreaCmpFiltered
+{
+    const double2* P;
+    const float2* Pf; // the same vertices as floats (exact: they are float points)
+    float ox, oy, tol;
+    __device__ __forceinline__ float af(int a, int b, int c) const
+    {
+        const float ax = Pf[a].x - ox, ay = Pf[a].y - oy;
+        const float bx = Pf[b].x - ox, by = Pf[b].y - oy;
+        const float cx = Pf[c].x - ox, cy = Pf[c].y - oy;
+        return fabsf((ax * (by - cy) + bx * (cy - ay) + cx * (ay - by)) * 0.5f);
+    }
+    __device__ __forceinline__ double ad(int a, int b, int c) const
+    {
+        return tri_area(P[a].x, P[a].y, P[b].x, P[b].y, P[c].x, P[c].y);
+    }
+    __device__ __forceinline__ bool gt(int a1, int b1, int c1, int a2, int b2, int c2) const
+    {
+        const float d = af(a1, b1, c1) - af(a2, b2, c2);
+        if (d > tol)
+            return true;
+        if (d < -tol)
+            return false;
+        return ad(a1, b1, c1) > ad(a2, b2, c2);
+    }
+    __device__ __forceinline__ bool eq(int a1, int b1, int c1, int a2, int b2, int c2) const
+    {
+        if (fabsf(af(a1, b1, c1) - af(a2, b2, c2)) > tol)
+            return false;
+        return ad(a1, b1, c1) == ad(a2, b2, c2);
+    }
+};
+
+template <typename Cmp>
+__device__ int antipodal_pairs(const Cmp& cmp, int n, int2* pairs, int cap)
 {
     int np = 0;
     if (n < 2)
         return 0;
     auto nx = [n](int i) { return (i + 1 == n) ? 0 : i + 1; };
-    auto ar = [P](int a, int b, int c) { return tri_area(P[a].x, P[a].y, P[b].x, P[b].y, P[c].x, P[c].y); };
     auto push = [&](int a, int b) {
         if (np < cap)
             pairs[np] = make_int2(a, b);
@@ -135,7 +168,8 @@ __device__ int antipodal_pairs(const double2* P, int n, int2* pairs, int cap)
     const int i0 = n - 1;
     int i = 0, j = 1;
     int guard = 0;
-    while (ar(i, nx(i), nx(j)) > ar(i, nx(i), j) && guard++ < 4 * n + 8)
+    // areaOfTriangle(i, i+1, j+1) > areaOfTriangle(i, i+1, j)
+    while (cmp.gt(i, nx(i), nx(j), i, nx(i), j) && guard++ < 4 * n + 8)
         j = nx(j);
     const int j0 = j;
     guard = 0;
@@ -144,7 +178,7 @@ __device__ int antipodal_pairs(const double2* P, int n, int2* pairs, int cap)
         i = nx(i);
         push(i, j);
         int g2 = 0;
-        while (ar(i, nx(i), nx(j)) > ar(i, nx(i), j) && g2++ < 4 * n + 8)
+        while (cmp.gt(i, nx(i), nx(j), i, nx(i), j) && g2++ < 4 * n + 8)
         {
             j = nx(j);
             if (!(i == j0 && j == i0))
@@ -152,7 +186,7 @@ __device__ int antipodal_pairs(const double2* P, int n, int2* pairs, int cap)
             else
                 return np;
         }
-        if (ar(j, nx(i), nx(j)) == ar(i, nx(i), j))
+        if (cmp.eq(j, nx(i), nx(j), i, nx(i), j))
         {
             if (!(i == j0 && j == i0))
                 push(i, nx(j));
@@ -161,6 +195,21 @@ __device__ int antipodal_pairs(const double2* P, int n, int2* pairs, int cap)
         }
     }
     return np;
+}
+
+__device__ __forceinline__ float warp_min_f(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max_f(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
 }
 
 // Rotating calipers (polygonizer.cpp:165-278) by one warp: all lanes return the same box.
@@ -304,6 +353,343 @@ __device__ void pca_box(const double2* P, int n, lp_bounding_box* out)
     *out = box;
 }
 
+// PCA box by one warp, the same arithmetic as pca_box: the sums run in the same order on every
+// lane; the rotated min/max is split across lanes (min and max are exact, so the extents are the
+// sequential loop's).
+__device__ void pca_box_warp(const double2* P, int n, lp_bounding_box* out)
+{
+    const uint32_t lane = lane_id();
+    lp_bounding_box box;
+    for (int k = 0; k < 4; ++k)
+        box.corners[k][0] = box.corners[k][1] = 0.0;
+    box.area = 0.0f;
+    box.angle_rad = 0.0f;
+    box.is_valid = 0;
+    if (n >= 3)
+    {
+        double mx = 0.0, my = 0.0;
+        for (int i = 0; i < n; ++i)
+        {
+            mx += P[i].x;
+            my += P[i].y;
+        }
+        mx /= n;
+        my /= n;
+        double sxx = 0.0, sxy = 0.0, syy = 0.0;
+        for (int i = 0; i < n; ++i)
+        {
+            const double dx = P[i].x - mx, dy = P[i].y - my;
+            sxx += dx * dx;
+            sxy += dx * dy;
+            syy += dy * dy;
+        }
+        sxx /= (n - 1);
+        sxy /= (n - 1);
+        syy /= (n - 1);
+        const double theta = 0.5 * atan2(2.0 * sxy, sxx - syy);
+        const double v00 = cos(theta), v10 = sin(theta);
+        const double v01 = -v10, v11 = v00;
+        double mnx = DBL_MAX, mxx = -DBL_MAX, mny = DBL_MAX, mxy = -DBL_MAX;
+        for (int i = static_cast<int>(lane); i < n; i += 32)
+        {
+            const double dx = P[i].x - mx, dy = P[i].y - my;
+            const double rx = dx * v00 + dy * v10;
+            const double ry = dx * v01 + dy * v11;
+            mnx = fmin(mnx, rx);
+            mxx = fmax(mxx, rx);
+            mny = fmin(mny, ry);
+            mxy = fmax(mxy, ry);
+        }
+        mnx = warp_min_d(mnx);
+        mxx = warp_max_d(mxx);
+        mny = warp_min_d(mny);
+        mxy = warp_max_d(mxy);
+        const double xs[4] = {mnx, mxx, mxx, mnx};
+        const double ys[4] = {mny, mny, mxy, mxy};
+        for (int k = 0; k < 4; ++k)
+        {
+            box.corners[k][0] = xs[k] * v00 + ys[k] * v01 + mx;
+            box.corners[k][1] = xs[k] * v10 + ys[k] * v11 + my;
+        }
+        box.area = __double2float_rn((mxx - mnx) * (mxy - mny));
+        box.angle_rad = __double2float_rn(atan2(v10, v00));
+        box.is_valid = 1;
+    }
+    if (lane == 0)
+        *out = box;
+}
+
+// FP64 rotated extents of P about (cx, cy) for the unit direction (ux, uy), by one warp.
+__device__ __forceinline__ void extents_fp64(const double2* P, int n, double cx, double cy, double ux, double uy,
+                                             double& mnx, double& mxx, double& mny, double& mxy)
+{
+    mnx = DBL_MAX, mxx = -DBL_MAX, mny = DBL_MAX, mxy = -DBL_MAX;
+    for (int k = static_cast<int>(lane_id()); k < n; k += 32)
+    {
+        const double tx = P[k].x - cx, ty = P[k].y - cy;
+        const double rx = tx * ux + ty * uy;
+        const double ry = -tx * uy + ty * ux;
+        mnx = fmin(mnx, rx);
+        mxx = fmax(mxx, rx);
+        mny = fmin(mny, ry);
+        mxy = fmax(mxy, ry);
+    }
+    mnx = warp_min_d(mnx);
+    mxx = warp_max_d(mxx);
+    mny = warp_min_d(mny);
+    mxy = warp_max_d(mxy);
+}
+
+// Rotating calipers with the candidate boxes screened in FP32 (same result as calipers_warp).
+//
+// The reference walks the edges named by the antipodal pairs and keeps a box when its FP64 area
+// is below the float `best` of the boxes kept so far. An edge's box area is the same for both
+// directions of the edge (every term only changes sign), so it is computed once per hull edge j
+// (P[j] -> P[j+1]): ea[j] = FP32 area, within e = 1e-4 R^2 of the FP64 area (the rounding of
+// the float frame, direction and extents stays below 6e-6 R^2, R = largest |P - P[0]|). Edges with
+// ea[j] <= T are the contenders, with T grown from the smallest ea until no other edge lies within
+// G = 2e + 1e-6 (T + 2e) above it. Every other edge then has a float area above every contender's
+// FP64 area and above the float of the smallest area, so (i) the last box the reference keeps is a
+// contender's and (ii) replaying the reference's walk over the contenders alone, with their FP64
+// areas, keeps the same boxes among them. The winner's box is computed in FP64 as written.
+// Up to 32 contenders (one per lane) are handled; more fall back to calipers_warp.
+__device__ void calipers_fast(const double2* P, const float2* Pf, int n, const int2* pairs, int npairs, float* ea,
+                              float r2, lp_bounding_box* out)
+{
+    const uint32_t lane = lane_id();
+    lp_bounding_box box;
+    for (int k = 0; k < 4; ++k)
+        box.corners[k][0] = box.corners[k][1] = 0.0;
+    box.area = 0.0f;
+    box.angle_rad = 0.0f;
+    box.is_valid = 0;
+    if (n < 3)
+    {
+        if (lane == 0)
+            *out = box;
+        return;
+    }
+    const float ox = Pf[0].x, oy = Pf[0].y;
+    const float e = 1e-4f * r2 + 1e-30f;
+    float amin = INFINITY;
+    for (int j = static_cast<int>(lane); j < n; j += 32)
+    {
+        const int j1 = (j + 1 == n) ? 0 : j + 1;
+        const double dx = P[j1].x - P[j].x, dy = P[j1].y - P[j].y;
+        float a = INFINITY; // edges the reference skips never compete
+        if (!(sqrt(dx * dx + dy * dy) < 1.0e-6))
+        {
+            const float fx = Pf[j1].x - Pf[j].x, fy = Pf[j1].y - Pf[j].y;
+            const float fl = sqrtf(fx * fx + fy * fy);
+            const float ux = fx / fl, uy = fy / fl;
+            float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
+            for (int k = 0; k < n; ++k)
+            {
+                const float tx = Pf[k].x - ox, ty = Pf[k].y - oy;
+                const float rx = tx * ux + ty * uy;
+                const float ry = -tx * uy + ty * ux;
+                mnx = fminf(mnx, rx);
+                mxx = fmaxf(mxx, rx);
+                mny = fminf(mny, ry);
+                mxy = fmaxf(mxy, ry);
+            }
+            a = (mxx - mnx) * (mxy - mny);
+        }
+        ea[j] = a;
+        amin = fminf(amin, a);
+    }
+    amin = warp_min_f(amin);
+    __syncwarp();
+    if (amin == INFINITY)
+    {
+        if (lane == 0)
+            *out = box; // every edge is skipped: no box, as in the reference
+        return;
+    }
+    float T = amin;
+    for (int it = 0; it <= n; ++it)
+    {
+        const float G = 2.0f * e + 1e-6f * (T + 2.0f * e);
+        float nt = T;
+        for (int j = static_cast<int>(lane); j < n; j += 32)
+            if (ea[j] > T && ea[j] <= T + G)
+                nt = fmaxf(nt, ea[j]);
+        nt = warp_max_f(nt);
+        if (nt == T)
+            break;
+        T = nt;
+    }
+    // FP64 centroid of the hull vertices, summed in the reference's order
+    double cx = 0.0, cy = 0.0;
+    for (int k = 0; k < n; ++k)
+    {
+        cx += P[k].x;
+        cy += P[k].y;
+    }
+    cx /= n;
+    cy /= n;
+    // contender c (in edge order) is held by lane c: its edge and FP64 area
+    int my_j = -1;
+    double my_area = 0.0;
+    int ncont = 0;
+    for (int base = 0; base < n; base += 32)
+    {
+        const int j = base + static_cast<int>(lane);
+        const uint32_t mask = __ballot_sync(0xffffffffu, j < n && ea[j] <= T);
+        for (uint32_t mm = mask; mm != 0u; mm &= mm - 1u)
+        {
+            const int jj = base + __ffs(mm) - 1;
+            if (ncont < 32)
+            {
+                const int j1 = (jj + 1 == n) ? 0 : jj + 1;
+                const double ex = P[j1].x - P[jj].x, ey = P[j1].y - P[jj].y;
+                const double len = sqrt(ex * ex + ey * ey);
+                const double ux = ex / len, uy = ey / len;
+                double mnx, mxx, mny, mxy;
+                extents_fp64(P, n, cx, cy, ux, uy, mnx, mxx, mny, mxy);
+                if (static_cast<int>(lane) == ncont)
+                {
+                    my_j = jj;
+                    my_area = (mxx - mnx) * (mxy - mny);
+                }
+            }
+            ++ncont;
+        }
+    }
+    if (ncont > 32)
+    {
+        calipers_warp(P, n, pairs, npairs, out);
+        return;
+    }
+    // the reference's walk over the contenders
+    float best = __double2float_rn(DBL_MAX);
+    int wi = -1, wnb = -1;
+    for (int pi = 0; pi < npairs; ++pi)
+    {
+        const int2 pr = pairs[pi];
+        for (int e2 = 0; e2 < 2; ++e2)
+        {
+            const int index = e2 == 0 ? pr.x : pr.y;
+            for (int o = 0; o < 2; ++o)
+            {
+                int nb = index + (o == 0 ? -1 : 1);
+                if (nb < 0)
+                    nb += n;
+                else if (nb >= n)
+                    nb -= n;
+                const int j = (o == 1) ? index : nb; // hull edge j joins P[j] and P[j+1]
+                if (!(ea[j] <= T))
+                    continue;
+                const uint32_t hold = __ballot_sync(0xffffffffu, my_j == j);
+                const double area = __shfl_sync(0xffffffffu, my_area, __ffs(hold) - 1);
+                if (area < static_cast<double>(best))
+                {
+                    best = __double2float_rn(area);
+                    wi = index;
+                    wnb = nb;
+                }
+            }
+        }
+    }
+    if (wi >= 0)
+    {
+        const double ex = P[wnb].x - P[wi].x;
+        const double ey = P[wnb].y - P[wi].y;
+        const double len = sqrt(ex * ex + ey * ey);
+        const double ux = ex / len, uy = ey / len;
+        double mnx, mxx, mny, mxy;
+        extents_fp64(P, n, cx, cy, ux, uy, mnx, mxx, mny, mxy);
+        box.area = best;
+        box.corners[0][0] = mnx * ux - mny * uy + cx;
+        box.corners[0][1] = mnx * uy + mny * ux + cy;
+        box.corners[1][0] = mxx * ux - mny * uy + cx;
+        box.corners[1][1] = mxx * uy + mny * ux + cy;
+        box.corners[2][0] = mxx * ux - mxy * uy + cx;
+        box.corners[2][1] = mxx * uy + mxy * ux + cy;
+        box.corners[3][0] = mnx * ux - mxy * uy + cx;
+        box.corners[3][1] = mnx * uy + mxy * ux + cy;
+        box.angle_rad = lpm::atan2_approx(__double2float_rn(uy), __double2float_rn(ux));
+        box.is_valid = 1;
+    }
+    if (lane == 0)
+        *out = box;
+}
+
+// Antipodal pairs and the rotating-calipers box of hull P (h vertices) by one warp. With float
+// copies Pf and h floats of scratch ea the comparisons are screened in FP32; without them
+// (Pf == nullptr) everything runs in FP64.
+__device__ void calipers_box(ScanState* st, const double2* P, const float2* Pf, float* ea, int h, int2* pairs,
+                             lp_bounding_box* out)
+{
+    const uint32_t lane = lane_id();
+    const int cap = 4 * h + 16;
+    int npairs = 0;
+    if (Pf != nullptr)
+    {
+        const float ox = Pf[0].x, oy = Pf[0].y;
+        float r2 = 0.0f, mabs = 0.0f;
+        for (int k = static_cast<int>(lane); k < h; k += 32)
+        {
+            const float lx = Pf[k].x - ox, ly = Pf[k].y - oy;
+            r2 = fmaxf(r2, lx * lx + ly * ly);
+            mabs = fmaxf(mabs, fmaxf(fabsf(Pf[k].x), fabsf(Pf[k].y)));
+        }
+        r2 = warp_max_f(r2) * 1.001f;
+        mabs = warp_max_f(mabs);
+        const AreaCmpFiltered cmp{P, Pf, ox, oy, 2.0f * (4e-6f * r2 + 1e-13f * mabs * sqrtf(r2)) + 1e-30f};
+        if (lane == 0)
+            npairs = antipodal_pairs(cmp, h, pairs, cap);
+        npairs = __shfl_sync(0xffffffffu, npairs, 0);
+        if (npairs > cap)
+        {
+            if (lane == 0)
+                raise_err(st, ERR_INTERNAL);
+            npairs = cap;
+        }
+        __syncwarp();
+        calipers_fast(P, Pf, h, pairs, npairs, ea, r2, out);
+    }
+    else
+    {
+        if (lane == 0)
+            npairs = antipodal_pairs(AreaCmpFp64{P}, h, pairs, cap);
+        npairs = __shfl_sync(0xffffffffu, npairs, 0);
+        if (npairs > cap)
+        {
+            if (lane == 0)
+                raise_err(st, ERR_INTERNAL);
+            npairs = cap;
+        }
+        __syncwarp();
+        calipers_warp(P, h, pairs, npairs, out);
+    }
+}
+
+// Orientation test of the monotone chain for float points: decided in FP32 when the float
+// determinant exceeds 2^-21 (|t1| + |t2|) in magnitude (its rounding error stays below
+// 6 * 2^-24 of that sum, the FP64 form's below 3 * 2^-53), else evaluated in FP64 as written.
+__device__ __forceinline__ bool ccw_or_colinear_f(float ax, float ay, float bx, float by, float cx, float cy)
+{
+    const float t1 = (bx - ax) * (cy - ay);
+    const float t2 = (by - ay) * (cx - ax);
+    const float d = t1 - t2;
+    const float bound = (fabsf(t1) + fabsf(t2)) * 4.76837158203125e-7f + 1e-30f;
+    if (d > bound)
+        return false;
+    if (d < -bound)
+        return true;
+    return ccw_or_colinear(ax, ay, bx, by, cx, cy);
+}
+
+__device__ __forceinline__ bool chain_pops(const HPt<float>& a, const HPt<float>& b, const HPt<float>& c)
+{
+    return ccw_or_colinear_f(a.x, a.y, b.x, b.y, c.x, c.y);
+}
+__device__ __forceinline__ bool chain_pops(const HPt<double>& a, const HPt<double>& b, const HPt<double>& c)
+{
+    return ccw_or_colinear(a.x, a.y, b.x, b.y, c.x, c.y);
+}
+
 // Monotone chain over sorted candidates C[0..m) (polygonizer.cpp:62-88) by one thread.
 // Writes candidate positions of the hull to H (capacity 2m) and returns the hull size.
 template <typename T>
@@ -312,17 +698,27 @@ __device__ int monotone_chain(const HPt<T>* C, int m, int* H)
     int k = 0;
     for (int i = 0; i < m; ++i)
     {
-        while (k > 1 && ccw_or_colinear(C[H[k - 2]].x, C[H[k - 2]].y, C[H[k - 1]].x, C[H[k - 1]].y, C[i].x, C[i].y))
+        while (k > 1 && chain_pops(C[H[k - 2]], C[H[k - 1]], C[i]))
             --k;
         H[k++] = i;
     }
     for (int i = m - 2, t = k + 1; i >= 0; --i)
     {
-        while (k >= t && ccw_or_colinear(C[H[k - 2]].x, C[H[k - 2]].y, C[H[k - 1]].x, C[H[k - 1]].y, C[i].x, C[i].y))
+        while (k >= t && chain_pops(C[H[k - 2]], C[H[k - 1]], C[i]))
             --k;
         H[k++] = i;
     }
     return k - 1;
+}
+
+// Strictly left of a -> b by a relative margin of 1e-5: the float cross product errs by less
+// than 2.4e-7 (|ex| + |ey|)(|qx| + |qy|), so a point passing is strictly left in exact arithmetic.
+__device__ __forceinline__ bool left_strict_f(float ax, float ay, float bx, float by, float px, float py)
+{
+    const float ex = bx - ax, ey = by - ay, qx = px - ax, qy = py - ay;
+    const float cr = ex * qy - ey * qx;
+    const float scale = (fabsf(ex) + fabsf(ey)) * (fabsf(qx) + fabsf(qy));
+    return cr > 1e-5f * scale + 1e-30f;
 }
 
 // Bitonic sort of n candidates (capacity next_pow2(n)) in global memory by one block.
@@ -364,6 +760,7 @@ struct HullSmem
     HPt<float> cand[kHullSmem];
     int stack[2 * kHullSmem + 2];
     double2 hp[kHullSmem];
+    float2 pf[kHullSmem];     // hull vertices as floats
     uint32_t hkey[kHullSmem]; // hull vertex member keys, sorted
     int32_t diff[kHullSmem + 1];
     float2 poly[kPolyCap];
@@ -560,16 +957,16 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
     }
 
     // 3. candidates: active members not strictly inside the polygon by a relative margin far
-    //    above double rounding (a hull vertex is never strictly inside a polygon of members)
+    //    above float rounding (a hull vertex is never strictly inside a polygon of members)
     const int npf = sm.npoly;
     HPt<float>* gs = reinterpret_cast<HPt<float>*>(b.hs_cand) + 2ull * start; // capacity 2n >= next_pow2(n)
-    auto inside = [&](double px, double py) {
+    auto inside = [&](float px, float py) {
         if (npf < 3)
             return false;
         for (int d = 0; d < npf; ++d)
         {
             const float2 a = sm.poly[d], c = sm.poly[(d + 1 == npf) ? 0 : d + 1];
-            if (!left_strict(a.x, a.y, c.x, c.y, px, py))
+            if (!left_strict_f(a.x, a.y, c.x, c.y, px, py))
                 return false;
         }
         return true;
@@ -694,29 +1091,21 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
     // 6. boxes on the hull vertices (one warp)
     if (compute_obb)
     {
-        double2* P = (h <= kHullSmem) ? sm.hp : (b.hs_pts + start);
+        const bool fast = h <= kHullSmem;
+        double2* P = fast ? sm.hp : (b.hs_pts + start);
         for (int j = threadIdx.x; j < h; j += blockDim.x)
-            P[j] = make_double2(static_cast<double>(C[H[j]].x), static_cast<double>(C[H[j]].y));
-        __syncthreads();
-        if (warp == 0)
         {
-            int2* pairs = b.hs_pairs + 4ull * start + 16ull * g;
-            const int cap = 4 * h + 16;
-            int npairs = 0;
-            if (lane == 0)
-                npairs = antipodal_pairs(P, h, pairs, cap);
-            npairs = __shfl_sync(0xffffffffu, npairs, 0);
-            if (npairs > cap)
-            {
-                if (lane == 0)
-                    raise_err(st, ERR_INTERNAL);
-                npairs = cap;
-            }
-            __syncwarp();
-            calipers_warp(P, h, pairs, npairs, &b.obb_c[g]);
-            if (lane == 0)
-                pca_box(P, h, &b.obb_p[g]);
+            const HPt<float> c = C[H[j]];
+            P[j] = make_double2(static_cast<double>(c.x), static_cast<double>(c.y));
+            if (fast)
+                sm.pf[j] = make_float2(c.x, c.y);
         }
+        __syncthreads();
+        if (warp == 0) // hkey is free again: float scratch of the calipers screen
+            calipers_box(st, P, fast ? sm.pf : nullptr, reinterpret_cast<float*>(sm.hkey), h,
+                         b.hs_pairs + 4ull * start + 16ull * g, &b.obb_c[g]);
+        else if (warp == 1)
+            pca_box_warp(P, h, &b.obb_p[g]);
     }
     __syncthreads();
 }
@@ -733,6 +1122,7 @@ struct WarpSmem
     HPt<float> cand[kWarpCand];
     int stack[2 * kWarpCand + 2];
     double2 hp[kWarpCand];
+    float2 pf[kWarpCand];
     float2 poly[kDirs];
     int npoly;
 };
@@ -811,13 +1201,13 @@ __device__ void hull_one_warp(const BatchDev& b, WarpSmem& ws, const float2* dir
         return;
     }
     const int npf = ws.npoly;
-    auto inside = [&](double px, double py) {
+    auto inside = [&](float px, float py) {
         if (npf < 3)
             return false;
         for (int d = 0; d < npf; ++d)
         {
             const float2 a = ws.poly[d], c = ws.poly[(d + 1 == npf) ? 0 : d + 1];
-            if (!left_strict(a.x, a.y, c.x, c.y, px, py))
+            if (!left_strict_f(a.x, a.y, c.x, c.y, px, py))
                 return false;
         }
         return true;
@@ -876,26 +1266,20 @@ __device__ void hull_one_warp(const BatchDev& b, WarpSmem& ws, const float2* dir
         b.hull_cnt[g] = static_cast<uint32_t>(h);
     if (compute_obb)
     {
-        double2* P = (h <= kWarpCand) ? ws.hp : (b.hs_pts + start);
+        const bool fast = h <= kWarpCand;
+        double2* P = fast ? ws.hp : (b.hs_pts + start);
         for (int j = static_cast<int>(lane); j < h; j += 32)
-            P[j] = make_double2(static_cast<double>(C[H[j]].x), static_cast<double>(C[H[j]].y));
-        __syncwarp();
-        int2* pairs = b.hs_pairs + 4ull * start + 16ull * g;
-        const int cap = 4 * h + 16;
-        int npairs = 0;
-        if (lane == 0)
-            npairs = antipodal_pairs(P, h, pairs, cap);
-        npairs = __shfl_sync(0xffffffffu, npairs, 0);
-        if (npairs > cap)
         {
-            if (lane == 0)
-                raise_err(st, ERR_INTERNAL);
-            npairs = cap;
+            const HPt<float> c = C[H[j]];
+            P[j] = make_double2(static_cast<double>(c.x), static_cast<double>(c.y));
+            if (fast)
+                ws.pf[j] = make_float2(c.x, c.y);
         }
         __syncwarp();
-        calipers_warp(P, h, pairs, npairs, &b.obb_c[g]);
-        if (lane == 0)
-            pca_box(P, h, &b.obb_p[g]);
+        // the chain stack is free again: float scratch of the calipers screen
+        calipers_box(st, P, fast ? ws.pf : nullptr, reinterpret_cast<float*>(ws.stack), h,
+                     b.hs_pairs + 4ull * start + 16ull * g, &b.obb_c[g]);
+        pca_box_warp(P, h, &b.obb_p[g]);
     }
     __syncwarp();
 }
@@ -1016,7 +1400,7 @@ __global__ void k_boxes_single(const double2* P, uint32_t n, int2* pairs, int ca
     const uint32_t lane = lane_id();
     int np = 0;
     if (lane == 0)
-        np = antipodal_pairs(P, static_cast<int>(n), pairs, cap);
+        np = antipodal_pairs(AreaCmpFp64{P}, static_cast<int>(n), pairs, cap);
     np = __shfl_sync(0xffffffffu, np, 0);
     if (lane == 0 && npairs_out)
         *npairs_out = np;
