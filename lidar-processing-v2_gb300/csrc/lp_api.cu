@@ -284,7 +284,8 @@ size_t carve(lp_batch& B, char* base)
         put(b.pix_state, b.npix);
         put(b.row_cols, b.npix);
         put(b.row_cnt, b.nrows + 1);
-        put(b.jw, static_cast<size_t>(b.npix) * 26);
+        put(b.jw, static_cast<size_t>(b.npix) * kJwStride);
+        put(b.jn, static_cast<size_t>(b.npix) * kJwStride);
         put(b.jmap, b.npix);
         if (R.stages & ST_IMAGE)
             put(B.d_image, static_cast<size_t>(b.npix) * 3);

@@ -36,6 +36,10 @@ enum : uint8_t
     V_O = 2
 };
 
+// Jump-convolution weight record of a queued pixel: 24 fresh weights, their sum, padding to a
+// multiple of 16 bytes (vector loads).
+constexpr uint32_t kJwStride = 28;
+
 struct BatchDev
 {
     int nscan;
@@ -94,7 +98,8 @@ struct BatchDev
     uint32_t nrows;
     uint16_t* row_cols;        // per pixel slot: intersection columns of the row in order
     uint32_t* row_cnt;         // per global row
-    float* jw;                 // per entry: 24 fresh weights + sum (stride 26)
+    float* jw;                 // per entry: 24 fresh weights + sum (stride kJwStride)
+    float* jn;                 // per entry: 24 normalized weights, sum, slot label codes (stride kJwStride)
     unsigned long long* jmap;  // per entry: 9-state transition map
 
     // ---- segmentation output -----------------------------------------------------------------

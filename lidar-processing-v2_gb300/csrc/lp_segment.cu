@@ -720,11 +720,34 @@ __global__ void __launch_bounds__(256) k_dilate_rows(BatchDev b)
 // Offsets of the 24-neighbour kernel, segmenter.cpp:527-530.
 __constant__ int8_t kOffH[24] = {-2, -2, -2, -2, -2, -1, -1, -1, -1, -1, 0, 0, 0, 0, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2};
 __constant__ int8_t kOffW[24] = {-2, -1, 0, 1, 2, -2, -1, 0, 1, 2, -2, -1, 1, 2, -2, -1, 0, 1, 2, -2, -1, 0, 1, 2};
+// The same offsets as arithmetic on the slot index (folds to constants in unrolled loops).
+__device__ __forceinline__ constexpr int32_t jcp_dh(int k)
+{
+    return k < 10 ? -2 + k / 5 : (k < 14 ? 0 : 1 + (k - 14) / 5);
+}
+__device__ __forceinline__ constexpr int32_t jcp_dw(int k)
+{
+    return k < 10 ? k % 5 - 2 : (k < 14 ? (k < 12 ? k - 12 : k - 11) : (k - 14) % 5 - 2);
+}
+
+__device__ __forceinline__ uint8_t final_view(uint8_t st)
+{
+    return (st == PX_GROUND || st == PX_RES_G) ? V_G : ((st == PX_OBSTACLE || st == PX_RES_O) ? V_O : V_U);
+}
+__device__ __forceinline__ uint8_t pre_view(uint8_t st)
+{
+    return (st == PX_GROUND) ? V_G : ((st == PX_OBSTACLE) ? V_O : V_U);
+}
 
 // Fresh (not stale) weight of every in-bounds neighbour slot of every queued pixel: 0 for an
 // empty neighbour or one farther than the kernel threshold, else expf(-amp * dist)
 // (segmenter.cpp:545-607). These depend on geometry only, so they are computed in parallel
-// before the ordered vote.
+// before the ordered vote. Two records per queued pixel:
+//   jw: the raw weights and their sum (read back when a later pixel's slot leaves the image),
+//   jn: the weights divided by the sum, the sum, and a 2-bit label code per slot: the label the
+//       vote will read (unknown / ground / obstacle) wherever it is already fixed, or 3 where it
+//       is not: a queued pixel in a row above (its final colour comes from its own vote) or a
+//       queued pixel to the left in the same row (the symbolic outcome of the in-row chain).
 __global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
 {
     const uint32_t r = blockIdx.x;
@@ -735,17 +758,24 @@ __global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
     const uint32_t row_base = sd.pix_off + static_cast<uint32_t>(h * W);
     const uint32_t m = b.row_cnt[r];
     const int32_t* map = b.pix_map + sd.pix_off;
+    const uint8_t* st = b.pix_state + sd.pix_off;
     const float4* pts = b.pts + sd.pt_off;
     for (uint32_t j = threadIdx.x; j < m; j += blockDim.x)
     {
         const int32_t w = b.row_cols[row_base + j];
         const float4 cp = pts[map[h * W + w]];
-        float* out = b.jw + static_cast<size_t>(row_base + j) * 26;
+        float* out = b.jw + static_cast<size_t>(row_base + j) * kJwStride;
+        float* nrm = b.jn + static_cast<size_t>(row_base + j) * kJwStride;
+        float wt[24];
+        unsigned long long codes = 0ull;
         float sum = 0.0F;
+#pragma unroll
         for (int k = 0; k < 24; ++k)
         {
-            const int32_t hh = h + kOffH[k], ww = w + kOffW[k];
-            float wt = 0.0F;
+            const int32_t dh = jcp_dh(k), dw = jcp_dw(k);
+            const int32_t hh = h + dh, ww = w + dw;
+            wt[k] = 0.0F;
+            uint32_t code = V_U;
             if (hh >= 0 && hh < H && ww >= 0 && ww < W)
             {
                 const int32_t ni = map[hh * W + ww];
@@ -759,24 +789,32 @@ __global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
                     if (!(d2 > sd.kthr2))
                     {
                         const float dist = sqrtf(d2);
-                        wt = lpm::cr_expf(-sd.amp * dist);
-                        sum += wt;
+                        wt[k] = lpm::cr_expf(-sd.amp * dist);
+                        sum += wt[k];
                     }
                 }
+                if (wt[k] != 0.0F)
+                {
+                    const uint8_t ns = st[hh * W + ww];
+                    if (dh > 0 || (dh == 0 && dw > 0))
+                        code = pre_view(ns); // not voted before this pixel
+                    else
+                        code = (ns == PX_INTERSECT) ? 3u : final_view(ns);
+                }
             }
-            out[k] = wt;
+            out[k] = wt[k];
+            codes |= static_cast<unsigned long long>(code) << (2 * k);
         }
         out[24] = sum;
+        const bool live = fabsf(sum) > FLT_EPSILON;
+#pragma unroll
+        for (int k = 0; k < 24; ++k)
+            nrm[k] = live ? wt[k] / sum : 0.0F;
+        nrm[24] = sum;
+        nrm[25] = __uint_as_float(static_cast<uint32_t>(codes));
+        nrm[26] = __uint_as_float(static_cast<uint32_t>(codes >> 32));
+        nrm[27] = 0.0F;
     }
-}
-
-__device__ __forceinline__ uint8_t final_view(uint8_t st)
-{
-    return (st == PX_GROUND || st == PX_RES_G) ? V_G : ((st == PX_OBSTACLE || st == PX_RES_O) ? V_O : V_U);
-}
-__device__ __forceinline__ uint8_t pre_view(uint8_t st)
-{
-    return (st == PX_GROUND) ? V_G : ((st == PX_OBSTACLE) ? V_O : V_U);
 }
 
 __device__ __forceinline__ unsigned long long map_compose(unsigned long long later, unsigned long long earlier)
@@ -861,27 +899,49 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
         for (uint32_t j = j0; j < j1; ++j)
         {
             const int32_t c = cols[j];
-            const float* wj = b.jw + static_cast<size_t>(row_base + j) * 26;
-            const float sum = wj[24];
-            uint8_t outc[9];
+            // every load of the pixel is issued up front: its normalized record and the states
+            // of the queued pixels above it
+            const float* rec = b.jn + static_cast<size_t>(row_base + j) * kJwStride;
+            float wn[24];
+#pragma unroll
+            for (int q = 0; q < 6; ++q)
+            {
+                const float4 v = reinterpret_cast<const float4*>(rec)[q];
+                wn[4 * q] = v.x;
+                wn[4 * q + 1] = v.y;
+                wn[4 * q + 2] = v.z;
+                wn[4 * q + 3] = v.w;
+            }
+            const float4 tail = reinterpret_cast<const float4*>(rec)[6];
+            const float sum = tail.x;
+            const unsigned long long codes =
+                static_cast<unsigned long long>(__float_as_uint(tail.y)) |
+                (static_cast<unsigned long long>(__float_as_uint(tail.z)) << 32);
+            uint8_t nsv[10];
+#pragma unroll
+            for (int k = 0; k < 10; ++k) // code 3 above: a queued pixel, inside the image
+                nsv[k] = (((codes >> (2 * k)) & 3ull) == 3ull) ? st[(h + jcp_dh(k)) * W + c + jcp_dw(k)]
+                                                                : static_cast<uint8_t>(PX_EMPTY);
+            uint32_t outc = 0u; // outcome of vote table entry (a, b) in bits 2 (3a + b)
             if (fabsf(sum) > FLT_EPSILON)
             {
-                float wv[24];
                 uint8_t lb[24];
                 bool sym_a = false, sym_b = false;
+#pragma unroll
                 for (int k = 0; k < 24; ++k)
                 {
-                    const int32_t dh = kOffH[k], dw = kOffW[k];
+                    const int32_t dh = jcp_dh(k), dw = jcp_dw(k);
                     const int32_t hh = h + dh, ww = c + dw;
                     if (hh < 0 || hh >= H || ww < 0 || ww >= W)
                     {
-                        // stale slot
+                        // stale slot: the raw weight an earlier pixel left there, over this sum
+                        float wv;
                         const int32_t qd = dw > 0 ? dw : 0;
                         const int32_t q = (dw > 0 && hh >= 0 && hh < H) ? lastq[qd] : -1;
                         if (q >= 0)
                         {
-                            const float qw = b.jw[static_cast<size_t>(row_base + q) * 26 + k];
-                            wv[k] = qw;
+                            const float qw = b.jw[static_cast<size_t>(row_base + q) * kJwStride + k];
+                            wv = qw;
                             if (qw == 0.0F)
                                 lb[k] = V_U;
                             else
@@ -892,42 +952,29 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                         }
                         else
                         {
-                            wv[k] = run_w[k];
+                            wv = run_w[k];
                             lb[k] = run_l[k];
                         }
+                        wn[k] = wv / sum;
                         continue;
                     }
-                    const float wt = wj[k];
-                    wv[k] = wt;
-                    if (wt == 0.0F)
-                    {
-                        lb[k] = V_U;
-                        continue;
-                    }
-                    const uint8_t ns = st[hh * W + ww];
-                    if (dh < 0)
-                        lb[k] = final_view(ns);
-                    else if (dh > 0 || dw > 0)
-                        lb[k] = pre_view(ns);
+                    const uint32_t code = static_cast<uint32_t>((codes >> (2 * k)) & 3ull);
+                    if (code != 3u)
+                        lb[k] = static_cast<uint8_t>(code);
+                    else if (dh < 0)
+                        lb[k] = final_view(nsv[k < 10 ? k : 0]);
                     else
                     {
-                        // same row, left of c: symbolic when queued (vote outcome), else fixed
-                        if (ns == PX_INTERSECT)
-                        {
-                            lb[k] = V_U;
-                            if (dw == -1)
-                                sym_a = true;
-                            else
-                                sym_b = true;
-                        }
+                        // same row, left of c, queued: symbolic (the chain's outcome)
+                        lb[k] = V_U;
+                        if (dw == -1)
+                            sym_a = true;
                         else
-                            lb[k] = final_view(ns);
+                            sym_b = true;
                     }
                 }
-                float wn[24];
-                for (int k = 0; k < 24; ++k)
-                    wn[k] = wv[k] / sum;
                 float g9 = 0.0F, o9 = 0.0F;
+#pragma unroll
                 for (int k = 0; k < 10; ++k)
                 {
                     if (lb[k] == V_G)
@@ -935,7 +982,9 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                     else if (lb[k] == V_O)
                         o9 += wn[k];
                 }
+#pragma unroll
                 for (int a = 0; a < 3; ++a)
+#pragma unroll
                     for (int bb = 0; bb < 3; ++bb)
                     {
                         float g = g9, o = o9;
@@ -949,6 +998,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                             g += wn[11];
                         else if (l11 == V_O)
                             o += wn[11];
+#pragma unroll
                         for (int k = 12; k < 24; ++k)
                         {
                             if (lb[k] == V_G)
@@ -956,16 +1006,12 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                             else if (lb[k] == V_O)
                                 o += wn[k];
                         }
-                        outc[3 * a + bb] = (o > g) ? V_O : V_G;
+                        outc |= static_cast<uint32_t>((o > g) ? V_O : V_G) << (2 * (3 * a + bb));
                     }
-            }
-            else
-            {
-                for (int k = 0; k < 9; ++k)
-                    outc[k] = V_U;
             }
             const int32_t gap = (j > 0) ? (c - static_cast<int32_t>(cols[j - 1])) : 1000;
             unsigned long long t = 0ull;
+#pragma unroll
             for (int sidx = 0; sidx < 9; ++sidx)
             {
                 const int a = sidx / 3, bb = sidx % 3;
@@ -988,7 +1034,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                     bp = V_U;
                     an = V_U;
                 }
-                const int x = outc[3 * ap + bp];
+                const int x = static_cast<int>((outc >> (2 * (3 * ap + bp))) & 3u); // V_U when sum ~ 0
                 t |= static_cast<unsigned long long>(3 * x + an) << (4 * sidx);
             }
             b.jmap[row_base + j] = t;
@@ -1036,7 +1082,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                 const int32_t q = lastq[dw > 0 ? dw : 0];
                 if (q >= 0 && static_cast<int32_t>(cols[q]) >= (dw < 0 ? -dw : 0))
                 {
-                    const float qw = b.jw[static_cast<size_t>(row_base + q) * 26 + k];
+                    const float qw = b.jw[static_cast<size_t>(row_base + q) * kJwStride + k];
                     uint8_t l = V_U;
                     if (qw != 0.0F)
                     {
