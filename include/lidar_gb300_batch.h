@@ -39,8 +39,16 @@ lp_status lp_batch_time(lp_context* ctx, lp_batch* batch, uint32_t iters, int32_
 lp_status lp_batch_profile(lp_context* ctx, lp_batch* batch, char* names, uint32_t name_len, float* ms,
                            uint32_t cap, uint32_t* count);
 /* Device evaluation of the library's correctly rounded binary32 functions (kind 0 atan2(a, b),
- * 1 atan(a), 2 exp(a), 3 the reference's atan2 approximation); used by the parity tests. */
+ * 1 atan(a), 2 exp(a), 3 the reference's atan2 approximation; 4, 5, 6 the same three functions
+ * without their float-float first stage); used by the parity tests. */
 lp_status lp_debug_math(lp_context* ctx, int32_t kind, const float* a, const float* b, uint32_t n, float* out);
+/* Check of the float-float first stage of those functions against the binary64 / double-double
+ * stages over `count` arguments starting at index `first` (kind 1 atan, 2 exp: the float with bits
+ * first + i; kind 0 atan2: hashed pairs). stats[0] = decided by the first stage, stats[1] = left
+ * to the later stages, stats[2] = decided differently (must be 0); *first_bad = lowest index of
+ * such a difference (UINT64_MAX when none). */
+lp_status lp_debug_math_sweep(lp_context* ctx, int32_t kind, uint64_t first, uint64_t count, uint64_t stats[3],
+                              uint64_t* first_bad);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Serving: scans from several sensors submitted as they arrive, continuous batching.          */

@@ -1222,4 +1222,30 @@ lp_status lp_debug_math(lp_context* ctx, int32_t kind, const float* a, const flo
     return LP_OK;
 }
 
+lp_status lp_debug_math_sweep(lp_context* ctx, int32_t kind, uint64_t first, uint64_t count, uint64_t stats[3],
+                              uint64_t* first_bad)
+{
+    if (!ctx || !stats || !first_bad || kind < 0 || kind > 2)
+        return LP_ERR_BAD_ARG;
+    LP_TRY(ensure_device(ctx));
+    char* m;
+    LP_TRY(poly_scratch(ctx, 1024, &m));
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(m);
+    const unsigned long long init[4] = {0ull, 0ull, 0ull, ~0ull};
+    LP_CUDA(ctx, cudaMemcpyAsync(d, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
+    Launcher L;
+    L.stream = ctx->stream;
+    L.launches = &ctx->launches;
+    launch_debug_math_sweep(L, kind, first, count, d, d + 3);
+    if (L.err != cudaSuccess)
+        return cuda_fail(ctx, L.err, "lp_debug_math_sweep launch");
+    unsigned long long res[4];
+    LP_CUDA(ctx, cudaMemcpyAsync(res, d, sizeof(res), cudaMemcpyDeviceToHost, ctx->stream));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < 3; ++k)
+        stats[k] = res[k];
+    *first_bad = res[3];
+    return LP_OK;
+}
+
 } // extern "C"

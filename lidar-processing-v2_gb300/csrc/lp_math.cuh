@@ -5,20 +5,35 @@
 // builds, so the device implements the one platform-independent definition: the binary32
 // value nearest to the exact result (round to nearest, ties to even).
 //
-// Method (Ziv's two-step rounding test): evaluate in binary64 with the CUDA double functions
-// (documented max error 2 ulp for atan2/atan, 1 ulp for exp); if that value lies further than
-// 2^-49 relative from every binary32 rounding boundary, its rounding is the correct one.
-// Otherwise re-evaluate in double-double arithmetic (about 2^-100 relative error) from the
-// mathematical definitions below and round that:
-//   exp(x)  = 2^k * exp(r),  r = x - k ln2 (|r| <= ln2/2), Taylor series of exp(r)
-//   atan(t) = 4 atan(t''), t' = t / (1 + sqrt(1 + t^2)) applied twice (|t''| <= tan(pi/16)),
-//             odd Taylor series; atan(t) = pi/2 - atan(1/t) for t > 1
-//   atan2(y, x) from atan(min/max) with the quadrant identities.
-// Double-double primitives are Dekker/Knuth error-free transformations (two_sum, two_prod
-// with fma). Constants ln2, pi/2 and pi are split into double-double pairs (computed to 200
-// bits with mpmath).
+// Three stages, each used only when the one before cannot decide the rounding (Ziv's strategy):
+//
+// 1. float-float (FP32 units only; the GPU's FP64 rate is a small fraction of its FP32 rate):
+//      exp(x)  = 2^m * 2^(j/64) * exp(r),  n = rint(64 x / ln2) = 64 m + j,
+//                r = x - n ln2/64 (|r| <= ln2/128), exp(r) by its Taylor polynomial of degree 5
+//                (P. T. P. Tang, "Table-driven implementation of the exponential function in IEEE
+//                floating-point arithmetic", ACM TOMS 15(2), 1989),
+//      atan(t) = atan(c) + atan((t - c) / (1 + t c)),  c = rint(128 t) / 128 (0 <= t <= 1),
+//                atan(u) = u - u^3/3 + u^5/5 - u^7/7 (|u| <= 1/256);  atan(t) = pi/2 - atan(1/t)
+//                above 1; atan2 from atan(min/max) with the quadrant identities.
+//    Products and sums that must be exact use the error-free transformations of Dekker and Knuth
+//    (two_sum, two_prod with fma). The result hi + lo is within 2^-36 of the exact value
+//    (relative; the analysis beside each function gives about 2^-38); if that interval does not
+//    contain a binary32 rounding boundary, hi + lo rounds like the exact value.
+// 2. binary64 with the CUDA double functions (documented max error 2 ulp for atan2/atan, 1 ulp
+//    for exp); if that value lies further than 2^-49 relative from every binary32 rounding
+//    boundary, its rounding is the correct one.
+// 3. double-double arithmetic (about 2^-100 relative error) from the mathematical definitions
+//    below, then rounded:
+//      exp(x)  = 2^k * exp(r),  r = x - k ln2 (|r| <= ln2/2), Taylor series of exp(r)
+//      atan(t) = 4 atan(t''), t' = t / (1 + sqrt(1 + t^2)) applied twice (|t''| <= tan(pi/16)),
+//                odd Taylor series; atan(t) = pi/2 - atan(1/t) for t > 1
+//      atan2(y, x) from atan(min/max) with the quadrant identities.
+// Constants ln2, pi/2 and pi are split into double-double pairs (computed to 200 bits with
+// mpmath); the float-float tables are written by gen_math_tables.py.
 #pragma once
 #include <cstdint>
+
+#include "lp_math_tables.cuh"
 
 namespace lpm
 {
@@ -186,7 +201,7 @@ __device__ __forceinline__ bool near_boundary(double v)
     return fabs(v - m_up) <= tol || fabs(v - m_dn) <= tol;
 }
 
-__device__ __forceinline__ float cr_expf(float x)
+__device__ __forceinline__ float cr_expf_fp64(float x)
 {
     if (x < -104.0f)
         return 0.0f;
@@ -198,7 +213,7 @@ __device__ __forceinline__ float cr_expf(float x)
     return round_dd(dd_exp(x));
 }
 
-__device__ __forceinline__ float cr_atanf(float x)
+__device__ __forceinline__ float cr_atanf_fp64(float x)
 {
     if (isnan(x))
         return x;
@@ -211,7 +226,7 @@ __device__ __forceinline__ float cr_atanf(float x)
     return round_dd(r);
 }
 
-__device__ __forceinline__ float cr_atan2f(float y, float x)
+__device__ __forceinline__ float cr_atan2f_fp64(float y, float x)
 {
     const double v = atan2(static_cast<double>(y), static_cast<double>(x));
     if (!near_boundary(v) || isnan(v))
@@ -227,6 +242,191 @@ __device__ __forceinline__ float cr_atan2f(float y, float x)
     if (signbit(y))
         r = dd_neg(r);
     return round_dd(r);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Stage 1: float-float evaluation.
+// ---------------------------------------------------------------------------------------------
+struct ff
+{
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff two_sum_f(float a, float b)
+{
+    const float s = a + b;
+    const float bb = s - a;
+    const float e = (a - (s - bb)) + (b - bb);
+    return {s, e};
+}
+__device__ __forceinline__ ff fast_two_sum_f(float a, float b) // |a| >= |b| or a == 0
+{
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ ff two_prod_f(float a, float b)
+{
+    const float p = a * b;
+    return {p, fmaf(a, b, -p)};
+}
+
+// Rounding test: v = hi + lo approximates y with |v - y| <= 2^-36 |y|. Writes the binary32
+// nearest y and returns true when every value of that interval rounds to the same float; returns
+// false (undecided) otherwise. hi + lo is first renormalised exactly (s = fl(hi + lo), e the
+// remainder); y rounds to s when s + e stays, by more than the error bound, inside the rounding
+// interval of s: half the gap to the neighbour on e's side (a quarter ulp below a power of two).
+__device__ __forceinline__ bool ff_round(ff v, float* out)
+{
+    const ff n = fast_two_sum_f(v.hi, v.lo);
+    const float s = n.hi, e = n.lo;
+    const float as = fabsf(s);
+    if (!(as >= 0x1p-100f && as <= 0x1p100f))
+        return false;
+    const uint32_t bits = __float_as_uint(as);
+    const float up = __uint_as_float(bits + 1u) - as;                      // gap above |s|
+    const float dn = ((bits & 0x7fffffu) == 0u) ? 0.5f * up : up;         // gap below |s|
+    const bool away = (e > 0.0f) == (s > 0.0f);                           // e points away from 0
+    const float half = 0.5f * (away ? up : dn);
+    const float room = half - fabsf(e);       // exact or within 2^-24 of it (|e| <= half)
+    if (room > as * 0x1p-35f)                 // twice the error bound: covers the rounding of room
+    {
+        *out = s;
+        return true;
+    }
+    return false;
+}
+
+// exp(x) for -87 <= x <= 88.5 (normal results). Error (relative, before scaling by 2^m):
+// reduction r = x - n ln2/64 in float-float, exact but for the ln2/64 tail and the float sums of
+// small terms (< 2^-50); polynomial: 1 + r exact, r^2/2 exact product, the rest in float
+// (< 2^-40 each for the two float sums, truncation 2^-54); table pair 2^-48; the float-float
+// product with the table < 2^-40. Total below 2^-38.
+__device__ __forceinline__ bool ff_expf(float x, float* out)
+{
+    const float nf = rintf(x * 92.332482616893656f); // 64 / ln2: it only chooses n
+    const int n = static_cast<int>(nf);
+    const int j = n & 63;
+    const int m = (n - j) >> 6;
+    const ff a = two_sum_f(x, -nf * kLn2By64Head);   // nf * head is exact (|n| < 2^14)
+    const ff p2 = two_prod_f(nf, kLn2By64Mid);
+    ff r = two_sum_f(a.hi, -p2.hi);
+    r.lo = r.lo + ((a.lo - p2.lo) - nf * kLn2By64Tail);
+    r = fast_two_sum_f(r.hi, r.lo);
+    const float rh = r.hi, rl = r.lo;
+    const ff q = two_prod_f(rh, rh);                  // r^2 (of the head)
+    const float small = q.lo * 0.5f + rh * rl + q.hi * rh * (1.0f / 6.0f) + q.hi * q.hi * (1.0f / 24.0f) +
+                        q.hi * q.hi * rh * (1.0f / 120.0f);
+    const ff s1 = two_sum_f(1.0f, rh);
+    const float t = q.hi * 0.5f + (rl + small);
+    const ff e = fast_two_sum_f(s1.hi, s1.lo + t);     // exp(r)
+    const float2 T = kExp2Tab[j];
+    ff p = two_prod_f(e.hi, T.x);
+    p.lo = p.lo + (e.hi * T.y + e.lo * T.x);
+    float f;
+    if (!ff_round(p, &f))
+        return false;
+    *out = scalbnf(f, m); // exact: the result is a normal float
+    return true;
+}
+
+// atan(t) for t = th + tl in [0, 1] (tl = 0 or |tl| <= 2^-23 th). c = j/128, j = rint(128 th):
+// th - c is exact (Sterbenz), 1 + t c is formed from an exact product; u = (t - c) / (1 + t c) in
+// float-float (relative error < 2^-45), |u| <= 1/256; atan(u) = u - u^3/3 + u^5/5 - u^7/7 with
+// the cubic and higher terms in float (< 2^-39.5 |u| with the u_lo contribution; |u| is at most
+// atan(t) for j <= 1 and below it otherwise), truncation u^9/9 < 2^-66 |u|; table pair 2^-48;
+// the final float sums < 2^-46. The result is within 2^-39 relative of atan(t).
+__device__ __forceinline__ ff ff_atan_unit(float th, float tl)
+{
+    const float jf = fminf(fmaxf(rintf(th * 128.0f), 0.0f), 128.0f); // table bounds, whatever th is
+    const int j = static_cast<int>(jf);
+    const float c = jf * (1.0f / 128.0f);
+    const ff nu = two_sum_f(th - c, tl);
+    const ff pc = two_prod_f(th, c);
+    ff d = two_sum_f(1.0f, pc.hi);
+    d.lo = d.lo + (pc.lo + tl * c);
+    d = fast_two_sum_f(d.hi, d.lo);
+    const float q1 = nu.hi / d.hi;
+    float rem = fmaf(-q1, d.hi, nu.hi); // exact
+    rem = (rem + nu.lo) - q1 * d.lo;
+    const float q2 = rem / d.hi;
+    const ff u = fast_two_sum_f(q1, q2);
+    const float u2 = u.hi * u.hi;
+    const float corr = u.hi * u2 * (-1.0f / 3.0f) + u.hi * u2 * u2 * (1.0f / 5.0f) +
+                       u.hi * u2 * u2 * u2 * (-1.0f / 7.0f) - u2 * u.lo;
+    const float2 A = kAtanTab[j];
+    const ff s = two_sum_f(A.x, u.hi);
+    return fast_two_sum_f(s.hi, s.lo + (A.y + (u.lo + corr)));
+}
+
+// pi/2 - a or pi - a in float-float (a >= 0 no larger than the constant).
+__device__ __forceinline__ ff ff_const_minus(float chi, float clo, ff a)
+{
+    const ff s = two_sum_f(chi, -a.hi);
+    return fast_two_sum_f(s.hi, s.lo + (clo - a.lo));
+}
+
+__device__ __forceinline__ bool ff_atanf(float x, float* out)
+{
+    const float t = fabsf(x);
+    if (!(t >= 0x1p-60f && t <= 0x1p60f))
+        return false;
+    ff r;
+    if (t <= 1.0f)
+        r = ff_atan_unit(t, 0.0f);
+    else
+    {
+        const float q1 = 1.0f / t;
+        const float rem = fmaf(-q1, t, 1.0f); // exact
+        const ff inv = fast_two_sum_f(q1, rem / t);
+        r = ff_const_minus(kPi2FHi, kPi2FLo, ff_atan_unit(inv.hi, inv.lo));
+    }
+    if (x < 0.0f)
+        r = {-r.hi, -r.lo};
+    return ff_round(r, out);
+}
+
+__device__ __forceinline__ bool ff_atan2f(float y, float x, float* out)
+{
+    const float ax = fabsf(x), ay = fabsf(y);
+    // zeros, huge, tiny, inf, nan (each compared on its own: fminf/fmaxf would drop a nan)
+    if (!(ax >= 0x1p-60f && ax <= 0x1p60f && ay >= 0x1p-60f && ay <= 0x1p60f))
+        return false;
+    const float mn = fminf(ax, ay), mx = fmaxf(ax, ay);
+    const float q1 = mn / mx;
+    const float rem = fmaf(-q1, mx, mn); // exact
+    const ff t = fast_two_sum_f(q1, rem / mx);
+    ff r = ff_atan_unit(t.hi, t.lo);
+    if (ay > ax)
+        r = ff_const_minus(kPi2FHi, kPi2FLo, r);
+    if (x < 0.0f)
+        r = ff_const_minus(kPiFHi, kPiFLo, r);
+    if (y < 0.0f)
+        r = {-r.hi, -r.lo};
+    return ff_round(r, out);
+}
+
+__device__ __forceinline__ float cr_expf(float x)
+{
+    float f;
+    if (x >= -87.0f && x <= 88.5f && ff_expf(x, &f))
+        return f;
+    return cr_expf_fp64(x);
+}
+
+__device__ __forceinline__ float cr_atanf(float x)
+{
+    float f;
+    if (ff_atanf(x, &f))
+        return f;
+    return cr_atanf_fp64(x);
+}
+
+__device__ __forceinline__ float cr_atan2f(float y, float x)
+{
+    float f;
+    if (ff_atan2f(y, x, &f))
+        return f;
+    return cr_atan2f_fp64(y, x);
 }
 
 // The reference's own minimax atan2 (lidar_processing_lib/include/lidar_processing_lib/common.hpp:33-62):

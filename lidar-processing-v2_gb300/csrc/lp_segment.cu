@@ -1171,6 +1171,15 @@ __global__ void k_debug_math(int kind, const float* a, const float* bb, uint32_t
     case 2:
         r = lpm::cr_expf(a[i]);
         break;
+    case 4:
+        r = lpm::cr_atan2f_fp64(a[i], bb[i]);
+        break;
+    case 5:
+        r = lpm::cr_atanf_fp64(a[i]);
+        break;
+    case 6:
+        r = lpm::cr_expf_fp64(a[i]);
+        break;
     default:
         r = lpm::atan2_approx(a[i], bb[i]);
         break;
@@ -1181,6 +1190,86 @@ __global__ void k_debug_math(int kind, const float* a, const float* bb, uint32_t
 void launch_debug_math(Launcher& L, int kind, const float* a, const float* bb, uint32_t n, float* out)
 {
     LP_LAUNCH(L, k_debug_math, div_up(n, 256u), 256, kind, a, bb, n, out);
+}
+
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long z)
+{
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+// Sweep of the float-float first stage against the binary64 / double-double stages. kind 1
+// (atan) and 2 (exp): argument = the float whose bits are `first + i`; kind 0 (atan2): (y, x) from
+// a hash of first + i, either arbitrary finite floats or the same with their exponents drawn
+// close (ratios near 1, the axes and the diagonals). stats: [0] decided by stage 1, [1] left to
+// the later stages, [2] stage 1 decided differently; first_bad: lowest such index.
+__global__ void k_debug_math_sweep(int kind, unsigned long long first, unsigned long long count,
+                                   unsigned long long* stats, unsigned long long* first_bad)
+{
+    unsigned long long dec = 0, und = 0, bad = 0;
+    const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+    for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < count;
+         i += stride)
+    {
+        const unsigned long long idx = first + i;
+        float f = 0.0f, want = 0.0f;
+        bool ok = false;
+        if (kind == 1)
+        {
+            const float x = __uint_as_float(static_cast<uint32_t>(idx));
+            ok = lpm::ff_atanf(x, &f);
+            if (ok)
+                want = lpm::cr_atanf_fp64(x);
+        }
+        else if (kind == 2)
+        {
+            const float x = __uint_as_float(static_cast<uint32_t>(idx));
+            ok = x >= -87.0f && x <= 88.5f && lpm::ff_expf(x, &f);
+            if (ok)
+                want = lpm::cr_expf_fp64(x);
+        }
+        else
+        {
+            const unsigned long long h = splitmix64(idx);
+            uint32_t by = static_cast<uint32_t>(h), bx = static_cast<uint32_t>(h >> 32);
+            if (idx & 1ull) // exponents within a few of each other
+                bx = (bx & 0x807fffffu) | ((((by >> 23) & 0xffu) + ((bx >> 23) & 7u) - 3u) & 0xffu) << 23;
+            if ((idx & 6ull) == 2ull) // ties of magnitude: the diagonals
+                bx = (bx & 0x80000000u) | (by & 0x7fffffffu);
+            const float y = __uint_as_float(by), x = __uint_as_float(bx);
+            ok = lpm::ff_atan2f(y, x, &f);
+            if (ok)
+                want = lpm::cr_atan2f_fp64(y, x);
+        }
+        if (!ok)
+            ++und;
+        else
+        {
+            ++dec;
+            if (__float_as_uint(f) != __float_as_uint(want))
+            {
+                ++bad;
+                atomicMin(first_bad, idx);
+            }
+        }
+    }
+    dec = __reduce_add_sync(0xffffffffu, static_cast<uint32_t>(dec));
+    und = __reduce_add_sync(0xffffffffu, static_cast<uint32_t>(und));
+    bad = __reduce_add_sync(0xffffffffu, static_cast<uint32_t>(bad));
+    if (lane_id() == 0)
+    {
+        atomicAdd(&stats[0], dec);
+        atomicAdd(&stats[1], und);
+        atomicAdd(&stats[2], bad);
+    }
+}
+
+void launch_debug_math_sweep(Launcher& L, int kind, unsigned long long first, unsigned long long count,
+                             unsigned long long* stats, unsigned long long* first_bad)
+{
+    LP_LAUNCH(L, k_debug_math_sweep, 152u * 16u, 256, kind, first, count, stats, first_bad);
 }
 
 void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, uint8_t* d_image)

@@ -143,4 +143,6 @@ void launch_hull_single(Launcher& L, const double2* pts, uint32_t n, void* scrat
 void launch_boxes_single(Launcher& L, const double2* P, uint32_t n, int2* pairs, int cap, int kind,
                          lp_bounding_box* out, int* npairs_out);
 void launch_debug_math(Launcher& L, int kind, const float* a, const float* b, uint32_t n, float* out);
+void launch_debug_math_sweep(Launcher& L, int kind, unsigned long long first, unsigned long long count,
+                             unsigned long long* stats, unsigned long long* first_bad);
 } // namespace lpg

@@ -250,6 +250,7 @@ def _declare(lib):
         "lp_batch_time": (c.c_int32, [P, P, c.c_uint32, c.c_int32, c.POINTER(c.c_float)]),
         "lp_batch_profile": (c.c_int32, [P, P, P, c.c_uint32, P, c.c_uint32, c.POINTER(c.c_uint32)]),
         "lp_debug_math": (c.c_int32, [P, c.c_int32, P, P, c.c_uint32, P]),
+        "lp_debug_math_sweep": (c.c_int32, [P, c.c_int32, c.c_uint64, c.c_uint64, P, P]),
         "lp_server_config_default": (None, [P]),
         "lp_server_create": (c.c_int32, [c.c_int32, P, P, c.POINTER(P)]),
         "lp_server_submit": (c.c_int32, [P, P, P, c.c_uint64]),

@@ -52,6 +52,31 @@ def test_correctly_rounded_math(ctx):
     assert same.all()
 
 
+def f32_bits(v):
+    return int(np.array([v], np.float32).view(np.uint32)[0])
+
+
+@pytest.mark.parametrize("kind,count", [(1, 1 << 32), (2, 1 << 32), (0, 1 << 31)])
+def test_math_first_stage_sweep(ctx, kind, count):
+    """The float-float first stage decides the rounding exactly as the binary64 / double-double
+    stages do: every binary32 argument of atan and exp, 2^31 hashed atan2 pairs."""
+    lib = lp.library()
+    stats = (ctypes.c_uint64 * 3)()
+    bad = ctypes.c_uint64()
+    lp.check(lib.lp_debug_math_sweep(ctx.handle, kind, 0, count, stats, ctypes.byref(bad)), ctx)
+    decided, undecided, wrong = list(stats)
+    assert wrong == 0, (kind, decided, undecided, hex(bad.value))
+    assert decided + undecided == count
+    if kind == 2:  # the first stage covers [-87, 88.5]
+        domain = (f32_bits(88.5) + 1) + (f32_bits(-87.0) - 0x80000000 + 1)
+        assert undecided - (count - domain) < domain * 1e-3, (decided, undecided)
+    elif kind == 1:  # and |x| in [2^-60, 2^60]
+        domain = 2 * (f32_bits(2.0 ** 60) - f32_bits(2.0 ** -60) + 1)
+        assert undecided - (count - domain) < domain * 1e-3, (decided, undecided)
+    else:
+        assert decided > count // 4, (decided, undecided)
+
+
 # ------------------------------------------------------------------------------------ per stage
 def scans(spec):
     return [T.synth_scan(w, s) for w, s in spec]
