@@ -736,6 +736,7 @@ lp_status lp_context_create(int32_t device, lp_context** out)
         return LP_ERR_CUDA;
     }
     init_kernel_attributes();
+    init_segment_tables();
     *out = ctx;
     return LP_OK;
 }

@@ -343,22 +343,25 @@ __global__ void k_keep(BatchDev b)
 __global__ void k_obs_label(BatchDev b)
 {
     const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= b.obs_flag[b.npts])
-        return;
-    const int s = scan_of_obs(b, o);
-    const ScanDev& sd = b.scans[s];
-    const ScanState& st = b.state[s];
-    const uint32_t slot = b.obs_hslot[o];
+    const bool in = o < b.obs_flag[b.npts];
     int32_t label = LP_INVALID_CLUSTER;
-    if (slot != kEmpty)
+    uint32_t g = 0u;
+    if (in)
     {
-        const uint32_t root = b.parent[b.hvid[slot]];
-        if (b.ccnt[root] >= sd.min_cluster)
-            label = static_cast<int32_t>(b.kflag[st.obs_off + b.cmin[root]] - b.kflag[st.obs_off]);
+        const int s = scan_of_obs(b, o);
+        const ScanDev& sd = b.scans[s];
+        const ScanState& st = b.state[s];
+        const uint32_t slot = b.obs_hslot[o];
+        if (slot != kEmpty)
+        {
+            const uint32_t root = b.parent[b.hvid[slot]];
+            if (b.ccnt[root] >= sd.min_cluster)
+                label = static_cast<int32_t>(b.kflag[st.obs_off + b.cmin[root]] - b.kflag[st.obs_off]);
+        }
+        b.obs_label[o] = label;
+        g = sd.cl_off + static_cast<uint32_t>(label);
     }
-    b.obs_label[o] = label;
-    if (label >= 0)
-        atomicAdd(&b.cl_cnt[sd.cl_off + static_cast<uint32_t>(label)], 1u);
+    warp_aggregated_inc(b.cl_cnt, g, in && label >= 0);
 }
 
 __global__ void k_cl_state(BatchDev b)
@@ -376,15 +379,13 @@ __global__ void k_cl_state(BatchDev b)
 __global__ void k_cl_scatter(BatchDev b)
 {
     const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= b.obs_flag[b.npts])
-        return;
-    const int32_t label = b.obs_label[o];
-    if (label < 0)
-        return;
-    const int s = scan_of_obs(b, o);
-    const uint32_t g = b.scans[s].cl_off + static_cast<uint32_t>(label);
-    const uint32_t pos = b.cl_start[g] + atomicAdd(&b.cl_fill[g], 1u);
-    b.members[pos] = o;
+    const int32_t label = (o < b.obs_flag[b.npts]) ? b.obs_label[o] : -1;
+    uint32_t g = 0u;
+    if (label >= 0)
+        g = b.scans[scan_of_obs(b, o)].cl_off + static_cast<uint32_t>(label);
+    const uint32_t rank = warp_aggregated_inc(b.cl_fill, g, label >= 0);
+    if (label >= 0)
+        b.members[b.cl_start[g] + rank] = o;
 }
 } // namespace
 

@@ -24,6 +24,24 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v)
     return v;
 }
 
+// Warp-aggregated counter increment: every valid lane adds 1 to counters[key] and receives the
+// counter's old value plus its rank among the valid lanes with the same key, as if the lanes'
+// atomicAdds had run in lane order. One atomic per distinct key of the warp (consecutive points
+// of a cluster or cell share a counter, so same-address atomics drop by up to 32x). All 32 lanes
+// must call it; invalid lanes take no part and receive 0.
+__device__ __forceinline__ uint32_t warp_aggregated_inc(uint32_t* counters, uint32_t key, bool valid)
+{
+    const uint32_t lane = lane_id();
+    const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? key : 0xffffffffu) & vmask;
+    const uint32_t leader = peers ? static_cast<uint32_t>(__ffs(peers) - 1) : lane;
+    uint32_t old = 0u;
+    if (valid && lane == leader)
+        old = atomicAdd(&counters[key], static_cast<uint32_t>(__popc(peers)));
+    old = __shfl_sync(0xffffffffu, old, static_cast<int>(leader));
+    return valid ? old + static_cast<uint32_t>(__popc(peers & ((1u << lane) - 1u))) : 0u;
+}
+
 __device__ __forceinline__ uint32_t warp_sum(uint32_t v)
 {
 #pragma unroll

@@ -7,6 +7,9 @@
 // multiply-add is contracted.
 #include <cfloat>
 
+#include <mutex>
+#include <random>
+
 #include "lp_batch.cuh"
 #include "lp_common.cuh"
 #include "lp_math.cuh"
@@ -143,23 +146,19 @@ __global__ void __launch_bounds__(256) k_ring_apply(BatchDev b)
 // ------------------------------------------------------------------------------------------
 // Polar grid (constructPolarGrid, segmenter.cpp:103-204).
 // ------------------------------------------------------------------------------------------
-__global__ void k_bin(BatchDev b)
+__device__ __forceinline__ int32_t bin_point(const BatchDev& b, uint32_t i)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.npts)
-        return;
     const int s = scan_of_point(b, i);
     const ScanDev& sd = b.scans[s];
-    b.pt_cell[i] = -1;
     if (i - sd.pt_off >= b.state[s].n_pts)
-        return; // slot left empty by noise removal
+        return -1; // slot left empty by noise removal
     const float4 p = b.pts[i];
     if (p.z < sd.zmin_adj || p.z > sd.zmax_adj)
-        return;
+        return -1;
     const float d = sqrtf(p.x * p.x + p.y * p.y);
     const int32_t radial = static_cast<int32_t>(d / sd.spacing);
     if (d < sd.min_d || d > sd.max_d || radial >= sd.nrad)
-        return;
+        return -1;
     float az = lpm::atan2_approx(p.y, p.x);
     az = (az < 0) ? (az + kTwoPiF) : az;
     const int32_t slice = min(static_cast<int32_t>(az / sd.slice_res), sd.nslice - 1);
@@ -168,20 +167,30 @@ __global__ void k_bin(BatchDev b)
     {
         h = b.ring[i];
         if (h >= sd.H)
-            return;
+            return -1;
     }
     else
     {
         const float el = lpm::cr_atanf(p.z / d);
         h = static_cast<int32_t>((el - sd.down_rad) / sd.rad_per_px);
         if (h < 0 || h >= sd.H)
-            return;
+            return -1;
     }
     const int32_t w = static_cast<int32_t>(static_cast<uint16_t>(static_cast<float>(sd.W - 1) * az / kTwoPiF));
-    const uint32_t cell = sd.cell_off + static_cast<uint32_t>(slice * sd.nrad + radial);
-    b.pt_cell[i] = static_cast<int32_t>(cell);
     b.pt_pix[i] = h * sd.W + w;
-    b.pt_slot[i] = atomicAdd(&b.cell_cnt[cell], 1u);
+    return static_cast<int32_t>(sd.cell_off + static_cast<uint32_t>(slice * sd.nrad + radial));
+}
+
+__global__ void k_bin(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t cell = (i < b.npts) ? bin_point(b, i) : -1;
+    if (i < b.npts)
+        b.pt_cell[i] = cell;
+    // slot of the point in its cell (the order within a cell is free: cells are sorted later)
+    const uint32_t slot = warp_aggregated_inc(b.cell_cnt, static_cast<uint32_t>(cell), cell >= 0);
+    if (cell >= 0)
+        b.pt_slot[i] = slot;
 }
 
 __global__ void k_scatter(BatchDev b)
@@ -199,12 +208,10 @@ __global__ void k_scatter(BatchDev b)
 }
 
 // zlow of a sorted cell (segmenter.cpp:249-260): z[k*] for the largest k in [1, n/2] with
-// z[k] - z[k-1] > 0.5, else z[0].
-__global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
+// z[k] - z[k-1] > 0.5, else z[0]. Persistent warps stride over the cells (most are empty), so
+// the grid is not quantised by its slowest medium cell.
+__device__ __forceinline__ void cell_small_one(const BatchDev& b, uint32_t c, float* zs, int32_t* is)
 {
-    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (c >= b.ncell)
-        return;
     const uint32_t lane = lane_id();
     const uint32_t n = b.cell_cnt[c];
     if (n == 0)
@@ -224,11 +231,7 @@ __global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
     const uint32_t start = b.cell_start[c];
     if (n > kSmallCell)
     {
-        // one warp sorts the cell in its slice of shared memory (bitonic, __syncwarp per stage)
-        __shared__ float wz[8][kMediumCell];
-        __shared__ int32_t wi[8][kMediumCell];
-        const uint32_t warp = threadIdx.x >> 5;
-        float* zs = wz[warp];
+        // the warp sorts the cell in its slice of shared memory (bitonic, __syncwarp per stage)
         const uint32_t np2 = next_pow2(n);
         for (uint32_t k = lane; k < np2; k += 32)
             zs[k] = (k < n) ? b.csr_z[start + k] : INFINITY;
@@ -243,7 +246,6 @@ __global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
             b.zlow[c] = zs[kbest];
         if (near)
         {
-            int32_t* is = wi[warp];
             for (uint32_t k = lane; k < np2; k += 32)
                 is[k] = (k < n) ? b.csr_idx[start + k] : INT32_MAX;
             __syncwarp();
@@ -251,6 +253,7 @@ __global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
             for (uint32_t k = lane; k < n; k += 32)
                 b.csr_idx[start + k] = is[k];
         }
+        __syncwarp();
         return;
     }
     float z = (lane < n) ? b.csr_z[start + lane] : INFINITY;
@@ -269,6 +272,16 @@ __global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
         if (lane < n)
             b.csr_idx[start + lane] = idx;
     }
+}
+
+__global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
+{
+    __shared__ float wz[8][kMediumCell];
+    __shared__ int32_t wi[8][kMediumCell];
+    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + warp; c < b.ncell; c += nwarps)
+        cell_small_one(b, c, wz[warp], wi[warp]);
 }
 
 __global__ void __launch_bounds__(512) k_cell_large(BatchDev b)
@@ -402,9 +415,9 @@ struct Mt19937
 {
     uint32_t mt[624];
     int idx;
-    __device__ explicit Mt19937(uint32_t seed)
+    __device__ void seed(uint32_t s)
     {
-        mt[0] = seed;
+        mt[0] = s;
         for (int i = 1; i < 624; ++i)
             mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + static_cast<uint32_t>(i);
         idx = 624;
@@ -428,6 +441,31 @@ struct Mt19937
         y ^= (y << 15) & 0xefc60000u;
         y ^= y >> 18;
         return y;
+    }
+};
+
+// Every scan draws from MT19937 seeded with 42 (segmenter.cpp:328), so its first outputs are the
+// same for all scans: they are computed once per device on the host (std::mt19937) and read from
+// this table; a scan that needs more (many redraws) runs the generator itself past the table.
+constexpr int kMtTable = 4 * 624;
+__device__ uint32_t g_mt42[kMtTable];
+
+struct Mt42Stream
+{
+    Mt19937 gen; // seeded only past the table
+    int idx = 0;
+    __device__ uint32_t next()
+    {
+        if (idx < kMtTable)
+            return g_mt42[idx++];
+        if (idx == kMtTable)
+        {
+            gen.seed(42u);
+            for (int k = 0; k < kMtTable; ++k)
+                gen.next();
+        }
+        ++idx;
+        return gen.next();
     }
     __device__ uint32_t bounded(uint32_t range) // uniform in [0, range)
     {
@@ -463,7 +501,7 @@ __global__ void k_ransac_draw(BatchDev b)
     b.pvalid[s] = 0ull;
     if (N < 2)
         return; // the reference never ends its p3 draw for N == 1 (segmenter.cpp:382-386)
-    Mt19937 gen(42u);
+    Mt42Stream gen;
     const float p1x = 0.0F, p1y = 0.0F, p1z = -sd.sensor_h;
     unsigned long long valid = 0ull;
     for (int it = 0; it < kMaxRansacIters; ++it)
@@ -1187,6 +1225,23 @@ __global__ void k_debug_math(int kind, const float* a, const float* bb, uint32_t
     out[i] = r;
 }
 
+void init_segment_tables()
+{
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev >= 0 && dev < 64 && done[dev])
+        return;
+    std::mt19937 gen(42u);
+    uint32_t table[kMtTable];
+    for (int k = 0; k < kMtTable; ++k)
+        table[k] = static_cast<uint32_t>(gen());
+    if (cudaMemcpyToSymbol(g_mt42, table, sizeof(table)) == cudaSuccess && dev >= 0 && dev < 64)
+        done[dev] = true;
+}
+
 void launch_debug_math(Launcher& L, int kind, const float* a, const float* bb, uint32_t n, float* out)
 {
     LP_LAUNCH(L, k_debug_math, div_up(n, 256u), 256, kind, a, bb, n, out);
@@ -1280,7 +1335,7 @@ void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, ui
     LP_LAUNCH(L, k_bin, div_up(b.npts, T), T, b);
     L.scan(b.cell_cnt, b.cell_start, b.ncell + 1);
     LP_LAUNCH(L, k_scatter, div_up(b.npts, T), T, b);
-    LP_LAUNCH(L, k_cell_small, div_up(b.ncell * 32u, 256u), 256, b);
+    LP_LAUNCH(L, k_cell_small, std::min(div_up(b.ncell * 32u, 256u), static_cast<uint32_t>(sm_count()) * 8u), 256, b);
     LP_LAUNCH(L, k_cell_large, 152u * 2u, 512, b);
     LP_LAUNCH(L, k_chain, div_up(hb.nslices, 128u), 128, b, hb.nslices);
     LP_LAUNCH(L, k_near, div_up(b.nnear * 32u, 256u), 256, b, 0);

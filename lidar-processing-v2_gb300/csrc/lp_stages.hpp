@@ -115,6 +115,7 @@ struct Launcher
 
 // One-time kernel attributes (dynamic shared memory opt-in); called when a context is created.
 void init_kernel_attributes();
+void init_segment_tables(); // per-device constant tables (the seed-42 MT19937 stream)
 // Streaming multiprocessors of the current device (persistent grids are sized by it).
 int sm_count();
 
