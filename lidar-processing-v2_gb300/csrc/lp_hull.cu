@@ -353,9 +353,11 @@ __device__ void pca_box(const double2* P, int n, lp_bounding_box* out)
     *out = box;
 }
 
-// PCA box by one warp, the same arithmetic as pca_box: the sums run in the same order on every
-// lane; the rotated min/max is split across lanes (min and max are exact, so the extents are the
-// sequential loop's).
+// PCA box by one warp. The mean and the covariance sums run in FP64 in the reference's order (the
+// principal angle is ill-conditioned exactly where those sums nearly cancel, so they are kept
+// bit-identical); a = sxx - syy and b = 2 sxy are formed in FP64 too. From there the angle, the
+// rotation and the extents use FP32 (relative error ~1e-7 of the cluster extent, far inside the
+// tolerance the box is held to), the corners add the FP64 mean back.
 __device__ void pca_box_warp(const double2* P, int n, lp_bounding_box* out)
 {
     const uint32_t lane = lane_id();
@@ -386,33 +388,34 @@ __device__ void pca_box_warp(const double2* P, int n, lp_bounding_box* out)
         sxx /= (n - 1);
         sxy /= (n - 1);
         syy /= (n - 1);
-        const double theta = 0.5 * atan2(2.0 * sxy, sxx - syy);
-        const double v00 = cos(theta), v10 = sin(theta);
-        const double v01 = -v10, v11 = v00;
-        double mnx = DBL_MAX, mxx = -DBL_MAX, mny = DBL_MAX, mxy = -DBL_MAX;
+        const float theta = 0.5f * lpm::cr_atan2f(__double2float_rn(2.0 * sxy), __double2float_rn(sxx - syy));
+        float v10, v00;
+        sincosf(theta, &v10, &v00);
+        const float v01 = -v10, v11 = v00;
+        float mnx = FLT_MAX, mxx = -FLT_MAX, mny = FLT_MAX, mxy = -FLT_MAX;
         for (int i = static_cast<int>(lane); i < n; i += 32)
         {
-            const double dx = P[i].x - mx, dy = P[i].y - my;
-            const double rx = dx * v00 + dy * v10;
-            const double ry = dx * v01 + dy * v11;
-            mnx = fmin(mnx, rx);
-            mxx = fmax(mxx, rx);
-            mny = fmin(mny, ry);
-            mxy = fmax(mxy, ry);
+            const float dx = __double2float_rn(P[i].x - mx), dy = __double2float_rn(P[i].y - my);
+            const float rx = dx * v00 + dy * v10;
+            const float ry = dx * v01 + dy * v11;
+            mnx = fminf(mnx, rx);
+            mxx = fmaxf(mxx, rx);
+            mny = fminf(mny, ry);
+            mxy = fmaxf(mxy, ry);
         }
-        mnx = warp_min_d(mnx);
-        mxx = warp_max_d(mxx);
-        mny = warp_min_d(mny);
-        mxy = warp_max_d(mxy);
-        const double xs[4] = {mnx, mxx, mxx, mnx};
-        const double ys[4] = {mny, mny, mxy, mxy};
+        mnx = warp_min_f(mnx);
+        mxx = warp_max_f(mxx);
+        mny = warp_min_f(mny);
+        mxy = warp_max_f(mxy);
+        const float xs[4] = {mnx, mxx, mxx, mnx};
+        const float ys[4] = {mny, mny, mxy, mxy};
         for (int k = 0; k < 4; ++k)
         {
-            box.corners[k][0] = xs[k] * v00 + ys[k] * v01 + mx;
-            box.corners[k][1] = xs[k] * v10 + ys[k] * v11 + my;
+            box.corners[k][0] = static_cast<double>(xs[k] * v00 + ys[k] * v01) + mx;
+            box.corners[k][1] = static_cast<double>(xs[k] * v10 + ys[k] * v11) + my;
         }
-        box.area = __double2float_rn((mxx - mnx) * (mxy - mny));
-        box.angle_rad = __double2float_rn(atan2(v10, v00));
+        box.area = (mxx - mnx) * (mxy - mny);
+        box.angle_rad = theta; // atan2(sin t, cos t) = t for t in (-pi/2, pi/2]
         box.is_valid = 1;
     }
     if (lane == 0)
@@ -443,15 +446,18 @@ __device__ __forceinline__ void extents_fp64(const double2* P, int n, double cx,
 // Rotating calipers with the candidate boxes screened in FP32 (same result as calipers_warp).
 //
 // The reference walks the edges named by the antipodal pairs and keeps a box when its FP64 area
-// is below the float `best` of the boxes kept so far. An edge's box area is the same for both
-// directions of the edge (every term only changes sign), so it is computed once per hull edge j
-// (P[j] -> P[j+1]): ea[j] = FP32 area, within e = 1e-4 R^2 of the FP64 area (the rounding of
-// the float frame, direction and extents stays below 6e-6 R^2, R = largest |P - P[0]|). Edges with
-// ea[j] <= T are the contenders, with T grown from the smallest ea until no other edge lies within
-// G = 2e + 1e-6 (T + 2e) above it. Every other edge then has a float area above every contender's
-// FP64 area and above the float of the smallest area, so (i) the last box the reference keeps is a
-// contender's and (ii) replaying the reference's walk over the contenders alone, with their FP64
-// areas, keeps the same boxes among them. The winner's box is computed in FP64 as written.
+// is below the float `best` of the boxes kept so far. An edge's box is the same for both
+// directions of the edge (every term only changes sign, exactly), so it is evaluated once per
+// hull edge j (P[j] -> P[j+1]): ea[j] = FP32 area, within e = 1e-4 R^2 of the FP64 area (the
+// rounding of the float frame, direction and extents stays below 6e-6 R^2, R = largest
+// |P - P[0]|). Edges with ea[j] <= T are the contenders, with T grown from the smallest ea until
+// no other edge lies within G = 2e + 1e-6 (T + 2e) above it. Every other edge then has a float
+// area above every contender's FP64 area and above the float of the smallest area, so (i) the
+// last box the reference keeps is a contender's and (ii) replaying the reference's walk over the
+// contenders alone, with their FP64 areas, keeps the same boxes among them. Each contender's FP64
+// extents are kept by one lane; the winner's corners come from them, negated for the reverse
+// direction (exact), so they are the reference's. The skip test (edge length < 1e-6) is screened
+// in FP32 too (|float len^2 - len^2| < 2^-21 len^2) and evaluated in FP64 only near 1e-12.
 // Up to 32 contenders (one per lane) are handled; more fall back to calipers_warp.
 __device__ void calipers_fast(const double2* P, const float2* Pf, int n, const int2* pairs, int npairs, float* ea,
                               float r2, lp_bounding_box* out)
@@ -475,12 +481,18 @@ __device__ void calipers_fast(const double2* P, const float2* Pf, int n, const i
     for (int j = static_cast<int>(lane); j < n; j += 32)
     {
         const int j1 = (j + 1 == n) ? 0 : j + 1;
-        const double dx = P[j1].x - P[j].x, dy = P[j1].y - P[j].y;
-        float a = INFINITY; // edges the reference skips never compete
-        if (!(sqrt(dx * dx + dy * dy) < 1.0e-6))
+        const float fx = Pf[j1].x - Pf[j].x, fy = Pf[j1].y - Pf[j].y;
+        const float fl2 = fx * fx + fy * fy;
+        bool skip = fl2 < 0.9999e-12f;
+        if (!skip && !(fl2 > 1.0001e-12f))
         {
-            const float fx = Pf[j1].x - Pf[j].x, fy = Pf[j1].y - Pf[j].y;
-            const float fl = sqrtf(fx * fx + fy * fy);
+            const double dx = P[j1].x - P[j].x, dy = P[j1].y - P[j].y;
+            skip = sqrt(dx * dx + dy * dy) < 1.0e-6;
+        }
+        float a = INFINITY; // edges the reference skips never compete
+        if (!skip)
+        {
+            const float fl = sqrtf(fl2);
             const float ux = fx / fl, uy = fy / fl;
             float mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
             for (int k = 0; k < n; ++k)
@@ -528,9 +540,9 @@ __device__ void calipers_fast(const double2* P, const float2* Pf, int n, const i
     }
     cx /= n;
     cy /= n;
-    // contender c (in edge order) is held by lane c: its edge and FP64 area
+    // contender c (in edge order) is held by lane c: its edge, direction, FP64 extents and area
     int my_j = -1;
-    double my_area = 0.0;
+    double my_ux = 0.0, my_uy = 0.0, my_mnx = 0.0, my_mxx = 0.0, my_mny = 0.0, my_mxy = 0.0, my_area = 0.0;
     int ncont = 0;
     for (int base = 0; base < n; base += 32)
     {
@@ -550,6 +562,12 @@ __device__ void calipers_fast(const double2* P, const float2* Pf, int n, const i
                 if (static_cast<int>(lane) == ncont)
                 {
                     my_j = jj;
+                    my_ux = ux;
+                    my_uy = uy;
+                    my_mnx = mnx;
+                    my_mxx = mxx;
+                    my_mny = mny;
+                    my_mxy = mxy;
                     my_area = (mxx - mnx) * (mxy - mny);
                 }
             }
@@ -563,7 +581,8 @@ __device__ void calipers_fast(const double2* P, const float2* Pf, int n, const i
     }
     // the reference's walk over the contenders
     float best = __double2float_rn(DBL_MAX);
-    int wi = -1, wnb = -1;
+    int wj = -1;
+    bool wrev = false;
     for (int pi = 0; pi < npairs; ++pi)
     {
         const int2 pr = pairs[pi];
@@ -585,20 +604,29 @@ __device__ void calipers_fast(const double2* P, const float2* Pf, int n, const i
                 if (area < static_cast<double>(best))
                 {
                     best = __double2float_rn(area);
-                    wi = index;
-                    wnb = nb;
+                    wj = j;
+                    wrev = (o == 0); // walked from P[j+1] to P[j]
                 }
             }
         }
     }
-    if (wi >= 0)
+    if (wj >= 0)
     {
-        const double ex = P[wnb].x - P[wi].x;
-        const double ey = P[wnb].y - P[wi].y;
-        const double len = sqrt(ex * ex + ey * ey);
-        const double ux = ex / len, uy = ey / len;
-        double mnx, mxx, mny, mxy;
-        extents_fp64(P, n, cx, cy, ux, uy, mnx, mxx, mny, mxy);
+        const int src = __ffs(__ballot_sync(0xffffffffu, my_j == wj)) - 1;
+        double ux = __shfl_sync(0xffffffffu, my_ux, src), uy = __shfl_sync(0xffffffffu, my_uy, src);
+        double mnx = __shfl_sync(0xffffffffu, my_mnx, src), mxx = __shfl_sync(0xffffffffu, my_mxx, src);
+        double mny = __shfl_sync(0xffffffffu, my_mny, src), mxy = __shfl_sync(0xffffffffu, my_mxy, src);
+        if (wrev)
+        {
+            // reverse direction: u and every projection change sign exactly
+            ux = -ux;
+            uy = -uy;
+            const double a0 = mnx, a1 = mny;
+            mnx = -mxx;
+            mxx = -a0;
+            mny = -mxy;
+            mxy = -a1;
+        }
         box.area = best;
         box.corners[0][0] = mnx * ux - mny * uy + cx;
         box.corners[0][1] = mnx * uy + mny * ux + cy;

@@ -207,10 +207,110 @@ __global__ void k_scatter(BatchDev b)
     b.csr_z[pos] = b.pts[i].z;
 }
 
-// zlow of a sorted cell (segmenter.cpp:249-260): z[k*] for the largest k in [1, n/2] with
-// z[k] - z[k-1] > 0.5, else z[0]. Persistent warps stride over the cells (most are empty), so
-// the grid is not quantised by its slowest medium cell.
-__device__ __forceinline__ void cell_small_one(const BatchDev& b, uint32_t c, float* zs, int32_t* is)
+// zlow of a cell (segmenter.cpp:249-260): with the cell's heights sorted, z[k] for the largest k
+// in [1, n/2] with z[k] - z[k-1] > 0.5, else z[0].
+//
+// No sort is needed for it. Heights fall into half-metre buckets [q/2, (q+1)/2) with
+// q = floor(2z) (2z and floor are exact in binary32). Two heights of one bucket differ by less
+// than 0.5, so their float difference is at most 0.5: a qualifying k can only be where the sorted
+// order crosses from a non-empty bucket A to the next non-empty bucket B, with z[k] = min(B),
+// z[k-1] = max(A) and k = the number of heights below B. A warp therefore accumulates count, min
+// and max per bucket and evaluates exactly the reference's test at those boundaries. Cells whose
+// heights leave the bucket range (a nan, a range over 16 m) take the sorting path.
+__device__ __forceinline__ uint32_t zord(float f)
+{
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float zunord(uint32_t u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+struct CellHist
+{
+    uint32_t cnt[32], lo[32], hi[32];
+};
+
+__device__ bool cell_zlow_hist(const BatchDev& b, const ScanDev& sd, uint32_t c, uint32_t n, uint32_t start,
+                               CellHist& hs)
+{
+    const uint32_t lane = lane_id();
+    const int32_t q0 = static_cast<int32_t>(floorf(2.0f * sd.zmin_adj));
+    const int32_t nb = static_cast<int32_t>(floorf(2.0f * sd.zmax_adj)) - q0 + 1;
+    if (!(nb >= 1 && nb <= 32))
+        return false;
+    hs.cnt[lane] = 0u;
+    hs.lo[lane] = 0xffffffffu;
+    hs.hi[lane] = 0u;
+    __syncwarp();
+    bool bad = false;
+    for (uint32_t k = lane; k < n; k += 32)
+    {
+        const float z = b.csr_z[start + k];
+        const float f = floorf(2.0f * z);
+        if (!(f >= static_cast<float>(q0) && f < static_cast<float>(q0 + nb)))
+        {
+            bad = true; // nan or outside the bucket range
+            continue;
+        }
+        const int32_t q = static_cast<int32_t>(f) - q0;
+        atomicAdd(&hs.cnt[q], 1u);
+        atomicMin(&hs.lo[q], zord(z));
+        atomicMax(&hs.hi[q], zord(z));
+    }
+    if (__any_sync(0xffffffffu, bad))
+        return false;
+    __syncwarp();
+    // lane q = bucket q: position of its first height, previous non-empty bucket
+    const uint32_t cnt = hs.cnt[lane];
+    const uint32_t below = warp_incl_scan(cnt) - cnt;
+    int32_t last = (cnt > 0u) ? static_cast<int32_t>(lane) : -1; // inclusive max-scan of non-empty
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const int32_t t = __shfl_up_sync(0xffffffffu, last, o);
+        if (lane >= static_cast<uint32_t>(o))
+            last = max(last, t);
+    }
+    int32_t prev = __shfl_up_sync(0xffffffffu, last, 1);
+    if (lane == 0)
+        prev = -1;
+    bool qual = false;
+    if (cnt > 0u && prev >= 0 && below <= n / 2)
+        qual = (zunord(hs.lo[lane]) - zunord(hs.hi[prev])) > 0.5F;
+    const uint32_t qm = __ballot_sync(0xffffffffu, qual);
+    const uint32_t ne = __ballot_sync(0xffffffffu, cnt > 0u);
+    const int32_t pick = qm ? (31 - __clz(qm)) : (__ffs(ne) - 1); // no boundary: z[0], the lowest bucket
+    if (lane == 0)
+        b.zlow[c] = zunord(hs.lo[pick]);
+    __syncwarp();
+    return true;
+}
+
+// Fallback for a cell the buckets cannot take (at most kMediumCell heights): warp bitonic sort.
+__device__ void cell_zlow_sorted(const BatchDev& b, uint32_t c, uint32_t n, uint32_t start, float* zs)
+{
+    const uint32_t lane = lane_id();
+    const uint32_t np2 = next_pow2(n);
+    for (uint32_t k = lane; k < np2; k += 32)
+        zs[k] = (k < n) ? b.csr_z[start + k] : INFINITY;
+    __syncwarp();
+    warp_bitonic_smem(zs, np2, [](float a, float bb) { return a < bb; });
+    int kbest = 0;
+    for (uint32_t k = 1 + lane; k <= n / 2; k += 32)
+        if (zs[k] - zs[k - 1] > 0.5F)
+            kbest = static_cast<int>(k); // lanes visit k in increasing order
+    kbest = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(kbest)));
+    if (lane == 0)
+        b.zlow[c] = zs[kbest];
+    __syncwarp();
+}
+
+// large_list entries: the cell, bit 31 set when its zlow still has to be found by sorting.
+constexpr uint32_t kLargeNeedsZ = 0x80000000u;
+
+__device__ __forceinline__ void cell_small_one(const BatchDev& b, uint32_t c, float* zs, int32_t* is, CellHist& hs)
 {
     const uint32_t lane = lane_id();
     const uint32_t n = b.cell_cnt[c];
@@ -219,69 +319,52 @@ __device__ __forceinline__ void cell_small_one(const BatchDev& b, uint32_t c, fl
     const int s = scan_of_cell(b, c);
     const ScanDev& sd = b.scans[s];
     const bool near = static_cast<int32_t>((c - sd.cell_off) % static_cast<uint32_t>(sd.nrad)) < kRansacRadialBins;
-    if (n > kMediumCell)
+    const uint32_t start = b.cell_start[c];
+    bool need_z = !cell_zlow_hist(b, sd, c, n, start, hs);
+    if (need_z && n <= static_cast<uint32_t>(kMediumCell))
+    {
+        cell_zlow_sorted(b, c, n, start, zs);
+        need_z = false;
+    }
+    // the RANSAC candidates of a near cell are read in cloud order: sort its indices
+    if (need_z || (near && n > static_cast<uint32_t>(kMediumCell)))
     {
         if (lane == 0)
         {
             const uint32_t k = atomicAdd(b.n_large, 1u);
-            b.large_list[k] = c;
+            b.large_list[k] = c | (need_z ? kLargeNeedsZ : 0u);
         }
         return;
     }
-    const uint32_t start = b.cell_start[c];
+    if (!near)
+        return;
     if (n > kSmallCell)
     {
-        // the warp sorts the cell in its slice of shared memory (bitonic, __syncwarp per stage)
         const uint32_t np2 = next_pow2(n);
         for (uint32_t k = lane; k < np2; k += 32)
-            zs[k] = (k < n) ? b.csr_z[start + k] : INFINITY;
+            is[k] = (k < n) ? b.csr_idx[start + k] : INT32_MAX;
         __syncwarp();
-        warp_bitonic_smem(zs, np2, [](float a, float bb) { return a < bb; });
-        int kbest = 0;
-        for (uint32_t k = 1 + lane; k <= n / 2; k += 32)
-            if (zs[k] - zs[k - 1] > 0.5F)
-                kbest = static_cast<int>(k); // lanes visit k in increasing order
-        kbest = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(kbest)));
-        if (lane == 0)
-            b.zlow[c] = zs[kbest];
-        if (near)
-        {
-            for (uint32_t k = lane; k < np2; k += 32)
-                is[k] = (k < n) ? b.csr_idx[start + k] : INT32_MAX;
-            __syncwarp();
-            warp_bitonic_smem(is, np2, [](int32_t a, int32_t bb) { return a < bb; });
-            for (uint32_t k = lane; k < n; k += 32)
-                b.csr_idx[start + k] = is[k];
-        }
+        warp_bitonic_smem(is, np2, [](int32_t a, int32_t bb) { return a < bb; });
+        for (uint32_t k = lane; k < n; k += 32)
+            b.csr_idx[start + k] = is[k];
         __syncwarp();
         return;
     }
-    float z = (lane < n) ? b.csr_z[start + lane] : INFINITY;
-    z = warp_bitonic_sort(z, [](float a, float bb) { return a < bb; });
-    const float zp = __shfl_up_sync(0xffffffffu, z, 1);
-    const bool gap = (lane >= 1 && lane <= n / 2 && (z - zp) > 0.5F);
-    const uint32_t mask = __ballot_sync(0xffffffffu, gap);
-    const int ks = mask ? (31 - __clz(mask)) : 0;
-    const float zl = __shfl_sync(0xffffffffu, z, ks);
-    if (lane == 0)
-        b.zlow[c] = zl;
-    if (near)
-    {
-        int32_t idx = (lane < n) ? b.csr_idx[start + lane] : INT32_MAX;
-        idx = warp_bitonic_sort(idx, [](int32_t a, int32_t bb) { return a < bb; });
-        if (lane < n)
-            b.csr_idx[start + lane] = idx;
-    }
+    int32_t idx = (lane < n) ? b.csr_idx[start + lane] : INT32_MAX;
+    idx = warp_bitonic_sort(idx, [](int32_t a, int32_t bb) { return a < bb; });
+    if (lane < n)
+        b.csr_idx[start + lane] = idx;
 }
 
 __global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
 {
     __shared__ float wz[8][kMediumCell];
     __shared__ int32_t wi[8][kMediumCell];
+    __shared__ CellHist wh[8];
     const uint32_t warp = threadIdx.x >> 5;
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + warp; c < b.ncell; c += nwarps)
-        cell_small_one(b, c, wz[warp], wi[warp]);
+        cell_small_one(b, c, wz[warp], wi[warp], wh[warp]);
 }
 
 __global__ void __launch_bounds__(512) k_cell_large(BatchDev b)
@@ -291,7 +374,9 @@ __global__ void __launch_bounds__(512) k_cell_large(BatchDev b)
     const uint32_t nl = *b.n_large;
     for (uint32_t li = blockIdx.x; li < nl; li += gridDim.x)
     {
-        const uint32_t c = b.large_list[li];
+        const uint32_t entry = b.large_list[li];
+        const uint32_t c = entry & ~kLargeNeedsZ;
+        const bool need_z = (entry & kLargeNeedsZ) != 0u;
         const uint32_t n = b.cell_cnt[c];
         const uint32_t start = b.cell_start[c];
         const int s = scan_of_cell(b, c);
@@ -301,24 +386,28 @@ __global__ void __launch_bounds__(512) k_cell_large(BatchDev b)
             if (threadIdx.x == 0)
             {
                 raise_err(&b.state[s], ERR_CELL_TOO_LARGE);
-                b.zlow[c] = b.csr_z[start];
+                if (need_z)
+                    b.zlow[c] = b.csr_z[start];
             }
             continue;
         }
         const uint32_t np2 = next_pow2(n);
-        for (uint32_t k = threadIdx.x; k < np2; k += blockDim.x)
-            sz[k] = (k < n) ? b.csr_z[start + k] : INFINITY;
-        if (threadIdx.x == 0)
-            sk = 0;
-        __syncthreads();
-        block_bitonic_sort(sz, np2, [](float a, float bb) { return a < bb; });
-        for (uint32_t k = 1 + threadIdx.x; k <= n / 2; k += blockDim.x)
-            if (sz[k] - sz[k - 1] > 0.5F)
-                atomicMax(&sk, static_cast<int32_t>(k));
-        __syncthreads();
-        if (threadIdx.x == 0)
-            b.zlow[c] = sz[sk];
-        __syncthreads();
+        if (need_z)
+        {
+            for (uint32_t k = threadIdx.x; k < np2; k += blockDim.x)
+                sz[k] = (k < n) ? b.csr_z[start + k] : INFINITY;
+            if (threadIdx.x == 0)
+                sk = 0;
+            __syncthreads();
+            block_bitonic_sort(sz, np2, [](float a, float bb) { return a < bb; });
+            for (uint32_t k = 1 + threadIdx.x; k <= n / 2; k += blockDim.x)
+                if (sz[k] - sz[k - 1] > 0.5F)
+                    atomicMax(&sk, static_cast<int32_t>(k));
+            __syncthreads();
+            if (threadIdx.x == 0)
+                b.zlow[c] = sz[sk];
+            __syncthreads();
+        }
         const bool near = static_cast<int32_t>((c - sd.cell_off) % static_cast<uint32_t>(sd.nrad)) < kRansacRadialBins;
         if (near)
         {
