@@ -634,47 +634,57 @@ __global__ void k_ransac_draw(BatchDev b)
     b.pvalid[s] = valid;
 }
 
+// Inlier counts of every hypothesis plane of a scan (segmenter.cpp:409-430): lane l of every
+// warp holds planes l and l + 32 as a float pair and counts, for the candidates its warp takes,
+// |((n.x p.x + n.y p.y) + n.z p.z) - d| < thr with packed binary32 operations (each half rounds
+// like the scalar operation, in the reference's order).
 __global__ void __launch_bounds__(256) k_ransac_inliers(BatchDev b)
 {
-    __shared__ float4 pl[kMaxRansacIters];
-    __shared__ uint32_t cnt[kMaxRansacIters];
+    static_assert(kMaxRansacIters <= 64, "two planes per lane");
     const int s = blockIdx.y;
+    const unsigned long long valid = b.pvalid[s];
+    if (valid == 0ull)
+        return; // uniform over the block
     const ScanDev& sd = b.scans[s];
     const ScanState& st = b.state[s];
-    const unsigned long long valid = b.pvalid[s];
-    if (threadIdx.x < kMaxRansacIters)
-    {
-        pl[threadIdx.x] = b.planes[s * kMaxRansacIters + threadIdx.x];
-        cnt[threadIdx.x] = 0u;
-    }
-    __syncthreads();
+    const uint32_t lane = lane_id();
+    const uint32_t i0 = lane, i1 = lane + 32u;
+    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float4 qa = (i0 < static_cast<uint32_t>(kMaxRansacIters)) ? b.planes[s * kMaxRansacIters + i0] : zero;
+    const float4 qb = (i1 < static_cast<uint32_t>(kMaxRansacIters)) ? b.planes[s * kMaxRansacIters + i1] : zero;
+    const float2 qx = make_float2(qa.x, qb.x), qy = make_float2(qa.y, qb.y), qz = make_float2(qa.z, qb.z);
+    const float2 nqw = make_float2(-qa.w, -qb.w); // x - w == x + (-w) exactly
+    const float thr = sd.thr;
     const uint32_t N = st.n_cand;
-    if (valid != 0ull)
+    const float4* cand = b.cand + st.cand_off;
+    uint32_t ca = 0u, cb = 0u;
+    // candidates staged per block in shared memory (coalesced), read by each warp as broadcasts
+    constexpr uint32_t kTile = 1024;
+    __shared__ float4 tile[kTile];
+    const uint32_t warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (uint32_t base = blockIdx.x * kTile; base < N; base += gridDim.x * kTile)
     {
-        const uint32_t lane = lane_id();
-        const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-        const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-        for (uint32_t base = warp_global * 32; base < N; base += nwarps * 32)
+        const uint32_t cnt = min(kTile, N - base);
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x)
+            tile[k] = cand[base + k];
+        __syncthreads();
+#pragma unroll 4
+        for (uint32_t k = warp; k < cnt; k += nwarp)
         {
-            const uint32_t j = base + lane;
-            float4 p = make_float4(0, 0, 0, 0);
-            if (j < N)
-                p = b.cand[st.cand_off + j];
-            for (int it = 0; it < kMaxRansacIters; ++it)
-            {
-                if (!((valid >> it) & 1ull))
-                    continue;
-                const float4 q = pl[it];
-                const bool in = (j < N) && (fabsf((q.x * p.x) + (q.y * p.y) + (q.z * p.z) - q.w) < sd.thr);
-                const uint32_t m = __ballot_sync(0xffffffffu, in);
-                if (lane == 0 && m)
-                    atomicAdd(&cnt[it], static_cast<uint32_t>(__popc(m)));
-            }
+            const float4 p = tile[k];
+            float2 t = __fmul2_rn(qx, make_float2(p.x, p.x));
+            t = __fadd2_rn(t, __fmul2_rn(qy, make_float2(p.y, p.y)));
+            t = __fadd2_rn(t, __fmul2_rn(qz, make_float2(p.z, p.z)));
+            t = __fadd2_rn(t, nqw);
+            ca += (fabsf(t.x) < thr) ? 1u : 0u;
+            cb += (fabsf(t.y) < thr) ? 1u : 0u;
         }
     }
-    __syncthreads();
-    if (threadIdx.x < kMaxRansacIters && cnt[threadIdx.x])
-        atomicAdd(&b.inliers[s * kMaxRansacIters + threadIdx.x], cnt[threadIdx.x]);
+    if (i0 < static_cast<uint32_t>(kMaxRansacIters) && ((valid >> i0) & 1ull) && ca)
+        atomicAdd(&b.inliers[s * kMaxRansacIters + i0], ca);
+    if (i1 < static_cast<uint32_t>(kMaxRansacIters) && ((valid >> i1) & 1ull) && cb)
+        atomicAdd(&b.inliers[s * kMaxRansacIters + i1], cb);
 }
 
 __global__ void k_ransac_select(BatchDev b)
