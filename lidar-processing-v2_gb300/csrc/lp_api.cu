@@ -286,6 +286,7 @@ size_t carve(lp_batch& B, char* base)
         put(b.row_cnt, b.nrows + 1);
         put(b.jw, static_cast<size_t>(b.npix) * kJwStride);
         put(b.jn, static_cast<size_t>(b.npix) * kJwStride);
+        put(b.jrow, static_cast<size_t>(b.nrows) * kJrowWords);
         put(b.jmap, b.npix);
         if (R.stages & ST_IMAGE)
             put(B.d_image, static_cast<size_t>(b.npix) * 3);

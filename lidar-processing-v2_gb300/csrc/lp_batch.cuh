@@ -39,6 +39,12 @@ enum : uint8_t
 // Jump-convolution weight record of a queued pixel: 24 fresh weights, their sum, padding to a
 // multiple of 16 bytes (vector loads).
 constexpr uint32_t kJwStride = 28;
+// Per image row of the jump convolution: lastq[3], pad, 24 stale weights, 24 stale label infos
+// (kJrowNoUpdate: the row leaves the slot as it was; kJrowDynamic | pixel: the final colour of
+// that pixel; else the label), padded to 64 words.
+constexpr uint32_t kJrowWords = 64;
+constexpr uint32_t kJrowNoUpdate = 0xffffffffu;
+constexpr uint32_t kJrowDynamic = 0x80000000u;
 
 struct BatchDev
 {
@@ -100,6 +106,7 @@ struct BatchDev
     uint32_t* row_cnt;         // per global row
     float* jw;                 // per entry: 24 fresh weights + sum (stride kJwStride)
     float* jn;                 // per entry: 24 normalized weights, sum, slot label codes (stride kJwStride)
+    uint32_t* jrow;            // per image row: kJrowWords words (lastq, stale-buffer update)
     unsigned long long* jmap;  // per entry: 9-state transition map
 
     // ---- segmentation output -----------------------------------------------------------------

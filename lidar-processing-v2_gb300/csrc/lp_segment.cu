@@ -797,9 +797,31 @@ __global__ void k_pixel(BatchDev b)
 // Dilation of the obstacle channel by a 5x5 rectangle clipped at the image border, and the
 // row-major intersection queue (segmenter.cpp:486-514): one block per image row.
 // ------------------------------------------------------------------------------------------
+// Bit-mask form: a warp takes 32 consecutive pixels at a time; a ballot over each of the five
+// rows h-2..h+2 gives the obstacle bits of that segment, the rows are OR-ed, and the +-2 column
+// dilation is done with shifts, the two halo bits on each side coming from the neighbouring
+// segments (zero outside the image: the rectangle is clipped at the border). Dilation changes
+// only ground and empty pixels, never the obstacle channel, so rows are independent. Each warp
+// walks a contiguous run of segments; the queue keeps column order through per-warp counts.
+__device__ __forceinline__ uint32_t obstacle_bits(const uint8_t* st, int32_t H, int32_t W, int32_t h, int32_t seg)
+{
+    uint32_t m = 0u;
+    const int32_t w = seg * 32 + static_cast<int32_t>(lane_id());
+    const bool colok = seg >= 0 && w < W;
+#pragma unroll
+    for (int32_t dh = -2; dh <= 2; ++dh)
+    {
+        const int32_t hh = h + dh;
+        const bool ok = colok && hh >= 0 && hh < H;
+        m |= __ballot_sync(0xffffffffu, ok && st[hh * W + w] == PX_OBSTACLE);
+    }
+    return m;
+}
+
 __global__ void __launch_bounds__(256) k_dilate_rows(BatchDev b)
 {
-    __shared__ uint32_t sm[33];
+    __shared__ uint32_t wcount[8];
+    __shared__ uint32_t woff[8];
     const uint32_t r = blockIdx.x;
     const int s = scan_of_row(b, r);
     const ScanDev& sd = b.scans[s];
@@ -807,51 +829,61 @@ __global__ void __launch_bounds__(256) k_dilate_rows(BatchDev b)
     const int32_t H = sd.H, W = sd.W;
     uint8_t* st = b.pix_state + sd.pix_off;
     const uint32_t row_base = sd.pix_off + static_cast<uint32_t>(h * W);
-    uint32_t count = 0;
-    for (int32_t base = 0; base < W; base += blockDim.x)
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    const int32_t nseg = (W + 31) / 32;
+    const int32_t per = (nseg + 7) / 8;
+    const int32_t s0 = static_cast<int32_t>(warp) * per, s1 = min(nseg, s0 + per);
+    // pass 1: dilate, update the states, count the queued (ground -> intersection) pixels
+    uint32_t count = 0u;
+    uint32_t left = (s0 < s1) ? obstacle_bits(st, H, W, h, s0 - 1) : 0u;
+    uint32_t cur = (s0 < s1) ? obstacle_bits(st, H, W, h, s0) : 0u;
+    for (int32_t seg = s0; seg < s1; ++seg)
     {
-        const int32_t w = base + static_cast<int32_t>(threadIdx.x);
+        const uint32_t right = obstacle_bits(st, H, W, h, seg + 1);
+        const uint32_t d = cur | (cur << 1) | (cur << 2) | (cur >> 1) | (cur >> 2) | (left >> 31) | (left >> 30) |
+                           (right << 31) | (right << 30);
+        const int32_t w = seg * 32 + static_cast<int32_t>(lane);
         bool inter = false;
-        if (w < W)
+        if (w < W && ((d >> lane) & 1u))
         {
-            const uint8_t cur = st[h * W + w];
-            bool dil = false;
-            for (int32_t dh = -2; dh <= 2 && !dil; ++dh)
+            const uint8_t c = st[h * W + w];
+            if (c == PX_GROUND)
             {
-                const int32_t hh = h + dh;
-                if (hh < 0 || hh >= H)
-                    continue;
-                for (int32_t dw = -2; dw <= 2; ++dw)
-                {
-                    const int32_t ww = w + dw;
-                    if (ww >= 0 && ww < W && st[hh * W + ww] == PX_OBSTACLE)
-                    {
-                        dil = true;
-                        break;
-                    }
-                }
+                inter = true;
+                st[h * W + w] = PX_INTERSECT;
             }
-            if (dil)
-            {
-                if (cur == PX_GROUND)
-                {
-                    inter = true; // valid index is implied by a ground colour
-                    st[h * W + w] = PX_INTERSECT;
-                }
-                else if (cur == PX_EMPTY)
-                {
-                    st[h * W + w] = PX_EMPTY_RED;
-                }
-            }
+            else if (c == PX_EMPTY)
+                st[h * W + w] = PX_EMPTY_RED;
         }
-        uint32_t tot;
-        const uint32_t pre = block_excl_scan(inter ? 1u : 0u, sm, &tot);
-        if (inter)
-            b.row_cols[row_base + count + pre] = static_cast<uint16_t>(w);
-        count += tot;
+        count += static_cast<uint32_t>(__popc(__ballot_sync(0xffffffffu, inter)));
+        left = cur;
+        cur = right;
     }
+    if (lane == 0)
+        wcount[warp] = count;
+    __syncthreads();
     if (threadIdx.x == 0)
-        b.row_cnt[r] = count;
+    {
+        uint32_t run = 0u;
+        for (int k = 0; k < 8; ++k)
+        {
+            woff[k] = run;
+            run += wcount[k];
+        }
+        b.row_cnt[r] = run;
+    }
+    __syncthreads();
+    // pass 2: queue entries in column order (this row's states now hold the intersections)
+    uint32_t pos = woff[warp];
+    for (int32_t seg = s0; seg < s1; ++seg)
+    {
+        const int32_t w = seg * 32 + static_cast<int32_t>(lane);
+        const bool inter = w < W && st[h * W + w] == PX_INTERSECT;
+        const uint32_t m = __ballot_sync(0xffffffffu, inter);
+        if (inter)
+            b.row_cols[row_base + pos + static_cast<uint32_t>(__popc(m & ((1u << lane) - 1u)))] = static_cast<uint16_t>(w);
+        pos += static_cast<uint32_t>(__popc(m));
+    }
 }
 
 // Offsets of the 24-neighbour kernel, segmenter.cpp:527-530.
@@ -952,6 +984,55 @@ __global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
         nrm[26] = __uint_as_float(static_cast<uint32_t>(codes >> 32));
         nrm[27] = 0.0F;
     }
+    if (m == 0u || threadIdx.x >= 24u)
+        return;
+    // Row record (kJrowWords words): lastq[d] = the last of the row's final three queued pixels
+    // with column <= W-1-d; per slot k, what the row leaves in the reference's stale weight/label
+    // buffer: the raw weight of the last queued pixel for which slot k is inside the image, and
+    // its label, fixed already or (a queued pixel before it in vote order) read after the vote.
+    uint32_t* rec = b.jrow + static_cast<size_t>(r) * kJrowWords;
+    const uint16_t* cols = b.row_cols + row_base;
+    int32_t lq[3];
+    for (int32_t d = 0; d < 3; ++d)
+    {
+        lq[d] = -1;
+        for (int32_t j = static_cast<int32_t>(m) - 1; j >= 0 && j >= static_cast<int32_t>(m) - 3; --j)
+            if (cols[j] <= W - 1 - d)
+            {
+                lq[d] = j;
+                break;
+            }
+    }
+    const int k = static_cast<int>(threadIdx.x);
+    if (k < 3)
+        rec[k] = static_cast<uint32_t>(lq[k]);
+    const int32_t dh = jcp_dh(k), dw = jcp_dw(k);
+    const int32_t hh = h + dh;
+    uint32_t info = kJrowNoUpdate;
+    float qw = 0.0F;
+    if (hh >= 0 && hh < H)
+    {
+        const int32_t q = lq[dw > 0 ? dw : 0];
+        if (q >= 0 && static_cast<int32_t>(cols[q]) >= (dw < 0 ? -dw : 0))
+        {
+            qw = b.jw[static_cast<size_t>(row_base + q) * kJwStride + k];
+            info = V_U;
+            if (qw != 0.0F)
+            {
+                const uint32_t addr = static_cast<uint32_t>(hh * W + cols[q] + dw);
+                const uint8_t ns = st[addr];
+                const bool before = (dh < 0) || (dh == 0 && dw < 0);
+                if (!before)
+                    info = pre_view(ns);
+                else if (ns == PX_INTERSECT)
+                    info = kJrowDynamic | addr; // its colour is its own vote's outcome
+                else
+                    info = final_view(ns);
+            }
+        }
+    }
+    rec[4 + k] = __float_as_uint(qw);
+    rec[28 + k] = info;
 }
 
 __device__ __forceinline__ unsigned long long map_compose(unsigned long long later, unsigned long long earlier)
@@ -992,7 +1073,6 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
 {
     __shared__ float run_w[24];
     __shared__ uint8_t run_l[24];
-    __shared__ int32_t lastq[3]; // entry index of the last queued pixel with col <= W-1-d
     __shared__ unsigned long long wmaps[8];
     const int s = blockIdx.x;
     const ScanDev& sd = b.scans[s];
@@ -1014,19 +1094,17 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
             continue;
         const uint32_t row_base = sd.pix_off + static_cast<uint32_t>(h * W);
         const uint16_t* cols = b.row_cols + row_base;
-        if (threadIdx.x < 3)
+        // the row's record (from the parallel pass): lastq and the stale-buffer update
+        const uint32_t* rrec = b.jrow + static_cast<size_t>(r) * kJrowWords;
+        const int32_t lastq[3] = {static_cast<int32_t>(rrec[0]), static_cast<int32_t>(rrec[1]),
+                                  static_cast<int32_t>(rrec[2])};
+        float upd_w = 0.0F;
+        uint32_t upd_info = kJrowNoUpdate;
+        if (threadIdx.x < 24)
         {
-            const int32_t d = static_cast<int32_t>(threadIdx.x);
-            int32_t q = -1;
-            for (int32_t j = static_cast<int32_t>(m) - 1; j >= 0 && j >= static_cast<int32_t>(m) - 3; --j)
-                if (cols[j] <= W - 1 - d)
-                {
-                    q = j;
-                    break;
-                }
-            lastq[d] = q;
+            upd_w = __uint_as_float(rrec[4 + threadIdx.x]);
+            upd_info = rrec[28 + threadIdx.x];
         }
-        __syncthreads();
 
         // ---- per queued pixel: vote table -> 9-state transition map --------------------------
         const uint32_t chunk = (m + blockDim.x - 1) / blockDim.x;
@@ -1209,28 +1287,11 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
         __syncthreads();
 
         // ---- running stale values: last queued pixel of this row with the slot in bounds ------
-        if (threadIdx.x < 24)
+        if (upd_info != kJrowNoUpdate)
         {
-            const int k = threadIdx.x;
-            const int32_t dh = kOffH[k], dw = kOffW[k];
-            const int32_t hh = h + dh;
-            if (hh >= 0 && hh < H)
-            {
-                const int32_t q = lastq[dw > 0 ? dw : 0];
-                if (q >= 0 && static_cast<int32_t>(cols[q]) >= (dw < 0 ? -dw : 0))
-                {
-                    const float qw = b.jw[static_cast<size_t>(row_base + q) * kJwStride + k];
-                    uint8_t l = V_U;
-                    if (qw != 0.0F)
-                    {
-                        const uint8_t ns = st[hh * W + cols[q] + dw];
-                        const bool before = (dh < 0) || (dh == 0 && dw < 0);
-                        l = before ? final_view(ns) : pre_view(ns);
-                    }
-                    run_w[k] = qw;
-                    run_l[k] = l;
-                }
-            }
+            run_w[threadIdx.x] = upd_w;
+            run_l[threadIdx.x] = (upd_info & kJrowDynamic) ? final_view(st[upd_info & ~kJrowDynamic])
+                                                           : static_cast<uint8_t>(upd_info);
         }
         __syncthreads();
     }
