@@ -984,6 +984,7 @@ __global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
         nrm[26] = __uint_as_float(static_cast<uint32_t>(codes >> 32));
         nrm[27] = 0.0F;
     }
+    __syncthreads(); // the row record reads weight records other threads of the block wrote
     if (m == 0u || threadIdx.x >= 24u)
         return;
     // Row record (kJrowWords words): lastq[d] = the last of the row's final three queued pixels

@@ -222,6 +222,22 @@ def test_batch_equals_alone(ctx):
         compare_scan(b, alone)
 
 
+def test_batch_composition_independent(ctx):
+    """A scan's results do not depend on which scans share its batch or on what earlier batches
+    left in device memory (sizes 18k-201k points, several groupings, after a large unrelated
+    batch has been run through the same buffers)."""
+    data = [T.synth_scan(5, i) for i in range(10, 17)]
+    pipe = lp.PipelineConfig.default()
+    alone = [lp.process_batch(ctx, [d[0]], pipe, [d[2]], [d[1]])[0] for d in data]
+    junk = [T.synth_scan(3, i) for i in range(4)]
+    for grp in ([1, 2], [2, 3], [0, 1, 2], [1, 2, 3, 4], [0, 1, 2, 3, 4, 5, 6]):
+        lp.process_batch(ctx, [d[0] for d in junk], pipe, [d[2] for d in junk], [d[1] for d in junk])
+        res = lp.process_batch(ctx, [data[i][0] for i in grp], pipe, [data[i][2] for i in grp],
+                               [data[i][1] for i in grp])
+        for i, r in zip(grp, res):
+            compare_scan(r, alone[i], f"scan {10 + i} in group {grp}")
+
+
 def test_edge_cases(ctx):
     x, ring, cfg = T.synth_scan(1, 0)
     pipe = lp.PipelineConfig.default()
