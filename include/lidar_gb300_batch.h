@@ -38,6 +38,13 @@ lp_status lp_batch_time(lp_context* ctx, lp_batch* batch, uint32_t iters, int32_
  * to cap launches in launch order; *count receives the number of launches. */
 lp_status lp_batch_profile(lp_context* ctx, lp_batch* batch, char* names, uint32_t name_len, float* ms,
                            uint32_t cap, uint32_t* count);
+/* Page-locked host memory (cudaMallocHost) for scan inputs and result buffers: the library's
+ * copies to and from it run asynchronously at the host link's full rate, where pageable memory is
+ * staged through a bounce buffer. Not zeroed. No counterpart in the reference (its callers own
+ * plain std::vector buffers, which remain accepted everywhere). */
+lp_status lp_host_alloc(uint64_t bytes, void** out);
+void lp_host_free(void* p);
+
 /* Device evaluation of the library's correctly rounded binary32 functions (kind 0 atan2(a, b),
  * 1 atan(a), 2 exp(a), 3 the reference's atan2 approximation; 4, 5, 6 the same three functions
  * without their float-float first stage); used by the parity tests. */

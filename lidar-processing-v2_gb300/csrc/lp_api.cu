@@ -545,14 +545,20 @@ lp_status copy_d2h(lp_context* ctx, void* dst, const void* src, size_t bytes)
     return LP_OK;
 }
 
-// Per-scan results of a pipeline batch into the caller's lp_scan_output structs.
+// Per-scan results of a pipeline batch into the caller's lp_scan_output structs. Two phases with
+// one stream synchronisation each: first the labels and every scan's hull-offset range (cluster
+// counts are known from the fetched state), then, with the offsets on the host, the hull indices,
+// z ranges and boxes. Copies into page-locked caller buffers run asynchronously.
 lp_status download(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
 {
     const BatchDev& b = B.b;
     const bool hull = B.run.stages & ST_HULL;
-    std::vector<uint32_t> hoff;
-    lp_status worst = LP_OK;
-    for (size_t s = 0; s < B.run.scans.size(); ++s)
+    const size_t S = B.run.scans.size();
+    std::vector<size_t> hbase(S + 1, 0);
+    for (size_t s = 0; s < S; ++s)
+        hbase[s + 1] = hbase[s] + (hull ? static_cast<size_t>(B.h_state[s].n_clusters) + 1 : 0);
+    std::vector<uint32_t> hoff(hbase[S]);
+    for (size_t s = 0; s < S; ++s)
     {
         const ScanDev& sd = B.hb.scans[s];
         const ScanState& st = B.h_state[s];
@@ -564,9 +570,17 @@ lp_status download(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
         o.n_obstacles = st.n_obs;
         o.n_clusters = st.n_clusters;
         o.status = LP_OK;
-        if (!hull)
-            continue;
-        const uint32_t k = st.n_clusters;
+        if (hull && st.n_clusters <= o.cluster_capacity)
+            LP_TRY(copy_d2h(ctx, hoff.data() + hbase[s], b.hull_cnt + sd.cl_off, (hbase[s + 1] - hbase[s]) * 4));
+    }
+    if (hull)
+        LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    lp_status worst = LP_OK;
+    for (size_t s = 0; hull && s < S; ++s)
+    {
+        const ScanDev& sd = B.hb.scans[s];
+        const uint32_t k = B.h_state[s].n_clusters;
+        lp_scan_output& o = outs[s];
         if (k > o.cluster_capacity)
         {
             o.status = LP_ERR_CAPACITY;
@@ -574,11 +588,9 @@ lp_status download(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
                 worst = fail(ctx, LP_ERR_CAPACITY, "scan " + std::to_string(s) + ": cluster_capacity too small");
             continue;
         }
-        hoff.resize(k + 1);
-        LP_CUDA(ctx, cudaMemcpyAsync(hoff.data(), b.hull_cnt + sd.cl_off, (k + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        const uint32_t base = hoff[0];
-        const uint32_t nh = hoff[k] - base;
+        const uint32_t* ho = hoff.data() + hbase[s];
+        const uint32_t base = ho[0];
+        const uint32_t nh = ho[k] - base;
         if (nh > o.hull_capacity)
         {
             o.status = LP_ERR_CAPACITY;
@@ -588,7 +600,7 @@ lp_status download(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
         }
         if (o.hull_offsets)
             for (uint32_t i = 0; i <= k; ++i)
-                o.hull_offsets[i] = hoff[i] - base;
+                o.hull_offsets[i] = ho[i] - base;
         o.n_hull_indices = nh;
         LP_TRY(copy_d2h(ctx, o.hull_indices, b.hull_out + base, static_cast<size_t>(nh) * 4));
         LP_TRY(copy_d2h(ctx, o.z_min, b.cl_zmin + sd.cl_off, static_cast<size_t>(k) * 4));
@@ -1222,6 +1234,28 @@ lp_status lp_debug_math(lp_context* ctx, int32_t kind, const float* a, const flo
     LP_CUDA(ctx, cudaMemcpyAsync(out, dout, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost, ctx->stream));
     LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return LP_OK;
+}
+
+lp_status lp_host_alloc(uint64_t bytes, void** out)
+{
+    if (!out)
+        return LP_ERR_BAD_ARG;
+    *out = nullptr;
+    if (bytes == 0)
+        return LP_OK;
+    if (cudaMallocHost(out, static_cast<size_t>(bytes)) != cudaSuccess)
+    {
+        cudaGetLastError();
+        *out = nullptr;
+        return LP_ERR_CUDA;
+    }
+    return LP_OK;
+}
+
+void lp_host_free(void* p)
+{
+    if (p)
+        cudaFreeHost(p);
 }
 
 lp_status lp_debug_math_sweep(lp_context* ctx, int32_t kind, uint64_t first, uint64_t count, uint64_t stats[3],

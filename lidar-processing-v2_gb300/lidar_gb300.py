@@ -191,21 +191,61 @@ class ScanResult:
         return self.hull_indices[self.hull_offsets[k]:self.hull_offsets[k + 1]]
 
 
-class ResultBuffers:
-    """Host result buffers for one scan, in the layout lp_scan_output points at."""
+class _PinnedBlock:
+    """One lp_host_alloc allocation, freed when the last array viewing it is gone."""
 
-    def __init__(self, n, cluster_capacity=None, hull_capacity=None):
+    def __init__(self, nbytes):
+        p = ctypes.c_void_p()
+        check(library().lp_host_alloc(max(1, int(nbytes)), ctypes.byref(p)))
+        self.ptr = p.value
+        self.nbytes = int(nbytes)
+
+    def __del__(self):
+        try:
+            library().lp_host_free(ctypes.c_void_p(self.ptr))
+        except Exception:
+            pass
+
+
+def pinned_empty(shape, dtype):
+    """numpy array in page-locked host memory (lp_host_alloc); contents undefined."""
+    dt = np.dtype(dtype)
+    count = int(np.prod(shape)) if np.ndim(shape) else int(shape)
+    blk = _PinnedBlock(count * dt.itemsize)
+    buf = (ctypes.c_char * max(1, blk.nbytes)).from_address(blk.ptr)
+    buf._owner = blk  # the array's base is `buf`, which keeps the allocation alive
+    return np.frombuffer(buf, dtype=dt, count=count).reshape(shape)
+
+
+def pinned_copy(a):
+    """Page-locked copy of a numpy array."""
+    out = pinned_empty(a.shape, a.dtype)
+    out[...] = a
+    return out
+
+
+class ResultBuffers:
+    """Host result buffers for one scan, in the layout lp_scan_output points at. With pinned=True
+    they live in page-locked memory (lp_host_alloc) and can be reused call after call."""
+
+    def __init__(self, n, cluster_capacity=None, hull_capacity=None, pinned=False):
         cc = cluster_capacity if cluster_capacity is not None else max(64, n // 3 + 1)
         hc = hull_capacity if hull_capacity is not None else max(256, n + cc)
-        self.noise = np.zeros(n, np.uint8)
-        self.seg = np.zeros(n, np.uint32)
-        self.cl = np.zeros(n, np.int32)
-        self.hoff = np.zeros(cc + 1, np.uint32)
-        self.hidx = np.zeros(hc, np.int32)
-        self.zmin = np.zeros(cc, np.float32)
-        self.zmax = np.zeros(cc, np.float32)
-        self.obb_c = (BoundingBox * cc)()
-        self.obb_p = (BoundingBox * cc)()
+        alloc = pinned_empty if pinned else (lambda shape, dt: np.zeros(shape, dt))
+        self.noise = alloc(n, np.uint8)
+        self.seg = alloc(n, np.uint32)
+        self.cl = alloc(n, np.int32)
+        self.hoff = alloc(cc + 1, np.uint32)
+        self.hidx = alloc(hc, np.int32)
+        self.zmin = alloc(cc, np.float32)
+        self.zmax = alloc(cc, np.float32)
+        if pinned:
+            self._obb = alloc(2 * cc * ctypes.sizeof(BoundingBox), np.uint8)
+            self.obb_c = (BoundingBox * cc).from_address(self._obb.ctypes.data)
+            self.obb_p = (BoundingBox * cc).from_address(self._obb.ctypes.data + cc * ctypes.sizeof(BoundingBox))
+        else:
+            self.obb_c = (BoundingBox * cc)()
+            self.obb_p = (BoundingBox * cc)()
         self.out = ScanOutput(ptr(self.noise), ptr(self.seg), ptr(self.cl), cc, hc, ptr(self.hoff),
                               ptr(self.hidx), ptr(self.zmin), ptr(self.zmax),
                               ctypes.cast(self.obb_c, ctypes.c_void_p), ctypes.cast(self.obb_p, ctypes.c_void_p),
@@ -250,6 +290,8 @@ def _declare(lib):
         "lp_batch_time": (c.c_int32, [P, P, c.c_uint32, c.c_int32, c.POINTER(c.c_float)]),
         "lp_batch_profile": (c.c_int32, [P, P, P, c.c_uint32, P, c.c_uint32, c.POINTER(c.c_uint32)]),
         "lp_debug_math": (c.c_int32, [P, c.c_int32, P, P, c.c_uint32, P]),
+        "lp_host_alloc": (c.c_int32, [c.c_uint64, c.POINTER(P)]),
+        "lp_host_free": (None, [P]),
         "lp_debug_math_sweep": (c.c_int32, [P, c.c_int32, c.c_uint64, c.c_uint64, P, P]),
         "lp_server_config_default": (None, [P]),
         "lp_server_create": (c.c_int32, [c.c_int32, P, P, c.POINTER(P)]),
@@ -584,11 +626,13 @@ class Server:
             pass
 
 
-def process_batch(ctx, scans, pipeline=None, seg_configs=None, rings=None):
+def process_batch(ctx, scans, pipeline=None, seg_configs=None, rings=None, outputs=None, raw=False):
     """Run the whole per-scan path on a batch of scans in one launch sequence.
 
     scans: list of N_i x 4 float32 arrays; seg_configs: list of SegmenterConfig (default each);
-    rings: list of uint16 arrays or None. Returns a list of ScanResult.
+    rings: list of uint16 arrays or None. Returns a list of ScanResult. outputs: ResultBuffers to
+    fill (reused across calls, e.g. pinned ones) instead of fresh buffers; raw=True returns those
+    buffers (arrays filled in place, counts in .out) without building ScanResult objects.
     """
     pipeline = pipeline or PipelineConfig.default()
     n = len(scans)
@@ -597,13 +641,16 @@ def process_batch(ctx, scans, pipeline=None, seg_configs=None, rings=None):
           for i in range(n)]
     cfgs = seg_configs or [SegmenterConfig.default() for _ in range(n)]
     ins = (ScanInput * n)()
-    bufs = []
+    bufs = list(outputs) if outputs is not None else []
     for i in range(n):
         ins[i] = ScanInput(arrs[i].ctypes.data, None if rr[i] is None else rr[i].ctypes.data, len(arrs[i]), cfgs[i])
-        bufs.append(ResultBuffers(len(arrs[i])))
+        if outputs is None:
+            bufs.append(ResultBuffers(len(arrs[i])))
+        elif len(bufs[i].seg) < len(arrs[i]):
+            raise ValueError("output buffers smaller than the scan")
     outs = (ScanOutput * n)(*[b.out for b in bufs])
     st = library().lp_process_batch(ctx.handle, ctypes.byref(pipeline), ins, outs, n)
     for i in range(n):
         bufs[i].out = outs[i]
     check(st, ctx)
-    return [b.result() for b in bufs]
+    return bufs if raw else [b.result() for b in bufs]

@@ -222,6 +222,20 @@ def test_batch_equals_alone(ctx):
         compare_scan(b, alone)
 
 
+def test_pinned_reused_outputs(ctx):
+    """Page-locked inputs and result buffers reused across calls give the fresh-buffer results."""
+    data = scans([(3, 4), (3, 5)])
+    pipe = lp.PipelineConfig.default()
+    want = lp.process_batch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
+    px = [lp.pinned_copy(d[0]) for d in data]
+    pr = [lp.pinned_copy(d[1]) for d in data]
+    bufs = [lp.ResultBuffers(len(d[0]), pinned=True) for d in data]
+    for _ in range(2):  # the second call overwrites the first call's results in place
+        lp.process_batch(ctx, px, pipe, [d[2] for d in data], pr, outputs=bufs, raw=True)
+        for b, w in zip(bufs, want):
+            compare_scan(b.result(), w)
+
+
 def test_batch_composition_independent(ctx):
     """A scan's results do not depend on which scans share its batch or on what earlier batches
     left in device memory (sizes 18k-201k points, several groupings, after a large unrelated
