@@ -324,6 +324,19 @@ def run_dror(args):
     ctx.close()
 
 
+def traffic_bytes(kernel, alg_bytes):
+    """DRAM bytes per launch of `kernel`: the measured ratio of DRAM traffic (dram__bytes_read.sum +
+    dram__bytes_write.sum from one ncu capture, summarised under profiles/) to the launch's
+    algorithmic bytes, times this launch's algorithmic bytes; None without a capture."""
+    import glob
+    for path in glob.glob(os.path.join(REPO, "profiles", "*.md")):
+        for line in open(path):
+            f = line.split()
+            if len(f) == 3 and f[0] == "traffic_ratio" and f[1] == kernel:
+                return int(float(f[2]) * alg_bytes)
+    return None
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--serve", action="store_true", help="multi-sensor serving workload instead of the batch bench")
@@ -462,8 +475,8 @@ def main():
             "e2e": e2e,
             "gpu_launches": int(kernels_per_step * args.steps),
             "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
-                         "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": top_ms},
+                         "frac": achieved / peak, "traffic": traffic_bytes(top_name, alg_bytes),
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": top_ms},
             "kernel_share": {k: round(v[1] / total_ms, 4) for k, v in sorted(agg2.items(), key=lambda kv: -kv[1][1])[:10]},
             "clocks": clocks.summary(),
             "cpu_baseline": cb,
