@@ -43,6 +43,7 @@ constexpr uint32_t kJwStride = 28;
 // (kJrowNoUpdate: the row leaves the slot as it was; kJrowDynamic | pixel: the final colour of
 // that pixel; else the label), padded to 64 words.
 constexpr uint32_t kJrowWords = 64;
+constexpr uint32_t kFinRingW = 4096; // image width up to which the vote keeps final colours in shared memory
 constexpr uint32_t kJrowNoUpdate = 0xffffffffu;
 constexpr uint32_t kJrowDynamic = 0x80000000u;
 

@@ -908,6 +908,76 @@ __device__ __forceinline__ uint8_t pre_view(uint8_t st)
     return (st == PX_GROUND) ? V_G : ((st == PX_OBSTACLE) ? V_O : V_U);
 }
 
+// A queued pixel's vote (segmenter.cpp:585-631) as a 9-state transition map of the in-row chain:
+// for every outcome pair (a, b) of the queued pixels at columns c-1 and c-2 (symbolic where
+// sym_a / sym_b), the label sums g and o are accumulated in slot order exactly like the reference
+// (skipping a slot adds nothing), outcome obstacle iff o > g; then the map (state = 3 x + a) is
+// built for the column gap to the previous queued pixel.
+__device__ __forceinline__ unsigned long long vote_map(const float* wn, const uint8_t* lb, bool sym_a, bool sym_b,
+                                                       bool live, int32_t gap)
+{
+    uint32_t outc = 0u; // outcome of vote table entry (a, b) in bits 2 (3a + b); V_U when not live
+    if (live)
+    {
+        // (g, o) as one packed pair: a slot adds (w, 0), (0, w) or (0, 0); weights and sums are
+        // never negative, so adding +0 is exactly the reference's skip, and each half rounds like
+        // its scalar addition in the same slot order
+        auto gw = [&](uint8_t l, float w) {
+            return make_float2(l == V_G ? w : 0.0F, l == V_O ? w : 0.0F);
+        };
+        float2 head = make_float2(0.0F, 0.0F);
+#pragma unroll
+        for (int k = 0; k < 10; ++k)
+            head = __fadd2_rn(head, gw(lb[k], wn[k]));
+        float2 tail[12];
+#pragma unroll
+        for (int k = 12; k < 24; ++k)
+            tail[k - 12] = gw(lb[k], wn[k]);
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int bb = 0; bb < 3; ++bb)
+            {
+                const uint8_t l10 = sym_b ? static_cast<uint8_t>(bb) : lb[10];
+                const uint8_t l11 = sym_a ? static_cast<uint8_t>(a) : lb[11];
+                float2 v = __fadd2_rn(head, gw(l10, wn[10]));
+                v = __fadd2_rn(v, gw(l11, wn[11]));
+#pragma unroll
+                for (int k = 0; k < 12; ++k)
+                    v = __fadd2_rn(v, tail[k]);
+                outc |= static_cast<uint32_t>((v.y > v.x) ? V_O : V_G) << (2 * (3 * a + bb));
+            }
+    }
+    unsigned long long t = 0ull;
+#pragma unroll
+    for (int sidx = 0; sidx < 9; ++sidx)
+    {
+        const int a = sidx / 3, bb = sidx % 3;
+        int ap, bp, an;
+        if (gap == 1)
+        {
+            ap = a;
+            bp = bb;
+            an = a;
+        }
+        else if (gap == 2)
+        {
+            ap = V_U;
+            bp = a;
+            an = V_U;
+        }
+        else
+        {
+            ap = V_U;
+            bp = V_U;
+            an = V_U;
+        }
+        const int x = static_cast<int>((outc >> (2 * (3 * ap + bp))) & 3u); // V_U when sum ~ 0
+        t |= static_cast<unsigned long long>(3 * x + an) << (4 * sidx);
+    }
+    return t;
+}
+
 // Fresh (not stale) weight of every in-bounds neighbour slot of every queued pixel: 0 for an
 // empty neighbour or one farther than the kernel threshold, else expf(-amp * dist)
 // (segmenter.cpp:545-607). These depend on geometry only, so they are computed in parallel
@@ -971,18 +1041,21 @@ __global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
                         code = (ns == PX_INTERSECT) ? 3u : final_view(ns);
                 }
             }
-            out[k] = wt[k];
             codes |= static_cast<unsigned long long>(code) << (2 * k);
         }
-        out[24] = sum;
         const bool live = fabsf(sum) > FLT_EPSILON;
+        float4* out4 = reinterpret_cast<float4*>(out);
+        float4* nrm4 = reinterpret_cast<float4*>(nrm);
 #pragma unroll
-        for (int k = 0; k < 24; ++k)
-            nrm[k] = live ? wt[k] / sum : 0.0F;
-        nrm[24] = sum;
-        nrm[25] = __uint_as_float(static_cast<uint32_t>(codes));
-        nrm[26] = __uint_as_float(static_cast<uint32_t>(codes >> 32));
-        nrm[27] = 0.0F;
+        for (int q = 0; q < 6; ++q)
+        {
+            out4[q] = make_float4(wt[4 * q], wt[4 * q + 1], wt[4 * q + 2], wt[4 * q + 3]);
+            nrm4[q] = live ? make_float4(wt[4 * q] / sum, wt[4 * q + 1] / sum, wt[4 * q + 2] / sum, wt[4 * q + 3] / sum)
+                           : make_float4(0.0F, 0.0F, 0.0F, 0.0F);
+        }
+        out4[6] = make_float4(sum, 0.0F, 0.0F, 0.0F);
+        nrm4[6] = make_float4(sum, __uint_as_float(static_cast<uint32_t>(codes)),
+                              __uint_as_float(static_cast<uint32_t>(codes >> 32)), 0.0F);
     }
     __syncthreads(); // the row record reads weight records other threads of the block wrote
     if (m == 0u || threadIdx.x >= 24u)
@@ -1075,9 +1148,14 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
     __shared__ float run_w[24];
     __shared__ uint8_t run_l[24];
     __shared__ unsigned long long wmaps[8];
+    // final colour (V_U/V_G/V_O) of the queued pixels of the last three rows, by column: the
+    // labels a pixel reads from queued pixels above it, without a global load (images up to
+    // kFinRingW columns; wider ones read the pixel states)
+    __shared__ uint8_t fin[3][kFinRingW];
     const int s = blockIdx.x;
     const ScanDev& sd = b.scans[s];
     const int32_t H = sd.H, W = sd.W;
+    const bool ring = W <= static_cast<int32_t>(kFinRingW);
     uint8_t* st = b.pix_state + sd.pix_off;
     const int32_t* map = b.pix_map + sd.pix_off;
     if (threadIdx.x < 24)
@@ -1133,14 +1211,18 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
             const unsigned long long codes =
                 static_cast<unsigned long long>(__float_as_uint(tail.y)) |
                 (static_cast<unsigned long long>(__float_as_uint(tail.z)) << 32);
-            uint8_t nsv[10];
-#pragma unroll
-            for (int k = 0; k < 10; ++k) // code 3 above: a queued pixel, inside the image
-                nsv[k] = (((codes >> (2 * k)) & 3ull) == 3ull) ? st[(h + jcp_dh(k)) * W + c + jcp_dw(k)]
-                                                                : static_cast<uint8_t>(PX_EMPTY);
-            uint32_t outc = 0u; // outcome of vote table entry (a, b) in bits 2 (3a + b)
-            if (fabsf(sum) > FLT_EPSILON)
+            unsigned long long t;
             {
+                uint8_t nsv[10]; // final colour of the queued pixels above (code 3: inside the image)
+#pragma unroll
+                for (int k = 0; k < 10; ++k)
+                {
+                    const int32_t hh = h + jcp_dh(k), ww = c + jcp_dw(k);
+                    nsv[k] = V_U;
+                    if (((codes >> (2 * k)) & 3ull) == 3ull)
+                        nsv[k] = ring ? fin[hh % 3][ww] : final_view(st[hh * W + ww]);
+                }
+                const bool live = fabsf(sum) > FLT_EPSILON;
                 uint8_t lb[24];
                 bool sym_a = false, sym_b = false;
 #pragma unroll
@@ -1151,34 +1233,36 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                     if (hh < 0 || hh >= H || ww < 0 || ww >= W)
                     {
                         // stale slot: the raw weight an earlier pixel left there, over this sum
-                        float wv;
-                        const int32_t qd = dw > 0 ? dw : 0;
-                        const int32_t q = (dw > 0 && hh >= 0 && hh < H) ? lastq[qd] : -1;
-                        if (q >= 0)
+                        float wv = 0.0F;
+                        lb[k] = V_U;
+                        if (live)
                         {
-                            const float qw = b.jw[static_cast<size_t>(row_base + q) * kJwStride + k];
-                            wv = qw;
-                            if (qw == 0.0F)
-                                lb[k] = V_U;
+                            const int32_t qd = dw > 0 ? dw : 0;
+                            const int32_t q = (dw > 0 && hh >= 0 && hh < H) ? lastq[qd] : -1;
+                            if (q >= 0)
+                            {
+                                const float qw = b.jw[static_cast<size_t>(row_base + q) * kJwStride + k];
+                                wv = qw;
+                                if (qw != 0.0F)
+                                {
+                                    const uint8_t ns = st[hh * W + cols[q] + dw];
+                                    lb[k] = (dh < 0) ? final_view(ns) : pre_view(ns);
+                                }
+                            }
                             else
                             {
-                                const uint8_t ns = st[hh * W + cols[q] + dw];
-                                lb[k] = (dh < 0) ? final_view(ns) : pre_view(ns);
+                                wv = run_w[k];
+                                lb[k] = run_l[k];
                             }
+                            wn[k] = wv / sum;
                         }
-                        else
-                        {
-                            wv = run_w[k];
-                            lb[k] = run_l[k];
-                        }
-                        wn[k] = wv / sum;
                         continue;
                     }
                     const uint32_t code = static_cast<uint32_t>((codes >> (2 * k)) & 3ull);
                     if (code != 3u)
                         lb[k] = static_cast<uint8_t>(code);
                     else if (dh < 0)
-                        lb[k] = final_view(nsv[k < 10 ? k : 0]);
+                        lb[k] = nsv[k < 10 ? k : 0];
                     else
                     {
                         // same row, left of c, queued: symbolic (the chain's outcome)
@@ -1189,71 +1273,10 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                             sym_b = true;
                     }
                 }
-                float g9 = 0.0F, o9 = 0.0F;
-#pragma unroll
-                for (int k = 0; k < 10; ++k)
-                {
-                    if (lb[k] == V_G)
-                        g9 += wn[k];
-                    else if (lb[k] == V_O)
-                        o9 += wn[k];
-                }
-#pragma unroll
-                for (int a = 0; a < 3; ++a)
-#pragma unroll
-                    for (int bb = 0; bb < 3; ++bb)
-                    {
-                        float g = g9, o = o9;
-                        const uint8_t l10 = sym_b ? static_cast<uint8_t>(bb) : lb[10];
-                        const uint8_t l11 = sym_a ? static_cast<uint8_t>(a) : lb[11];
-                        if (l10 == V_G)
-                            g += wn[10];
-                        else if (l10 == V_O)
-                            o += wn[10];
-                        if (l11 == V_G)
-                            g += wn[11];
-                        else if (l11 == V_O)
-                            o += wn[11];
-#pragma unroll
-                        for (int k = 12; k < 24; ++k)
-                        {
-                            if (lb[k] == V_G)
-                                g += wn[k];
-                            else if (lb[k] == V_O)
-                                o += wn[k];
-                        }
-                        outc |= static_cast<uint32_t>((o > g) ? V_O : V_G) << (2 * (3 * a + bb));
-                    }
+                const int32_t gap = (j > 0) ? (c - static_cast<int32_t>(cols[j - 1])) : 1000;
+                t = vote_map(wn, lb, sym_a, sym_b, live, gap);
+                b.jmap[row_base + j] = t;
             }
-            const int32_t gap = (j > 0) ? (c - static_cast<int32_t>(cols[j - 1])) : 1000;
-            unsigned long long t = 0ull;
-#pragma unroll
-            for (int sidx = 0; sidx < 9; ++sidx)
-            {
-                const int a = sidx / 3, bb = sidx % 3;
-                int ap, bp, an;
-                if (gap == 1)
-                {
-                    ap = a;
-                    bp = bb;
-                    an = a;
-                }
-                else if (gap == 2)
-                {
-                    ap = V_U;
-                    bp = a;
-                    an = V_U;
-                }
-                else
-                {
-                    ap = V_U;
-                    bp = V_U;
-                    an = V_U;
-                }
-                const int x = static_cast<int>((outc >> (2 * (3 * ap + bp))) & 3u); // V_U when sum ~ 0
-                t |= static_cast<unsigned long long>(3 * x + an) << (4 * sidx);
-            }
-            b.jmap[row_base + j] = t;
             agg = map_compose(t, agg);
         }
 
@@ -1284,6 +1307,8 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
             const uint32_t x = state / 3;
             if (x != V_U)
                 st[h * W + cols[j]] = (x == V_O) ? PX_RES_O : PX_RES_G;
+            if (ring)
+                fin[h % 3][cols[j]] = static_cast<uint8_t>(x); // final_view of the new state
         }
         __syncthreads();
 
@@ -1291,8 +1316,14 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
         if (upd_info != kJrowNoUpdate)
         {
             run_w[threadIdx.x] = upd_w;
-            run_l[threadIdx.x] = (upd_info & kJrowDynamic) ? final_view(st[upd_info & ~kJrowDynamic])
-                                                           : static_cast<uint8_t>(upd_info);
+            uint8_t l = static_cast<uint8_t>(upd_info);
+            if (upd_info & kJrowDynamic)
+            {
+                const uint32_t addr = upd_info & ~kJrowDynamic; // a queued pixel of rows h-2..h
+                l = ring ? fin[(addr / static_cast<uint32_t>(W)) % 3u][addr % static_cast<uint32_t>(W)]
+                         : final_view(st[addr]);
+            }
+            run_l[threadIdx.x] = l;
         }
         __syncthreads();
     }
