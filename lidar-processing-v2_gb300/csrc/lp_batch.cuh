@@ -44,6 +44,13 @@ constexpr uint32_t kJwStride = 28;
 // that pixel; else the label), padded to 64 words.
 constexpr uint32_t kJrowWords = 64;
 constexpr uint32_t kFinRingW = 4096; // image width up to which the vote keeps final colours in shared memory
+// Staging of the vote's next row: queued pixels per row and image rows it covers, bytes per buffer
+// (normalised records, the queue entries with 16-byte slack on both sides, the row record).
+constexpr uint32_t kStageRec = 256;
+constexpr uint32_t kRowCache = 1024;
+constexpr uint32_t kStageRecBytes = kStageRec * kJwStride * 4u;
+constexpr uint32_t kStageColBytes = (kStageRec * 2u + 32u + 15u) & ~15u;
+constexpr uint32_t kStageBytes = kStageRecBytes + kStageColBytes + kJrowWords * 4u; // + the row record
 constexpr uint32_t kJrowNoUpdate = 0xffffffffu;
 constexpr uint32_t kJrowDynamic = 0x80000000u;
 

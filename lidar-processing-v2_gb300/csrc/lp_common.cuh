@@ -24,6 +24,51 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v)
     return v;
 }
 
+// ---- TMA bulk copies (global -> shared) completing on an mbarrier ------------------------------
+// cp.async.bulk moves a contiguous range (16-byte aligned, size a multiple of 16) through the
+// tensor memory accelerator; the issuing thread announces the byte count on the mbarrier, and
+// the barrier's phase flips when that many bytes have landed.
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+// Waits until the barrier has completed the phase with the given parity; gives up after
+// `limit` polls and returns false (the caller reports it and stops using the buffer).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity, uint32_t limit)
+{
+    for (uint32_t i = 0; i < limit; ++i)
+    {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done)
+            return true;
+    }
+    return false;
+}
+
 // Warp-aggregated counter increment: every valid lane adds 1 to counters[key] and receives the
 // counter's old value plus its rank among the valid lanes with the same key, as if the lanes'
 // atomicAdds had run in lane order. One atomic per distinct key of the warp (consecutive points

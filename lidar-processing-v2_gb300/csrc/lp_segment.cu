@@ -1152,10 +1152,62 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
     // labels a pixel reads from queued pixels above it, without a global load (images up to
     // kFinRingW columns; wider ones read the pixel states)
     __shared__ uint8_t fin[3][kFinRingW];
+    // Double-buffered staging: while a row votes, one thread copies the next non-empty row's
+    // normalised records and queue entries into shared memory with a TMA bulk copy (rows of at
+    // most kStageRec queued pixels, images of at most kRowCache rows; others load directly).
+    extern __shared__ __align__(16) unsigned char stage[];
+    __shared__ uint32_t mrow[kRowCache];
+    __shared__ unsigned long long mbar[2];
+    __shared__ int32_t st_row[2], st_coff[2];
     const int s = blockIdx.x;
     const ScanDev& sd = b.scans[s];
     const int32_t H = sd.H, W = sd.W;
     const bool ring = W <= static_cast<int32_t>(kFinRingW);
+    const bool cache = H <= static_cast<int32_t>(kRowCache);
+    if (cache)
+        for (int32_t i = threadIdx.x; i < H; i += blockDim.x)
+            mrow[i] = b.row_cnt[sd.row_off + static_cast<uint32_t>(i)];
+    if (threadIdx.x == 0)
+    {
+        mbar_init(&mbar[0], 1u);
+        mbar_init(&mbar[1], 1u);
+        st_row[0] = st_row[1] = -1;
+    }
+    __syncthreads();
+    // thread 0: copy row hh into buffer bf (queue entries widened to 16-byte bounds)
+    auto issue = [&](int32_t hh, int bf) {
+        const uint32_t mm = mrow[hh];
+        const uint32_t rb = sd.pix_off + static_cast<uint32_t>(hh * W);
+        const uint32_t rec_bytes = mm * kJwStride * 4u;
+        const uintptr_t c0 = reinterpret_cast<uintptr_t>(b.row_cols + rb);
+        const uintptr_t ca = c0 & ~static_cast<uintptr_t>(15);
+        const uintptr_t ce = (reinterpret_cast<uintptr_t>(b.row_cols + rb + mm) + 15) & ~static_cast<uintptr_t>(15);
+        unsigned char* dst = stage + bf * kStageBytes;
+        mbar_expect_tx(&mbar[bf], rec_bytes + static_cast<uint32_t>(ce - ca) + kJrowWords * 4u);
+        bulk_g2s(dst, b.jn + static_cast<size_t>(rb) * kJwStride, rec_bytes, &mbar[bf]);
+        bulk_g2s(dst + kStageRecBytes, reinterpret_cast<const void*>(ca), static_cast<uint32_t>(ce - ca), &mbar[bf]);
+        bulk_g2s(dst + kStageRecBytes + kStageColBytes,
+                 b.jrow + static_cast<size_t>(sd.row_off + static_cast<uint32_t>(hh)) * kJrowWords, kJrowWords * 4u,
+                 &mbar[bf]);
+        st_row[bf] = hh;
+        st_coff[bf] = static_cast<int32_t>((c0 - ca) / 2);
+    };
+    auto stageable = [&](int32_t hh) { return cache && mrow[hh] > 0 && mrow[hh] <= kStageRec; };
+    auto next_row = [&](int32_t hh) {
+        for (int32_t q = hh + 1; q < H; ++q)
+            if (mrow[q] > 0)
+                return q;
+        return -1;
+    };
+    uint32_t parity[2] = {0u, 0u};
+    int cur = 0;
+    if (threadIdx.x == 0 && cache)
+    {
+        const int32_t h0 = next_row(-1);
+        if (h0 >= 0 && stageable(h0))
+            issue(h0, 0);
+    }
+    __syncthreads();
     uint8_t* st = b.pix_state + sd.pix_off;
     const int32_t* map = b.pix_map + sd.pix_off;
     if (threadIdx.x < 24)
@@ -1168,13 +1220,39 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
     for (int32_t h = 0; h < H; ++h)
     {
         const uint32_t r = sd.row_off + static_cast<uint32_t>(h);
-        const uint32_t m = b.row_cnt[r];
+        const uint32_t m = cache ? mrow[h] : b.row_cnt[r];
         if (m == 0)
             continue;
         const uint32_t row_base = sd.pix_off + static_cast<uint32_t>(h * W);
         const uint16_t* cols = b.row_cols + row_base;
+        const bool staged = st_row[cur] == h;
+        const float4* srec = reinterpret_cast<const float4*>(stage + cur * kStageBytes);
+        const uint16_t* scols = reinterpret_cast<const uint16_t*>(stage + cur * kStageBytes + kStageRecBytes) + st_coff[cur];
+        __syncthreads(); // every thread has read st_row / st_coff before thread 0 reissues
+        if (threadIdx.x == 0 && cache)
+        {
+            const int32_t hn = next_row(h);
+            st_row[cur ^ 1] = -1;
+            if (hn >= 0 && stageable(hn))
+                issue(hn, cur ^ 1);
+        }
+        if (staged)
+        {
+            // every thread waits (bounded); the block decides together whether the copy landed
+            const bool landed = mbar_wait(&mbar[cur], parity[cur], 1u << 22);
+            if (!__syncthreads_and(landed))
+            {
+                // report, give the copy a last bounded chance to drain, stop
+                if (threadIdx.x == 0)
+                    raise_err(&b.state[s], ERR_INTERNAL);
+                mbar_wait(&mbar[cur], parity[cur], 1u << 24);
+                return;
+            }
+            parity[cur] ^= 1u;
+        }
         // the row's record (from the parallel pass): lastq and the stale-buffer update
-        const uint32_t* rrec = b.jrow + static_cast<size_t>(r) * kJrowWords;
+        const uint32_t* rrec = staged ? reinterpret_cast<const uint32_t*>(stage + cur * kStageBytes + kStageRecBytes + kStageColBytes)
+                                      : b.jrow + static_cast<size_t>(r) * kJrowWords;
         const int32_t lastq[3] = {static_cast<int32_t>(rrec[0]), static_cast<int32_t>(rrec[1]),
                                   static_cast<int32_t>(rrec[2])};
         float upd_w = 0.0F;
@@ -1192,21 +1270,21 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
         unsigned long long agg = map_identity();
         for (uint32_t j = j0; j < j1; ++j)
         {
-            const int32_t c = cols[j];
-            // every load of the pixel is issued up front: its normalized record and the states
-            // of the queued pixels above it
-            const float* rec = b.jn + static_cast<size_t>(row_base + j) * kJwStride;
+            // the pixel's queue entry and normalised record: staged in shared memory, or loaded
+            const int32_t c = staged ? scols[j] : cols[j];
+            const float4* rec = staged ? srec + 7u * j
+                                       : reinterpret_cast<const float4*>(b.jn + static_cast<size_t>(row_base + j) * kJwStride);
             float wn[24];
 #pragma unroll
             for (int q = 0; q < 6; ++q)
             {
-                const float4 v = reinterpret_cast<const float4*>(rec)[q];
+                const float4 v = rec[q];
                 wn[4 * q] = v.x;
                 wn[4 * q + 1] = v.y;
                 wn[4 * q + 2] = v.z;
                 wn[4 * q + 3] = v.w;
             }
-            const float4 tail = reinterpret_cast<const float4*>(rec)[6];
+            const float4 tail = rec[6];
             const float sum = tail.x;
             const unsigned long long codes =
                 static_cast<unsigned long long>(__float_as_uint(tail.y)) |
@@ -1273,7 +1351,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                             sym_b = true;
                     }
                 }
-                const int32_t gap = (j > 0) ? (c - static_cast<int32_t>(cols[j - 1])) : 1000;
+                const int32_t gap = (j > 0) ? (c - static_cast<int32_t>(staged ? scols[j - 1] : cols[j - 1])) : 1000;
                 t = vote_map(wn, lb, sym_a, sym_b, live, gap);
                 b.jmap[row_base + j] = t;
             }
@@ -1326,6 +1404,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
             run_l[threadIdx.x] = l;
         }
         __syncthreads();
+        cur ^= 1;
     }
     (void)map;
 }
@@ -1430,7 +1509,9 @@ void init_segment_tables()
     uint32_t table[kMtTable];
     for (int k = 0; k < kMtTable; ++k)
         table[k] = static_cast<uint32_t>(gen());
-    if (cudaMemcpyToSymbol(g_mt42, table, sizeof(table)) == cudaSuccess && dev >= 0 && dev < 64)
+    const bool attr = cudaFuncSetAttribute(k_jcp_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(2u * kStageBytes)) == cudaSuccess;
+    if (cudaMemcpyToSymbol(g_mt42, table, sizeof(table)) == cudaSuccess && attr && dev >= 0 && dev < 64)
         done[dev] = true;
 }
 
@@ -1541,7 +1622,7 @@ void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, ui
     LP_LAUNCH(L, k_pixel, div_up(b.npix, T), T, b);
     LP_LAUNCH(L, k_dilate_rows, b.nrows, 256, b);
     LP_LAUNCH(L, k_jcp_weights, b.nrows, 256, b);
-    LP_LAUNCH(L, k_jcp_rows, static_cast<uint32_t>(b.nscan), 256, b);
+    LP_LAUNCH_SMEM(L, k_jcp_rows, static_cast<uint32_t>(b.nscan), 256, 2u * kStageBytes, b);
     LP_LAUNCH(L, k_populate, div_up(b.npix, T), T, b, d_image);
 }
 } // namespace lpg
