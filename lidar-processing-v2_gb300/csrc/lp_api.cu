@@ -219,7 +219,6 @@ size_t carve(lp_batch& B, char* base)
     put(scans, S);
     b.scans = scans;
     put(b.state, S);
-    put(b.d_scan_total, 4);
     const uint32_t maxlen = std::max({N, b.npix, b.nhash, b.ncell, b.ndhash, b.ncl, b.ntiles, b.nnear}) + 2;
     put(B.scan_sums, div_up(maxlen, static_cast<uint32_t>(kScanTile)) + 4);
     float4* src;
@@ -406,7 +405,7 @@ lp_status execute(lp_context* ctx, lp_batch& B)
     L.stream = st;
     L.launches = &ctx->launches;
     L.scan_sums = B.scan_sums;
-    L.scan_total = b.d_scan_total;
+    L.scan_err = &b.state->err; // scan 0's error word: a failed scan fails the batch
     L.event_pool = &ctx->events;
     if (B.profiling)
         L.prof = &B.prof;

@@ -59,7 +59,6 @@ struct BatchDev
     int nscan;
     const ScanDev* scans;
     ScanState* state;
-    uint32_t* d_scan_total; // scratch for device-wide scan grand totals
 
     // ---- input / points --------------------------------------------------------------------
     uint32_t nsrc;            // input points (before noise compaction)

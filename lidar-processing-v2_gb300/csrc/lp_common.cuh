@@ -121,9 +121,6 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* smem, 
     return res;
 }
 
-__global__ void k_scan_reduce(const uint32_t* __restrict__ in, uint32_t n, uint32_t* __restrict__ sums);
-__global__ void k_scan_sums(uint32_t* sums, uint32_t nb, uint32_t* grand_total);
-__global__ void k_scan_down(const uint32_t* in, uint32_t* out, uint32_t n, const uint32_t* __restrict__ sums);
 
 // Bitonic sort of `n` (power of two) keys in shared memory by the whole block.
 template <typename T, typename Less>

@@ -9,8 +9,8 @@
 
 namespace lpg
 {
-void scan_exclusive(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* sums,
-                    uint32_t* grand_total, uint64_t& launches);
+void scan_exclusive(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* sums, uint32_t* err,
+                    uint64_t& launches);
 
 // One timed launch (profiling mode only).
 struct LaunchRecord
@@ -26,7 +26,7 @@ struct Launcher
     cudaStream_t stream = nullptr;
     uint64_t* launches = nullptr;
     uint32_t* scan_sums = nullptr; // scratch for device-wide scans
-    uint32_t* scan_total = nullptr;
+    uint32_t* scan_err = nullptr;  // error word the device-wide scans report into
     cudaError_t err = cudaSuccess;
     std::vector<LaunchRecord>* prof = nullptr;
     std::vector<cudaEvent_t>* event_pool = nullptr;
@@ -92,7 +92,7 @@ struct Launcher
         if (n == 0)
             return;
         begin("k_scan");
-        scan_exclusive(stream, in, out, n, scan_sums, scan_total, *launches);
+        scan_exclusive(stream, in, out, n, scan_sums, scan_err, *launches);
         end();
         note_only();
     }
