@@ -14,7 +14,7 @@ namespace lpg
 // 1 + ntiles words before each scan.
 // ---------------------------------------------------------------------------------------------
 constexpr uint32_t kLbThreads = 256;
-constexpr uint32_t kLbItems = 16;
+constexpr uint32_t kLbItems = 32;
 constexpr uint32_t kLbTile = kLbThreads * kLbItems;
 constexpr unsigned long long kLbAgg = 1ull << 62, kLbPre = 2ull << 62;
 
