@@ -10,6 +10,8 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -219,6 +221,8 @@ size_t carve(lp_batch& B, char* base)
     put(scans, S);
     b.scans = scans;
     put(b.state, S);
+    put(b.io, S);
+    put(b.io_ret, S);
     const uint32_t maxlen = std::max({N, b.npix, b.nhash, b.ncell, b.ndhash, b.ncl, b.ntiles, b.nnear}) + 2;
     put(B.scan_sums, div_up(maxlen, static_cast<uint32_t>(kScanTile)) + 4);
     float4* src;
@@ -469,11 +473,19 @@ lp_status execute(lp_context* ctx, lp_batch& B)
     return LP_OK;
 }
 
+lp_status report_state(lp_context* ctx, lp_batch& B);
+
 lp_status fetch_state(lp_context* ctx, lp_batch& B)
 {
     LP_CUDA(ctx, cudaMemcpyAsync(B.h_state.data(), B.b.state, B.h_state.size() * sizeof(ScanState),
                                  cudaMemcpyDeviceToHost, ctx->stream));
     LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return report_state(ctx, B);
+}
+
+// Status of a batch from the fetched per-scan error words.
+lp_status report_state(lp_context* ctx, lp_batch& B)
+{
     lp_status worst = LP_OK;
     for (size_t s = 0; s < B.h_state.size(); ++s)
     {
@@ -651,6 +663,114 @@ using namespace lprt;
 // =============================================================================================
 // C ABI
 // =============================================================================================
+namespace lprt
+{
+// Page-locked host allocations made by lp_host_alloc: [base, base + bytes).
+std::mutex g_pin_mu;
+std::map<uintptr_t, size_t> g_pinned;
+
+bool pinned_range(const void* p, size_t bytes)
+{
+    if (!p)
+        return true;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    auto it = g_pinned.upper_bound(a);
+    if (it == g_pinned.begin())
+        return false;
+    --it;
+    return a + bytes <= it->first + it->second;
+}
+
+// Direct host I/O applies when every buffer of the call lies in lp_host_alloc memory (inputs as
+// XYZI); the GPU then reads and writes them itself over the coherent host link.
+bool direct_io_ok(const lp_batch& B, const lp_scan_input* scans, const lp_scan_output* outs)
+{
+    const bool hull = B.run.stages & ST_HULL, obb = B.run.stages & ST_OBB;
+    for (size_t s = 0; s < B.run.scans.size(); ++s)
+    {
+        const ScanIn& in = B.run.scans[s];
+        const lp_scan_output& o = outs[s];
+        const size_t n = in.n;
+        if (in.n && (in.stride != 4 || !in.xyzi || !pinned_range(in.xyzi, n * 16)))
+            return false;
+        if (!pinned_range(in.ring, n * 2) || !pinned_range(o.noise_labels, n) || !pinned_range(o.seg_labels, n * 4) ||
+            !pinned_range(o.cluster_labels, n * 4))
+            return false;
+        if (hull)
+        {
+            const size_t cc = o.cluster_capacity, hc = o.hull_capacity;
+            if (!pinned_range(o.hull_offsets, (cc + 1) * 4) || !pinned_range(o.hull_indices, hc * 4) ||
+                !pinned_range(o.z_min, cc * 4) || !pinned_range(o.z_max, cc * 4))
+                return false;
+            if (obb && (!pinned_range(o.obb_calipers, cc * sizeof(lp_bounding_box)) ||
+                        !pinned_range(o.obb_pca, cc * sizeof(lp_bounding_box))))
+                return false;
+        }
+    }
+    (void)scans;
+    return true;
+}
+
+lp_status run_direct(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
+{
+    LP_TRY(build(ctx, B));
+    BatchDev& b = B.b;
+    const cudaStream_t st = ctx->stream;
+    const size_t S = B.run.scans.size();
+    const bool hull = B.run.stages & ST_HULL, obb = B.run.stages & ST_OBB;
+    std::vector<IoScan> io(S);
+    for (size_t s = 0; s < S; ++s)
+    {
+        const ScanIn& in = B.run.scans[s];
+        const lp_scan_output& o = outs[s];
+        io[s] = IoScan{in.xyzi, in.ring, o.noise_labels, o.seg_labels, o.cluster_labels,
+                       hull ? o.hull_offsets : nullptr, hull ? o.hull_indices : nullptr,
+                       hull ? o.z_min : nullptr, hull ? o.z_max : nullptr,
+                       obb ? o.obb_calipers : nullptr, obb ? o.obb_pca : nullptr,
+                       o.cluster_capacity, o.hull_capacity};
+    }
+    LP_CUDA(ctx, cudaMemcpyAsync(const_cast<ScanDev*>(b.scans), B.hb.scans.data(), S * sizeof(ScanDev),
+                                 cudaMemcpyHostToDevice, st));
+    LP_CUDA(ctx, cudaMemcpyAsync(b.io, io.data(), S * sizeof(IoScan), cudaMemcpyHostToDevice, st));
+    Launcher L;
+    L.stream = st;
+    L.launches = &ctx->launches;
+    launch_io_in(L, b, b.io);
+    if (L.err != cudaSuccess)
+        return cuda_fail(ctx, L.err, "direct input launch");
+    LP_TRY(execute(ctx, B));
+    launch_io_out(L, b, b.io, b.io_ret, hull ? 1 : 0, obb ? 1 : 0);
+    if (L.err != cudaSuccess)
+        return cuda_fail(ctx, L.err, "direct output launch");
+    std::vector<uint32_t> nh(S, 0u);
+    LP_CUDA(ctx, cudaMemcpyAsync(B.h_state.data(), b.state, S * sizeof(ScanState), cudaMemcpyDeviceToHost, st));
+    if (hull)
+        LP_CUDA(ctx, cudaMemcpyAsync(nh.data(), b.io_ret, S * 4, cudaMemcpyDeviceToHost, st));
+    LP_CUDA(ctx, cudaStreamSynchronize(st));
+    lp_status worst = report_state(ctx, B);
+    if (worst != LP_OK && worst != LP_ERR_CAPACITY)
+        return worst;
+    for (size_t s = 0; s < S; ++s)
+    {
+        lp_scan_output& o = outs[s];
+        const ScanState& sst = B.h_state[s];
+        o.n_obstacles = sst.n_obs;
+        o.n_clusters = sst.n_clusters;
+        o.n_hull_indices = hull ? nh[s] : 0u;
+        o.status = LP_OK;
+        if (hull && (sst.n_clusters > o.cluster_capacity || nh[s] > o.hull_capacity))
+        {
+            o.status = LP_ERR_CAPACITY;
+            o.n_hull_indices = 0;
+            if (worst == LP_OK)
+                worst = fail(ctx, LP_ERR_CAPACITY, "scan " + std::to_string(s) + ": cluster or hull capacity too small");
+        }
+    }
+    return worst;
+}
+} // namespace lprt
+
 extern "C" {
 
 void lp_segmenter_config_default(lp_segmenter_config* c)
@@ -1021,6 +1141,8 @@ lp_status lp_process_batch(lp_context* ctx, const lp_pipeline_config* cfg, const
     LP_TRY(ensure_device(ctx));
     lp_batch& B = cached(ctx);
     LP_TRY(fill_pipeline(ctx, B, cfg, scans, nscans));
+    if (direct_io_ok(B, scans, outs))
+        return run_direct(ctx, B, outs);
     const lp_status st = run_once(ctx, B);
     if (st != LP_OK && st != LP_ERR_CAPACITY)
         return st;
@@ -1248,13 +1370,20 @@ lp_status lp_host_alloc(uint64_t bytes, void** out)
         *out = nullptr;
         return LP_ERR_CUDA;
     }
+    std::lock_guard<std::mutex> lk(lprt::g_pin_mu);
+    lprt::g_pinned[reinterpret_cast<uintptr_t>(*out)] = static_cast<size_t>(bytes);
     return LP_OK;
 }
 
 void lp_host_free(void* p)
 {
-    if (p)
-        cudaFreeHost(p);
+    if (!p)
+        return;
+    {
+        std::lock_guard<std::mutex> lk(lprt::g_pin_mu);
+        lprt::g_pinned.erase(reinterpret_cast<uintptr_t>(p));
+    }
+    cudaFreeHost(p);
 }
 
 lp_status lp_debug_math_sweep(lp_context* ctx, int32_t kind, uint64_t first, uint64_t count, uint64_t stats[3],

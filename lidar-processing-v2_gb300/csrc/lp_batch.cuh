@@ -54,6 +54,23 @@ constexpr uint32_t kStageBytes = kStageRecBytes + kStageColBytes + kJrowWords * 
 constexpr uint32_t kJrowNoUpdate = 0xffffffffu;
 constexpr uint32_t kJrowDynamic = 0x80000000u;
 
+// A scan's buffers in the caller's page-locked host memory (device-accessible addresses).
+struct IoScan
+{
+    const float* xyzi;
+    const uint16_t* ring;
+    uint8_t* noise;
+    uint32_t* seg;
+    int32_t* cl;
+    uint32_t* hoff;
+    int32_t* hidx;
+    float* zmin;
+    float* zmax;
+    lp_bounding_box* obbc;
+    lp_bounding_box* obbp;
+    uint32_t cluster_cap, hull_cap;
+};
+
 struct BatchDev
 {
     int nscan;
@@ -70,6 +87,8 @@ struct BatchDev
     int32_t* pt_src;          // compacted point -> input point (global)
     uint16_t* ring;           // per compacted point
     const uint16_t* ring_in;  // per input point, or null
+    IoScan* io;               // per scan: the caller's page-locked buffers (direct host I/O)
+    uint32_t* io_ret;         // per scan: hull index count written by the direct output kernel
 
     // ---- ring partition ---------------------------------------------------------------------
     uint8_t* quad;            // per point quadrant

@@ -1,0 +1,104 @@
+// lp_io.cu — scan inputs read and results written directly in the caller's page-locked host
+// buffers, over the GPU's coherent host link (NVLink-C2C on GB300), one kernel each way instead of
+// one copy per array per scan. Used by lp_process_batch when every buffer of the call was
+// allocated with lp_host_alloc.
+#include "lp_batch.cuh"
+#include "lp_common.cuh"
+#include "lp_stages.hpp"
+
+namespace lpg
+{
+namespace
+{
+// Input points (and rings) of every scan into the batch arrays.
+__global__ void k_io_in(BatchDev b, const IoScan* io)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.nsrc)
+        return;
+    const int s = find_scan(b.nscan, i, [&](int q) { return b.scans[q].src_off; });
+    const ScanDev& sd = b.scans[s];
+    const uint32_t k = i - sd.src_off;
+    if (k >= sd.n_src)
+        return;
+    const IoScan& d = io[s];
+    const_cast<float4*>(b.src)[i] = reinterpret_cast<const float4*>(d.xyzi)[k];
+    if (b.ring_in && d.ring)
+        const_cast<uint16_t*>(b.ring_in)[i] = d.ring[k];
+}
+
+// Per-point labels of every scan into the caller's buffers.
+__global__ void k_io_out_points(BatchDev b, const IoScan* io)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.nsrc)
+        return;
+    const int s = find_scan(b.nscan, i, [&](int q) { return b.scans[q].src_off; });
+    const ScanDev& sd = b.scans[s];
+    const uint32_t k = i - sd.src_off;
+    if (k >= sd.n_src)
+        return;
+    const IoScan& d = io[s];
+    if (d.noise)
+        d.noise[k] = b.noise[i];
+    if (d.seg)
+        d.seg[k] = b.out_seg[i];
+    if (d.cl)
+        d.cl[k] = static_cast<int32_t>(b.out_cl[i]);
+}
+
+// Per-cluster results: hull offsets (relative to the scan), hull indices, z range, boxes. A scan
+// whose clusters or hull indices exceed the caller's capacities gets none of them (the host
+// reports LP_ERR_CAPACITY for it). ret[s] = the scan's hull index count.
+__global__ void k_io_out_clusters(BatchDev b, const IoScan* io, uint32_t* ret, int with_obb)
+{
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= b.ncl)
+        return;
+    const int s = find_scan(b.nscan, g, [&](int q) { return b.scans[q].cl_off; });
+    const ScanDev& sd = b.scans[s];
+    const uint32_t kcl = b.state[s].n_clusters;
+    const uint32_t k = g - sd.cl_off;
+    if (k > kcl)
+        return;
+    const uint32_t base = b.hull_cnt[sd.cl_off];
+    const uint32_t nh = b.hull_cnt[sd.cl_off + kcl] - base;
+    if (k == 0)
+        ret[s] = nh;
+    const IoScan& d = io[s];
+    if (kcl > d.cluster_cap || nh > d.hull_cap)
+        return;
+    if (d.hoff)
+        d.hoff[k] = b.hull_cnt[g] - base;
+    if (k == kcl)
+        return;
+    const uint32_t h0 = b.hull_cnt[g], h1 = b.hull_cnt[g + 1];
+    if (d.hidx)
+        for (uint32_t j = h0; j < h1; ++j)
+            d.hidx[j - base] = b.hull_out[j];
+    if (d.zmin)
+        d.zmin[k] = b.cl_zmin[g];
+    if (d.zmax)
+        d.zmax[k] = b.cl_zmax[g];
+    if (with_obb)
+    {
+        if (d.obbc)
+            d.obbc[k] = b.obb_c[g];
+        if (d.obbp)
+            d.obbp[k] = b.obb_p[g];
+    }
+}
+} // namespace
+
+void launch_io_in(Launcher& L, const BatchDev& b, const IoScan* io)
+{
+    LP_LAUNCH(L, k_io_in, div_up(b.nsrc, 256u), 256, b, io);
+}
+
+void launch_io_out(Launcher& L, const BatchDev& b, const IoScan* io, uint32_t* ret, int with_hull, int with_obb)
+{
+    LP_LAUNCH(L, k_io_out_points, div_up(b.nsrc, 256u), 256, b, io);
+    if (with_hull)
+        LP_LAUNCH(L, k_io_out_clusters, div_up(b.ncl, 256u), 256, b, io, ret, with_obb);
+}
+} // namespace lpg
