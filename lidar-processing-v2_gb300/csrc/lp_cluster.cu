@@ -266,11 +266,8 @@ __device__ __forceinline__ uint32_t hash_lookup(const BatchDev& b, const ScanDev
 }
 
 // Neighbour offsets (clusterer.hpp:101-105): all 26 (dr, da, de) != (0, 0, 0).
-__global__ void k_uf_hook(BatchDev b)
+__device__ __forceinline__ void k_uf_hook_one(const BatchDev& b, uint32_t v)
 {
-    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= b.hvid[b.nhash])
-        return;
     const uint32_t slot = b.vslot[v];
     const int s = scan_of_hash(b, slot);
     const ScanDev& sd = b.scans[s];
@@ -304,11 +301,15 @@ __global__ void k_uf_hook(BatchDev b)
             }
 }
 
-__global__ void k_uf_flatten(BatchDev b)
+__global__ void k_uf_hook(BatchDev b)
 {
-    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= b.hvid[b.nhash])
-        return;
+    const uint32_t nv = b.hvid[b.nhash]; // occupied voxels: persistent threads stride over them
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x)
+        k_uf_hook_one(b, v);
+}
+
+__device__ __forceinline__ void k_uf_flatten_one(const BatchDev& b, uint32_t v)
+{
     const uint32_t slot = b.vslot[v];
     const int s = scan_of_hash(b, slot);
     int budget = kMaxIters;
@@ -316,26 +317,43 @@ __global__ void k_uf_flatten(BatchDev b)
     b.parent[v] = root;
 }
 
-__global__ void k_comp_stats(BatchDev b)
+__global__ void k_uf_flatten(BatchDev b)
 {
-    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= b.hvid[b.nhash])
-        return;
+    const uint32_t nv = b.hvid[b.nhash]; // occupied voxels: persistent threads stride over them
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x)
+        k_uf_flatten_one(b, v);
+}
+
+__device__ __forceinline__ void k_comp_stats_one(const BatchDev& b, uint32_t v)
+{
     const uint32_t root = b.parent[v];
     const uint32_t slot = b.vslot[v];
     atomicMin(&b.cmin[root], b.hmin[slot]);
     atomicAdd(&b.ccnt[root], b.hcnt[slot]);
 }
 
-__global__ void k_keep(BatchDev b)
+__global__ void k_comp_stats(BatchDev b)
 {
-    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= b.hvid[b.nhash] || b.parent[v] != v)
+    const uint32_t nv = b.hvid[b.nhash]; // occupied voxels: persistent threads stride over them
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x)
+        k_comp_stats_one(b, v);
+}
+
+__device__ __forceinline__ void k_keep_one(const BatchDev& b, uint32_t v)
+{
+    if (b.parent[v] != v)
         return;
     const uint32_t slot = b.vslot[v];
     const int s = scan_of_hash(b, slot);
     if (b.ccnt[v] >= b.scans[s].min_cluster)
         b.kflag[b.state[s].obs_off + b.cmin[v]] = 1u;
+}
+
+__global__ void k_keep(BatchDev b)
+{
+    const uint32_t nv = b.hvid[b.nhash];
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x)
+        k_keep_one(b, v);
 }
 
 // kflag now holds the exclusive scan: rank of each kept component among the scan's kept
@@ -418,10 +436,11 @@ void launch_clustering(Launcher& L, const BatchDev& b, const BatchHost& hb)
     L.scan(b.hvid, b.hvid, b.nhash + 1);
     LP_LAUNCH(L, k_vox_init, div_up(b.nhash, T), T, b);
     LP_LAUNCH(L, k_vox_count, div_up(ns, 64u), 64, b);
-    LP_LAUNCH(L, k_uf_hook, div_up(b.nhash, T), T, b);
-    LP_LAUNCH(L, k_uf_flatten, div_up(b.nhash, T), T, b);
-    LP_LAUNCH(L, k_comp_stats, div_up(b.nhash, T), T, b);
-    LP_LAUNCH(L, k_keep, div_up(b.nhash, T), T, b);
+    const uint32_t vgrid = std::min(div_up(b.nhash, T), static_cast<uint32_t>(sm_count()) * 8u); // <= voxels
+    LP_LAUNCH(L, k_uf_hook, vgrid, T, b);
+    LP_LAUNCH(L, k_uf_flatten, vgrid, T, b);
+    LP_LAUNCH(L, k_comp_stats, vgrid, T, b);
+    LP_LAUNCH(L, k_keep, vgrid, T, b);
     L.scan(b.kflag, b.kflag, b.npts + 1);
     LP_LAUNCH(L, k_obs_label, div_up(b.npts, T), T, b);
     LP_LAUNCH(L, k_cl_state, div_up(ns, 64u), 64, b);

@@ -987,7 +987,7 @@ __device__ __forceinline__ unsigned long long vote_map(const float* wn, const ui
 //       vote will read (unknown / ground / obstacle) wherever it is already fixed, or 3 where it
 //       is not: a queued pixel in a row above (its final colour comes from its own vote) or a
 //       queued pixel to the left in the same row (the symbolic outcome of the in-row chain).
-__global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
+__global__ void __launch_bounds__(256, 3) k_jcp_weights(BatchDev b)
 {
     const uint32_t r = blockIdx.x;
     const int s = scan_of_row(b, r);
@@ -1057,9 +1057,25 @@ __global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
         nrm4[6] = make_float4(sum, __uint_as_float(static_cast<uint32_t>(codes)),
                               __uint_as_float(static_cast<uint32_t>(codes >> 32)), 0.0F);
     }
-    __syncthreads(); // the row record reads weight records other threads of the block wrote
-    if (m == 0u || threadIdx.x >= 24u)
+}
+
+// Row record of the ordered vote (kJrowWords words per image row with queued pixels), one warp per
+// row (lanes 0-23: slots), after k_jcp_weights has written every pixel's raw weight record.
+__global__ void __launch_bounds__(256) k_jcp_rowrec(BatchDev b)
+{
+    const uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (r >= b.nrows || lane_id() >= 24u)
         return;
+    const uint32_t m = b.row_cnt[r];
+    if (m == 0u)
+        return;
+    const int s = scan_of_row(b, r);
+    const ScanDev& sd = b.scans[s];
+    const int32_t h = static_cast<int32_t>(r - sd.row_off);
+    const int32_t H = sd.H, W = sd.W;
+    const uint32_t row_base = sd.pix_off + static_cast<uint32_t>(h * W);
+    const uint8_t* st = b.pix_state + sd.pix_off;
+
     // Row record (kJrowWords words): lastq[d] = the last of the row's final three queued pixels
     // with column <= W-1-d; per slot k, what the row leaves in the reference's stale weight/label
     // buffer: the raw weight of the last queued pixel for which slot k is inside the image, and
@@ -1077,7 +1093,7 @@ __global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
                 break;
             }
     }
-    const int k = static_cast<int>(threadIdx.x);
+    const int k = static_cast<int>(lane_id());
     if (k < 3)
         rec[k] = static_cast<uint32_t>(lq[k]);
     const int32_t dh = jcp_dh(k), dw = jcp_dw(k);
@@ -1622,6 +1638,7 @@ void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, ui
     LP_LAUNCH(L, k_pixel, div_up(b.npix, T), T, b);
     LP_LAUNCH(L, k_dilate_rows, b.nrows, 256, b);
     LP_LAUNCH(L, k_jcp_weights, b.nrows, 256, b);
+    LP_LAUNCH(L, k_jcp_rowrec, div_up(b.nrows * 32u, 256u), 256, b);
     LP_LAUNCH_SMEM(L, k_jcp_rows, static_cast<uint32_t>(b.nscan), 256, 2u * kStageBytes, b);
     LP_LAUNCH(L, k_populate, div_up(b.npix, T), T, b, d_image);
 }
