@@ -150,7 +150,7 @@ struct BatchDev
     uint32_t* hkey;       // per slot: voxel flat key or 0xffffffff
     uint32_t* hmin;       // per slot: min local obstacle index
     uint32_t* hcnt;       // per slot: points in voxel
-    uint32_t* hvid;       // per slot: 1 if occupied -> exclusive scan in place (voxel id)
+    uint32_t* hvid;       // per slot: number of occupied slots before it (voxel id of an occupied slot)
     uint32_t* vslot;      // per voxel id: hash slot
     uint32_t* parent;     // per voxel id
     uint32_t* cmin;       // per voxel id (valid at roots)

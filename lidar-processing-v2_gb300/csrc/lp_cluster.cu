@@ -172,26 +172,51 @@ __global__ void k_vox_insert(BatchDev b)
     b.obs_hslot[o] = kEmpty;
 }
 
-__global__ void k_hash_flag(BatchDev b)
+// Voxel ids in hash-slot order: one look-back scan reads the occupancy of the hash slots, writes
+// hvid[h] = the number of occupied slots before h (nhash + 1 entries: the last is the total) and
+// initialises the union-find record of every occupied slot's voxel.
+struct VoxFlagsSrc
 {
-    const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h > b.nhash)
-        return;
-    b.hvid[h] = (h < b.nhash && b.hkey[h] != kEmpty) ? 1u : 0u;
-}
-
-// hvid now holds voxel ids (exclusive scan of the occupancy flags).
-__global__ void k_vox_init(BatchDev b)
+    const uint32_t* hkey;
+    uint32_t nhash;
+    __device__ __forceinline__ uint4 get4(uint32_t i) const
+    {
+        uint4 k;
+        if (i + 4u <= nhash)
+            k = *reinterpret_cast<const uint4*>(hkey + i);
+        else
+        {
+            k.x = (i < nhash) ? hkey[i] : kEmpty;
+            k.y = (i + 1u < nhash) ? hkey[i + 1u] : kEmpty;
+            k.z = (i + 2u < nhash) ? hkey[i + 2u] : kEmpty;
+            k.w = (i + 3u < nhash) ? hkey[i + 3u] : kEmpty;
+        }
+        return make_uint4(k.x != kEmpty, k.y != kEmpty, k.z != kEmpty, k.w != kEmpty);
+    }
+};
+struct VoxInitDst
 {
-    const uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= b.nhash || b.hkey[h] == kEmpty)
-        return;
-    const uint32_t v = b.hvid[h];
-    b.vslot[v] = h;
-    b.parent[v] = v;
-    b.cmin[v] = kEmpty;
-    b.ccnt[v] = 0u;
-}
+    uint32_t *hvid, *vslot, *parent, *cmin, *ccnt;
+    uint32_t n; // nhash + 1
+    __device__ __forceinline__ void one(uint32_t h, uint32_t v, uint32_t occupied) const
+    {
+        if (occupied)
+        {
+            vslot[v] = h;
+            parent[v] = v;
+            cmin[v] = kEmpty;
+            ccnt[v] = 0u;
+        }
+    }
+    __device__ __forceinline__ void put4(uint32_t i, uint4 e, uint4 f) const
+    {
+        ScanDstU32{hvid, n, true}.put4(i, e, f);
+        one(i, e.x, f.x);
+        one(i + 1u, e.y, f.y);
+        one(i + 2u, e.z, f.z);
+        one(i + 3u, e.w, f.w);
+    }
+};
 
 __global__ void k_vox_count(BatchDev b)
 {
@@ -432,9 +457,11 @@ void launch_clustering(Launcher& L, const BatchDev& b, const BatchHost& hb)
     LP_LAUNCH(L, k_obs_gather, div_up(b.npts, T), T, b);
     LP_LAUNCH(L, k_dims, div_up(ns, 64u), 64, b);
     LP_LAUNCH(L, k_vox_insert, div_up(b.npts, T), T, b);
-    LP_LAUNCH(L, k_hash_flag, div_up(b.nhash + 1, T), T, b);
-    L.scan(b.hvid, b.hvid, b.nhash + 1);
-    LP_LAUNCH(L, k_vox_init, div_up(b.nhash, T), T, b);
+    L.begin("k_vox_ids");
+    scan_lookback(L.stream, VoxFlagsSrc{b.hkey, b.nhash}, VoxInitDst{b.hvid, b.vslot, b.parent, b.cmin, b.ccnt, b.nhash + 1},
+                  b.nhash + 1, L.scan_sums, L.scan_err);
+    L.end();
+    L.note();
     LP_LAUNCH(L, k_vox_count, div_up(ns, 64u), 64, b);
     const uint32_t vgrid = std::min(div_up(b.nhash, T), static_cast<uint32_t>(sm_count()) * 8u); // <= voxels
     LP_LAUNCH(L, k_uf_hook, vgrid, T, b);

@@ -215,4 +215,182 @@ __host__ __device__ inline uint32_t div_up(uint32_t a, uint32_t b)
 {
     return (a + b - 1) / b;
 }
+
+// ---------------------------------------------------------------------------------------------
+// Single-pass exclusive scan with decoupled look-back (Merrill & Garland, "Single-pass Parallel
+// Prefix Scan with Decoupled Look-back", 2016). Tiles of kLbTile elements take dynamic tickets, so
+// every tile a block waits for has already started (and waits only for earlier ones): each
+// look-back ends. A tile publishes (flag, value) in one 64-bit word: flag 1 = the tile's own sum,
+// flag 2 = the inclusive prefix through the tile. Waits are bounded anyway; running out sets
+// ERR_INTERNAL in *err (the result of that scan is then wrong and the batch reports an error).
+// state[0] holds the ticket counter, state[1 + t] tile t's word; the launcher zeroes them.
+//
+// Each warp owns 1024 consecutive elements of its tile and moves them as 8 rows of 32 x uint4
+// (every load and store instruction of a warp covers 512 contiguous bytes). `Src::get4(i)` gives
+// elements i..i+3 (zero past the end), `Dst::put4(i, excl, val)` receives their exclusive
+// prefixes and values, so producers and consumers of a scan can be fused into it.
+// ---------------------------------------------------------------------------------------------
+constexpr uint32_t kLbThreads = 256;
+constexpr uint32_t kLbRows = 8;
+constexpr uint32_t kLbWarpSpan = kLbRows * 32u * 4u;           // 1024 elements per warp
+constexpr uint32_t kLbTile = (kLbThreads / 32u) * kLbWarpSpan; // 8192 elements per tile
+constexpr unsigned long long kLbAgg = 1ull << 62, kLbPre = 2ull << 62;
+
+__device__ __forceinline__ unsigned long long ld_status(const unsigned long long* p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_status(unsigned long long* p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Exclusive prefix of the tile `tile` whose own total is `total` (warp 0 of the block; the
+// result is valid in every lane).
+__device__ __forceinline__ uint32_t lb_tile_prefix(unsigned long long* tiles, uint32_t tile, uint32_t total,
+                                                   uint32_t* err)
+{
+    const uint32_t lane = lane_id();
+    if (tile == 0)
+    {
+        if (lane == 0)
+            st_status(&tiles[0], kLbPre | total);
+        return 0u;
+    }
+    if (lane == 0)
+        st_status(&tiles[tile], kLbAgg | total);
+    uint32_t prefix = 0;
+    bool ok = true;
+    for (int64_t hi = static_cast<int64_t>(tile) - 1; hi >= 0; hi -= 32)
+    {
+        const int64_t t = hi - static_cast<int64_t>(lane);
+        unsigned long long w = kLbPre; // lanes past tile 0 contribute nothing
+        if (t >= 0)
+        {
+            uint32_t polls = 0;
+            do
+                w = ld_status(&tiles[t]);
+            while ((w >> 62) == 0u && ++polls < (1u << 24));
+            if ((w >> 62) == 0u)
+            {
+                ok = false;
+                w = kLbPre;
+            }
+        }
+        const uint32_t pre = __ballot_sync(0xffffffffu, (w >> 62) == 2u);
+        const uint32_t upto = pre ? static_cast<uint32_t>(__ffs(pre) - 1) : 31u; // nearest prefix
+        const uint32_t val = (lane <= upto) ? static_cast<uint32_t>(w) : 0u;
+        prefix += warp_sum(val);
+        if (pre)
+            break;
+    }
+    if (!__all_sync(0xffffffffu, ok) && lane == 0 && err)
+        atomicOr(err, static_cast<uint32_t>(ERR_INTERNAL));
+    if (lane == 0)
+        st_status(&tiles[tile], kLbPre | (prefix + total));
+    return prefix;
+}
+
+template <class Src, class Dst>
+__global__ void __launch_bounds__(kLbThreads) k_scan_lb(Src src, Dst dst, unsigned long long* state, uint32_t* err)
+{
+    __shared__ uint32_t s_warp[kLbThreads / 32];
+    __shared__ uint32_t s_tile, s_prefix;
+    if (threadIdx.x == 0)
+        s_tile = atomicAdd(reinterpret_cast<unsigned int*>(state), 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    const uint32_t wbase = tile * kLbTile + warp * kLbWarpSpan;
+    uint4 v[kLbRows];
+#pragma unroll
+    for (uint32_t q = 0; q < kLbRows; ++q)
+        v[q] = src.get4(wbase + (q * 32u + lane) * 4u);
+    uint32_t rowx[kLbRows]; // exclusive prefix of this lane's 4 elements within the warp's span
+    uint32_t wrun = 0;
+#pragma unroll
+    for (uint32_t q = 0; q < kLbRows; ++q)
+    {
+        const uint32_t sq = v[q].x + v[q].y + v[q].z + v[q].w;
+        const uint32_t inc = warp_incl_scan(sq);
+        rowx[q] = wrun + inc - sq;
+        wrun += __shfl_sync(0xffffffffu, inc, 31);
+    }
+    if (lane == 0)
+        s_warp[warp] = wrun;
+    __syncthreads();
+    if (warp == 0)
+    {
+        const uint32_t wv = (lane < kLbThreads / 32) ? s_warp[lane] : 0u;
+        const uint32_t wi = warp_incl_scan(wv);
+        const uint32_t total = __shfl_sync(0xffffffffu, wi, 31);
+        const uint32_t prefix = lb_tile_prefix(state + 1, tile, total, err);
+        if (lane < kLbThreads / 32)
+            s_warp[lane] = prefix + wi - wv;
+    }
+    __syncthreads();
+    const uint32_t wpre = s_warp[warp];
+#pragma unroll
+    for (uint32_t q = 0; q < kLbRows; ++q)
+    {
+        uint4 e;
+        e.x = wpre + rowx[q];
+        e.y = e.x + v[q].x;
+        e.z = e.y + v[q].y;
+        e.w = e.z + v[q].z;
+        dst.put4(wbase + (q * 32u + lane) * 4u, e, v[q]);
+    }
+}
+
+template <class Src, class Dst>
+void scan_lookback(cudaStream_t st, Src src, Dst dst, uint32_t n, uint32_t* sums, uint32_t* err)
+{
+    const uint32_t nt = div_up(n, kLbTile);
+    unsigned long long* state = reinterpret_cast<unsigned long long*>(sums);
+    cudaMemsetAsync(state, 0, (static_cast<size_t>(nt) + 1) * sizeof(unsigned long long), st);
+    k_scan_lb<<<nt, kLbThreads, 0, st>>>(src, dst, state, err);
+}
+
+// Plain u32 arrays as scan source and destination (vector accesses when 16-byte aligned).
+struct ScanSrcU32
+{
+    const uint32_t* p;
+    uint32_t n;
+    bool vec;
+    __device__ __forceinline__ uint4 get4(uint32_t i) const
+    {
+        if (vec && i + 4u <= n)
+            return *reinterpret_cast<const uint4*>(p + i);
+        uint4 r;
+        r.x = (i < n) ? p[i] : 0u;
+        r.y = (i + 1u < n) ? p[i + 1u] : 0u;
+        r.z = (i + 2u < n) ? p[i + 2u] : 0u;
+        r.w = (i + 3u < n) ? p[i + 3u] : 0u;
+        return r;
+    }
+};
+struct ScanDstU32
+{
+    uint32_t* p;
+    uint32_t n;
+    bool vec;
+    __device__ __forceinline__ void put4(uint32_t i, uint4 e, uint4) const
+    {
+        if (vec && i + 4u <= n)
+        {
+            *reinterpret_cast<uint4*>(p + i) = e;
+            return;
+        }
+        if (i < n)
+            p[i] = e.x;
+        if (i + 1u < n)
+            p[i + 1u] = e.y;
+        if (i + 2u < n)
+            p[i + 2u] = e.z;
+        if (i + 3u < n)
+            p[i + 3u] = e.w;
+    }
+};
 } // namespace lpg

@@ -227,43 +227,54 @@ __device__ __forceinline__ float zunord(uint32_t u)
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
-struct CellHist
-{
-    uint32_t cnt[32], lo[32], hi[32];
-};
-
-__device__ bool cell_zlow_hist(const BatchDev& b, const ScanDev& sd, uint32_t c, uint32_t n, uint32_t start,
-                               CellHist& hs)
+__device__ __forceinline__ bool cell_zlow_hist(const BatchDev& b, const ScanDev& sd, uint32_t c, uint32_t n, uint32_t start)
 {
     const uint32_t lane = lane_id();
     const int32_t q0 = static_cast<int32_t>(floorf(2.0f * sd.zmin_adj));
     const int32_t nb = static_cast<int32_t>(floorf(2.0f * sd.zmax_adj)) - q0 + 1;
     if (!(nb >= 1 && nb <= 32))
         return false;
-    hs.cnt[lane] = 0u;
-    hs.lo[lane] = 0xffffffffu;
-    hs.hi[lane] = 0u;
-    __syncwarp();
+    // lane q accumulates bucket q; each step of 32 heights is folded in once per distinct bucket
+    // (ground cells hold one or two) with warp reductions instead of contended atomics
+    uint32_t cnt = 0u, lo = 0xffffffffu, hi = 0u;
     bool bad = false;
-    for (uint32_t k = lane; k < n; k += 32)
+    for (uint32_t base = 0; base < n; base += 32)
     {
-        const float z = b.csr_z[start + k];
-        const float f = floorf(2.0f * z);
-        if (!(f >= static_cast<float>(q0) && f < static_cast<float>(q0 + nb)))
+        const uint32_t k = base + lane;
+        int32_t q = -1;
+        uint32_t zo = 0u;
+        if (k < n)
         {
-            bad = true; // nan or outside the bucket range
-            continue;
+            const float z = b.csr_z[start + k];
+            const float f = floorf(2.0f * z);
+            if (f >= static_cast<float>(q0) && f < static_cast<float>(q0 + nb))
+            {
+                q = static_cast<int32_t>(f) - q0;
+                zo = zord(z);
+            }
+            else
+                bad = true; // nan or outside the bucket range
         }
-        const int32_t q = static_cast<int32_t>(f) - q0;
-        atomicAdd(&hs.cnt[q], 1u);
-        atomicMin(&hs.lo[q], zord(z));
-        atomicMax(&hs.hi[q], zord(z));
+        uint32_t todo = __ballot_sync(0xffffffffu, q >= 0);
+        while (todo)
+        {
+            const int32_t lq = __shfl_sync(0xffffffffu, q, __ffs(todo) - 1);
+            const bool mine = q == lq;
+            const uint32_t gm = __ballot_sync(0xffffffffu, mine);
+            const uint32_t glo = __reduce_min_sync(0xffffffffu, mine ? zo : 0xffffffffu);
+            const uint32_t ghi = __reduce_max_sync(0xffffffffu, mine ? zo : 0u);
+            if (lane == static_cast<uint32_t>(lq))
+            {
+                cnt += static_cast<uint32_t>(__popc(gm));
+                lo = min(lo, glo);
+                hi = max(hi, ghi);
+            }
+            todo &= ~gm;
+        }
     }
     if (__any_sync(0xffffffffu, bad))
         return false;
-    __syncwarp();
     // lane q = bucket q: position of its first height, previous non-empty bucket
-    const uint32_t cnt = hs.cnt[lane];
     const uint32_t below = warp_incl_scan(cnt) - cnt;
     int32_t last = (cnt > 0u) ? static_cast<int32_t>(lane) : -1; // inclusive max-scan of non-empty
 #pragma unroll
@@ -276,20 +287,21 @@ __device__ bool cell_zlow_hist(const BatchDev& b, const ScanDev& sd, uint32_t c,
     int32_t prev = __shfl_up_sync(0xffffffffu, last, 1);
     if (lane == 0)
         prev = -1;
+    const uint32_t hprev = __shfl_sync(0xffffffffu, hi, max(prev, 0));
     bool qual = false;
     if (cnt > 0u && prev >= 0 && below <= n / 2)
-        qual = (zunord(hs.lo[lane]) - zunord(hs.hi[prev])) > 0.5F;
+        qual = (zunord(lo) - zunord(hprev)) > 0.5F;
     const uint32_t qm = __ballot_sync(0xffffffffu, qual);
     const uint32_t ne = __ballot_sync(0xffffffffu, cnt > 0u);
     const int32_t pick = qm ? (31 - __clz(qm)) : (__ffs(ne) - 1); // no boundary: z[0], the lowest bucket
+    const uint32_t zpick = __shfl_sync(0xffffffffu, lo, pick);
     if (lane == 0)
-        b.zlow[c] = zunord(hs.lo[pick]);
-    __syncwarp();
+        b.zlow[c] = zunord(zpick);
     return true;
 }
 
 // Fallback for a cell the buckets cannot take (at most kMediumCell heights): warp bitonic sort.
-__device__ void cell_zlow_sorted(const BatchDev& b, uint32_t c, uint32_t n, uint32_t start, float* zs)
+__device__ __forceinline__ void cell_zlow_sorted(const BatchDev& b, uint32_t c, uint32_t n, uint32_t start, float* zs)
 {
     const uint32_t lane = lane_id();
     const uint32_t np2 = next_pow2(n);
@@ -310,17 +322,151 @@ __device__ void cell_zlow_sorted(const BatchDev& b, uint32_t c, uint32_t n, uint
 // large_list entries: the cell, bit 31 set when its zlow still has to be found by sorting.
 constexpr uint32_t kLargeNeedsZ = 0x80000000u;
 
-__device__ __forceinline__ void cell_small_one(const BatchDev& b, uint32_t c, float* zs, int32_t* is, CellHist& hs)
+// Per-warp scratch of the near-cell ordering: run starts and run destinations.
+struct RunScratch
+{
+    uint16_t rs[kMediumCell + 1];
+    uint16_t rd[kMediumCell];
+};
+
+// Puts the indices of a near cell (32 < n <= kMediumCell) in ascending order, as the reference's
+// cell vectors hold them (segmenter.cpp:99-131 appends in cloud order).
+//
+// k_bin hands each warp's points of a cell one contiguous slot range in lane order, and a warp
+// covers 32 consecutive indices, so a cell's list is a few ascending runs (one per contributing
+// warp) over disjoint index ranges. The list is split into runs at every descent and at every
+// change of 32-index window (`wofs` = the scan's first batch index mod 32 aligns the windows with
+// the warps), the runs are ordered by their first index (a sort of r keys instead of n), and every
+// run moves as a block. The result is checked: when one run's last index is not below the next
+// run's first, the ranges overlap and the whole list is sorted instead. `is` holds n rounded up
+// to a power of two entries, `key` as many.
+__device__ __forceinline__ void warp_order_near(int32_t* csr, uint32_t n, uint32_t wofs, int32_t* is, uint32_t* key, RunScratch& rsc)
 {
     const uint32_t lane = lane_id();
-    const uint32_t n = b.cell_cnt[c];
-    if (n == 0)
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t r = 0;
+    int32_t prev = 0, vmin = INT32_MAX, vmax = INT32_MIN;
+    for (uint32_t base = 0; base < n; base += 32)
+    {
+        const uint32_t k = base + lane;
+        const int32_t v = (k < n) ? csr[k] : INT32_MAX;
+        is[k] = v;
+        int32_t up = __shfl_up_sync(0xffffffffu, v, 1);
+        if (lane == 0)
+            up = prev;
+        const bool head = (k < n) && (k == 0 || v <= up || ((v + wofs) >> 5) != ((up + wofs) >> 5));
+        const uint32_t hm = __ballot_sync(0xffffffffu, head);
+        if (head)
+            rsc.rs[r + __popc(hm & lt)] = static_cast<uint16_t>(k);
+        r += __popc(hm);
+        prev = __shfl_sync(0xffffffffu, v, 31);
+        if (k < n)
+        {
+            vmin = min(vmin, v);
+            vmax = max(vmax, v);
+        }
+    }
+    if (r == 1)
+        return; // already ascending
+    vmin = __reduce_min_sync(0xffffffffu, vmin);
+    vmax = __reduce_max_sync(0xffffffffu, vmax);
+    if (lane == 0)
+        rsc.rs[r] = static_cast<uint16_t>(n);
+    __syncwarp();
+    const uint32_t np2 = next_pow2(n);
+    // run keys: first index relative to the cell's smallest (24 bits), run id (8 bits)
+    bool ok = static_cast<uint32_t>(vmax - vmin) < (1u << 24);
+    if (ok && r <= 32)
+    {
+        uint32_t kv = UINT32_MAX;
+        if (lane < r)
+            kv = (static_cast<uint32_t>(is[rsc.rs[lane]] - vmin) << 8) | lane;
+        kv = warp_bitonic_sort(kv, [](uint32_t a, uint32_t bb) { return a < bb; });
+        const uint32_t rid = kv & 0xffu;
+        const bool live = lane < r;
+        const uint32_t len = live ? static_cast<uint32_t>(rsc.rs[rid + 1] - rsc.rs[rid]) : 0u;
+        const int32_t last = live ? is[rsc.rs[rid + 1] - 1] : INT32_MIN;
+        const int32_t nhead = live ? is[rsc.rs[rid]] : INT32_MAX;
+        const int32_t nxt = __shfl_down_sync(0xffffffffu, nhead, 1);
+        ok = __all_sync(0xffffffffu, lane + 1 >= r || last < nxt);
+        uint32_t dst = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, dst, o);
+            if (lane >= static_cast<uint32_t>(o))
+                dst += t;
+        }
+        if (ok && live)
+            rsc.rd[rid] = static_cast<uint16_t>(dst - len);
+    }
+    else if (ok)
+    {
+        const uint32_t rp2 = next_pow2(r);
+        for (uint32_t j = lane; j < rp2; j += 32)
+            key[j] = (j < r) ? ((static_cast<uint32_t>(is[rsc.rs[j]] - vmin) << 8) | j) : UINT32_MAX;
+        __syncwarp();
+        warp_bitonic_smem(key, rp2, [](uint32_t a, uint32_t bb) { return a < bb; });
+        uint32_t carry = 0;
+        bool good = true;
+        for (uint32_t base = 0; base < r; base += 32)
+        {
+            const uint32_t p = base + lane;
+            const bool live = p < r;
+            const uint32_t rid = live ? (key[p] & 0xffu) : 0u;
+            const uint32_t len = live ? static_cast<uint32_t>(rsc.rs[rid + 1] - rsc.rs[rid]) : 0u;
+            if (live && p + 1 < r)
+                good &= is[rsc.rs[rid + 1] - 1] < is[rsc.rs[key[p + 1] & 0xffu]];
+            uint32_t dst = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, dst, o);
+                if (lane >= static_cast<uint32_t>(o))
+                    dst += t;
+            }
+            if (live)
+                rsc.rd[rid] = static_cast<uint16_t>(carry + dst - len);
+            carry += __shfl_sync(0xffffffffu, dst, 31);
+        }
+        ok = __all_sync(0xffffffffu, good);
+    }
+    __syncwarp();
+    if (!ok)
+    {
+        for (uint32_t k = ((n + 31u) & ~31u) + lane; k < np2; k += 32)
+            is[k] = INT32_MAX;
+        __syncwarp();
+        warp_bitonic_smem(is, np2, [](int32_t a, int32_t bb) { return a < bb; });
+        for (uint32_t k = lane; k < n; k += 32)
+            csr[k] = is[k];
+        __syncwarp();
         return;
+    }
+    uint32_t seen = 0;
+    for (uint32_t base = 0; base < n; base += 32)
+    {
+        const uint32_t k = base + lane;
+        const bool head = (k < n) && (k == 0 || is[k] <= is[k - 1] || ((is[k] + wofs) >> 5) != ((is[k - 1] + wofs) >> 5));
+        const uint32_t hm = __ballot_sync(0xffffffffu, head);
+        if (k < n)
+        {
+            const uint32_t rid = seen + __popc(hm & (lt | (1u << lane))) - 1u;
+            csr[rsc.rd[rid] + (k - rsc.rs[rid])] = is[k];
+        }
+        seen += __popc(hm);
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ void cell_small_one(const BatchDev& b, uint32_t c, uint32_t n, uint32_t start, float* zs,
+                                               int32_t* is, RunScratch& rsc)
+{
+    const uint32_t lane = lane_id();
     const int s = scan_of_cell(b, c);
     const ScanDev& sd = b.scans[s];
     const bool near = static_cast<int32_t>((c - sd.cell_off) % static_cast<uint32_t>(sd.nrad)) < kRansacRadialBins;
-    const uint32_t start = b.cell_start[c];
-    bool need_z = !cell_zlow_hist(b, sd, c, n, start, hs);
+    bool need_z = !cell_zlow_hist(b, sd, c, n, start);
     if (need_z && n <= static_cast<uint32_t>(kMediumCell))
     {
         cell_zlow_sorted(b, c, n, start, zs);
@@ -340,14 +486,7 @@ __device__ __forceinline__ void cell_small_one(const BatchDev& b, uint32_t c, fl
         return;
     if (n > kSmallCell)
     {
-        const uint32_t np2 = next_pow2(n);
-        for (uint32_t k = lane; k < np2; k += 32)
-            is[k] = (k < n) ? b.csr_idx[start + k] : INT32_MAX;
-        __syncwarp();
-        warp_bitonic_smem(is, np2, [](int32_t a, int32_t bb) { return a < bb; });
-        for (uint32_t k = lane; k < n; k += 32)
-            b.csr_idx[start + k] = is[k];
-        __syncwarp();
+        warp_order_near(b.csr_idx + start, n, sd.pt_off & 31u, is, reinterpret_cast<uint32_t*>(zs), rsc);
         return;
     }
     int32_t idx = (lane < n) ? b.csr_idx[start + lane] : INT32_MAX;
@@ -360,11 +499,25 @@ __global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
 {
     __shared__ float wz[8][kMediumCell];
     __shared__ int32_t wi[8][kMediumCell];
-    __shared__ CellHist wh[8];
-    const uint32_t warp = threadIdx.x >> 5;
+    __shared__ RunScratch wr[8];
+    const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + warp; c < b.ncell; c += nwarps)
-        cell_small_one(b, c, wz[warp], wi[warp], wh[warp]);
+    // 32 consecutive cells per warp step: one coalesced read of their counts, then only the
+    // occupied ones are visited (most cells of a scan are empty)
+    for (uint32_t c0 = (blockIdx.x * (blockDim.x >> 5) + warp) * 32u; c0 < b.ncell; c0 += nwarps * 32u)
+    {
+        const uint32_t c = c0 + lane;
+        const uint32_t cnt = (c < b.ncell) ? b.cell_cnt[c] : 0u;
+        const uint32_t st = (cnt != 0u) ? b.cell_start[c] : 0u;
+        uint32_t m = __ballot_sync(0xffffffffu, cnt != 0u);
+        while (m)
+        {
+            const int j = __ffs(m) - 1;
+            m &= m - 1u;
+            cell_small_one(b, c0 + static_cast<uint32_t>(j), __shfl_sync(0xffffffffu, cnt, j),
+                           __shfl_sync(0xffffffffu, st, j), wz[warp], wi[warp], wr[warp]);
+        }
+    }
 }
 
 __global__ void __launch_bounds__(512) k_cell_large(BatchDev b)
@@ -886,10 +1039,8 @@ __global__ void __launch_bounds__(256) k_dilate_rows(BatchDev b)
     }
 }
 
-// Offsets of the 24-neighbour kernel, segmenter.cpp:527-530.
-__constant__ int8_t kOffH[24] = {-2, -2, -2, -2, -2, -1, -1, -1, -1, -1, 0, 0, 0, 0, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2};
-__constant__ int8_t kOffW[24] = {-2, -1, 0, 1, 2, -2, -1, 0, 1, 2, -2, -1, 1, 2, -2, -1, 0, 1, 2, -2, -1, 0, 1, 2};
-// The same offsets as arithmetic on the slot index (folds to constants in unrolled loops).
+// Offsets of the 24-neighbour kernel (segmenter.cpp:527-530: the 5x5 window without its centre,
+// row-major) as arithmetic on the slot index (folds to constants in unrolled loops).
 __device__ __forceinline__ constexpr int32_t jcp_dh(int k)
 {
     return k < 10 ? -2 + k / 5 : (k < 14 ? 0 : 1 + (k - 14) / 5);
@@ -1225,7 +1376,6 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
     }
     __syncthreads();
     uint8_t* st = b.pix_state + sd.pix_off;
-    const int32_t* map = b.pix_map + sd.pix_off;
     if (threadIdx.x < 24)
     {
         run_w[threadIdx.x] = 0.0F;
@@ -1422,7 +1572,6 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
         __syncthreads();
         cur ^= 1;
     }
-    (void)map;
 }
 
 // populateLabels (segmenter.cpp:640-669) and the colour image of Segmenter::image().
@@ -1624,8 +1773,8 @@ void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, ui
     LP_LAUNCH(L, k_bin, div_up(b.npts, T), T, b);
     L.scan(b.cell_cnt, b.cell_start, b.ncell + 1);
     LP_LAUNCH(L, k_scatter, div_up(b.npts, T), T, b);
-    LP_LAUNCH(L, k_cell_small, std::min(div_up(b.ncell * 32u, 256u), static_cast<uint32_t>(sm_count()) * 8u), 256, b);
-    LP_LAUNCH(L, k_cell_large, 152u * 2u, 512, b);
+    LP_LAUNCH(L, k_cell_small, std::min(div_up(b.ncell, 256u), static_cast<uint32_t>(sm_count()) * 8u), 256, b);
+    LP_LAUNCH(L, k_cell_large, static_cast<uint32_t>(sm_count()) * 2u, 512, b);
     LP_LAUNCH(L, k_chain, div_up(hb.nslices, 128u), 128, b, hb.nslices);
     LP_LAUNCH(L, k_near, div_up(b.nnear * 32u, 256u), 256, b, 0);
     L.scan(b.near_cnt, b.near_start, b.nnear + 1); // near_cnt[nnear] == 0: last entry is the total
