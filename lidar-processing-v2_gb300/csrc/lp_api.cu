@@ -317,6 +317,8 @@ size_t carve(lp_batch& B, char* base)
         put(b.cl_start, b.ncl + 1);
         put(b.cl_fill, b.ncl + 1);
         put(b.members, N);
+        put(b.mxy, N);
+        put(b.cl_zkey, 2ull * b.ncl);
     }
     if (hull)
     {
@@ -458,6 +460,7 @@ lp_status execute(lp_context* ctx, lp_batch& B)
         LP_CUDA(ctx, cudaMemsetAsync(b.kflag, 0, (static_cast<size_t>(N) + 1) * 4, st));
         LP_CUDA(ctx, cudaMemsetAsync(b.cl_cnt, 0, (static_cast<size_t>(b.ncl) + 1) * 4, st));
         LP_CUDA(ctx, cudaMemsetAsync(b.cl_fill, 0, (static_cast<size_t>(b.ncl) + 1) * 4, st));
+        LP_CUDA(ctx, cudaMemsetAsync(b.cl_zkey, 0, static_cast<size_t>(b.ncl) * 8, st));
         launch_clustering(L, b, B.hb);
     }
     if (R.stages & ST_HULL)

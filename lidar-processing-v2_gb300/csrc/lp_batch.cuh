@@ -164,6 +164,8 @@ struct BatchDev
     uint32_t* cl_start;   // exclusive scan of cl_cnt
     uint32_t* cl_fill;
     uint32_t* members;    // obstacle indices grouped by cluster (unordered within)
+    float2* mxy;          // x, y of each member, by member slot
+    uint32_t* cl_zkey;    // per cluster: max of ~ord(z) (the lowest z), max of ord(z) (the highest)
     uint32_t* hull_cnt;   // hull vertices per cluster -> exclusive scan in place
     int32_t* hull_tmp;    // per member slot: hull local indices at cl_start
     int32_t* hull_out;    // dense hull local indices (batch)

@@ -419,16 +419,50 @@ __global__ void k_cl_state(BatchDev b)
         raise_err(&st, ERR_CLUSTER_CAPACITY);
 }
 
+// Members grouped by cluster (slot order within a cluster is free), with their x, y alongside for
+// the hull stage, and each cluster's z range (ordered-key maxima, one atomic pair per cluster
+// and warp).
+__device__ __forceinline__ uint32_t z_ord(float f)
+{
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
 __global__ void k_cl_scatter(BatchDev b)
 {
     const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = lane_id();
     const int32_t label = (o < b.obs_flag[b.npts]) ? b.obs_label[o] : -1;
+    const bool in = label >= 0;
     uint32_t g = 0u;
-    if (label >= 0)
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (in)
+    {
         g = b.scans[scan_of_obs(b, o)].cl_off + static_cast<uint32_t>(label);
-    const uint32_t rank = warp_aggregated_inc(b.cl_fill, g, label >= 0);
-    if (label >= 0)
-        b.members[b.cl_start[g] + rank] = o;
+        p = b.obs_pts[o];
+    }
+    const uint32_t rank = warp_aggregated_inc(b.cl_fill, g, in);
+    if (in)
+    {
+        const uint32_t slot = b.cl_start[g] + rank;
+        b.members[slot] = o;
+        b.mxy[slot] = make_float2(p.x, p.y);
+    }
+    const uint32_t zo = z_ord(p.z);
+    for (uint32_t todo = __ballot_sync(0xffffffffu, in); todo != 0u;)
+    {
+        const int l = __ffs(todo) - 1;
+        const uint32_t lg = __shfl_sync(0xffffffffu, g, l);
+        const bool mine = in && g == lg;
+        const uint32_t lo = __reduce_max_sync(0xffffffffu, mine ? ~zo : 0u);
+        const uint32_t hi = __reduce_max_sync(0xffffffffu, mine ? zo : 0u);
+        if (lane == static_cast<uint32_t>(l))
+        {
+            atomicMax(&b.cl_zkey[2u * lg], lo);
+            atomicMax(&b.cl_zkey[2u * lg + 1u], hi);
+        }
+        todo &= ~__ballot_sync(0xffffffffu, mine);
+    }
 }
 } // namespace
 

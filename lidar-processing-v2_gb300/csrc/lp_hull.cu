@@ -353,6 +353,63 @@ __device__ void pca_box(const double2* P, int n, lp_bounding_box* out)
     *out = box;
 }
 
+// Sums of the x and of the y coordinates of P[0..n) as the reference's loop computes them in
+// binary64 (left to right), by one warp; every lane returns both. Each term is a multiple of
+// 2^g (g from its exponent and the trailing zeros of its significand) and below 2^t in
+// magnitude; when log2(n) + max t - min g <= 53 every partial sum of any order is exact, so a warp
+// tree gives the loop's result. Otherwise (tiny next to large coordinates) the loop runs as written.
+__device__ __forceinline__ void sum_xy_fp64(const double2* P, int n, double& sx, double& sy)
+{
+    const uint32_t lane = lane_id();
+    int tmax = -4096, gmin = 4096;
+    bool ok = true;
+    double px = 0.0, py = 0.0;
+    auto scan = [&](double v) {
+        const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(v));
+        const int e = static_cast<int>((u >> 52) & 0x7ffull);
+        if ((u << 1) == 0ull)
+            return; // zero
+        if (e == 0 || e == 0x7ff)
+        {
+            ok = false; // subnormal, infinite or nan
+            return;
+        }
+        const unsigned long long m = (u & 0xfffffffffffffull) | (1ull << 52);
+        tmax = max(tmax, e - 1022);
+        gmin = min(gmin, e - 1075 + (__ffsll(static_cast<long long>(m)) - 1));
+    };
+    for (int k = static_cast<int>(lane); k < n; k += 32)
+    {
+        scan(P[k].x);
+        scan(P[k].y);
+        px += P[k].x;
+        py += P[k].y;
+    }
+    ok = __all_sync(0xffffffffu, ok);
+    tmax = __reduce_max_sync(0xffffffffu, tmax);
+    gmin = __reduce_min_sync(0xffffffffu, gmin);
+    const int lg = 32 - __clz(n); // >= log2(n)
+    if (ok && lg + tmax - gmin <= 53)
+    {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            px += __shfl_xor_sync(0xffffffffu, px, o);
+            py += __shfl_xor_sync(0xffffffffu, py, o);
+        }
+        sx = px;
+        sy = py;
+        return;
+    }
+    sx = 0.0;
+    sy = 0.0;
+    for (int k = 0; k < n; ++k)
+    {
+        sx += P[k].x;
+        sy += P[k].y;
+    }
+}
+
 // PCA box by one warp. The mean and the covariance sums run in FP64 in the reference's order (the
 // principal angle is ill-conditioned exactly where those sums nearly cancel, so they are kept
 // bit-identical); a = sxx - syy and b = 2 sxy are formed in FP64 too. From there the angle, the
@@ -369,25 +426,37 @@ __device__ void pca_box_warp(const double2* P, int n, lp_bounding_box* out)
     box.is_valid = 0;
     if (n >= 3)
     {
-        double mx = 0.0, my = 0.0;
-        for (int i = 0; i < n; ++i)
+        double sx, sy;
+        sum_xy_fp64(P, n, sx, sy);
+        // mx = sx / n and my = sy / n on lanes 0 and 1 (one division sequence)
+        const double mq = ((lane & 1u) ? sy : sx) / static_cast<double>(n);
+        const double mx = __shfl_sync(0xffffffffu, mq, 0), my = __shfl_sync(0xffffffffu, mq, 1);
+        // the three covariance sums keep the reference's order: the products of vertex k come from
+        // lane k mod 32, lanes 0, 1 and 2 accumulate sxx, sxy and syy in one instruction per step
+        double acc = 0.0;
+        for (int base = 0; base < n; base += 32)
         {
-            mx += P[i].x;
-            my += P[i].y;
+            const int k = base + static_cast<int>(lane);
+            double txx = 0.0, txy = 0.0, tyy = 0.0;
+            if (k < n)
+            {
+                const double dx = P[k].x - mx, dy = P[k].y - my;
+                txx = dx * dx;
+                txy = dx * dy;
+                tyy = dy * dy;
+            }
+            const int cnt = min(32, n - base);
+            for (int j = 0; j < cnt; ++j)
+            {
+                const double a0 = __shfl_sync(0xffffffffu, txx, j);
+                const double a1 = __shfl_sync(0xffffffffu, txy, j);
+                const double a2 = __shfl_sync(0xffffffffu, tyy, j);
+                acc += (lane == 0u) ? a0 : ((lane == 1u) ? a1 : a2);
+            }
         }
-        mx /= n;
-        my /= n;
-        double sxx = 0.0, sxy = 0.0, syy = 0.0;
-        for (int i = 0; i < n; ++i)
-        {
-            const double dx = P[i].x - mx, dy = P[i].y - my;
-            sxx += dx * dx;
-            sxy += dx * dy;
-            syy += dy * dy;
-        }
-        sxx /= (n - 1);
-        sxy /= (n - 1);
-        syy /= (n - 1);
+        const double cq = acc / static_cast<double>(n - 1);
+        const double sxx = __shfl_sync(0xffffffffu, cq, 0), sxy = __shfl_sync(0xffffffffu, cq, 1),
+                     syy = __shfl_sync(0xffffffffu, cq, 2);
         const float theta = 0.5f * lpm::cr_atan2f(__double2float_rn(2.0 * sxy), __double2float_rn(sxx - syy));
         float v10, v00;
         sincosf(theta, &v10, &v00);
@@ -441,6 +510,50 @@ __device__ __forceinline__ void extents_fp64(const double2* P, int n, double cx,
     mxx = warp_max_d(mxx);
     mny = warp_min_d(mny);
     mxy = warp_max_d(mxy);
+}
+
+// extents_fp64 for n <= 32 (vertex k on lane k). The FP32 projections of the float vertices about
+// the float centroid along the float direction lie within tol / 2 of the FP64 ones, so a lane more
+// than tol above the FP32 minimum cannot hold the FP64 minimum: only the lanes within tol of each
+// FP32 extreme compare their FP64 values (usually one or two lanes instead of a five-level tree).
+__device__ __forceinline__ double pick_min_fp64(double v, float f, float tol)
+{
+    const float m = warp_min_f(f);
+    double r = DBL_MAX;
+    for (uint32_t c = __ballot_sync(0xffffffffu, f <= m + tol); c != 0u; c &= c - 1u)
+        r = fmin(r, __shfl_sync(0xffffffffu, v, __ffs(c) - 1));
+    return r;
+}
+__device__ __forceinline__ double pick_max_fp64(double v, float f, float tol)
+{
+    const float m = warp_max_f(f);
+    double r = -DBL_MAX;
+    for (uint32_t c = __ballot_sync(0xffffffffu, f >= m - tol); c != 0u; c &= c - 1u)
+        r = fmax(r, __shfl_sync(0xffffffffu, v, __ffs(c) - 1));
+    return r;
+}
+__device__ __forceinline__ void extents_screened(const double2* P, const float2* Pf, int n, double cx, double cy,
+                                                 double ux, double uy, float cxf, float cyf, float tol, double& mnx,
+                                                 double& mxx, double& mny, double& mxy)
+{
+    const int lane = static_cast<int>(lane_id());
+    const bool live = lane < n;
+    const float uxf = __double2float_rn(ux), uyf = __double2float_rn(uy);
+    double rx = 0.0, ry = 0.0;
+    float fx = 0.0f, fy = 0.0f;
+    if (live)
+    {
+        const double tx = P[lane].x - cx, ty = P[lane].y - cy;
+        rx = tx * ux + ty * uy;
+        ry = -tx * uy + ty * ux;
+        const float sx = Pf[lane].x - cxf, sy = Pf[lane].y - cyf;
+        fx = sx * uxf + sy * uyf;
+        fy = -sx * uyf + sy * uxf;
+    }
+    mnx = pick_min_fp64(rx, live ? fx : INFINITY, tol);
+    mxx = pick_max_fp64(rx, live ? fx : -INFINITY, tol);
+    mny = pick_min_fp64(ry, live ? fy : INFINITY, tol);
+    mxy = pick_max_fp64(ry, live ? fy : -INFINITY, tol);
 }
 
 // Rotating calipers with the candidate boxes screened in FP32 (same result as calipers_warp).
@@ -531,84 +644,145 @@ __device__ void calipers_fast(const double2* P, const float2* Pf, int n, const i
             break;
         T = nt;
     }
-    // FP64 centroid of the hull vertices, summed in the reference's order
-    double cx = 0.0, cy = 0.0;
-    for (int k = 0; k < n; ++k)
-    {
-        cx += P[k].x;
-        cy += P[k].y;
-    }
-    cx /= n;
-    cy /= n;
+    // FP64 centroid of the hull vertices, as the reference's loop sums them
+    double sx, sy;
+    sum_xy_fp64(P, n, sx, sy);
+    const double cq = ((lane & 1u) ? sy : sx) / static_cast<double>(n);
+    const double cx = __shfl_sync(0xffffffffu, cq, 0), cy = __shfl_sync(0xffffffffu, cq, 1);
     // contender c (in edge order) is held by lane c: its edge, direction, FP64 extents and area
     int my_j = -1;
-    double my_ux = 0.0, my_uy = 0.0, my_mnx = 0.0, my_mxx = 0.0, my_mny = 0.0, my_mxy = 0.0, my_area = 0.0;
     int ncont = 0;
     for (int base = 0; base < n; base += 32)
     {
         const int j = base + static_cast<int>(lane);
         const uint32_t mask = __ballot_sync(0xffffffffu, j < n && ea[j] <= T);
-        for (uint32_t mm = mask; mm != 0u; mm &= mm - 1u)
-        {
-            const int jj = base + __ffs(mm) - 1;
-            if (ncont < 32)
-            {
-                const int j1 = (jj + 1 == n) ? 0 : jj + 1;
-                const double ex = P[j1].x - P[jj].x, ey = P[j1].y - P[jj].y;
-                const double len = sqrt(ex * ex + ey * ey);
-                const double ux = ex / len, uy = ey / len;
-                double mnx, mxx, mny, mxy;
-                extents_fp64(P, n, cx, cy, ux, uy, mnx, mxx, mny, mxy);
-                if (static_cast<int>(lane) == ncont)
-                {
-                    my_j = jj;
-                    my_ux = ux;
-                    my_uy = uy;
-                    my_mnx = mnx;
-                    my_mxx = mxx;
-                    my_mny = mny;
-                    my_mxy = mxy;
-                    my_area = (mxx - mnx) * (mxy - mny);
-                }
-            }
-            ++ncont;
-        }
+        for (uint32_t mm = mask; mm != 0u; mm &= mm - 1u, ++ncont)
+            if (static_cast<int>(lane) == ncont) // contender ncont goes to lane ncont
+                my_j = base + __ffs(mm) - 1;
+        if (ncont > 32)
+            break;
     }
     if (ncont > 32)
     {
         calipers_warp(P, n, pairs, npairs, out);
         return;
     }
-    // the reference's walk over the contenders
+    // each contender's unit direction on its own lane (one square root and division sequence)
+    double my_ux = 0.0, my_uy = 0.0, my_mnx = 0.0, my_mxx = 0.0, my_mny = 0.0, my_mxy = 0.0, my_area = 0.0;
+    if (my_j >= 0)
+    {
+        const int j1 = (my_j + 1 == n) ? 0 : my_j + 1;
+        const double ex = P[j1].x - P[my_j].x, ey = P[j1].y - P[my_j].y;
+        const double len = sqrt(ex * ex + ey * ey);
+        my_ux = ex / len;
+        my_uy = ey / len;
+    }
+    // FP32 projection error bound of extents_screened: the float centroid is within 2^-24 (|cx| +
+    // |cy|) of the FP64 one, the float direction within 2^-24 per component, and every difference,
+    // product and sum rounds by 2^-24 relative to |P - c|_1 <= 3 sqrt(r2); the window takes 4x
+    // (centroid) and 8x (rounding) those sums as tol / 2.
+    const float cxf = __double2float_rn(cx), cyf = __double2float_rn(cy);
+    const float tol = 2.0f * ((fabsf(cxf) + fabsf(cyf)) * 2.384185791015625e-7f + 3.0f * sqrtf(r2) * 1.9073486328125e-6f) + 1e-30f;
+    for (int c = 0; c < ncont; ++c)
+    {
+        const double ux = __shfl_sync(0xffffffffu, my_ux, c), uy = __shfl_sync(0xffffffffu, my_uy, c);
+        double mnx, mxx, mny, mxy;
+        if (n <= 32)
+            extents_screened(P, Pf, n, cx, cy, ux, uy, cxf, cyf, tol, mnx, mxx, mny, mxy);
+        else
+            extents_fp64(P, n, cx, cy, ux, uy, mnx, mxx, mny, mxy);
+        if (static_cast<int>(lane) == c)
+        {
+            my_mnx = mnx;
+            my_mxx = mxx;
+            my_mny = mny;
+            my_mxy = mxy;
+            my_area = (mxx - mnx) * (mxy - mny);
+        }
+    }
+    // The reference's walk over the contenders. Its float `best` only ever takes contenders' float
+    // areas F = fl32(A), and rounding is monotone, so a visit's test A < (double)best is F < best,
+    // or at F == best the contender's bit `below` = (A < (double)F). The final best is therefore
+    // the smallest F of all visits, and the kept box is the last visit with that F which passes:
+    // the first one (it meets a larger best; at F = +inf only with `below`) and every later one
+    // with `below`. Each lane takes every 32nd visit (pair pi, side e2, neighbour o).
+    float my_f = INFINITY;
+    int my_below = 0;
+    if (my_j >= 0)
+    {
+        my_f = __double2float_rn(my_area);
+        my_below = my_area < static_cast<double>(my_f);
+    }
+    const int nvis = 4 * npairs;
+    auto visit = [&](int v, int& j, bool& rev, float& f, int& below) {
+        const int2 pr = pairs[v >> 2];
+        const int index = ((v >> 1) & 1) ? pr.y : pr.x;
+        const int o = v & 1;
+        int nb = index + (o == 0 ? -1 : 1);
+        if (nb < 0)
+            nb += n;
+        else if (nb >= n)
+            nb -= n;
+        j = (o == 1) ? index : nb; // hull edge j joins P[j] and P[j+1]
+        rev = (o == 0);            // walked from P[j+1] to P[j]
+        const bool cont = ea[j] <= T;
+        f = INFINITY;
+        below = 0;
+        for (int c = 0; c < ncont; ++c)
+        {
+            const int jc = __shfl_sync(0xffffffffu, my_j, c);
+            const float fc = __shfl_sync(0xffffffffu, my_f, c);
+            const int bc = __shfl_sync(0xffffffffu, my_below, c);
+            if (cont && j == jc)
+            {
+                f = fc;
+                below = bc;
+            }
+        }
+        return cont;
+    };
+    float fmin = INFINITY;
+    bool any = false;
+    for (int v0 = 0; v0 < nvis; v0 += 32)
+    {
+        const int v = v0 + static_cast<int>(lane);
+        int j, below;
+        bool rev;
+        float f;
+        const bool cont = visit(min(v, nvis - 1), j, rev, f, below) && v < nvis;
+        if (cont)
+            fmin = fminf(fmin, f);
+        any |= cont;
+    }
+    fmin = warp_min_f(fmin);
+    any = __any_sync(0xffffffffu, any);
+    int first = INT32_MAX, lastb = -1;
+    for (int v0 = 0; any && v0 < nvis; v0 += 32)
+    {
+        const int v = v0 + static_cast<int>(lane);
+        int j, below;
+        bool rev;
+        float f;
+        const bool cont = visit(min(v, nvis - 1), j, rev, f, below) && v < nvis;
+        if (cont && f == fmin)
+        {
+            first = min(first, v);
+            if (below)
+                lastb = max(lastb, v);
+        }
+    }
+    first = static_cast<int>(__reduce_min_sync(0xffffffffu, static_cast<unsigned>(first)));
+    lastb = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(lastb + 1))) - 1;
+    const int win = (lastb >= 0) ? lastb : ((any && fmin < INFINITY) ? first : -1);
     float best = __double2float_rn(DBL_MAX);
     int wj = -1;
     bool wrev = false;
-    for (int pi = 0; pi < npairs; ++pi)
+    if (win >= 0)
     {
-        const int2 pr = pairs[pi];
-        for (int e2 = 0; e2 < 2; ++e2)
-        {
-            const int index = e2 == 0 ? pr.x : pr.y;
-            for (int o = 0; o < 2; ++o)
-            {
-                int nb = index + (o == 0 ? -1 : 1);
-                if (nb < 0)
-                    nb += n;
-                else if (nb >= n)
-                    nb -= n;
-                const int j = (o == 1) ? index : nb; // hull edge j joins P[j] and P[j+1]
-                if (!(ea[j] <= T))
-                    continue;
-                const uint32_t hold = __ballot_sync(0xffffffffu, my_j == j);
-                const double area = __shfl_sync(0xffffffffu, my_area, __ffs(hold) - 1);
-                if (area < static_cast<double>(best))
-                {
-                    best = __double2float_rn(area);
-                    wj = j;
-                    wrev = (o == 0); // walked from P[j+1] to P[j]
-                }
-            }
-        }
+        int below;
+        float f;
+        visit(win, wj, wrev, f, below);
+        best = fmin;
     }
     if (wj >= 0)
     {
@@ -696,16 +870,42 @@ __device__ void calipers_box(ScanState* st, const double2* P, const float2* Pf, 
 // Orientation test of the monotone chain for float points: decided in FP32 when the float
 // determinant exceeds 2^-21 (|t1| + |t2|) in magnitude (its rounding error stays below
 // 6 * 2^-24 of that sum, the FP64 form's below 3 * 2^-53), else evaluated in FP64 as written.
+// b - a is exact in binary32 (Knuth's TwoSum of b and -a leaves no error).
+__device__ __forceinline__ bool diff_exact(float b, float a, float s)
+{
+    const float a1 = s - b;
+    const float b1 = s - a1;
+    return ((-a) - a1) + (b - b1) == 0.0f;
+}
+
+// u * v has an exact binary32 error term (no underflow in the product).
+__device__ __forceinline__ bool prod_err_exact(float u, float v, float t)
+{
+    return fabsf(t) >= 1e-30f || u == 0.0f || v == 0.0f;
+}
+
 __device__ __forceinline__ bool ccw_or_colinear_f(float ax, float ay, float bx, float by, float cx, float cy)
 {
-    const float t1 = (bx - ax) * (cy - ay);
-    const float t2 = (by - ay) * (cx - ax);
+    const float u = bx - ax, v = cy - ay, w = by - ay, z = cx - ax;
+    const float t1 = u * v;
+    const float t2 = w * z;
     const float d = t1 - t2;
     const float bound = (fabsf(t1) + fabsf(t2)) * 4.76837158203125e-7f + 1e-30f;
     if (d > bound)
         return false;
     if (d < -bound)
         return true;
+    // Near-tie. When the four differences are exact binary32 values, each product of two of them
+    // is exact in binary64 (48 significant bits), so the binary64 expression above has the sign
+    // of u v - w z exactly. Rounding to binary32 is monotone, so t1 < t2 implies u v < w z (and
+    // t1 > t2 the converse); at t1 == t2 the difference is e1 - e2, the exact product errors.
+    if (diff_exact(bx, ax, u) && diff_exact(cy, ay, v) && diff_exact(by, ay, w) && diff_exact(cx, ax, z) &&
+        prod_err_exact(u, v, t1) && prod_err_exact(w, z, t2))
+    {
+        if (t1 != t2)
+            return t1 < t2;
+        return __fmaf_rn(u, v, -t1) <= __fmaf_rn(w, z, -t2);
+    }
     return ccw_or_colinear(ax, ay, bx, by, cx, cy);
 }
 
@@ -718,25 +918,44 @@ __device__ __forceinline__ bool chain_pops(const HPt<double>& a, const HPt<doubl
     return ccw_or_colinear(a.x, a.y, b.x, b.y, c.x, c.y);
 }
 
-// Monotone chain over sorted candidates C[0..m) (polygonizer.cpp:62-88) by one thread.
-// Writes candidate positions of the hull to H (capacity 2m) and returns the hull size.
+// One half of the monotone chain over sorted candidates C[0..m) (polygonizer.cpp:62-88) by one
+// thread: the lower half walks C forwards, the upper half backwards from C[m - 1]. The reference's
+// second loop continues on the stack of the first but never pops below C[m - 1] (its k >= t
+// test), so the upper half is the same walk on its own stack starting from that point. The two
+// points below the top stay in registers. Writes the stack to S, returns its size.
+template <typename T>
+__device__ int chain_half(const HPt<T>* C, int m, int* S, bool upper)
+{
+    int k = 0;
+    HPt<T> a{}, b{};
+    for (int j = 0; j < m; ++j)
+    {
+        const int i = upper ? m - 1 - j : j;
+        const HPt<T> c = C[i];
+        while (k > 1 && chain_pops(a, b, c))
+        {
+            --k;
+            b = a;
+            if (k > 1)
+                a = C[S[k - 2]];
+        }
+        a = b;
+        b = c;
+        S[k++] = i;
+    }
+    return k;
+}
+
+// The whole chain by one thread: hull positions into H (capacity 2m), returns the hull size
+// (the reference's k - 1: the last point repeats the first).
 template <typename T>
 __device__ int monotone_chain(const HPt<T>* C, int m, int* H)
 {
-    int k = 0;
-    for (int i = 0; i < m; ++i)
-    {
-        while (k > 1 && chain_pops(C[H[k - 2]], C[H[k - 1]], C[i]))
-            --k;
-        H[k++] = i;
-    }
-    for (int i = m - 2, t = k + 1; i >= 0; --i)
-    {
-        while (k >= t && chain_pops(C[H[k - 2]], C[H[k - 1]], C[i]))
-            --k;
-        H[k++] = i;
-    }
-    return k - 1;
+    if (m == 0)
+        return -1;
+    const int kl = chain_half(C, m, H, false);
+    const int ku = chain_half(C, m, H + kl - 1, true); // its first entry is H[kl - 1] = m - 1 again
+    return kl + ku - 2;
 }
 
 // Strictly left of a -> b by a relative margin of 1e-5: the float cross product errs by less
@@ -793,10 +1012,11 @@ struct HullSmem
     int32_t diff[kHullSmem + 1];
     float2 poly[kPolyCap];
     float2 poly2[kPolyCap];
+    float4 erec[kPolyCap]; // refinement edge e: start point and direction
+    float2 emar[kPolyCap]; // its inside and outside margins per unit of |q|_1
     unsigned long long pkey[kPolyCap];
     unsigned long long ext[kDirs][kHullThreads / 32];
     float2 dirs[kDirs];
-    float zr[2][kHullThreads / 32];
     int npoly;
     int grew;
     int ncand;
@@ -809,6 +1029,63 @@ __device__ __forceinline__ unsigned long long fkey_payload(float v, uint32_t i)
     return (static_cast<unsigned long long>(ford(v)) << 32) | i;
 }
 
+// A cluster's z range from the ordered keys the cluster scatter accumulates (max of ~ord(z), max
+// of ord(z)).
+__device__ __forceinline__ float zkey_unord(uint32_t u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+__device__ __forceinline__ float zkey_min(uint32_t k)
+{
+    return zkey_unord(~k);
+}
+__device__ __forceinline__ float zkey_max(uint32_t k)
+{
+    return zkey_unord(k);
+}
+
+// Members extreme in the kDirs = 16 directions 2 pi d / 16 (counter-clockwise). Directions d and
+// d + 8 are opposite, so eight projections give both: the largest along d, and for d + 8 the
+// smallest along d. Any extreme member serves (the polygon only has to consist of members); ties
+// keep the first member a thread sees and, across threads, the larger member position.
+struct Extremes16
+{
+    float hi[8], lo[8];
+    uint32_t ih[8], il[8];
+    __device__ __forceinline__ void init()
+    {
+#pragma unroll
+        for (int d = 0; d < 8; ++d)
+        {
+            hi[d] = -INFINITY;
+            lo[d] = INFINITY;
+            ih[d] = il[d] = 0u;
+        }
+    }
+    __device__ __forceinline__ void add(const float2* dirs, float x, float y, uint32_t i)
+    {
+#pragma unroll
+        for (int d = 0; d < 8; ++d)
+        {
+            const float v = x * dirs[d].x + y * dirs[d].y;
+            if (v > hi[d])
+            {
+                hi[d] = v;
+                ih[d] = i;
+            }
+            if (v < lo[d])
+            {
+                lo[d] = v;
+                il[d] = i;
+            }
+        }
+    }
+    __device__ __forceinline__ unsigned long long key(int d) const
+    {
+        return d < 8 ? fkey_payload(hi[d], ih[d]) : fkey_payload(-lo[d - 8], il[d - 8]);
+    }
+};
+
 // Cluster g of scan s: z range, hull (local indices into hull_tmp at cl_start), boxes.
 __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int compute_obb)
 {
@@ -820,53 +1097,45 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
     if (threadIdx.x == 0)
         sm.ncand = 0;
 
-    // 1. z range and the extreme member in each of kDirs directions (float projections: any
-    //    member is a valid polygon vertex, exactness is not needed here)
-    float zmn = INFINITY, zmx = -INFINITY;
+    // 1. the extreme member in each of kDirs directions (float projections: any member is a valid
+    //    polygon vertex, exactness is not needed here), from the members' x, y stored contiguously
+    //    by the cluster scatter (four loads in flight per thread); the z range is already known
+    const float2* xy = b.mxy + start;
+    HPt<float>* gs = reinterpret_cast<HPt<float>*>(b.hs_cand) + 2ull * start; // capacity 2n >= next_pow2(n)
+    Extremes16 ex;
+    ex.init();
+    for (uint32_t i0 = threadIdx.x; i0 < n; i0 += 4u * blockDim.x)
+    {
+        float2 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            const uint32_t i = i0 + static_cast<uint32_t>(u) * blockDim.x;
+            q[u] = (i < n) ? xy[i] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            const uint32_t i = i0 + static_cast<uint32_t>(u) * blockDim.x;
+            if (i < n)
+                ex.add(sm.dirs, q[u].x, q[u].y, i);
+        }
+    }
     unsigned long long ext[kDirs];
 #pragma unroll
     for (int d = 0; d < kDirs; ++d)
-        ext[d] = 0ull;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
-    {
-        const float4 p = b.obs_pts[mem[i]];
-        zmn = fminf(zmn, p.z);
-        zmx = fmaxf(zmx, p.z);
-#pragma unroll
-        for (int d = 0; d < kDirs; ++d)
-        {
-            const unsigned long long key = fkey_payload(p.x * sm.dirs[d].x + p.y * sm.dirs[d].y, i);
-            ext[d] = key > ext[d] ? key : ext[d];
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        zmn = fminf(zmn, __shfl_xor_sync(0xffffffffu, zmn, o));
-        zmx = fmaxf(zmx, __shfl_xor_sync(0xffffffffu, zmx, o));
-    }
-#pragma unroll
-    for (int d = 0; d < kDirs; ++d)
-        ext[d] = warp_max64(ext[d]);
+        ext[d] = warp_max64(ex.key(d));
     if (lane == 0)
     {
 #pragma unroll
         for (int d = 0; d < kDirs; ++d)
             sm.ext[d][warp] = ext[d];
-        sm.zr[0][warp] = zmn;
-        sm.zr[1][warp] = zmx;
     }
     __syncthreads();
     if (threadIdx.x == 0)
     {
-        float a = sm.zr[0][0], c = sm.zr[1][0];
-        for (int w = 1; w < kHullThreads / 32; ++w)
-        {
-            a = fminf(a, sm.zr[0][w]);
-            c = fmaxf(c, sm.zr[1][w]);
-        }
-        b.cl_zmin[g] = a;
-        b.cl_zmax[g] = c;
+        b.cl_zmin[g] = zkey_min(b.cl_zkey[2u * g]);
+        b.cl_zmax[g] = zkey_max(b.cl_zkey[2u * g + 1u]);
         // initial polygon: extreme members in direction order (counter-clockwise), repeats dropped
         int np = 0;
         uint32_t prev = 0xffffffffu;
@@ -878,8 +1147,7 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
             const uint32_t i = static_cast<uint32_t>(best & 0xffffffffull);
             if (n > 0 && i != prev)
             {
-                const float4 p = b.obs_pts[mem[i]];
-                sm.poly[np++] = make_float2(p.x, p.y);
+                sm.poly[np++] = xy[i];
                 prev = i;
             }
         }
@@ -924,33 +1192,52 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
         if (np < 3)
             break;
         for (int e = threadIdx.x; e < np; e += blockDim.x)
+        {
             sm.pkey[e] = 0ull;
+            const float2 a = sm.poly[e], c = sm.poly[(e + 1 == np) ? 0 : e + 1];
+            const float ex = c.x - a.x, ey = c.y - a.y;
+            const float l1 = fabsf(ex) + fabsf(ey);
+            sm.erec[e] = make_float4(a.x, a.y, ex, ey);
+            sm.emar[e] = make_float2(1e-5f * l1, 1e-6f * l1);
+        }
         if (threadIdx.x == 0)
             sm.ncand = 0;
         __syncthreads();
         const int nxt = (cur == 0) ? 1 : 0;
-        for (uint32_t t = threadIdx.x; t < nact; t += blockDim.x)
+        // two members per thread and edge load; q = p - a, cr < 0: right of the edge, outside
+        auto edge = [&](const float4& r, const float2& mg, int e, float px, float py, uint32_t i, bool& in) {
+            const float qx = px - r.x, qy = py - r.y;
+            const float cr = r.z * qy - r.w * qx;
+            const float aq = fabsf(qx) + fabsf(qy);
+            if (!(cr > mg.x * aq))
+                in = false;
+            if (cr < -(mg.y * aq))
+            {
+                const unsigned long long key = fkey_payload(-cr, i);
+                if (key > sm.pkey[e])
+                    atomicMax(&sm.pkey[e], key);
+            }
+        };
+        for (uint32_t t = threadIdx.x; t < nact; t += 2u * blockDim.x)
         {
-            const uint32_t i = (cur < 0) ? t : act[cur][t];
-            const float4 p = b.obs_pts[mem[i]];
-            bool in = true;
+            const uint32_t t1 = t + blockDim.x;
+            const bool two = t1 < nact;
+            const uint32_t i0 = (cur < 0) ? t : act[cur][t];
+            const uint32_t i1 = two ? ((cur < 0) ? t1 : act[cur][t1]) : i0;
+            const float2 p0 = xy[i0], p1 = xy[i1];
+            const float p0x = p0.x, p0y = p0.y, p1x = p1.x, p1y = p1.y;
+            bool in0 = true, in1 = true;
             for (int e = 0; e < np; ++e)
             {
-                const float2 a = sm.poly[e], c = sm.poly[(e + 1 == np) ? 0 : e + 1];
-                const float ex = c.x - a.x, ey = c.y - a.y, qx = p.x - a.x, qy = p.y - a.y;
-                const float cr = ex * qy - ey * qx; // < 0: right of the edge, outside
-                const float scale = (fabsf(ex) + fabsf(ey)) * (fabsf(qx) + fabsf(qy));
-                if (!(cr > 1e-5f * scale))
-                    in = false;
-                if (cr < -1e-6f * scale)
-                {
-                    const unsigned long long key = fkey_payload(-cr, i);
-                    if (key > sm.pkey[e])
-                        atomicMax(&sm.pkey[e], key);
-                }
+                const float4 r = sm.erec[e];
+                const float2 mg = sm.emar[e];
+                edge(r, mg, e, p0x, p0y, i0, in0);
+                edge(r, mg, e, p1x, p1y, i1, in1);
             }
-            if (!in)
-                act[nxt][atomicAdd(&sm.ncand, 1)] = i;
+            if (!in0)
+                act[nxt][atomicAdd(&sm.ncand, 1)] = i0;
+            if (two && !in1)
+                act[nxt][atomicAdd(&sm.ncand, 1)] = i1;
         }
         __syncthreads();
         cur = nxt;
@@ -969,8 +1256,8 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
                     sm.poly2[w++] = sm.poly[e];
                     if (sm.pkey[e] != 0ull)
                     {
-                        const float4 p = b.obs_pts[mem[static_cast<uint32_t>(sm.pkey[e] & 0xffffffffull)]];
-                        sm.poly2[w++] = make_float2(p.x, p.y);
+                        const uint32_t i = static_cast<uint32_t>(sm.pkey[e] & 0xffffffffull);
+                        sm.poly2[w++] = xy[i];
                     }
                 }
                 for (int e = 0; e < w; ++e)
@@ -987,7 +1274,6 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
     // 3. candidates: active members not strictly inside the polygon by a relative margin far
     //    above float rounding (a hull vertex is never strictly inside a polygon of members)
     const int npf = sm.npoly;
-    HPt<float>* gs = reinterpret_cast<HPt<float>*>(b.hs_cand) + 2ull * start; // capacity 2n >= next_pow2(n)
     auto inside = [&](float px, float py) {
         if (npf < 3)
             return false;
@@ -1004,8 +1290,9 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
     __syncthreads();
     for (uint32_t t = threadIdx.x; t < nact; t += blockDim.x)
     {
-        const uint32_t o = mem[(cur < 0) ? t : act[cur][t]];
-        const float4 p = b.obs_pts[o];
+        const uint32_t i = (cur < 0) ? t : act[cur][t];
+        const uint32_t o = mem[i];
+        const float2 p = xy[i];
         if (!inside(p.x, p.y))
         {
             const int pos = atomicAdd(&sm.ncand, 1);
@@ -1038,8 +1325,20 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
         H = b.hs_stack + 2ull * start + 2ull * g; // capacity 2n + 2 >= 2m + 2
     }
     __syncthreads();
+    // lower half on thread 0, upper half on thread 32 (another warp) into H + m + 1; then the
+    // upper half moves down behind the lower one (forwards: the source lies above the target)
     if (threadIdx.x == 0)
-        sm.nhull = monotone_chain(C, m, H);
+        sm.nhull = chain_half(C, m, H, false);
+    else if (threadIdx.x == 32)
+        sm.grew = chain_half(C, m, H + m + 1, true);
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        const int kl = sm.nhull, ku = sm.grew;
+        for (int j = 1; j < ku - 1; ++j)
+            H[kl - 1 + j] = H[m + 1 + j];
+        sm.nhull = (m == 0) ? -1 : kl + ku - 2;
+    }
     __syncthreads();
     const int h = sm.nhull;
 
@@ -1055,21 +1354,45 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
             sm.diff[j] = 0;
         __syncthreads();
         block_bitonic_sort(sm.hkey, np2, [](uint32_t a, uint32_t c) { return a < c; });
-        // member o adds 1 to every hull vertex with a larger key: diff[upper_bound(o)] += 1
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        // member o adds 1 to every hull vertex with a larger key: diff[upper_bound(o)] += 1. The
+        // 32 members a warp reads mostly share one bin (they come from a few index runs): equal
+        // bins are counted once per warp.
+        for (uint32_t base = warp * 32u; base < n; base += 4u * blockDim.x)
         {
-            const uint32_t o = mem[i];
-            int lo = 0, hi = h;
-            while (lo < hi)
+            uint32_t o[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
             {
-                const int mid = (lo + hi) >> 1;
-                if (sm.hkey[mid] > o)
-                    hi = mid;
-                else
-                    lo = mid + 1;
+                const uint32_t i = base + static_cast<uint32_t>(u) * blockDim.x + lane;
+                o[u] = (i < n) ? mem[i] : 0xffffffffu;
             }
-            if (lo < h)
-                atomicAdd(&sm.diff[lo], 1);
+            int lo[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+            {
+                int l = 0, hi = h;
+                while (l < hi)
+                {
+                    const int mid = (l + hi) >> 1;
+                    if (sm.hkey[mid] > o[u])
+                        hi = mid;
+                    else
+                        l = mid + 1;
+                }
+                lo[u] = (o[u] != 0xffffffffu) ? l : h; // bin h: no member (counted nowhere)
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+            {
+                // lanes with the bin of their left neighbour extend its segment; segment heads
+                // add the segment's length
+                const int up = __shfl_up_sync(0xffffffffu, lo[u], 1);
+                const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0u || up != lo[u]);
+                const uint32_t after = heads & ~((2u << lane) - 1u); // heads right of this lane
+                const int len = (after ? __ffs(after) - 1 : 32) - static_cast<int>(lane);
+                if (((heads >> lane) & 1u) && lo[u] < h)
+                    atomicAdd(&sm.diff[lo[u]], len);
+            }
         }
         __syncthreads();
         if (threadIdx.x == 0)
@@ -1144,6 +1467,8 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
 // and then the sort and the chain stack move to global scratch).
 // ---------------------------------------------------------------------------------------------
 constexpr int kWarpCand = 256;
+constexpr uint32_t kWarpRefineMin = 48; // more candidates than this: refine the polygon first
+constexpr int kWarpPoly = 64;           // refined polygon capacity of the warp path
 
 struct WarpSmem
 {
@@ -1155,6 +1480,119 @@ struct WarpSmem
     int npoly;
 };
 
+// Scratch of the warp path's polygon refinement (inside WarpSmem::hp, unused until the boxes).
+struct WarpRefine
+{
+    float2 rp[kWarpPoly], rp2[kWarpPoly];
+    float4 erec[kWarpPoly];
+    float2 emar[kWarpPoly];
+    unsigned long long pkey[kWarpPoly];
+};
+static_assert(sizeof(WarpRefine) <= sizeof(double2) * kWarpCand, "refinement scratch exceeds the box scratch");
+
+// Quickhull rounds over the candidates C[0..m) (at most 16 per lane), starting from the warp's
+// 16-direction polygon: each round tests every candidate against the polygon's edges (keeping
+// the farthest candidate outside each edge), compacts away the candidates strictly inside, and
+// inserts the farthest ones. Returns the number of candidates left in C.
+__device__ uint32_t warp_refine(WarpSmem& ws, HPt<float>* C, uint32_t m, int np)
+{
+    WarpRefine& wr = *reinterpret_cast<WarpRefine*>(ws.hp);
+    const uint32_t lane = lane_id();
+    for (int e = static_cast<int>(lane); e < np; e += 32)
+        wr.rp[e] = ws.poly[e];
+    __syncwarp();
+    for (int round = 0; round < 4 && m > kWarpRefineMin; ++round)
+    {
+        for (int e = static_cast<int>(lane); e < np; e += 32)
+        {
+            const float2 a = wr.rp[e], c = wr.rp[(e + 1 == np) ? 0 : e + 1];
+            const float ex = c.x - a.x, ey = c.y - a.y;
+            const float l1 = fabsf(ex) + fabsf(ey);
+            wr.erec[e] = make_float4(a.x, a.y, ex, ey);
+            wr.emar[e] = make_float2(1e-5f * l1, 1e-6f * l1);
+            wr.pkey[e] = 0ull;
+        }
+        __syncwarp();
+        uint32_t inbits = 0u;
+        for (uint32_t base = 0, q = 0; base < m; base += 32, ++q)
+        {
+            const uint32_t k = base + lane;
+            bool in = false;
+            if (k < m)
+            {
+                const HPt<float> c = C[k];
+                in = true;
+                for (int e = 0; e < np; ++e)
+                {
+                    const float4 r = wr.erec[e];
+                    const float2 mg = wr.emar[e];
+                    const float qx = c.x - r.x, qy = c.y - r.y;
+                    const float cr = r.z * qy - r.w * qx; // < 0: right of the edge, outside
+                    const float aq = fabsf(qx) + fabsf(qy);
+                    if (!(cr > mg.x * aq))
+                        in = false;
+                    if (cr < -(mg.y * aq))
+                    {
+                        const unsigned long long key = fkey_payload(-cr, k);
+                        if (key > wr.pkey[e])
+                            atomicMax(&wr.pkey[e], key);
+                    }
+                }
+            }
+            inbits |= (in ? 1u : 0u) << q;
+        }
+        __syncwarp();
+        // lane 0 inserts each edge's farthest outside candidate (positions before compaction)
+        int grew = 0, nnew = np;
+        if (lane == 0)
+        {
+            int add = 0;
+            for (int e = 0; e < np; ++e)
+                add += (wr.pkey[e] != 0ull);
+            if (add > 0 && np + add <= kWarpPoly)
+            {
+                int w = 0;
+                for (int e = 0; e < np; ++e)
+                {
+                    wr.rp2[w++] = wr.rp[e];
+                    if (wr.pkey[e] != 0ull)
+                    {
+                        const HPt<float> c = C[static_cast<uint32_t>(wr.pkey[e] & 0xffffffffull)];
+                        wr.rp2[w++] = make_float2(c.x, c.y);
+                    }
+                }
+                for (int e = 0; e < w; ++e)
+                    wr.rp[e] = wr.rp2[e];
+                nnew = w;
+                grew = 1;
+            }
+        }
+        __syncwarp();
+        grew = __shfl_sync(0xffffffffu, grew, 0);
+        np = __shfl_sync(0xffffffffu, nnew, 0);
+        // compact in place (every chunk is read before any of its positions is written)
+        uint32_t wpos = 0;
+        for (uint32_t base = 0, q = 0; base < m; base += 32, ++q)
+        {
+            const uint32_t k = base + lane;
+            const bool keep = k < m && !((inbits >> q) & 1u);
+            HPt<float> c{0.0f, 0.0f, 0u};
+            if (keep)
+                c = C[k];
+            const uint32_t mask = __ballot_sync(0xffffffffu, keep);
+            __syncwarp();
+            if (keep)
+                C[wpos + __popc(mask & ((1u << lane) - 1u))] = c;
+            wpos += __popc(mask);
+        }
+        m = wpos;
+        __syncwarp();
+        if (!grew)
+            break;
+    }
+    return m;
+}
+
 __device__ void hull_one_warp(const BatchDev& b, WarpSmem& ws, const float2* dirs, uint32_t g, int s, int compute_obb)
 {
     ScanState* st = &b.state[s];
@@ -1162,36 +1600,22 @@ __device__ void hull_one_warp(const BatchDev& b, WarpSmem& ws, const float2* dir
     const uint32_t start = b.cl_start[g];
     const uint32_t* mem = b.members + start;
     const uint32_t lane = lane_id();
-    float zmn = INFINITY, zmx = -INFINITY;
+    const float2* xy = b.mxy + start;
+    Extremes16 ex;
+    ex.init();
+    for (uint32_t i = lane; i < n; i += 32)
+    {
+        const float2 p = xy[i];
+        ex.add(dirs, p.x, p.y, i);
+    }
     unsigned long long ext[kDirs];
 #pragma unroll
     for (int d = 0; d < kDirs; ++d)
-        ext[d] = 0ull;
-    for (uint32_t i = lane; i < n; i += 32)
-    {
-        const float4 p = b.obs_pts[mem[i]];
-        zmn = fminf(zmn, p.z);
-        zmx = fmaxf(zmx, p.z);
-#pragma unroll
-        for (int d = 0; d < kDirs; ++d)
-        {
-            const unsigned long long key = fkey_payload(p.x * dirs[d].x + p.y * dirs[d].y, i);
-            ext[d] = key > ext[d] ? key : ext[d];
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        zmn = fminf(zmn, __shfl_xor_sync(0xffffffffu, zmn, o));
-        zmx = fmaxf(zmx, __shfl_xor_sync(0xffffffffu, zmx, o));
-    }
-#pragma unroll
-    for (int d = 0; d < kDirs; ++d)
-        ext[d] = warp_max64(ext[d]);
+        ext[d] = warp_max64(ex.key(d));
     if (lane == 0)
     {
-        b.cl_zmin[g] = zmn;
-        b.cl_zmax[g] = zmx;
+        b.cl_zmin[g] = zkey_min(b.cl_zkey[2u * g]);
+        b.cl_zmax[g] = zkey_max(b.cl_zkey[2u * g + 1u]);
         int np = 0;
         uint32_t prev = 0xffffffffu;
         for (int d = 0; d < kDirs; ++d)
@@ -1199,8 +1623,7 @@ __device__ void hull_one_warp(const BatchDev& b, WarpSmem& ws, const float2* dir
             const uint32_t i = static_cast<uint32_t>(ext[d] & 0xffffffffull);
             if (n > 0 && i != prev)
             {
-                const float4 p = b.obs_pts[mem[i]];
-                ws.poly[np++] = make_float2(p.x, p.y);
+                ws.poly[np++] = xy[i];
                 prev = i;
             }
         }
@@ -1250,7 +1673,7 @@ __device__ void hull_one_warp(const BatchDev& b, WarpSmem& ws, const float2* dir
         if (i < n)
         {
             const uint32_t o = mem[i];
-            const float4 p = b.obs_pts[o];
+            const float2 p = xy[i];
             keep = !inside(p.x, p.y);
             c = HPt<float>{p.x, p.y, o};
         }
@@ -1265,14 +1688,52 @@ __device__ void hull_one_warp(const BatchDev& b, WarpSmem& ws, const float2* dir
         m += __popc(mask);
     }
     __syncwarp();
+    // Many candidates (members spread along the boundary, e.g. an arc): refine the polygon as the
+    // CTA path does (insert the candidate farthest outside each edge, drop the candidates proven
+    // strictly inside by the 1e-5 relative margin), a few rounds, in the box scratch (ws.hp).
+    HPt<float>* C0 = (m <= static_cast<uint32_t>(kWarpCand)) ? ws.cand : gs;
+    if (m > kWarpRefineMin && npf >= 3)
+        m = warp_refine(ws, C0, m, npf);
     const bool small = m <= static_cast<uint32_t>(kWarpCand);
+    if (small && C0 == gs)
+    {
+        for (uint32_t k = lane; k < m; k += 32)
+            ws.cand[k] = gs[k];
+        __syncwarp();
+    }
     HPt<float>* C = small ? ws.cand : gs;
     int* H = small ? ws.stack : (b.hs_stack + 2ull * start + 2ull * g);
-    const uint32_t np2 = next_pow2(m);
-    for (uint32_t i = m + lane; i < np2; i += 32)
-        C[i] = HPt<float>{INFINITY, INFINITY, 0xffffffffu};
-    __syncwarp();
-    warp_bitonic_smem(C, np2, [](const HPt<float>& x, const HPt<float>& y) { return hpt_less(x, y); });
+    if (m <= 32u)
+    {
+        // one candidate per lane, sorted in registers (hpt_less is a total order: any sort agrees)
+        HPt<float> v = (lane < m) ? C[lane] : HPt<float>{INFINITY, INFINITY, 0xffffffffu};
+#pragma unroll
+        for (uint32_t k = 2; k <= 32; k <<= 1)
+        {
+#pragma unroll
+            for (uint32_t j = k >> 1; j > 0; j >>= 1)
+            {
+                HPt<float> o;
+                o.x = __shfl_xor_sync(0xffffffffu, v.x, j);
+                o.y = __shfl_xor_sync(0xffffffffu, v.y, j);
+                o.key = __shfl_xor_sync(0xffffffffu, v.key, j);
+                const bool up = ((lane & k) == 0), lower = ((lane & j) == 0);
+                if ((lower == up) ? hpt_less(o, v) : hpt_less(v, o))
+                    v = o;
+            }
+        }
+        __syncwarp();
+        if (lane < m)
+            C[lane] = v;
+    }
+    else
+    {
+        const uint32_t np2 = next_pow2(m);
+        for (uint32_t i = m + lane; i < np2; i += 32)
+            C[i] = HPt<float>{INFINITY, INFINITY, 0xffffffffu};
+        __syncwarp();
+        warp_bitonic_smem(C, np2, [](const HPt<float>& x, const HPt<float>& y) { return hpt_less(x, y); });
+    }
     int h = 0;
     if (lane == 0)
         h = monotone_chain(C, static_cast<int>(m), H);

@@ -252,6 +252,20 @@ def test_batch_composition_independent(ctx):
             compare_scan(r, alone[i], f"scan {10 + i} in group {grp}")
 
 
+@pytest.mark.parametrize("step", [1.0 / 16.0, 0.05])
+def test_pipeline_quantized(ctx, step):
+    """Coordinates on a grid: on the 1/16 m grid every coordinate difference is exact and many hull
+    candidates are exactly collinear; on the 5 cm grid they are near-collinear. Both drive the
+    hull chain's orientation test into its near-tie branches."""
+    pipe = lp.PipelineConfig.default()
+    for s in (0, 1):
+        x, ring, cfg = T.synth_scan(3, s)
+        q = x.copy()
+        q[:, :3] = (np.round(x[:, :3].astype(np.float64) / step) * step).astype(np.float32)
+        got = lp.process_batch(ctx, [q], pipe, [cfg], [ring])[0]
+        compare_scan(got, T.o_process(q, ring, cfg, pipe), f"scan {s} step {step}")
+
+
 def test_edge_cases(ctx):
     x, ring, cfg = T.synth_scan(1, 0)
     pipe = lp.PipelineConfig.default()
