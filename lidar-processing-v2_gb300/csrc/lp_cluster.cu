@@ -303,11 +303,14 @@ __device__ __forceinline__ void k_uf_hook_one(const BatchDev& b, uint32_t v)
     const int32_t a = (key / nr) % na;
     const int32_t e = key / (nr * na);
     int budget = kMaxIters;
-    for (int de = -1; de <= 1; ++de)
+    // Only the 13 offsets after (0, 0, 0) in (de, da, dr) order: every adjacent pair of voxels is
+    // then met from one side (or both, where the azimuth wraps onto itself), which yields the same
+    // components as probing all 26.
+    for (int de = 0; de <= 1; ++de)
         for (int da = -1; da <= 1; ++da)
             for (int dr = -1; dr <= 1; ++dr)
             {
-                if (dr == 0 && da == 0 && de == 0)
+                if (de == 0 && (da < 0 || (da == 0 && dr <= 0)))
                     continue;
                 const int32_t rr = r + dr, ee = e + de;
                 if (rr < 0 || rr >= nr || ee < 0 || ee >= ne)
@@ -321,7 +324,7 @@ __device__ __forceinline__ void k_uf_hook_one(const BatchDev& b, uint32_t v)
                 if (nslot == kEmpty)
                     continue;
                 const uint32_t u = b.hvid[nslot];
-                if (u > v)
+                if (u != v)
                     uf_union(b.parent, v, u, st, budget);
             }
 }

@@ -1099,26 +1099,34 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
 
     // 1. the extreme member in each of kDirs directions (float projections: any member is a valid
     //    polygon vertex, exactness is not needed here), from the members' x, y stored contiguously
-    //    by the cluster scatter (four loads in flight per thread); the z range is already known
+    //    by the cluster scatter; the z range is already known. The members are read as aligned
+    //    pairs (slot v: members 2v - a and 2v - a + 1, a = start mod 2), four 16-byte loads in
+    //    flight per thread; the halves outside [0, n) are skipped (the loads stay inside the
+    //    allocation: it starts at or before member start - a and has 16 bytes after its end).
     const float2* xy = b.mxy + start;
     HPt<float>* gs = reinterpret_cast<HPt<float>*>(b.hs_cand) + 2ull * start; // capacity 2n >= next_pow2(n)
+    const int32_t a2 = static_cast<int32_t>(start & 1u);
+    const float4* xv = reinterpret_cast<const float4*>(b.mxy + (start - static_cast<uint32_t>(a2)));
+    const uint32_t npair = (n + static_cast<uint32_t>(a2) + 1u) / 2u;
     Extremes16 ex;
     ex.init();
-    for (uint32_t i0 = threadIdx.x; i0 < n; i0 += 4u * blockDim.x)
+    for (uint32_t v0 = threadIdx.x; v0 < npair; v0 += 4u * blockDim.x)
     {
-        float2 q[4];
+        float4 q[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u)
         {
-            const uint32_t i = i0 + static_cast<uint32_t>(u) * blockDim.x;
-            q[u] = (i < n) ? xy[i] : make_float2(0.f, 0.f);
+            const uint32_t v = v0 + static_cast<uint32_t>(u) * blockDim.x;
+            q[u] = (v < npair) ? xv[v] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u)
         {
-            const uint32_t i = i0 + static_cast<uint32_t>(u) * blockDim.x;
-            if (i < n)
-                ex.add(sm.dirs, q[u].x, q[u].y, i);
+            const int32_t i = 2 * static_cast<int32_t>(v0 + static_cast<uint32_t>(u) * blockDim.x) - a2;
+            if (i >= 0 && i < static_cast<int32_t>(n))
+                ex.add(sm.dirs, q[u].x, q[u].y, static_cast<uint32_t>(i));
+            if (i + 1 >= 0 && i + 1 < static_cast<int32_t>(n))
+                ex.add(sm.dirs, q[u].z, q[u].w, static_cast<uint32_t>(i + 1));
         }
     }
     unsigned long long ext[kDirs];
@@ -1218,26 +1226,52 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
                     atomicMax(&sm.pkey[e], key);
             }
         };
-        for (uint32_t t = threadIdx.x; t < nact; t += 2u * blockDim.x)
-        {
-            const uint32_t t1 = t + blockDim.x;
-            const bool two = t1 < nact;
-            const uint32_t i0 = (cur < 0) ? t : act[cur][t];
-            const uint32_t i1 = two ? ((cur < 0) ? t1 : act[cur][t1]) : i0;
-            const float2 p0 = xy[i0], p1 = xy[i1];
-            const float p0x = p0.x, p0y = p0.y, p1x = p1.x, p1y = p1.y;
+        // members ok0 / ok1 (at least one): a missing one repeats the other and is not listed
+        auto test2 = [&](float2 p0, uint32_t i0, bool ok0, float2 p1, uint32_t i1, bool ok1) {
+            if (!ok0)
+            {
+                p0 = p1;
+                i0 = i1;
+            }
+            if (!ok1)
+            {
+                p1 = p0;
+                i1 = i0;
+            }
             bool in0 = true, in1 = true;
             for (int e = 0; e < np; ++e)
             {
                 const float4 r = sm.erec[e];
                 const float2 mg = sm.emar[e];
-                edge(r, mg, e, p0x, p0y, i0, in0);
-                edge(r, mg, e, p1x, p1y, i1, in1);
+                edge(r, mg, e, p0.x, p0.y, i0, in0);
+                edge(r, mg, e, p1.x, p1.y, i1, in1);
             }
-            if (!in0)
+            if (ok0 && !in0)
                 act[nxt][atomicAdd(&sm.ncand, 1)] = i0;
-            if (two && !in1)
+            if (ok1 && !in1)
                 act[nxt][atomicAdd(&sm.ncand, 1)] = i1;
+        };
+        if (cur < 0)
+        {
+            // all members: the aligned pairs of step 1, one 16-byte load each
+            for (uint32_t v = threadIdx.x; v < npair; v += blockDim.x)
+            {
+                const float4 q = xv[v];
+                const int32_t i = 2 * static_cast<int32_t>(v) - a2;
+                test2(make_float2(q.x, q.y), static_cast<uint32_t>(max(i, 0)), i >= 0,
+                      make_float2(q.z, q.w), static_cast<uint32_t>(i + 1), i + 1 < static_cast<int32_t>(n));
+            }
+        }
+        else
+        {
+            for (uint32_t t = threadIdx.x; t < nact; t += 2u * blockDim.x)
+            {
+                const uint32_t t1 = t + blockDim.x;
+                const bool two = t1 < nact;
+                const uint32_t i0 = act[cur][t];
+                const uint32_t i1 = two ? act[cur][t1] : i0;
+                test2(xy[i0], i0, true, xy[i1], i1, two);
+            }
         }
         __syncthreads();
         cur = nxt;
@@ -1342,59 +1376,123 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
     __syncthreads();
     const int h = sm.nhull;
 
-    // 5. local index of each hull vertex = number of members before it in input order
-    if (h <= kHullSmem)
+    // 5 + 6. Local index of each hull vertex (the number of members before it in input order) and
+    //        the boxes. They only read the hull: warps 0 and 1 compute the calipers and PCA boxes
+    //        while the other warps count (all warps count when no boxes are asked for).
+    const bool fast = h <= kHullSmem;
+    double2* P = fast ? sm.hp : (b.hs_pts + start);
+    if (compute_obb)
+        for (int j = threadIdx.x; j < h; j += blockDim.x)
+        {
+            const HPt<float> c = C[H[j]];
+            P[j] = make_double2(static_cast<double>(c.x), static_cast<double>(c.y));
+            if (fast)
+                sm.pf[j] = make_float2(c.x, c.y);
+        }
+    const uint32_t np2 = next_pow2(static_cast<uint32_t>(h));
+    if (fast)
     {
         for (int j = threadIdx.x; j < h; j += blockDim.x)
             sm.hkey[j] = C[H[j]].key;
-        const uint32_t np2 = next_pow2(static_cast<uint32_t>(h));
         for (uint32_t j = h + threadIdx.x; j < np2; j += blockDim.x)
             sm.hkey[j] = 0xffffffffu;
         for (int j = threadIdx.x; j <= h; j += blockDim.x)
             sm.diff[j] = 0;
-        __syncthreads();
+    }
+    __syncthreads();
+    if (fast)
         block_bitonic_sort(sm.hkey, np2, [](uint32_t a, uint32_t c) { return a < c; });
-        // member o adds 1 to every hull vertex with a larger key: diff[upper_bound(o)] += 1. The
-        // 32 members a warp reads mostly share one bin (they come from a few index runs): equal
-        // bins are counted once per warp.
-        for (uint32_t base = warp * 32u; base < n; base += 4u * blockDim.x)
+    const uint32_t ix0 = compute_obb ? 64u : 0u; // first counting thread
+    const uint32_t ncount = blockDim.x - ix0;
+    if (compute_obb && warp < 2)
+    {
+        // the refinement's edge records are free: float scratch of the calipers screen
+        if (warp == 0)
+            calipers_box(st, P, fast ? sm.pf : nullptr, reinterpret_cast<float*>(sm.erec), h,
+                         b.hs_pairs + 4ull * start + 16ull * g, &b.obb_c[g]);
+        else
+            pca_box_warp(P, h, &b.obb_p[g]);
+    }
+    else if (fast)
+    {
+        // member o adds 1 to every hull vertex with a larger key: diff[upper_bound(o)] += 1. Each
+        // thread walks a contiguous chunk of the member list as aligned quadruples (slot v:
+        // members 4v - a .. 4v - a + 3, a = start mod 4; entries outside [0, n) skipped, the loads
+        // stay inside the allocation). Members come in ascending index runs, so consecutive
+        // members mostly fall into the same bin: a member inside the current bin's key interval
+        // skips the search, and a bin's count is added once when the bin changes.
+        const uint32_t a4 = start & 3u;
+        const uint4* mv = reinterpret_cast<const uint4*>(b.members + (start - a4));
+        const uint32_t nq = (n + a4 + 3u) / 4u;
+        const uint32_t per = (nq + ncount - 1u) / ncount;
+        const uint32_t q0 = (threadIdx.x - ix0) * per, q1 = min(nq, q0 + per);
+        int cb = h, cc = 0;               // current bin and its pending count
+        uint32_t blo = 1u, bhi = 0u;      // its key interval [blo, bhi) (empty: no bin yet)
+        auto member = [&](uint32_t o) {
+            if (o >= blo && o < bhi)
+            {
+                ++cc;
+                return;
+            }
+            int l = 0, hi = h;
+            while (l < hi)
+            {
+                const int mid = (l + hi) >> 1;
+                if (sm.hkey[mid] > o)
+                    hi = mid;
+                else
+                    l = mid + 1;
+            }
+            if (l != cb)
+            {
+                if (cc > 0 && cb < h)
+                    atomicAdd(&sm.diff[cb], cc);
+                cb = l;
+                cc = 0;
+            }
+            ++cc;
+            blo = (l > 0) ? sm.hkey[l - 1] : 0u;
+            bhi = (l < h) ? sm.hkey[l] : 0xffffffffu;
+        };
+        for (uint32_t v0 = q0; v0 < q1; v0 += 4u)
         {
-            uint32_t o[4];
+            uint4 q[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                q[u] = (v0 + u < q1) ? mv[v0 + u] : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
             for (int u = 0; u < 4; ++u)
             {
-                const uint32_t i = base + static_cast<uint32_t>(u) * blockDim.x + lane;
-                o[u] = (i < n) ? mem[i] : 0xffffffffu;
-            }
-            int lo[4];
+                const int32_t i = 4 * static_cast<int32_t>(v0 + u) - static_cast<int32_t>(a4);
+                const uint32_t oo[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
-            {
-                int l = 0, hi = h;
-                while (l < hi)
-                {
-                    const int mid = (l + hi) >> 1;
-                    if (sm.hkey[mid] > o[u])
-                        hi = mid;
-                    else
-                        l = mid + 1;
-                }
-                lo[u] = (o[u] != 0xffffffffu) ? l : h; // bin h: no member (counted nowhere)
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-            {
-                // lanes with the bin of their left neighbour extend its segment; segment heads
-                // add the segment's length
-                const int up = __shfl_up_sync(0xffffffffu, lo[u], 1);
-                const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0u || up != lo[u]);
-                const uint32_t after = heads & ~((2u << lane) - 1u); // heads right of this lane
-                const int len = (after ? __ffs(after) - 1 : 32) - static_cast<int>(lane);
-                if (((heads >> lane) & 1u) && lo[u] < h)
-                    atomicAdd(&sm.diff[lo[u]], len);
+                for (int c = 0; c < 4; ++c)
+                    if (v0 + u < q1 && i + c >= 0 && i + c < static_cast<int32_t>(n))
+                        member(oo[c]);
             }
         }
-        __syncthreads();
+        if (cc > 0 && cb < h)
+            atomicAdd(&sm.diff[cb], cc);
+    }
+    else
+    {
+        for (int j = static_cast<int>(warp - ix0 / 32u); j < h; j += static_cast<int>(ncount / 32u))
+        {
+            const uint32_t key = C[H[j]].key;
+            uint32_t cnt = 0;
+            for (uint32_t base = 0; base < n; base += 32)
+            {
+                const uint32_t i = base + lane;
+                const bool lt = (i < n) && (mem[i] < key);
+                cnt += __popc(__ballot_sync(0xffffffffu, lt));
+            }
+            if (lane == 0)
+                hull_dst[j] = static_cast<int32_t>(cnt);
+        }
+    }
+    __syncthreads();
+    if (fast)
+    {
         if (threadIdx.x == 0)
         {
             int run = 0;
@@ -1420,44 +1518,8 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
             hull_dst[j] = sm.diff[lo];
         }
     }
-    else
-    {
-        for (int j = static_cast<int>(warp); j < h; j += kHullThreads / 32)
-        {
-            const uint32_t key = C[H[j]].key;
-            uint32_t cnt = 0;
-            for (uint32_t base = 0; base < n; base += 32)
-            {
-                const uint32_t i = base + lane;
-                const bool lt = (i < n) && (mem[i] < key);
-                cnt += __popc(__ballot_sync(0xffffffffu, lt));
-            }
-            if (lane == 0)
-                hull_dst[j] = static_cast<int32_t>(cnt);
-        }
-    }
     if (threadIdx.x == 0)
         b.hull_cnt[g] = static_cast<uint32_t>(h);
-
-    // 6. boxes on the hull vertices (one warp)
-    if (compute_obb)
-    {
-        const bool fast = h <= kHullSmem;
-        double2* P = fast ? sm.hp : (b.hs_pts + start);
-        for (int j = threadIdx.x; j < h; j += blockDim.x)
-        {
-            const HPt<float> c = C[H[j]];
-            P[j] = make_double2(static_cast<double>(c.x), static_cast<double>(c.y));
-            if (fast)
-                sm.pf[j] = make_float2(c.x, c.y);
-        }
-        __syncthreads();
-        if (warp == 0) // hkey is free again: float scratch of the calipers screen
-            calipers_box(st, P, fast ? sm.pf : nullptr, reinterpret_cast<float*>(sm.hkey), h,
-                         b.hs_pairs + 4ull * start + 16ull * g, &b.obb_c[g]);
-        else if (warp == 1)
-            pca_box_warp(P, h, &b.obb_p[g]);
-    }
     __syncthreads();
 }
 
