@@ -1133,13 +1133,16 @@ __device__ __forceinline__ unsigned long long vote_map(const float* wn, const ui
 // empty neighbour or one farther than the kernel threshold, else expf(-amp * dist)
 // (segmenter.cpp:545-607). These depend on geometry only, so they are computed in parallel
 // before the ordered vote. Two records per queued pixel:
-//   jw: the raw weights and their sum (read back when a later pixel's slot leaves the image),
+//   jw: the raw weights and their sum (read back when a later pixel's slot leaves the image;
+//       written for the last three queued pixels of each row, the only ones read),
 //   jn: the weights divided by the sum, the sum, and a 2-bit label code per slot: the label the
 //       vote will read (unknown / ground / obstacle) wherever it is already fixed, or 3 where it
 //       is not: a queued pixel in a row above (its final colour comes from its own vote) or a
 //       queued pixel to the left in the same row (the symbolic outcome of the in-row chain).
-__global__ void __launch_bounds__(256, 3) k_jcp_weights(BatchDev b)
+__global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
 {
+    // one warp per queued pixel, lane k = kernel slot k (lanes 24-31 idle); the weights are summed
+    // by lane 0 in slot order, as the reference's loop adds them
     const uint32_t r = blockIdx.x;
     const int s = scan_of_row(b, r);
     const ScanDev& sd = b.scans[s];
@@ -1150,63 +1153,66 @@ __global__ void __launch_bounds__(256, 3) k_jcp_weights(BatchDev b)
     const int32_t* map = b.pix_map + sd.pix_off;
     const uint8_t* st = b.pix_state + sd.pix_off;
     const float4* pts = b.pts + sd.pt_off;
-    for (uint32_t j = threadIdx.x; j < m; j += blockDim.x)
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    const int k = static_cast<int>(lane);
+    const int32_t dh = jcp_dh(k), dw = jcp_dw(k);
+    for (uint32_t j = warp; j < m; j += blockDim.x >> 5)
     {
         const int32_t w = b.row_cols[row_base + j];
         const float4 cp = pts[map[h * W + w]];
-        float* out = b.jw + static_cast<size_t>(row_base + j) * kJwStride;
-        float* nrm = b.jn + static_cast<size_t>(row_base + j) * kJwStride;
-        float wt[24];
-        unsigned long long codes = 0ull;
+        float wt = 0.0F;
+        uint32_t code = V_U;
+        const int32_t hh = h + dh, ww = w + dw;
+        if (k < 24 && hh >= 0 && hh < H && ww >= 0 && ww < W)
+        {
+            const int32_t ni = map[hh * W + ww];
+            if (ni >= 0)
+            {
+                const float4 np = pts[ni];
+                const float dx = cp.x - np.x;
+                const float dy = cp.y - np.y;
+                const float dz = cp.z - np.z;
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                if (!(d2 > sd.kthr2))
+                    wt = lpm::cr_expf(-sd.amp * sqrtf(d2));
+            }
+            if (wt != 0.0F)
+            {
+                const uint8_t ns = st[hh * W + ww];
+                if (dh > 0 || (dh == 0 && dw > 0))
+                    code = pre_view(ns); // not voted before this pixel
+                else
+                    code = (ns == PX_INTERSECT) ? 3u : final_view(ns);
+            }
+        }
         float sum = 0.0F;
 #pragma unroll
-        for (int k = 0; k < 24; ++k)
-        {
-            const int32_t dh = jcp_dh(k), dw = jcp_dw(k);
-            const int32_t hh = h + dh, ww = w + dw;
-            wt[k] = 0.0F;
-            uint32_t code = V_U;
-            if (hh >= 0 && hh < H && ww >= 0 && ww < W)
-            {
-                const int32_t ni = map[hh * W + ww];
-                if (ni >= 0)
-                {
-                    const float4 np = pts[ni];
-                    const float dx = cp.x - np.x;
-                    const float dy = cp.y - np.y;
-                    const float dz = cp.z - np.z;
-                    const float d2 = dx * dx + dy * dy + dz * dz;
-                    if (!(d2 > sd.kthr2))
-                    {
-                        const float dist = sqrtf(d2);
-                        wt[k] = lpm::cr_expf(-sd.amp * dist);
-                        sum += wt[k];
-                    }
-                }
-                if (wt[k] != 0.0F)
-                {
-                    const uint8_t ns = st[hh * W + ww];
-                    if (dh > 0 || (dh == 0 && dw > 0))
-                        code = pre_view(ns); // not voted before this pixel
-                    else
-                        code = (ns == PX_INTERSECT) ? 3u : final_view(ns);
-                }
-            }
-            codes |= static_cast<unsigned long long>(code) << (2 * k);
-        }
-        const bool live = fabsf(sum) > FLT_EPSILON;
-        float4* out4 = reinterpret_cast<float4*>(out);
-        float4* nrm4 = reinterpret_cast<float4*>(nrm);
+        for (int q = 0; q < 24; ++q)
+            sum += __shfl_sync(0xffffffffu, wt, q);
+        unsigned long long codes = (k < 24) ? (static_cast<unsigned long long>(code) << (2 * k)) : 0ull;
 #pragma unroll
-        for (int q = 0; q < 6; ++q)
+        for (int o = 16; o > 0; o >>= 1)
+            codes |= __shfl_xor_sync(0xffffffffu, codes, o);
+        const bool live = fabsf(sum) > FLT_EPSILON;
+        // the raw record is only read for the row's last three queued pixels (the stale-slot
+        // sources of later rows and of the row's right border)
+        const bool raw = j + 3u >= m;
+        float* out = b.jw + static_cast<size_t>(row_base + j) * kJwStride;
+        float* nrm = b.jn + static_cast<size_t>(row_base + j) * kJwStride;
+        if (k < 24)
         {
-            out4[q] = make_float4(wt[4 * q], wt[4 * q + 1], wt[4 * q + 2], wt[4 * q + 3]);
-            nrm4[q] = live ? make_float4(wt[4 * q] / sum, wt[4 * q + 1] / sum, wt[4 * q + 2] / sum, wt[4 * q + 3] / sum)
-                           : make_float4(0.0F, 0.0F, 0.0F, 0.0F);
+            if (raw)
+                out[k] = wt;
+            nrm[k] = live ? wt / sum : 0.0F;
         }
-        out4[6] = make_float4(sum, 0.0F, 0.0F, 0.0F);
-        nrm4[6] = make_float4(sum, __uint_as_float(static_cast<uint32_t>(codes)),
-                              __uint_as_float(static_cast<uint32_t>(codes >> 32)), 0.0F);
+        else if (k < 28)
+        {
+            if (raw)
+                out[k] = (k == 24) ? sum : 0.0F;
+            nrm[k] = (k == 24) ? sum
+                               : ((k == 25) ? __uint_as_float(static_cast<uint32_t>(codes))
+                                            : ((k == 26) ? __uint_as_float(static_cast<uint32_t>(codes >> 32)) : 0.0F));
+        }
     }
 }
 
