@@ -286,7 +286,8 @@ size_t carve(lp_batch& B, char* base)
         put(b.pix_map, b.npix);
         put(b.pix_state, b.npix);
         put(b.row_cols, b.npix);
-        put(b.row_cnt, b.nrows + 1);
+        put(b.row_cnt, b.nrows + 1); // [nrows]: queued pixels of the batch
+        put(b.jq, b.npix);
         put(b.jw, static_cast<size_t>(b.npix) * kJwStride);
         put(b.jn, static_cast<size_t>(b.npix) * kJwStride);
         put(b.jrow, static_cast<size_t>(b.nrows) * kJrowWords);

@@ -129,6 +129,7 @@ struct BatchDev
     // ---- jump convolution -------------------------------------------------------------------
     uint32_t nrows;
     uint16_t* row_cols;        // per pixel slot: intersection columns of the row in order
+    uint4* jq;            // flat list of the batch's queued pixels: (image row, position | column << 16, point, scan)
     uint32_t* row_cnt;         // per global row
     float* jw;                 // per entry: 24 fresh weights + sum (stride kJwStride)
     float* jn;                 // per entry: 24 normalized weights, sum, slot label codes (stride kJwStride)

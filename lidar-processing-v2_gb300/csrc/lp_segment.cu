@@ -1015,6 +1015,7 @@ __global__ void __launch_bounds__(256) k_dilate_rows(BatchDev b)
     if (lane == 0)
         wcount[warp] = count;
     __syncthreads();
+    __shared__ uint32_t qbase;
     if (threadIdx.x == 0)
     {
         uint32_t run = 0u;
@@ -1024,6 +1025,8 @@ __global__ void __launch_bounds__(256) k_dilate_rows(BatchDev b)
             run += wcount[k];
         }
         b.row_cnt[r] = run;
+        // the row's segment of the flat list of queued pixels (row_cnt[nrows] counts them)
+        qbase = run ? atomicAdd(&b.row_cnt[b.nrows], run) : 0u;
     }
     __syncthreads();
     // pass 2: queue entries in column order (this row's states now hold the intersections)
@@ -1034,7 +1037,14 @@ __global__ void __launch_bounds__(256) k_dilate_rows(BatchDev b)
         const bool inter = w < W && st[h * W + w] == PX_INTERSECT;
         const uint32_t m = __ballot_sync(0xffffffffu, inter);
         if (inter)
-            b.row_cols[row_base + pos + static_cast<uint32_t>(__popc(m & ((1u << lane) - 1u)))] = static_cast<uint16_t>(w);
+        {
+            const uint32_t j = pos + static_cast<uint32_t>(__popc(m & ((1u << lane) - 1u)));
+            b.row_cols[row_base + j] = static_cast<uint16_t>(w);
+            // (row, position | column << 16, the pixel's point, scan): the weights pass starts here
+            b.jq[qbase + j] = make_uint4(r, j | (static_cast<uint32_t>(w) << 16),
+                                         static_cast<uint32_t>(b.pix_map[sd.pix_off + static_cast<uint32_t>(h * W + w)]),
+                                         static_cast<uint32_t>(s));
+        }
         pos += static_cast<uint32_t>(__popc(m));
     }
 }
@@ -1141,25 +1151,29 @@ __device__ __forceinline__ unsigned long long vote_map(const float* wn, const ui
 //       queued pixel to the left in the same row (the symbolic outcome of the in-row chain).
 __global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
 {
-    // one warp per queued pixel, lane k = kernel slot k (lanes 24-31 idle); the weights are summed
-    // by lane 0 in slot order, as the reference's loop adds them
-    const uint32_t r = blockIdx.x;
-    const int s = scan_of_row(b, r);
-    const ScanDev& sd = b.scans[s];
-    const int32_t h = static_cast<int32_t>(r - sd.row_off);
-    const int32_t H = sd.H, W = sd.W;
-    const uint32_t row_base = sd.pix_off + static_cast<uint32_t>(h * W);
-    const uint32_t m = b.row_cnt[r];
-    const int32_t* map = b.pix_map + sd.pix_off;
-    const uint8_t* st = b.pix_state + sd.pix_off;
-    const float4* pts = b.pts + sd.pt_off;
-    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    // one warp per queued pixel of the batch's flat list (rows of any length spread over the whole
+    // grid), lane k = kernel slot k (lanes 24-31 idle); the weights are summed by lane 0 in slot
+    // order, as the reference's loop adds them
+    const uint32_t total = b.row_cnt[b.nrows];
+    const uint32_t lane = lane_id();
     const int k = static_cast<int>(lane);
     const int32_t dh = jcp_dh(k), dw = jcp_dw(k);
-    for (uint32_t j = warp; j < m; j += blockDim.x >> 5)
+    const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < total; q += nw)
     {
-        const int32_t w = b.row_cols[row_base + j];
-        const float4 cp = pts[map[h * W + w]];
+        const uint4 e = b.jq[q];
+        const uint32_t r = e.x, j = e.y & 0xffffu;
+        const int32_t w = static_cast<int32_t>(e.y >> 16);
+        const int s = static_cast<int>(e.w);
+        const ScanDev& sd = b.scans[s];
+        const int32_t h = static_cast<int32_t>(r - sd.row_off);
+        const int32_t H = sd.H, W = sd.W;
+        const uint32_t row_base = sd.pix_off + static_cast<uint32_t>(h * W);
+        const uint32_t m = b.row_cnt[r];
+        const int32_t* map = b.pix_map + sd.pix_off;
+        const uint8_t* st = b.pix_state + sd.pix_off;
+        const float4* pts = b.pts + sd.pt_off;
+        const float4 cp = pts[e.z];
         float wt = 0.0F;
         uint32_t code = V_U;
         const int32_t hh = h + dh, ww = w + dw;
@@ -1792,7 +1806,7 @@ void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, ui
     LP_LAUNCH(L, k_project_key, div_up(b.npts, T), T, b);
     LP_LAUNCH(L, k_pixel, div_up(b.npix, T), T, b);
     LP_LAUNCH(L, k_dilate_rows, b.nrows, 256, b);
-    LP_LAUNCH(L, k_jcp_weights, b.nrows, 256, b);
+    LP_LAUNCH(L, k_jcp_weights, static_cast<uint32_t>(sm_count()) * 8u, 256, b);
     LP_LAUNCH(L, k_jcp_rowrec, div_up(b.nrows * 32u, 256u), 256, b);
     LP_LAUNCH_SMEM(L, k_jcp_rows, static_cast<uint32_t>(b.nscan), 256, 2u * kStageBytes, b);
     LP_LAUNCH(L, k_populate, div_up(b.npix, T), T, b, d_image);
