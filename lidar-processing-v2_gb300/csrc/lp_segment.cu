@@ -726,65 +726,94 @@ struct Mt42Stream
     }
 };
 
-__global__ void k_ransac_draw(BatchDev b)
+// One warp per scan: lane 0 walks the seed-42 stream (the draws are sequential: a rejected draw
+// shifts every later one) and records the index pairs; the lanes then fit the planes in parallel.
+__global__ void __launch_bounds__(32) k_ransac_draw(BatchDev b)
 {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= b.nscan)
-        return;
+    __shared__ uint32_t di2[kMaxRansacIters], di3[kMaxRansacIters];
+    __shared__ int bad;
+    const int s = blockIdx.x;
+    const uint32_t lane = lane_id();
     const ScanDev& sd = b.scans[s];
     ScanState& st = b.state[s];
     const uint32_t first = b.near_start[sd.near_off];
     const uint32_t nnear_s = static_cast<uint32_t>(sd.nslice * sd.nnear_per_slice);
     const uint32_t last = b.near_start[sd.near_off + nnear_s]; // near_start has nnear + 1 entries
     const uint32_t N = last - first;
-    st.cand_off = first;
-    st.n_cand = N;
-    st.ransac_ok = 0;
-    b.pvalid[s] = 0ull;
+    if (lane == 0)
+    {
+        st.cand_off = first;
+        st.n_cand = N;
+        st.ransac_ok = 0;
+        b.pvalid[s] = 0ull;
+    }
     if (N < 2)
         return; // the reference never ends its p3 draw for N == 1 (segmenter.cpp:382-386)
-    Mt42Stream gen;
+    if (lane == 0)
+    {
+        Mt42Stream gen;
+        bad = 0;
+        for (int it = 0; it < kMaxRansacIters; ++it)
+        {
+            const uint32_t i2 = gen.bounded(N);
+            uint32_t i3 = gen.bounded(N);
+            int guard = 0;
+            while (i3 == i2 && guard < (1 << 20))
+            {
+                i3 = gen.bounded(N);
+                ++guard;
+            }
+            if (guard >= (1 << 20))
+            {
+                bad = 1;
+                break;
+            }
+            di2[it] = i2;
+            di3[it] = i3;
+        }
+    }
+    __syncwarp();
+    if (bad)
+    {
+        if (lane == 0)
+            raise_err(&st, ERR_INTERNAL);
+        return;
+    }
     const float p1x = 0.0F, p1y = 0.0F, p1z = -sd.sensor_h;
     unsigned long long valid = 0ull;
-    for (int it = 0; it < kMaxRansacIters; ++it)
+    for (int base = 0; base < kMaxRansacIters; base += 32)
     {
-        const uint32_t i2 = gen.bounded(N);
-        uint32_t i3 = gen.bounded(N);
-        int guard = 0;
-        while (i3 == i2 && guard < (1 << 20))
+        const int it = base + static_cast<int>(lane);
+        bool ok = false;
+        if (it < kMaxRansacIters)
         {
-            i3 = gen.bounded(N);
-            ++guard;
-        }
-        if (guard >= (1 << 20))
-        {
-            raise_err(&st, ERR_INTERNAL);
-            return;
-        }
-        const float4 p2 = b.cand[first + i2];
-        const float4 p3 = b.cand[first + i3];
-        float nx = ((p2.y - p1y) * (p3.z - p1z)) - ((p2.z - p1z) * (p3.y - p1y));
-        float ny = ((p2.z - p1z) * (p3.x - p1x)) - ((p2.x - p1x) * (p3.z - p1z));
-        float nz = ((p2.x - p1x) * (p3.y - p1y)) - ((p2.y - p1y) * (p3.x - p1x));
-        const float den = (nx * nx) + (ny * ny) + (nz * nz);
-        float4 pl = make_float4(0, 0, 0, 0);
-        if (!(den < 1.0e-5F))
-        {
-            const float norm = 1.0F / sqrtf(den);
-            nz *= norm;
-            if (!(fabsf(nz) < sd.max_cos))
+            const float4 p2 = b.cand[first + di2[it]];
+            const float4 p3 = b.cand[first + di3[it]];
+            float nx = ((p2.y - p1y) * (p3.z - p1z)) - ((p2.z - p1z) * (p3.y - p1y));
+            float ny = ((p2.z - p1z) * (p3.x - p1x)) - ((p2.x - p1x) * (p3.z - p1z));
+            float nz = ((p2.x - p1x) * (p3.y - p1y)) - ((p2.y - p1y) * (p3.x - p1x));
+            const float den = (nx * nx) + (ny * ny) + (nz * nz);
+            float4 pl = make_float4(0, 0, 0, 0);
+            if (!(den < 1.0e-5F))
             {
-                nx *= norm;
-                ny *= norm;
-                const float pd = (nx * p1x) + (ny * p1y) + (nz * p1z);
-                pl = make_float4(nx, ny, nz, pd);
-                valid |= (1ull << it);
+                const float norm = 1.0F / sqrtf(den);
+                nz *= norm;
+                if (!(fabsf(nz) < sd.max_cos))
+                {
+                    nx *= norm;
+                    ny *= norm;
+                    const float pd = (nx * p1x) + (ny * p1y) + (nz * p1z);
+                    pl = make_float4(nx, ny, nz, pd);
+                    ok = true;
+                }
             }
+            b.planes[s * kMaxRansacIters + it] = pl;
+            b.inliers[s * kMaxRansacIters + it] = 0u;
         }
-        b.planes[s * kMaxRansacIters + it] = pl;
-        b.inliers[s * kMaxRansacIters + it] = 0u;
+        valid |= static_cast<unsigned long long>(__ballot_sync(0xffffffffu, ok)) << base;
     }
-    b.pvalid[s] = valid;
+    if (lane == 0)
+        b.pvalid[s] = valid;
 }
 
 // Inlier counts of every hypothesis plane of a scan (segmenter.cpp:409-430): lane l of every
@@ -1799,7 +1828,7 @@ void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, ui
     LP_LAUNCH(L, k_near, div_up(b.nnear * 32u, 256u), 256, b, 0);
     L.scan(b.near_cnt, b.near_start, b.nnear + 1); // near_cnt[nnear] == 0: last entry is the total
     LP_LAUNCH(L, k_near, div_up(b.nnear * 32u, 256u), 256, b, 1);
-    LP_LAUNCH(L, k_ransac_draw, div_up(static_cast<uint32_t>(b.nscan), 64u), 64, b);
+    LP_LAUNCH(L, k_ransac_draw, static_cast<uint32_t>(b.nscan), 32, b);
     LP_LAUNCH2D(L, k_ransac_inliers, dim3(16, static_cast<uint32_t>(b.nscan)), 256, b);
     LP_LAUNCH(L, k_ransac_select, div_up(static_cast<uint32_t>(b.nscan), 64u), 64, b);
     LP_LAUNCH(L, k_label_depth, div_up(b.npts, T), T, b);
