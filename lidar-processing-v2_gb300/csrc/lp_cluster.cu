@@ -70,13 +70,15 @@ __global__ void k_obs_state(BatchDev b)
 __global__ void k_obs_gather(BatchDev b)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < b.npts && b.seg_label[i] == LP_LABEL_OBSTACLE;
+    // the point and its slot are loaded before the label test and the scan lookup
+    const bool in = i < b.npts;
+    const float4 p = in ? b.pts[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const uint32_t o = in ? b.obs_flag[i] : 0u;
+    const bool valid = in && b.seg_label[i] == LP_LABEL_OBSTACLE;
     const int s = valid ? scan_of_point(b, i) : -1;
     uint32_t rb = 0u, ab = 0u, eb = 0u;
     if (valid)
     {
-        const uint32_t o = b.obs_flag[i];
-        const float4 p = b.pts[i];
         b.obs_pts[o] = p;
         b.obs_pt[o] = static_cast<int32_t>(i);
         float az = lpm::cr_atan2f(p.y, p.x);

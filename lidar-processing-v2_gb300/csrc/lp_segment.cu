@@ -146,13 +146,12 @@ __global__ void __launch_bounds__(256) k_ring_apply(BatchDev b)
 // ------------------------------------------------------------------------------------------
 // Polar grid (constructPolarGrid, segmenter.cpp:103-204).
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ int32_t bin_point(const BatchDev& b, uint32_t i)
+__device__ __forceinline__ int32_t bin_point(const BatchDev& b, uint32_t i, const float4 p)
 {
     const int s = scan_of_point(b, i);
     const ScanDev& sd = b.scans[s];
     if (i - sd.pt_off >= b.state[s].n_pts)
         return -1; // slot left empty by noise removal
-    const float4 p = b.pts[i];
     if (p.z < sd.zmin_adj || p.z > sd.zmax_adj)
         return -1;
     const float d = sqrtf(p.x * p.x + p.y * p.y);
@@ -181,30 +180,46 @@ __device__ __forceinline__ int32_t bin_point(const BatchDev& b, uint32_t i)
     return static_cast<int32_t>(sd.cell_off + static_cast<uint32_t>(slice * sd.nrad + radial));
 }
 
+// Two points per thread (i and i + blockDim.x), both loaded before either is binned. Each
+// aggregated slot increment covers 32 consecutive points of one warp: a cell's slots come in
+// index runs of one 32-point window each (the near-cell ordering relies on it, and checks it).
 __global__ void k_bin(BatchDev b)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int32_t cell = (i < b.npts) ? bin_point(b, i) : -1;
-    if (i < b.npts)
-        b.pt_cell[i] = cell;
-    // slot of the point in its cell (the order within a cell is free: cells are sorted later)
-    const uint32_t slot = warp_aggregated_inc(b.cell_cnt, static_cast<uint32_t>(cell), cell >= 0);
-    if (cell >= 0)
-        b.pt_slot[i] = slot;
+    const uint32_t i0 = blockIdx.x * blockDim.x * 2u + threadIdx.x;
+    const uint32_t i1 = i0 + blockDim.x;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 p0 = (i0 < b.npts) ? b.pts[i0] : z4;
+    const float4 p1 = (i1 < b.npts) ? b.pts[i1] : z4;
+    const int32_t c0 = (i0 < b.npts) ? bin_point(b, i0, p0) : -1;
+    const int32_t c1 = (i1 < b.npts) ? bin_point(b, i1, p1) : -1;
+    if (i0 < b.npts)
+        b.pt_cell[i0] = c0;
+    if (i1 < b.npts)
+        b.pt_cell[i1] = c1;
+    // slot of the point in its cell (the order within a cell is free: near cells are ordered later)
+    const uint32_t s0 = warp_aggregated_inc(b.cell_cnt, static_cast<uint32_t>(c0), c0 >= 0);
+    const uint32_t s1 = warp_aggregated_inc(b.cell_cnt, static_cast<uint32_t>(c1), c1 >= 0);
+    if (c0 >= 0)
+        b.pt_slot[i0] = s0;
+    if (c1 >= 0)
+        b.pt_slot[i1] = s1;
 }
 
+// (the per-point loads are issued before the scan lookup and the branch, which they do not need)
 __global__ void k_scatter(BatchDev b)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= b.npts)
         return;
     const int32_t c = b.pt_cell[i];
+    const uint32_t slot = b.pt_slot[i];
+    const float z = b.pts[i].z;
     if (c < 0)
         return;
     const int s = scan_of_point(b, i);
-    const uint32_t pos = b.cell_start[c] + b.pt_slot[i];
+    const uint32_t pos = b.cell_start[c] + slot;
     b.csr_idx[pos] = static_cast<int32_t>(i - b.scans[s].pt_off);
-    b.csr_z[pos] = b.pts[i].z;
+    b.csr_z[pos] = z;
 }
 
 // zlow of a cell (segmenter.cpp:249-260): with the cell's heights sorted, z[k] for the largest k
@@ -918,12 +933,13 @@ __global__ void k_label_depth(BatchDev b)
     if (i >= b.npts)
         return;
     const int32_t c = b.pt_cell[i];
+    const float4 p = b.pts[i];
+    const int32_t pix = b.pt_pix[i];
     if (c < 0)
         return;
     const int s = scan_of_point(b, i);
     const ScanDev& sd = b.scans[s];
     const ScanState& st = b.state[s];
-    const float4 p = b.pts[i];
     uint8_t lbl = (p.z >= b.elev[c] + sd.thr) ? LP_LABEL_OBSTACLE : LP_LABEL_GROUND;
     const int32_t radial = static_cast<int32_t>((static_cast<uint32_t>(c) - sd.cell_off) % static_cast<uint32_t>(sd.nrad));
     if (radial < kRansacRadialBins && st.ransac_ok)
@@ -934,7 +950,7 @@ __global__ void k_label_depth(BatchDev b)
     }
     b.pt_label[i] = lbl;
     const float d2 = (p.x * p.x) + (p.y * p.y);
-    atomicMin(&b.pix_depth[sd.pix_off + static_cast<uint32_t>(b.pt_pix[i])], __float_as_uint(d2));
+    atomicMin(&b.pix_depth[sd.pix_off + static_cast<uint32_t>(pix)], __float_as_uint(d2));
 }
 
 __global__ void k_project_key(BatchDev b)
@@ -943,13 +959,14 @@ __global__ void k_project_key(BatchDev b)
     if (i >= b.npts)
         return;
     const int32_t c = b.pt_cell[i];
+    const float4 p = b.pts[i];
+    const int32_t lpix = b.pt_pix[i];
     if (c < 0)
         return;
     const int s = scan_of_point(b, i);
     const ScanDev& sd = b.scans[s];
-    const float4 p = b.pts[i];
     const float d2 = (p.x * p.x) + (p.y * p.y);
-    const uint32_t pix = sd.pix_off + static_cast<uint32_t>(b.pt_pix[i]);
+    const uint32_t pix = sd.pix_off + static_cast<uint32_t>(lpix);
     if (__float_as_uint(d2) != b.pix_depth[pix])
         return;
     const unsigned long long key = (static_cast<unsigned long long>(static_cast<uint32_t>(c) - sd.cell_off) << 32) |
@@ -1819,7 +1836,7 @@ void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, ui
     const uint32_t T = 256;
     if (hb.any_compute_ring)
         launch_ring_only(L, b, hb);
-    LP_LAUNCH(L, k_bin, div_up(b.npts, T), T, b);
+    LP_LAUNCH(L, k_bin, div_up(b.npts, 2u * T), T, b);
     L.scan(b.cell_cnt, b.cell_start, b.ncell + 1);
     LP_LAUNCH(L, k_scatter, div_up(b.npts, T), T, b);
     LP_LAUNCH(L, k_cell_small, std::min(div_up(b.ncell, 256u), static_cast<uint32_t>(sm_count()) * 8u), 256, b);
