@@ -66,55 +66,82 @@ __global__ void k_obs_state(BatchDev b)
 }
 
 // Obstacle cloud in input order (processor.cpp:562-579) with the spherical coordinates of
-// Clusterer::cartesianToSpherical (clusterer.cpp:55-100).
-__global__ void k_obs_gather(BatchDev b)
+// Clusterer::cartesianToSpherical (clusterer.cpp:55-100). A block takes 1024 consecutive points
+// and first compacts its obstacle points in shared memory, so that every lane of the arithmetic
+// below (two correctly rounded arctangents) has one.
+constexpr uint32_t kObsChunk = 1024;
+
+__global__ void __launch_bounds__(256) k_obs_gather(BatchDev b)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    // the point and its slot are loaded before the label test and the scan lookup
-    const bool in = i < b.npts;
-    const float4 p = in ? b.pts[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const uint32_t o = in ? b.obs_flag[i] : 0u;
-    const bool valid = in && b.seg_label[i] == LP_LABEL_OBSTACLE;
-    const int s = valid ? scan_of_point(b, i) : -1;
-    uint32_t rb = 0u, ab = 0u, eb = 0u;
-    if (valid)
+    __shared__ uint32_t sidx[kObsChunk];
+    __shared__ uint32_t scnt;
+    const uint32_t base = blockIdx.x * kObsChunk;
+    if (threadIdx.x == 0)
+        scnt = 0u;
+    __syncthreads();
+#pragma unroll
+    for (uint32_t u = 0; u < kObsChunk / 256u; ++u)
     {
-        b.obs_pts[o] = p;
-        b.obs_pt[o] = static_cast<int32_t>(i);
-        float az = lpm::cr_atan2f(p.y, p.x);
-        az = (az < 0) ? (az + kTwoPiF) : az;
-        const float d2 = p.x * p.x + p.y * p.y;
-        const float d = sqrtf(d2);
-        const float r = sqrtf(d2 + p.z * p.z);
-        const float el = lpm::cr_atanf(p.z / d) + kPi2F;
-        b.obs_r[o] = r;
-        b.obs_a[o] = az;
-        b.obs_e[o] = el;
-        rb = r > 0.0f ? __float_as_uint(r) : 0u; // non-negative floats order like their bits
-        ab = az > 0.0f ? __float_as_uint(az) : 0u;
-        eb = el > 0.0f ? __float_as_uint(el) : 0u;
+        const uint32_t i = base + u * 256u + threadIdx.x;
+        const bool valid = i < b.npts && b.seg_label[i] == LP_LABEL_OBSTACLE;
+        const uint32_t m = __ballot_sync(0xffffffffu, valid);
+        uint32_t pos = 0u;
+        if (lane_id() == 0 && m)
+            pos = atomicAdd(&scnt, static_cast<uint32_t>(__popc(m)));
+        pos = __shfl_sync(0xffffffffu, pos, 0);
+        if (valid)
+            sidx[pos + static_cast<uint32_t>(__popc(m & ((1u << lane_id()) - 1u)))] = i;
     }
-    // one atomic per warp when the warp's obstacle points belong to a single scan
-    const int smax = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(s + 1))) - 1;
-    if (__all_sync(0xffffffffu, s == smax || s < 0))
+    __syncthreads();
+    const uint32_t cnt = scnt;
+    for (uint32_t k0 = 0; k0 < cnt; k0 += 256u)
     {
-        rb = __reduce_max_sync(0xffffffffu, rb);
-        ab = __reduce_max_sync(0xffffffffu, ab);
-        eb = __reduce_max_sync(0xffffffffu, eb);
-        if (lane_id() == 0 && smax >= 0)
+        const uint32_t k = k0 + threadIdx.x;
+        const bool valid = k < cnt;
+        const uint32_t i = valid ? sidx[k] : 0u;
+        const int s = valid ? scan_of_point(b, i) : -1;
+        uint32_t rb = 0u, ab = 0u, eb = 0u;
+        if (valid)
         {
-            ScanState& st = b.state[smax];
+            const uint32_t o = b.obs_flag[i];
+            const float4 p = b.pts[i];
+            b.obs_pts[o] = p;
+            b.obs_pt[o] = static_cast<int32_t>(i);
+            float az = lpm::cr_atan2f(p.y, p.x);
+            az = (az < 0) ? (az + kTwoPiF) : az;
+            const float d2 = p.x * p.x + p.y * p.y;
+            const float d = sqrtf(d2);
+            const float r = sqrtf(d2 + p.z * p.z);
+            const float el = lpm::cr_atanf(p.z / d) + kPi2F;
+            b.obs_r[o] = r;
+            b.obs_a[o] = az;
+            b.obs_e[o] = el;
+            rb = r > 0.0f ? __float_as_uint(r) : 0u; // non-negative floats order like their bits
+            ab = az > 0.0f ? __float_as_uint(az) : 0u;
+            eb = el > 0.0f ? __float_as_uint(el) : 0u;
+        }
+        // one atomic per warp when the warp's obstacle points belong to a single scan
+        const int smax = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(s + 1))) - 1;
+        if (__all_sync(0xffffffffu, s == smax || s < 0))
+        {
+            rb = __reduce_max_sync(0xffffffffu, rb);
+            ab = __reduce_max_sync(0xffffffffu, ab);
+            eb = __reduce_max_sync(0xffffffffu, eb);
+            if (lane_id() == 0 && smax >= 0)
+            {
+                ScanState& st = b.state[smax];
+                atomicMax(&st.max_r_bits, rb);
+                atomicMax(&st.max_a_bits, ab);
+                atomicMax(&st.max_e_bits, eb);
+            }
+        }
+        else if (valid)
+        {
+            ScanState& st = b.state[s];
             atomicMax(&st.max_r_bits, rb);
             atomicMax(&st.max_a_bits, ab);
             atomicMax(&st.max_e_bits, eb);
         }
-    }
-    else if (valid)
-    {
-        ScanState& st = b.state[s];
-        atomicMax(&st.max_r_bits, rb);
-        atomicMax(&st.max_a_bits, ab);
-        atomicMax(&st.max_e_bits, eb);
     }
 }
 
@@ -493,7 +520,7 @@ void launch_clustering(Launcher& L, const BatchDev& b, const BatchHost& hb)
     LP_LAUNCH(L, k_obs_flag, div_up(b.npts + 1, T), T, b);
     L.scan(b.obs_flag, b.obs_flag, b.npts + 1);
     LP_LAUNCH(L, k_obs_state, div_up(ns, 64u), 64, b);
-    LP_LAUNCH(L, k_obs_gather, div_up(b.npts, T), T, b);
+    LP_LAUNCH(L, k_obs_gather, div_up(b.npts, kObsChunk), 256, b);
     LP_LAUNCH(L, k_dims, div_up(ns, 64u), 64, b);
     LP_LAUNCH(L, k_vox_insert, div_up(b.npts, T), T, b);
     L.begin("k_vox_ids");
