@@ -354,8 +354,9 @@ struct RunScratch
 // the warps), the runs are ordered by their first index (a sort of r keys instead of n), and every
 // run moves as a block. The result is checked: when one run's last index is not below the next
 // run's first, the ranges overlap and the whole list is sorted instead. `is` holds n rounded up
-// to a power of two entries, `key` as many.
-__device__ __forceinline__ void warp_order_near(int32_t* csr, uint32_t n, uint32_t wofs, int32_t* is, uint32_t* key, RunScratch& rsc)
+// to a power of two entries, `key` as many. The heights cz (csr_z) are permuted alongside.
+__device__ __forceinline__ void warp_order_near(int32_t* csr, float* cz, const float4* pts, uint32_t n, uint32_t wofs,
+                                                int32_t* is, float* zb, uint32_t* key, RunScratch& rsc)
 {
     const uint32_t lane = lane_id();
     const uint32_t lt = (1u << lane) - 1u;
@@ -366,6 +367,7 @@ __device__ __forceinline__ void warp_order_near(int32_t* csr, uint32_t n, uint32
         const uint32_t k = base + lane;
         const int32_t v = (k < n) ? csr[k] : INT32_MAX;
         is[k] = v;
+        zb[k] = (k < n) ? cz[k] : 0.0F;
         int32_t up = __shfl_up_sync(0xffffffffu, v, 1);
         if (lane == 0)
             up = prev;
@@ -454,7 +456,10 @@ __device__ __forceinline__ void warp_order_near(int32_t* csr, uint32_t n, uint32
         __syncwarp();
         warp_bitonic_smem(is, np2, [](int32_t a, int32_t bb) { return a < bb; });
         for (uint32_t k = lane; k < n; k += 32)
+        {
             csr[k] = is[k];
+            cz[k] = pts[is[k]].z; // the height follows its index
+        }
         __syncwarp();
         return;
     }
@@ -467,7 +472,9 @@ __device__ __forceinline__ void warp_order_near(int32_t* csr, uint32_t n, uint32
         if (k < n)
         {
             const uint32_t rid = seen + __popc(hm & (lt | (1u << lane))) - 1u;
-            csr[rsc.rd[rid] + (k - rsc.rs[rid])] = is[k];
+            const uint32_t dst = rsc.rd[rid] + (k - rsc.rs[rid]);
+            csr[dst] = is[k];
+            cz[dst] = zb[k];
         }
         seen += __popc(hm);
     }
@@ -475,7 +482,7 @@ __device__ __forceinline__ void warp_order_near(int32_t* csr, uint32_t n, uint32
 }
 
 __device__ __forceinline__ void cell_small_one(const BatchDev& b, uint32_t c, uint32_t n, uint32_t start, float* zs,
-                                               int32_t* is, RunScratch& rsc)
+                                               int32_t* is, float* zb, RunScratch& rsc)
 {
     const uint32_t lane = lane_id();
     const int s = scan_of_cell(b, c);
@@ -501,13 +508,34 @@ __device__ __forceinline__ void cell_small_one(const BatchDev& b, uint32_t c, ui
         return;
     if (n > kSmallCell)
     {
-        warp_order_near(b.csr_idx + start, n, sd.pt_off & 31u, is, reinterpret_cast<uint32_t*>(zs), rsc);
+        warp_order_near(b.csr_idx + start, b.csr_z + start, b.pts + sd.pt_off, n, sd.pt_off & 31u, is, zb,
+                        reinterpret_cast<uint32_t*>(zs), rsc);
         return;
     }
+    // (index, height) pairs sorted by index in registers
     int32_t idx = (lane < n) ? b.csr_idx[start + lane] : INT32_MAX;
-    idx = warp_bitonic_sort(idx, [](int32_t a, int32_t bb) { return a < bb; });
+    float zv = (lane < n) ? b.csr_z[start + lane] : 0.0F;
+#pragma unroll
+    for (uint32_t k = 2; k <= 32; k <<= 1)
+    {
+#pragma unroll
+        for (uint32_t j = k >> 1; j > 0; j >>= 1)
+        {
+            const int32_t oi = __shfl_xor_sync(0xffffffffu, idx, j);
+            const float oz = __shfl_xor_sync(0xffffffffu, zv, j);
+            const bool up = ((lane & k) == 0), lower = ((lane & j) == 0);
+            if ((lower == up) ? (oi < idx) : (idx < oi))
+            {
+                idx = oi;
+                zv = oz;
+            }
+        }
+    }
     if (lane < n)
+    {
         b.csr_idx[start + lane] = idx;
+        b.csr_z[start + lane] = zv;
+    }
 }
 
 __global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
@@ -515,6 +543,7 @@ __global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
     __shared__ float wz[8][kMediumCell];
     __shared__ int32_t wi[8][kMediumCell];
     __shared__ RunScratch wr[8];
+    __shared__ float wzb[8][kMediumCell];
     const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     // 32 consecutive cells per warp step: one coalesced read of their counts, then only the
@@ -530,7 +559,7 @@ __global__ void __launch_bounds__(256) k_cell_small(BatchDev b)
             const int j = __ffs(m) - 1;
             m &= m - 1u;
             cell_small_one(b, c0 + static_cast<uint32_t>(j), __shfl_sync(0xffffffffu, cnt, j),
-                           __shfl_sync(0xffffffffu, st, j), wz[warp], wi[warp], wr[warp]);
+                           __shfl_sync(0xffffffffu, st, j), wz[warp], wi[warp], wzb[warp], wr[warp]);
         }
     }
 }
@@ -585,7 +614,10 @@ __global__ void __launch_bounds__(512) k_cell_large(BatchDev b)
             __syncthreads();
             block_bitonic_sort(si, np2, [](int32_t a, int32_t bb) { return a < bb; });
             for (uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+            {
                 b.csr_idx[start + k] = si[k];
+                b.csr_z[start + k] = b.pts[sd.pt_off + static_cast<uint32_t>(si[k])].z; // the height follows its index
+            }
         }
         __syncthreads();
     }
@@ -649,16 +681,14 @@ __global__ void __launch_bounds__(256) k_near(BatchDev b, int write)
     for (uint32_t base = 0; base < n; base += 32)
     {
         const uint32_t k = base + lane;
-        bool pred = false;
-        float4 p = make_float4(0, 0, 0, 0);
-        if (k < n)
-        {
-            p = b.pts[sd.pt_off + static_cast<uint32_t>(b.csr_idx[start + k])];
-            pred = fabsf(e - p.z) < lim;
-        }
+        // csr_z holds the near cells' heights in index order (permuted with csr_idx)
+        const bool pred = k < n && fabsf(e - b.csr_z[start + k]) < lim;
         const uint32_t m = __ballot_sync(0xffffffffu, pred);
         if (write && pred)
+        {
+            const float4 p = b.pts[sd.pt_off + static_cast<uint32_t>(b.csr_idx[start + k])];
             b.cand[pos + __popc(m & ((1u << lane) - 1u))] = make_float4(p.x, p.y, p.z, 0.0f);
+        }
         pos += __popc(m);
     }
     if (!write && lane == 0)
