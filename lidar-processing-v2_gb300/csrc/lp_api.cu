@@ -724,15 +724,19 @@ lp_status run_direct(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
     const size_t S = B.run.scans.size();
     const bool hull = B.run.stages & ST_HULL, obb = B.run.stages & ST_OBB;
     std::vector<IoScan> io(S);
+    uint32_t nq = 0; // 4-point chunks of the batch
+    auto aligned = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; };
     for (size_t s = 0; s < S; ++s)
     {
         const ScanIn& in = B.run.scans[s];
         const lp_scan_output& o = outs[s];
+        const uint32_t vec = aligned(o.noise_labels, 4) && aligned(o.seg_labels, 16) && aligned(o.cluster_labels, 16);
         io[s] = IoScan{in.xyzi, in.ring, o.noise_labels, o.seg_labels, o.cluster_labels,
                        hull ? o.hull_offsets : nullptr, hull ? o.hull_indices : nullptr,
                        hull ? o.z_min : nullptr, hull ? o.z_max : nullptr,
                        obb ? o.obb_calipers : nullptr, obb ? o.obb_pca : nullptr,
-                       o.cluster_capacity, o.hull_capacity};
+                       o.cluster_capacity, o.hull_capacity, nq, vec};
+        nq += (in.n + 3u) / 4u;
     }
     LP_CUDA(ctx, cudaMemcpyAsync(const_cast<ScanDev*>(b.scans), B.hb.scans.data(), S * sizeof(ScanDev),
                                  cudaMemcpyHostToDevice, st));
@@ -744,7 +748,7 @@ lp_status run_direct(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
     if (L.err != cudaSuccess)
         return cuda_fail(ctx, L.err, "direct input launch");
     LP_TRY(execute(ctx, B));
-    launch_io_out(L, b, b.io, b.io_ret, hull ? 1 : 0, obb ? 1 : 0);
+    launch_io_out(L, b, b.io, b.io_ret, hull ? 1 : 0, obb ? 1 : 0, nq);
     if (L.err != cudaSuccess)
         return cuda_fail(ctx, L.err, "direct output launch");
     std::vector<uint32_t> nh(S, 0u);

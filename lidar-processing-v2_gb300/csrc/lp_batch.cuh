@@ -69,6 +69,8 @@ struct IoScan
     lp_bounding_box* obbc;
     lp_bounding_box* obbp;
     uint32_t cluster_cap, hull_cap;
+    uint32_t q_off; // first 4-point chunk of the scan in the batch's chunk list
+    uint32_t vec;   // 1: the label buffers allow 4-point vector stores (4 B noise, 16 B seg and cluster)
 };
 
 struct BatchDev

@@ -27,24 +27,59 @@ __global__ void k_io_in(BatchDev b, const IoScan* io)
         const_cast<uint16_t*>(b.ring_in)[i] = d.ring[k];
 }
 
-// Per-point labels of every scan into the caller's buffers.
-__global__ void k_io_out_points(BatchDev b, const IoScan* io)
+// Per-point labels of every scan into the caller's buffers, four consecutive points per thread
+// (chunk q of the batch: scan s with io[s].q_off <= q, points 4 (q - q_off) ..): the host link
+// takes whole 16-byte stores (4 B of noise labels, 16 B of segmentation and of cluster labels)
+// where the caller's buffers are aligned for them, and one store per label otherwise.
+__global__ void k_io_out_points(BatchDev b, const IoScan* io, uint32_t nq)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.nsrc)
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq)
         return;
-    const int s = find_scan(b.nscan, i, [&](int q) { return b.scans[q].src_off; });
+    const int s = find_scan(b.nscan, q, [&](int t) { return io[t].q_off; });
     const ScanDev& sd = b.scans[s];
-    const uint32_t k = i - sd.src_off;
-    if (k >= sd.n_src)
-        return;
     const IoScan& d = io[s];
-    if (d.noise)
-        d.noise[k] = b.noise[i];
-    if (d.seg)
-        d.seg[k] = b.out_seg[i];
-    if (d.cl)
-        d.cl[k] = static_cast<int32_t>(b.out_cl[i]);
+    const uint32_t k0 = 4u * (q - d.q_off);
+    if (k0 >= sd.n_src)
+        return;
+    const uint32_t i0 = sd.src_off + k0;
+    const uint32_t cnt = min(4u, sd.n_src - k0);
+    uint8_t nz[4] = {0, 0, 0, 0};
+    uint32_t sg[4] = {0, 0, 0, 0};
+    int32_t cl[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (uint32_t u = 0; u < 4; ++u)
+        if (u < cnt)
+        {
+            // a device array is read only when the caller asked for it (stages may not produce it)
+            if (d.noise)
+                nz[u] = b.noise[i0 + u];
+            if (d.seg)
+                sg[u] = b.out_seg[i0 + u];
+            if (d.cl)
+                cl[u] = static_cast<int32_t>(b.out_cl[i0 + u]);
+        }
+    if (d.vec && cnt == 4u)
+    {
+        if (d.noise)
+            *reinterpret_cast<uint32_t*>(d.noise + k0) =
+                static_cast<uint32_t>(nz[0]) | (static_cast<uint32_t>(nz[1]) << 8) |
+                (static_cast<uint32_t>(nz[2]) << 16) | (static_cast<uint32_t>(nz[3]) << 24);
+        if (d.seg)
+            *reinterpret_cast<uint4*>(d.seg + k0) = make_uint4(sg[0], sg[1], sg[2], sg[3]);
+        if (d.cl)
+            *reinterpret_cast<int4*>(d.cl + k0) = make_int4(cl[0], cl[1], cl[2], cl[3]);
+        return;
+    }
+    for (uint32_t u = 0; u < cnt; ++u)
+    {
+        if (d.noise)
+            d.noise[k0 + u] = nz[u];
+        if (d.seg)
+            d.seg[k0 + u] = sg[u];
+        if (d.cl)
+            d.cl[k0 + u] = cl[u];
+    }
 }
 
 // Per-cluster results: hull offsets (relative to the scan), hull indices, z range, boxes. A scan
@@ -95,9 +130,10 @@ void launch_io_in(Launcher& L, const BatchDev& b, const IoScan* io)
     LP_LAUNCH(L, k_io_in, div_up(b.nsrc, 256u), 256, b, io);
 }
 
-void launch_io_out(Launcher& L, const BatchDev& b, const IoScan* io, uint32_t* ret, int with_hull, int with_obb)
+void launch_io_out(Launcher& L, const BatchDev& b, const IoScan* io, uint32_t* ret, int with_hull, int with_obb,
+                   uint32_t nq)
 {
-    LP_LAUNCH(L, k_io_out_points, div_up(b.nsrc, 256u), 256, b, io);
+    LP_LAUNCH(L, k_io_out_points, div_up(nq, 256u), 256, b, io, nq);
     if (with_hull)
         LP_LAUNCH(L, k_io_out_clusters, div_up(b.ncl, 256u), 256, b, io, ret, with_obb);
 }

@@ -117,7 +117,8 @@ struct Launcher
 void init_kernel_attributes();
 // Direct host I/O (lp_io.cu): inputs from and results into the caller's page-locked buffers.
 void launch_io_in(Launcher& L, const BatchDev& b, const IoScan* io);
-void launch_io_out(Launcher& L, const BatchDev& b, const IoScan* io, uint32_t* ret, int with_hull, int with_obb);
+void launch_io_out(Launcher& L, const BatchDev& b, const IoScan* io, uint32_t* ret, int with_hull, int with_obb,
+                   uint32_t nq);
 void init_segment_tables(); // per-device constant tables (the seed-42 MT19937 stream)
 // Streaming multiprocessors of the current device (persistent grids are sized by it).
 int sm_count();
