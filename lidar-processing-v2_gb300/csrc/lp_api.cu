@@ -407,7 +407,7 @@ lp_status execute(lp_context* ctx, lp_batch& B)
 {
     BatchDev& b = B.b;
     const Run& R = B.run;
-    const cudaStream_t st = ctx->stream;
+    const cudaStream_t st = B.stream ? B.stream : ctx->stream;
     Launcher L;
     L.stream = st;
     L.launches = &ctx->launches;
@@ -541,7 +541,38 @@ void destroy_batch(lp_batch* B)
         cudaGraphExecDestroy(B->graph);
     if (B->mem)
         cudaFree(B->mem);
+    for (lp_batch* P : B->parts)
+        destroy_batch(P);
+    for (cudaEvent_t e : B->fork_join)
+        cudaEventDestroy(e);
+    if (B->stream)
+        cudaStreamDestroy(B->stream);
     delete B;
+}
+
+// Parts a batch of n scans is split into: one below 16 scans, then one per 8 scans, at most 4.
+uint32_t split_parts(uint32_t n)
+{
+    return n < 16u ? 1u : std::min(4u, n / 8u);
+}
+
+// Launches a batch: a split batch forks its parts' streams from the context stream, launches every
+// part on its own stream and joins them back (also the shape a graph capture records).
+lp_status launch_batch(lp_context* ctx, lp_batch& B)
+{
+    if (B.parts.empty())
+        return execute(ctx, B);
+    LP_CUDA(ctx, cudaEventRecord(B.fork_join[0], ctx->stream));
+    for (size_t k = 0; k < B.parts.size(); ++k)
+    {
+        lp_batch& P = *B.parts[k];
+        LP_CUDA(ctx, cudaStreamWaitEvent(P.stream, B.fork_join[0], 0));
+        LP_TRY(execute(ctx, P));
+        LP_CUDA(ctx, cudaEventRecord(B.fork_join[1 + k], P.stream));
+    }
+    for (size_t k = 0; k < B.parts.size(); ++k)
+        LP_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, B.fork_join[1 + k], 0));
+    return LP_OK;
 }
 
 lp_status run_once(lp_context* ctx, lp_batch& B)
@@ -1175,13 +1206,47 @@ lp_status lp_batch_create(lp_context* ctx, const lp_pipeline_config* cfg, const 
     *out = nullptr;
     LP_TRY(ensure_device(ctx));
     lp_batch* B = new lp_batch();
-    lp_status st = fill_pipeline(ctx, *B, cfg, scans, nscans);
-    if (st == LP_OK)
-        st = build(ctx, *B);
-    if (st == LP_OK)
-        st = upload(ctx, *B);
+    const uint32_t K = split_parts(nscans);
+    lp_status st = LP_OK;
+    if (K == 1)
+    {
+        st = fill_pipeline(ctx, *B, cfg, scans, nscans);
+        if (st == LP_OK)
+            st = build(ctx, *B);
+        if (st == LP_OK)
+            st = upload(ctx, *B);
+    }
+    else
+    {
+        // scans dealt round-robin, so every part gets a similar mix of scan sizes
+        for (uint32_t k = 0; k < K && st == LP_OK; ++k)
+        {
+            std::vector<lp_scan_input> sub;
+            for (uint32_t i = k; i < nscans; i += K)
+                sub.push_back(scans[i]);
+            lp_batch* P = new lp_batch();
+            B->parts.push_back(P);
+            if (cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking) != cudaSuccess)
+                st = fail(ctx, LP_ERR_CUDA, "cudaStreamCreateWithFlags");
+            if (st == LP_OK)
+                st = fill_pipeline(ctx, *P, cfg, sub.data(), static_cast<uint32_t>(sub.size()));
+            if (st == LP_OK)
+                st = build(ctx, *P);
+            if (st == LP_OK)
+                st = upload(ctx, *P);
+        }
+        for (uint32_t k = 0; k <= K && st == LP_OK; ++k)
+        {
+            cudaEvent_t e;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                st = fail(ctx, LP_ERR_CUDA, "cudaEventCreateWithFlags");
+            else
+                B->fork_join.push_back(e);
+        }
+    }
     if (st != LP_OK)
     {
+        cudaStreamSynchronize(ctx->stream);
         destroy_batch(B);
         return st;
     }
@@ -1203,7 +1268,11 @@ lp_status lp_batch_upload(lp_context* ctx, lp_batch* B)
 {
     if (!ctx || !B)
         return LP_ERR_BAD_ARG;
-    return upload(ctx, *B);
+    if (B->parts.empty())
+        return upload(ctx, *B);
+    for (lp_batch* P : B->parts)
+        LP_TRY(upload(ctx, *P));
+    return LP_OK;
 }
 
 lp_status lp_batch_execute(lp_context* ctx, lp_batch* B)
@@ -1216,7 +1285,7 @@ lp_status lp_batch_execute(lp_context* ctx, lp_batch* B)
         ctx->launches += 1;
         return LP_OK;
     }
-    return execute(ctx, *B);
+    return launch_batch(ctx, *B);
 }
 
 lp_status lp_batch_capture_graph(lp_context* ctx, lp_batch* B)
@@ -1229,7 +1298,7 @@ lp_status lp_batch_capture_graph(lp_context* ctx, lp_batch* B)
     cudaGraph_t g;
     LP_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     const uint64_t before = ctx->launches;
-    const lp_status st = execute(ctx, *B);
+    const lp_status st = launch_batch(ctx, *B);
     const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     ctx->launches = before;
     if (st != LP_OK)
@@ -1247,6 +1316,25 @@ lp_status lp_batch_download(lp_context* ctx, lp_batch* B, lp_scan_output* outs)
 {
     if (!ctx || !B || !outs)
         return LP_ERR_BAD_ARG;
+    if (!B->parts.empty())
+    {
+        // each part's scans in their batch order; a part's status is that of its worst scan
+        const size_t K = B->parts.size();
+        lp_status worst = LP_OK;
+        for (size_t k = 0; k < K; ++k)
+        {
+            const size_t S = B->parts[k]->run.scans.size();
+            std::vector<lp_scan_output> sub(S);
+            for (size_t j = 0; j < S; ++j)
+                sub[j] = outs[j * K + k];
+            const lp_status st = lp_batch_download(ctx, B->parts[k], sub.data());
+            for (size_t j = 0; j < S; ++j)
+                outs[j * K + k] = sub[j];
+            if (st != LP_OK && (worst == LP_OK || worst == LP_ERR_CAPACITY))
+                worst = st;
+        }
+        return worst;
+    }
     const lp_status st = fetch_state(ctx, *B);
     if (st != LP_OK && st != LP_ERR_CAPACITY)
         return st;
@@ -1264,12 +1352,22 @@ lp_status lp_context_synchronize(lp_context* ctx)
 
 uint32_t lp_batch_points(const lp_batch* B)
 {
-    return B ? B->b.nsrc : 0;
+    if (!B)
+        return 0;
+    uint32_t n = B->b.nsrc;
+    for (const lp_batch* P : B->parts)
+        n += P->b.nsrc;
+    return n;
 }
 
 uint64_t lp_batch_device_bytes(const lp_batch* B)
 {
-    return B ? B->cap : 0;
+    if (!B)
+        return 0;
+    uint64_t n = B->cap;
+    for (const lp_batch* P : B->parts)
+        n += P->cap;
+    return n;
 }
 
 // Device time of `iters` executions with CUDA events on the context stream. flush_l2: write a
@@ -1314,26 +1412,36 @@ lp_status lp_batch_profile(lp_context* ctx, lp_batch* B, char* names, uint32_t n
 {
     if (!ctx || !B || !count)
         return LP_ERR_BAD_ARG;
-    B->prof.clear();
-    B->profiling = true;
-    const lp_status st = execute(ctx, *B);
-    B->profiling = false;
-    if (st != LP_OK)
-        return st;
-    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    *count = static_cast<uint32_t>(B->prof.size());
-    for (uint32_t i = 0; i < B->prof.size() && i < cap; ++i)
+    // a split batch: its parts one after the other (each on its own stream, alone on the device)
+    std::vector<lp_batch*> runs = B->parts;
+    if (runs.empty())
+        runs.push_back(B);
+    uint32_t k = 0;
+    for (lp_batch* P : runs)
     {
-        float t = 0.0f;
-        cudaEventElapsedTime(&t, B->prof[i].start, B->prof[i].stop);
-        if (ms)
-            ms[i] = t;
-        if (names && name_len)
+        P->prof.clear();
+        P->profiling = true;
+        const lp_status st = execute(ctx, *P);
+        P->profiling = false;
+        if (st != LP_OK)
+            return st;
+        LP_CUDA(ctx, cudaStreamSynchronize(P->stream ? P->stream : ctx->stream));
+        for (uint32_t i = 0; i < P->prof.size(); ++i, ++k)
         {
-            std::strncpy(names + static_cast<size_t>(i) * name_len, B->prof[i].name, name_len - 1);
-            names[static_cast<size_t>(i) * name_len + name_len - 1] = 0;
+            if (k >= cap)
+                continue;
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, P->prof[i].start, P->prof[i].stop);
+            if (ms)
+                ms[k] = t;
+            if (names && name_len)
+            {
+                std::strncpy(names + static_cast<size_t>(k) * name_len, P->prof[i].name, name_len - 1);
+                names[static_cast<size_t>(k) * name_len + name_len - 1] = 0;
+            }
         }
     }
+    *count = k;
     return LP_OK;
 }
 

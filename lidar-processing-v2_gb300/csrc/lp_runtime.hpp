@@ -70,6 +70,13 @@ struct lp_batch
     cudaGraphExec_t graph = nullptr;
     std::vector<lpg::LaunchRecord> prof;
     bool profiling = false;
+    // A part of a split batch runs on its own stream (null: the context stream).
+    cudaStream_t stream = nullptr;
+    // A split batch: scan i lives in parts[i % parts.size()] at position i / parts.size(); the parts
+    // run concurrently on their streams (fork from and join into the context stream), so one
+    // part's latency-bound tails overlap the others' work.
+    std::vector<lp_batch*> parts;
+    std::vector<cudaEvent_t> fork_join; // [0] fork, [1 + k] part k done
 };
 
 namespace lprt

@@ -314,6 +314,29 @@ def test_cpp_dropin_example(ctx, tmp_path):
     assert out.strip().endswith(f"checksum {h:016x}"), out
 
 
+def test_prepared_batch_split(ctx):
+    """A batch of 16 or more scans runs as concurrent parts on their own streams (scans dealt
+    round-robin): its results, with and without a captured graph, equal lp_process_batch's in the
+    caller's scan order."""
+    data = scans([(1, i) for i in range(6)] + [(3, i) for i in range(14)])
+    pipe = lp.PipelineConfig.default()
+    ref = lp.process_batch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
+    b = lp.PreparedBatch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
+    assert b.points == sum(len(d[0]) for d in data)
+    b.execute()
+    got = b.download()
+    b.capture_graph()
+    b.execute()
+    b.execute()
+    got2 = b.download()
+    for i, (r, g1, g2) in enumerate(zip(ref, got, got2)):
+        compare_scan(g1, r, f"scan {i}")
+        compare_scan(g2, r, f"scan {i} (graph)")
+    prof = b.profile()
+    assert sum(1 for n, _ in prof if n == "k_hull") == 2  # 20 scans: two parts
+    b.close()
+
+
 def test_prepared_batch_and_graph(ctx):
     """lp_batch_create / execute / capture_graph give the same results as lp_process_batch."""
     data = scans([(3, 11), (1, 4)])
