@@ -16,13 +16,16 @@ extern "C" {
 typedef struct lp_batch lp_batch;
 
 /* Plans the layout, allocates device memory and uploads the scans (host buffers must stay
- * valid for lp_batch_upload). */
+ * valid for lp_batch_upload). A batch of 16 or more scans is split into up to four parts (one per
+ * 8 scans, dealt round-robin) that execute concurrently on their own streams, forked from and
+ * joined into the context stream; results and their order are those of the unsplit batch. */
 lp_status lp_batch_create(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans,
                           uint32_t nscans, lp_batch** out);
 void lp_batch_destroy(lp_context* ctx, lp_batch* batch);
 /* Copies the scans' host buffers to the device again (asynchronous on the context stream). */
 lp_status lp_batch_upload(lp_context* ctx, lp_batch* batch);
-/* Runs the whole pipeline on the device-resident inputs (asynchronous). */
+/* Runs the whole pipeline on the device-resident inputs (asynchronous: complete when the context
+ * stream reaches this point). */
 lp_status lp_batch_execute(lp_context* ctx, lp_batch* batch);
 /* Captures the launch sequence into a CUDA graph; later lp_batch_execute calls replay it. */
 lp_status lp_batch_capture_graph(lp_context* ctx, lp_batch* batch);
