@@ -355,6 +355,8 @@ lp_status build(lp_context* ctx, lp_batch& B)
         if (B.mem)
         {
             cudaStreamSynchronize(ctx->stream);
+            if (B.stream)
+                cudaStreamSynchronize(B.stream);
             cudaFree(B.mem);
             B.mem = nullptr;
             B.cap = 0;
@@ -747,11 +749,13 @@ bool direct_io_ok(const lp_batch& B, const lp_scan_input* scans, const lp_scan_o
     return true;
 }
 
-lp_status run_direct(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
+// Launches of the direct host I/O path on the batch's stream: inputs gathered from the caller's
+// page-locked buffers, the pipeline, results scattered into them, the scans' states read back.
+lp_status direct_launch(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
 {
     LP_TRY(build(ctx, B));
     BatchDev& b = B.b;
-    const cudaStream_t st = ctx->stream;
+    const cudaStream_t st = B.stream ? B.stream : ctx->stream;
     const size_t S = B.run.scans.size();
     const bool hull = B.run.stages & ST_HULL, obb = B.run.stages & ST_OBB;
     std::vector<IoScan> io(S);
@@ -782,10 +786,22 @@ lp_status run_direct(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
     launch_io_out(L, b, b.io, b.io_ret, hull ? 1 : 0, obb ? 1 : 0, nq);
     if (L.err != cudaSuccess)
         return cuda_fail(ctx, L.err, "direct output launch");
-    std::vector<uint32_t> nh(S, 0u);
-    LP_CUDA(ctx, cudaMemcpyAsync(B.h_state.data(), b.state, S * sizeof(ScanState), cudaMemcpyDeviceToHost, st));
+    return LP_OK;
+}
+
+// Reads the scans' states back (a copy into pageable memory waits for the batch's stream, so it is
+// issued only here, after every part of a split call has been launched) and reports every scan's
+// status and counts in outs.
+lp_status direct_finish(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
+{
+    const cudaStream_t st = B.stream ? B.stream : ctx->stream;
+    const size_t S = B.run.scans.size();
+    const bool hull = B.run.stages & ST_HULL;
+    B.h_nh.assign(S, 0u);
+    const std::vector<uint32_t>& nh = B.h_nh;
+    LP_CUDA(ctx, cudaMemcpyAsync(B.h_state.data(), B.b.state, S * sizeof(ScanState), cudaMemcpyDeviceToHost, st));
     if (hull)
-        LP_CUDA(ctx, cudaMemcpyAsync(nh.data(), b.io_ret, S * 4, cudaMemcpyDeviceToHost, st));
+        LP_CUDA(ctx, cudaMemcpyAsync(B.h_nh.data(), B.b.io_ret, S * 4, cudaMemcpyDeviceToHost, st));
     LP_CUDA(ctx, cudaStreamSynchronize(st));
     lp_status worst = report_state(ctx, B);
     if (worst != LP_OK && worst != LP_ERR_CAPACITY)
@@ -805,6 +821,67 @@ lp_status run_direct(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
             if (worst == LP_OK)
                 worst = fail(ctx, LP_ERR_CAPACITY, "scan " + std::to_string(s) + ": cluster or hull capacity too small");
         }
+    }
+    return worst;
+}
+
+lp_status run_direct(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
+{
+    LP_TRY(direct_launch(ctx, B, outs));
+    return direct_finish(ctx, B, outs);
+}
+
+// The direct path for 16 or more scans: concurrent parts (scans dealt round-robin), each on its own
+// stream, ordered after earlier work on the context stream; each part's host reads and writes
+// overlap the other parts' kernels.
+lp_status run_direct_split(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans,
+                           lp_scan_output* outs, uint32_t nscans, uint32_t K)
+{
+    while (ctx->cached_parts.size() < K)
+    {
+        lp_batch* P = new lp_batch();
+        if (cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking) != cudaSuccess)
+        {
+            delete P;
+            return fail(ctx, LP_ERR_CUDA, "cudaStreamCreateWithFlags");
+        }
+        ctx->cached_parts.push_back(P);
+    }
+    if (!ctx->fork)
+        LP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
+    LP_CUDA(ctx, cudaEventRecord(ctx->fork, ctx->stream));
+    std::vector<std::vector<lp_scan_output>> sub(K);
+    lp_status worst = LP_OK;
+    uint32_t launched = 0;
+    for (uint32_t k = 0; k < K && worst == LP_OK; ++k)
+    {
+        lp_batch& P = *ctx->cached_parts[k];
+        std::vector<lp_scan_input> in;
+        for (uint32_t i = k; i < nscans; i += K)
+        {
+            in.push_back(scans[i]);
+            sub[k].push_back(outs[i]);
+        }
+        LP_CUDA(ctx, cudaStreamWaitEvent(P.stream, ctx->fork, 0));
+        worst = fill_pipeline(ctx, P, cfg, in.data(), static_cast<uint32_t>(in.size()));
+        if (worst == LP_OK)
+            worst = direct_launch(ctx, P, sub[k].data());
+        if (worst == LP_OK)
+            ++launched;
+    }
+    if (worst != LP_OK)
+    {
+        for (uint32_t k = 0; k < K; ++k)
+            cudaStreamSynchronize(ctx->cached_parts[k]->stream);
+        return worst;
+    }
+    for (uint32_t k = 0; k < launched; ++k)
+    {
+        const lp_status st = direct_finish(ctx, *ctx->cached_parts[k], sub[k].data());
+        for (size_t j = 0; j < sub[k].size(); ++j)
+            outs[k + j * K] = sub[k][j];
+        if (st != LP_OK && (worst == LP_OK || worst == LP_ERR_CAPACITY))
+            worst = st;
     }
     return worst;
 }
@@ -919,6 +996,13 @@ void lp_context_destroy(lp_context* ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     destroy_batch(ctx->cached);
+    for (lp_batch* P : ctx->cached_parts)
+    {
+        cudaStreamSynchronize(P->stream);
+        destroy_batch(P);
+    }
+    if (ctx->fork)
+        cudaEventDestroy(ctx->fork);
     for (cudaEvent_t e : ctx->events)
         cudaEventDestroy(e);
     if (ctx->flush)
@@ -1181,7 +1265,10 @@ lp_status lp_process_batch(lp_context* ctx, const lp_pipeline_config* cfg, const
     lp_batch& B = cached(ctx);
     LP_TRY(fill_pipeline(ctx, B, cfg, scans, nscans));
     if (direct_io_ok(B, scans, outs))
-        return run_direct(ctx, B, outs);
+    {
+        const uint32_t K = split_parts(nscans);
+        return K > 1 ? run_direct_split(ctx, cfg, scans, outs, nscans, K) : run_direct(ctx, B, outs);
+    }
     const lp_status st = run_once(ctx, B);
     if (st != LP_OK && st != LP_ERR_CAPACITY)
         return st;

@@ -52,6 +52,10 @@ struct lp_context
     std::string last_error;
     std::vector<cudaEvent_t> events;
     lp_batch* cached = nullptr;
+    // lp_process_batch on page-locked buffers with 16 or more scans: concurrent parts, each with
+    // its own stream and device region, reused call after call
+    std::vector<lp_batch*> cached_parts;
+    cudaEvent_t fork = nullptr;
     void* flush = nullptr; // buffer larger than L2 for cache flushing between timed runs
     size_t flush_bytes = 0;
 };
@@ -77,6 +81,7 @@ struct lp_batch
     // part's latency-bound tails overlap the others' work.
     std::vector<lp_batch*> parts;
     std::vector<cudaEvent_t> fork_join; // [0] fork, [1 + k] part k done
+    std::vector<uint32_t> h_nh;         // direct host I/O: hull index count per scan (read back)
 };
 
 namespace lprt

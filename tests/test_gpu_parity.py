@@ -236,6 +236,22 @@ def test_pinned_reused_outputs(ctx):
             compare_scan(b.result(), w)
 
 
+def test_pinned_split_batch(ctx):
+    """16 or more scans on page-locked buffers run as concurrent parts (scans dealt round-robin,
+    each part reading and writing the caller's buffers on its own stream): the results, call after
+    call into the same buffers, are those of the unsplit pageable path in the caller's order."""
+    data = scans([(1, i) for i in range(6)] + [(3, i) for i in range(10, 24)])
+    pipe = lp.PipelineConfig.default()
+    want = lp.process_batch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
+    px = [lp.pinned_copy(d[0]) for d in data]
+    pr = [lp.pinned_copy(d[1]) for d in data]
+    bufs = [lp.ResultBuffers(len(d[0]), pinned=True) for d in data]
+    for _ in range(2):
+        lp.process_batch(ctx, px, pipe, [d[2] for d in data], pr, outputs=bufs, raw=True)
+        for i, (b, w) in enumerate(zip(bufs, want)):
+            compare_scan(b.result(), w, f"scan {i}")
+
+
 def test_batch_composition_independent(ctx):
     """A scan's results do not depend on which scans share its batch or on what earlier batches
     left in device memory (sizes 18k-201k points, several groupings, after a large unrelated
