@@ -19,6 +19,9 @@
  *   lp_process_scan / lp_process_batch
  *                           Processor::run (segment → obstacle split → cluster → per-cluster
  *                           gather → convexHull), src/processor/src/processor.cpp:492-671
+ *   lp_split_clouds         Processor::run's ground / obstacle / unsegmented clouds,
+ *                           src/processor/src/processor.cpp:558-579
+ *   lp_unpack_pointcloud2   convert<PointT>(PointCloud2 -> pcl cloud), src/processor/src/processor.cpp:42-179
  */
 #ifndef LIDAR_GB300_H
 #define LIDAR_GB300_H
@@ -134,6 +137,33 @@ uint64_t lp_kernel_launch_count(const lp_context* ctx);
  * to 0. xyzi: n x 4 floats. */
 lp_status lp_add_ring_info(lp_context* ctx, const float* xyzi, uint32_t n, uint16_t first_ring,
                            uint16_t* ring_out);
+
+/* A field the cloud does not carry (lp_unpack_pointcloud2). */
+#define LP_NO_FIELD 0xffffffffu
+
+/* Unpacks a sensor_msgs/PointCloud2 byte buffer as convert<PointT> does (processor.cpp:42-179):
+ * point (row, col) starts at row * row_step + col * point_step; offsets[5] are the byte offsets of
+ * x, y, z, intensity (float32) and ring (uint16) within a point, intensity and ring LP_NO_FIELD when
+ * absent (intensity then 0). Little-endian data, fields need not be aligned. data: height *
+ * row_step bytes; xyzi_out: width * height x 4 floats; ring_out: NULL or width * height uint16. */
+lp_status lp_unpack_pointcloud2(lp_context* ctx, const uint8_t* data, uint32_t width, uint32_t height,
+                                uint32_t point_step, uint32_t row_step, const uint32_t* offsets, float* xyzi_out,
+                                uint16_t* ring_out);
+
+/* A point of the processor's coloured clouds (pcl::PointXYZRGB's position and colour; a = 255). */
+typedef struct lp_xyzrgb
+{
+    float x, y, z;
+    uint8_t r, g, b, a;
+} lp_xyzrgb;
+
+/* The processor's three clouds from a segmentation (processor.cpp:558-579): the points labelled
+ * GROUND coloured (124, 252, 0), OBSTACLE (200, 0, 0) and every other label (255, 255, 0), each in
+ * input order. xyzi: n x 4 floats; labels: n uint32 (LP_LABEL_*). ground / obstacle / unsegmented:
+ * host buffers of n entries each (any may be NULL: that cloud is counted, not copied). counts[3]
+ * receives the three cloud sizes. */
+lp_status lp_split_clouds(lp_context* ctx, const float* xyzi, const uint32_t* labels, uint32_t n, lp_xyzrgb* ground,
+                          lp_xyzrgb* obstacle, lp_xyzrgb* unsegmented, uint32_t* counts);
 
 /* Ground segmentation. xyzi: n x 4 floats (x, y, z, intensity). ring: per-point ring index, or
  * NULL for a cloud without a ring field (the height index then comes from the elevation angle,

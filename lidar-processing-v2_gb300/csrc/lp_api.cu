@@ -1003,6 +1003,8 @@ void lp_context_destroy(lp_context* ctx)
     }
     if (ctx->fork)
         cudaEventDestroy(ctx->fork);
+    if (ctx->split_mem)
+        cudaFree(ctx->split_mem);
     for (cudaEvent_t e : ctx->events)
         cudaEventDestroy(e);
     if (ctx->flush)
@@ -1019,6 +1021,102 @@ const char* lp_last_error(const lp_context* ctx)
 uint64_t lp_kernel_launch_count(const lp_context* ctx)
 {
     return ctx ? ctx->launches : 0;
+}
+
+namespace
+{
+// Device scratch of the standalone conversion entry points (grown on demand, kept by the context).
+lp_status scratch(lp_context* ctx, size_t bytes, char** out)
+{
+    if (bytes > ctx->split_cap)
+    {
+        if (ctx->split_mem)
+        {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->split_mem);
+            ctx->split_mem = nullptr;
+            ctx->split_cap = 0;
+        }
+        LP_CUDA(ctx, cudaMalloc(&ctx->split_mem, bytes));
+        ctx->split_cap = bytes;
+    }
+    *out = static_cast<char*>(ctx->split_mem);
+    return LP_OK;
+}
+} // namespace
+
+lp_status lp_unpack_pointcloud2(lp_context* ctx, const uint8_t* data, uint32_t width, uint32_t height,
+                                uint32_t point_step, uint32_t row_step, const uint32_t* offsets, float* xyzi_out,
+                                uint16_t* ring_out)
+{
+    const uint64_t n = static_cast<uint64_t>(width) * height;
+    if (!ctx || !offsets || (n && (!data || !xyzi_out)))
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument");
+    if (n == 0)
+        return LP_OK;
+    if (n > 0x7fffffffull / 4)
+        return fail(ctx, LP_ERR_CAPACITY, "cloud too large for 32-bit indexing");
+    const uint64_t need = static_cast<uint64_t>(width - 1) * point_step + point_step;
+    // every field inside the point record (64-bit sums: no offset can wrap past the check)
+    auto fits = [&](uint32_t off, uint64_t size) { return static_cast<uint64_t>(off) + size <= point_step; };
+    bool ok = point_step > 0 && row_step >= need && fits(offsets[0], 4) && fits(offsets[1], 4) && fits(offsets[2], 4);
+    ok = ok && (offsets[3] == LP_NO_FIELD || fits(offsets[3], 4));
+    ok = ok && (offsets[4] == LP_NO_FIELD || fits(offsets[4], 2));
+    if (!ok)
+        return fail(ctx, LP_ERR_BAD_ARG, "field offsets or steps outside the point record");
+    LP_TRY(ensure_device(ctx));
+    auto al = [](size_t v) { return (v + 255) & ~static_cast<size_t>(255); };
+    const size_t in_bytes = static_cast<size_t>(row_step) * height;
+    const size_t o_xyzi = al(in_bytes), o_ring = o_xyzi + al(n * 16);
+    char* m = nullptr;
+    LP_TRY(scratch(ctx, o_ring + al(n * 2), &m));
+    const cudaStream_t st = ctx->stream;
+    LP_CUDA(ctx, cudaMemcpyAsync(m, data, in_bytes, cudaMemcpyHostToDevice, st));
+    launch_unpack_pointcloud2(st, reinterpret_cast<const uint8_t*>(m), width, height, point_step, row_step, offsets,
+                              reinterpret_cast<float4*>(m + o_xyzi),
+                              ring_out ? reinterpret_cast<uint16_t*>(m + o_ring) : nullptr, ctx->launches);
+    LP_CUDA(ctx, cudaGetLastError());
+    LP_CUDA(ctx, cudaMemcpyAsync(xyzi_out, m + o_xyzi, n * 16, cudaMemcpyDeviceToHost, st));
+    if (ring_out)
+        LP_CUDA(ctx, cudaMemcpyAsync(ring_out, m + o_ring, n * 2, cudaMemcpyDeviceToHost, st));
+    LP_CUDA(ctx, cudaStreamSynchronize(st));
+    return LP_OK;
+}
+
+lp_status lp_split_clouds(lp_context* ctx, const float* xyzi, const uint32_t* labels, uint32_t n, lp_xyzrgb* ground,
+                          lp_xyzrgb* obstacle, lp_xyzrgb* unsegmented, uint32_t* counts)
+{
+    if (!ctx || !counts || (n && (!xyzi || !labels)))
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument");
+    counts[0] = counts[1] = counts[2] = 0;
+    if (n == 0)
+        return LP_OK;
+    if (n > 0x7fffffffu / 4u)
+        return fail(ctx, LP_ERR_CAPACITY, "cloud too large for 32-bit indexing");
+    LP_TRY(ensure_device(ctx));
+    auto al = [](size_t v) { return (v + 255) & ~static_cast<size_t>(255); };
+    const size_t N = n;
+    const size_t o_lab = al(N * 16), o_out = o_lab + al(N * 4), o_cnt = o_out + al(3 * N * sizeof(lp_xyzrgb));
+    const size_t o_sums = o_cnt + 256;
+    char* m = nullptr;
+    LP_TRY(scratch(ctx, o_sums + al((N + 1) / 8192 * 8 + 64), &m));
+    const cudaStream_t st = ctx->stream;
+    LP_CUDA(ctx, cudaMemcpyAsync(m, xyzi, N * 16, cudaMemcpyHostToDevice, st));
+    LP_CUDA(ctx, cudaMemcpyAsync(m + o_lab, labels, N * 4, cudaMemcpyHostToDevice, st));
+    lp_xyzrgb* out = reinterpret_cast<lp_xyzrgb*>(m + o_out);
+    uint32_t* dcnt = reinterpret_cast<uint32_t*>(m + o_cnt);
+    launch_split_clouds(st, reinterpret_cast<const float4*>(m), reinterpret_cast<const uint32_t*>(m + o_lab), n, out, dcnt,
+                        reinterpret_cast<uint32_t*>(m + o_sums), ctx->launches);
+    LP_CUDA(ctx, cudaGetLastError());
+    LP_CUDA(ctx, cudaMemcpyAsync(counts, dcnt, 3 * 4, cudaMemcpyDeviceToHost, st));
+    LP_CUDA(ctx, cudaStreamSynchronize(st));
+    lp_xyzrgb* dst[3] = {ground, obstacle, unsegmented};
+    for (int c = 0; c < 3; ++c)
+        if (dst[c] && counts[c])
+            LP_CUDA(ctx, cudaMemcpyAsync(dst[c], out + static_cast<size_t>(c) * N, counts[c] * sizeof(lp_xyzrgb),
+                                         cudaMemcpyDeviceToHost, st));
+    LP_CUDA(ctx, cudaStreamSynchronize(st));
+    return LP_OK;
 }
 
 lp_status lp_add_ring_info(lp_context* ctx, const float* xyzi, uint32_t n, uint16_t first_ring, uint16_t* ring_out)

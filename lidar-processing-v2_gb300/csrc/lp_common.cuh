@@ -297,7 +297,7 @@ template <class Src, class Dst>
 __global__ void __launch_bounds__(kLbThreads) k_scan_lb(Src src, Dst dst, unsigned long long* state, uint32_t* err)
 {
     __shared__ uint32_t s_warp[kLbThreads / 32];
-    __shared__ uint32_t s_tile, s_prefix;
+    __shared__ uint32_t s_tile;
     if (threadIdx.x == 0)
         s_tile = atomicAdd(reinterpret_cast<unsigned int*>(state), 1u);
     __syncthreads();

@@ -56,6 +56,8 @@ struct lp_context
     // its own stream and device region, reused call after call
     std::vector<lp_batch*> cached_parts;
     cudaEvent_t fork = nullptr;
+    void* split_mem = nullptr; // lp_split_clouds scratch
+    size_t split_cap = 0;
     void* flush = nullptr; // buffer larger than L2 for cache flushing between timed runs
     size_t flush_bytes = 0;
 };

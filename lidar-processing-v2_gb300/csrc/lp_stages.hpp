@@ -120,6 +120,13 @@ void launch_io_in(Launcher& L, const BatchDev& b, const IoScan* io);
 void launch_io_out(Launcher& L, const BatchDev& b, const IoScan* io, uint32_t* ret, int with_hull, int with_obb,
                    uint32_t nq);
 void init_segment_tables(); // per-device constant tables (the seed-42 MT19937 stream)
+// PointCloud2 bytes -> XYZI (+ ring) (lp_wire.cu); offsets: x, y, z, intensity, ring.
+void launch_unpack_pointcloud2(cudaStream_t st, const uint8_t* data, uint32_t width, uint32_t height,
+                               uint32_t point_step, uint32_t row_step, const uint32_t* offsets, float4* xyzi,
+                               uint16_t* ring, uint64_t& launches);
+// The processor's ground / obstacle / unsegmented clouds (lp_split.cu): out holds 3 x n records.
+void launch_split_clouds(cudaStream_t st, const float4* pts, const uint32_t* labels, uint32_t n, lp_xyzrgb* out,
+                         uint32_t* counts, uint32_t* sums, uint64_t& launches);
 // Streaming multiprocessors of the current device (persistent grids are sized by it).
 int sm_count();
 

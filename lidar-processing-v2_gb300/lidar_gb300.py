@@ -269,6 +269,8 @@ def _declare(lib):
         "lp_last_error": (c.c_char_p, [P]),
         "lp_kernel_launch_count": (c.c_uint64, [P]),
         "lp_add_ring_info": (c.c_int32, [P, P, c.c_uint32, c.c_uint16, P]),
+        "lp_split_clouds": (c.c_int32, [P, P, P, c.c_uint32, P, P, P, P]),
+        "lp_unpack_pointcloud2": (c.c_int32, [P, P, c.c_uint32, c.c_uint32, c.c_uint32, c.c_uint32, P, P, P]),
         "lp_segment": (c.c_int32, [P, P, P, c.c_uint32, P, P, P]),
         "lp_noise_remove": (c.c_int32, [P, P, c.c_uint32, c.c_uint32, P, P]),
         "lp_cluster": (c.c_int32, [P, P, c.c_uint32, c.c_uint32, P, P]),
@@ -379,6 +381,43 @@ def add_ring_info(ctx, cloud, first_ring=63):
     out = np.zeros(len(a), np.uint16)
     check(library().lp_add_ring_info(ctx.handle, ptr(a), len(a), first_ring, ptr(out)), ctx)
     return out
+
+
+# lp_xyzrgb: pcl::PointXYZRGB's position and colour
+XYZRGB = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("r", "u1"), ("g", "u1"), ("b", "u1"), ("a", "u1")])
+
+
+NO_FIELD = 0xFFFFFFFF
+
+
+def unpack_pointcloud2(ctx, data, width, height, point_step, row_step, x=0, y=4, z=8, intensity=NO_FIELD,
+                       ring=NO_FIELD):
+    """sensor_msgs/PointCloud2 bytes -> (xyzi float32 (n, 4), ring uint16 (n,) or None), as the
+    processor's convert<PointT> (processor.cpp:42-179); arguments are the message's layout and the
+    byte offsets of its fields (intensity / ring NO_FIELD when absent)."""
+    buf = np.ascontiguousarray(np.frombuffer(data, np.uint8) if not isinstance(data, np.ndarray) else data.view(np.uint8).reshape(-1))
+    n = width * height
+    xyzi = np.zeros((n, 4), np.float32)
+    rg = np.zeros(n, np.uint16) if ring != NO_FIELD else None
+    offs = np.array([x, y, z, intensity, ring], np.uint32)
+    check(library().lp_unpack_pointcloud2(ctx.handle, ptr(buf), width, height, point_step, row_step, ptr(offs),
+                                          ptr(xyzi), None if rg is None else ptr(rg)), ctx)
+    return xyzi, rg
+
+
+def split_clouds(ctx, cloud, labels):
+    """The processor's ground, obstacle and unsegmented clouds (processor.cpp:558-579): the points
+    of each segmentation label class in input order, coloured (124, 252, 0), (200, 0, 0) and
+    (255, 255, 0). Returns three XYZRGB structured arrays."""
+    a = _xyzi(cloud)
+    lab = np.ascontiguousarray(labels, np.uint32)
+    if len(lab) != len(a):
+        raise ValueError("one label per point")
+    outs = [np.zeros(len(a), XYZRGB) for _ in range(3)]
+    counts = np.zeros(3, np.uint32)
+    check(library().lp_split_clouds(ctx.handle, ptr(a), ptr(lab), len(a), ptr(outs[0]), ptr(outs[1]), ptr(outs[2]),
+                                    ptr(counts)), ctx)
+    return tuple(o[:k] for o, k in zip(outs, counts))
 
 
 class Segmenter:

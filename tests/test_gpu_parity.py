@@ -170,6 +170,62 @@ def test_polygons(ctx):
         assert T.box_corner_set_close(poly.boundingBoxPrincipalComponentAnalysis(hp), T.o_pca(hp)[0], 1e-4)
 
 
+@pytest.mark.parametrize("w,s", [(1, 0), (3, 0)])
+def test_split_clouds(ctx, w, s):
+    """Ground / obstacle / unsegmented clouds (processor.cpp:558-579) from a segmentation: each label
+    class's points in input order with its colour; empty input; a NULL output buffer only counts."""
+    x, ring, cfg = T.synth_scan(w, s)
+    lab = lp.Segmenter(ctx, cfg).segment(x, ring)
+    got = lp.split_clouds(ctx, x, lab)
+    classes = [(lab == lp.GROUND, (124, 252, 0)), (lab == lp.OBSTACLE, (200, 0, 0)),
+               ((lab != lp.GROUND) & (lab != lp.OBSTACLE), (255, 255, 0))]
+    assert sum(len(c) for c in got) == len(x)
+    for cloud, (sel, rgb) in zip(got, classes):
+        want = x[sel]
+        assert len(cloud) == len(want)
+        for k, f in enumerate("xyz"):
+            assert np.array_equal(cloud[f], want[:, k])
+        assert (cloud["r"] == rgb[0]).all() and (cloud["g"] == rgb[1]).all() and (cloud["b"] == rgb[2]).all()
+        assert (cloud["a"] == 255).all()
+    empty = lp.split_clouds(ctx, x[:0], lab[:0])
+    assert all(len(c) == 0 for c in empty)
+    counts = np.zeros(3, np.uint32)
+    a = np.ascontiguousarray(x, np.float32)
+    lp.check(lp.library().lp_split_clouds(ctx.handle, T.ptr(a), T.ptr(lab), len(a), None, None, None, T.ptr(counts)), ctx)
+    assert counts.tolist() == [int(c[0].sum()) for c in classes]
+
+
+@pytest.mark.parametrize("layout", ["xyzir_aligned", "xyzr_unaligned"])
+def test_unpack_pointcloud2(ctx, layout):
+    """PointCloud2 bytes (padded rows, fields at their offsets, aligned or not) unpacked as
+    convert<PointT> does (processor.cpp:42-179); a field outside the record is rejected."""
+    x, ring, _ = T.synth_scan(1, 0)
+    width, height = 1000, len(x) // 1000
+    n = width * height
+    if layout == "xyzir_aligned":
+        point_step, offs = 32, dict(x=0, y=4, z=8, intensity=16, ring=20)
+    else:
+        point_step, offs = 15, dict(x=1, y=5, z=9, intensity=lp.NO_FIELD, ring=13)
+    row_step = width * point_step + 7
+    buf = np.zeros(height * row_step, np.uint8)
+    for r in range(height):
+        rec = buf[r * row_step:r * row_step + width * point_step].reshape(width, point_step)
+        pts = x[r * width:(r + 1) * width]
+        for k, f in enumerate("xyz"):
+            rec[:, offs[f]:offs[f] + 4] = pts[:, k].astype("<f4").view(np.uint8).reshape(width, 4)
+        if offs["intensity"] != lp.NO_FIELD:
+            rec[:, offs["intensity"]:offs["intensity"] + 4] = pts[:, 3].astype("<f4").view(np.uint8).reshape(width, 4)
+        rec[:, offs["ring"]:offs["ring"] + 2] = ring[r * width:(r + 1) * width].astype("<u2").view(np.uint8).reshape(width, 2)
+    xyzi, rg = lp.unpack_pointcloud2(ctx, buf, width, height, point_step, row_step, **offs)
+    want = x[:n].copy()
+    if offs["intensity"] == lp.NO_FIELD:
+        want[:, 3] = 0.0
+    assert np.array_equal(xyzi.view(np.uint32), want.view(np.uint32))
+    assert np.array_equal(rg, ring[:n])
+    with pytest.raises(ValueError):  # LP_ERR_BAD_ARG
+        lp.unpack_pointcloud2(ctx, buf, width, height, point_step, row_step, x=point_step - 2)
+
+
 # ------------------------------------------------------------------------------------- pipeline
 def compare_scan(got, want, label=""):
     assert np.array_equal(got.seg_labels, want.seg_labels), label
