@@ -2,19 +2,22 @@
 //
 // Reference: lidar_processing_lib/src/polygonizer.cpp and Processor::run's per-cluster gather
 // (src/processor/src/processor.cpp:627-671). Persistent CTAs take clusters from a work queue
-// (largest first); per cluster:
-//   1. z range and the members extreme in 16 directions (an inscribed polygon of members),
+// (clusters above 512 members one CTA each, then the others one warp each). The cluster scatter
+// has already written each member's x, y contiguously and the cluster's z range. Per cluster:
+//   1. the members extreme in 16 directions (an inscribed polygon of members),
 //   2. Quickhull refinement: the member farthest outside each polygon edge is inserted, for a
 //      few rounds; members proven strictly inside leave the active set. Every polygon vertex is a
-//      member, so a member strictly inside the polygon (checked in FP64 with a relative margin
-//      far above rounding) cannot be a hull vertex,
-//   3. bitonic sort of the remaining candidates by (x, y, member order), Andrew's monotone chain
-//      with the reference's FP64 orientation predicate (polygonizer.cpp:45-50, 62-85): the same
-//      output as the reference's chain over all members,
+//      member, so a member strictly inside the polygon (an FP32 test with a 1e-5 relative margin,
+//      far above its rounding error) cannot be a hull vertex,
+//   3. sort of the remaining candidates by (x, y, member order), Andrew's monotone chain with the
+//      reference's FP64 orientation predicate (polygonizer.cpp:45-50, 62-85) decided in FP32
+//      wherever that is provably the same decision: the same output as the reference's chain over
+//      all members,
 //   4. local hull indices = rank of each hull vertex among the cluster's members in input
 //      order (the reference gathers a cluster's points in obstacle order, processor.cpp:640),
-//   5. rotating-calipers box (Shamos antipodal pairs, FP64, best area kept as a float exactly
-//      like BoundingBox::area) and the PCA box, by one warp.
+//   5. rotating-calipers box (Shamos antipodal pairs, best area kept as a float exactly like
+//      BoundingBox::area; comparisons screened in FP32) and the PCA box, one warp each (in the CTA
+//      path while the other warps count the ranks).
 #include <cfloat>
 #include <mutex>
 
