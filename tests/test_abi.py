@@ -57,3 +57,23 @@ def test_config_defaults_match_reference_structs(built):
         d = cls.default()
         for f, _ in cls._fields_:
             assert np.float32(getattr(c, f)) == np.float32(getattr(d, f)), (name, f)
+
+
+def test_xyzrgb_record_matches_the_c_struct():
+    """lp_xyzrgb (x, y, z float32; r, g, b, a uint8) is 16 bytes; the Python dtype mirrors it."""
+    dt = T.lp.XYZRGB
+    assert dt.itemsize == 16
+    assert [dt.fields[f][1] for f in ("x", "y", "z", "r", "g", "b", "a")] == [0, 4, 8, 12, 13, 14, 15]
+
+
+def test_bench_reads_traffic_ratios_from_profiles():
+    """bench.py's roofline traffic comes from the `traffic_ratio <kernel> <ratio>` line of the ncu
+    summaries under profiles/ (one per dominant kernel it may report)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(T.REPO, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    for kernel in ("k_hull", "k_jcp_rows"):
+        t = bench.traffic_bytes(kernel, 1_000_000)
+        assert t is not None and 0 < t < 10_000_000, (kernel, t)
+    assert bench.traffic_bytes("no_such_kernel", 1_000_000) is None
