@@ -409,6 +409,27 @@ def test_prepared_batch_split(ctx):
     b.close()
 
 
+def test_prepared_batch_split_noise(ctx):
+    """A split prepared batch with the outlier filter enabled (each part filters its own scans before
+    segmenting them) equals the unsplit batch, and its first scans equal the oracle."""
+    data = scans([(1, i) for i in range(16)])
+    pipe = lp.PipelineConfig.default(enable_noise_removal=1,
+                                     noise=lp.NoiseRemoverConfig(3 * 0.17 * np.pi / 180, 0.1, 3))
+    ref = lp.process_batch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
+    b = lp.PreparedBatch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
+    b.capture_graph()
+    b.execute()
+    got = b.download()
+    for i, (r, g) in enumerate(zip(ref, got)):
+        assert np.array_equal(g.noise_labels, r.noise_labels), i
+        compare_scan(g, r, f"scan {i}")
+    for (x, ring, cfg), g in list(zip(data, got))[:2]:
+        want = T.o_process(x, ring, cfg, pipe, dror_mode=T.DROR_EXACT)
+        assert np.array_equal(g.noise_labels, want.noise_labels)
+        compare_scan(g, want)
+    b.close()
+
+
 def test_prepared_batch_and_graph(ctx):
     """lp_batch_create / execute / capture_graph give the same results as lp_process_batch."""
     data = scans([(3, 11), (1, 4)])
