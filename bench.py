@@ -63,6 +63,12 @@ def barrier(dist):
         dist.barrier()
 
 
+def replica_rate(dist, world, units, seconds):
+    """Whole-job rate of N replicas: every rank processed `units` in its own `seconds`; the job
+    takes as long as its slowest rank, so the aggregate is N x units over the maximum time."""
+    return world * units / dist_max(dist, seconds)
+
+
 class ClockSampler:
     """nvidia-smi clock and throttle-reason samples while the timed region runs."""
 
@@ -405,7 +411,7 @@ def main():
     barrier(dist)
     dev_ms = sum(step_ms)
     dev_ms_max = dist_max(dist, dev_ms)
-    value = world * ns * args.steps / (dev_ms_max / 1e3)
+    value = replica_rate(dist, world, ns * args.steps, dev_ms / 1e3)
 
     # the dominant kernel's launch timed with events on the context stream (roofline)
     _, agg2 = kernel_profile(batch)
@@ -449,11 +455,11 @@ def main():
             dt = time.perf_counter() - t1
             if it > 0:
                 e2e_times.append(dt)
-        e2e_s = dist_max(dist, float(np.mean(e2e_times)))
+        e2e_rate = replica_rate(dist, world, ns, float(np.mean(e2e_times)))
         h2d = sum(x.nbytes + r.nbytes for x, r in zip(pin_x, pin_r))
         d2h = sum(len(b.seg) * 9 + 4 * (b.out.n_clusters + 1 + b.out.n_hull_indices) + 8 * b.out.n_clusters
                   + 2 * 72 * b.out.n_clusters for b in bufs)
-        e2e = {"value": world * ns / e2e_s, "unit": "scans/s", "h2d_bytes_per_step": int(h2d),
+        e2e = {"value": e2e_rate, "unit": "scans/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
 
     cb = None
