@@ -185,6 +185,8 @@ def run_reference_arm(args, rank, world):
     data = make_workload(args.scans)
     budget = max(10.0, min(120.0, 5.0 * args.steps))
     cb = cpu_baseline(data, budget_s=budget)
+    # the reference's own design: one processor thread
+    cb["single_thread"] = cpu_baseline(data, budget_s=min(budget, 20.0), threads=1)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "scans/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",

@@ -1,6 +1,6 @@
-"""Multi-process host logic of the replica benchmark on CPU (gloo, world size 2): rank discovery
-from the launcher's environment, the barrier, the maximum over ranks behind the whole-job rate,
-and the reference arm that only rank 0 runs."""
+"""Host logic of the benchmark on CPU: the multi-process replica path (gloo, world size 2) with rank
+discovery from the launcher's environment, the barrier, the maximum over ranks behind the whole-job
+rate and the reference arm that only rank 0 runs; and the CPU baseline's record."""
 import argparse
 import contextlib
 import io
@@ -63,3 +63,14 @@ def test_single_process_needs_no_process_group():
     assert bench.dist_init(1) is None
     assert bench.replica_rate(None, 1, 64, 0.5) == 128.0
     bench.barrier(None)
+
+
+def test_cpu_baseline_record(built):
+    """The CPU baseline's record: the oracle over a bounded sample, the thread count it used."""
+    sys.path.insert(0, REPO)
+    import bench
+    import lp_testlib as T
+
+    cb = bench.cpu_baseline([T.synth_scan(1, 0)], budget_s=0.2, threads=1)
+    assert cb["kind"] == "port" and cb["unit"] == "scans/s" and cb["cores"] == 1
+    assert cb["value"] > 0 and "1 threads" in cb["sample"]
