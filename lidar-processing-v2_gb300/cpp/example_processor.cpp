@@ -14,7 +14,10 @@
 
 #include "lidar_processing_gpu.hpp"
 
-namespace
+// Stand-ins for pcl::PointXYZIR, pcl::PointXYZ and pcl::PointCloud (same fields). They live in
+// their own namespace, as PCL's do: the drop-in namespace has a PointXYZ of its own (doubles, the
+// polygonizer's point type), exactly like lidar_processing_lib.
+namespace sensor
 {
 struct PointXYZIR
 {
@@ -30,6 +33,10 @@ struct Cloud
 {
     std::vector<P> points;
 };
+} // namespace sensor
+
+namespace
+{
 
 template <typename T>
 std::vector<T> read_all(const char* path)
@@ -52,7 +59,7 @@ int main(int argc, char** argv)
     }
     const std::vector<float> raw = read_all<float>(argv[1]);
     const std::vector<std::uint16_t> rings = (argc > 2) ? read_all<std::uint16_t>(argv[2]) : std::vector<std::uint16_t>{};
-    Cloud<PointXYZIR> cloud;
+    sensor::Cloud<sensor::PointXYZIR> cloud;
     cloud.points.resize(raw.size() / 4);
     for (std::size_t i = 0; i < cloud.points.size(); ++i)
         cloud.points[i] = {raw[4 * i], raw[4 * i + 1], raw[4 * i + 2], raw[4 * i + 3],
@@ -69,7 +76,7 @@ int main(int argc, char** argv)
     std::vector<Label> labels;
     segmenter.segment(cloud, labels);
 
-    Cloud<PointXYZ> obstacles;
+    sensor::Cloud<sensor::PointXYZ> obstacles;
     std::size_t ground = 0;
     for (std::size_t i = 0; i < labels.size(); ++i)
     {

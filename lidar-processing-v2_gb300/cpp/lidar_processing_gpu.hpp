@@ -3,13 +3,17 @@
 // (lidar_processing_lib/include/lidar_processing_lib/{segmenter,noise_remover,clusterer,polygonizer}.hpp).
 //
 // Header-only; needs include/lidar_gb300.h and links against liblp_gpu.so. Point clouds are any
-// container with `.points` (or `operator[]` + `size()`) of structs exposing x, y, z (and `ring`
-// for organised clouds), so pcl::PointCloud<pcl::PointXYZIR> works unchanged. Objects own a device
-// context and, like the reference objects, are not thread-safe.
+// type with a `.points` vector (pcl::PointCloud<P>), or a std::vector<P>, of structs exposing x, y,
+// z (and `ring` for organised clouds), so pcl::PointCloud<pcl::PointXYZIR> works unchanged. Objects
+// own a device context and, like the reference objects, are not thread-safe. The geometry helpers
+// the processor node calls next to the classes (polygonArea, distance, ...; polygonizer.hpp:158-231)
+// are here too, so a node can switch namespaces wholesale.
 #pragma once
 
 #include <array>
+#include <cmath>
 #include <cstdint>
+#include <limits>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -33,10 +37,28 @@ enum class NoiseRemoverLabel : std::uint8_t
 };
 using ClusterLabel = std::int32_t;
 
+enum class Orientation : std::uint8_t
+{
+    ANTICLOCKWISE = 0,
+    CLOCKWISE = 1,
+    COLINEAR = 2
+};
+enum class PolygonContour : std::uint8_t
+{
+    OPEN = 0,
+    ENCLOSED = 1
+};
+
 struct PointXY
 {
     double x;
     double y;
+};
+struct PointXYZ
+{
+    double x;
+    double y;
+    double z;
 };
 struct AntipodalPair
 {
@@ -116,6 +138,11 @@ auto& points_of(const Cloud& c)
 {
     return c.points;
 }
+template <typename P, typename A>
+const std::vector<P, A>& points_of(const std::vector<P, A>& v)
+{
+    return v;
+}
 
 template <typename Cloud>
 void pack(const Cloud& cloud, std::vector<float>& xyzi, std::vector<std::uint16_t>* ring)
@@ -164,6 +191,19 @@ struct SegmenterConfiguration
 class Segmenter
 {
   public:
+    // segmenter.hpp:135-151 (the colour constants are the BGR triples of image())
+    static constexpr float DEG_TO_RAD = static_cast<float>(M_PI / 180.0);
+    static constexpr float TWO_M_PIf = static_cast<float>(2.0 * M_PI);
+    static constexpr float INVALID_Z = std::numeric_limits<float>::max();
+    static constexpr float INVALID_DEPTH_M = std::numeric_limits<float>::max();
+    static constexpr std::int32_t INVALID_INDEX = -1;
+    static constexpr std::array<std::uint8_t, 3> CV_OBSTACLE{0, 0, 255};
+    static constexpr std::array<std::uint8_t, 3> CV_GROUND{0, 255, 0};
+    static constexpr std::array<std::uint8_t, 3> CV_INTERSECTION_OR_UNKNOWN{0, 255, 255};
+    static constexpr std::array<std::uint8_t, 3> CV_INTERSECTION{255, 0, 0};
+    static constexpr std::array<std::uint8_t, 3> CV_UNKNOWN{255, 255, 255};
+    static constexpr std::uint32_t MAX_CLOUD_SIZE = 200'000U;
+
     explicit Segmenter(int device = 0) : ctx_(device) {}
 
     void config(const SegmenterConfiguration& config)
@@ -279,6 +319,8 @@ struct ClustererConfiguration
 class Clusterer
 {
   public:
+    static constexpr float TWO_M_PIf = static_cast<float>(2.0 * M_PI);
+    static constexpr float DEG_TO_RAD = static_cast<float>(M_PI / 180.0);
     static constexpr std::int32_t INVALID_LABEL = -1;
     explicit Clusterer(int device = 0) : ctx_(device) {}
     void config(const ClustererConfiguration& config)
@@ -308,10 +350,33 @@ class Clusterer
     std::vector<float> xyzi_;
 };
 
+// polygonizer.hpp:54-60; the reference sizes its scratch from max_points and reads nothing else
+struct PolygonizerConfiguration
+{
+    Orientation orientation = Orientation::ANTICLOCKWISE;
+    PolygonContour contour = PolygonContour::OPEN;
+    std::uint32_t max_points = 100'000;
+};
+
 class Polygonizer
 {
   public:
     explicit Polygonizer(int device = 0) : ctx_(device) {}
+
+    void config(const PolygonizerConfiguration& config)
+    {
+        config_ = config;
+    }
+    const PolygonizerConfiguration& config() const noexcept
+    {
+        return config_;
+    }
+
+    // Polygonizer::concaveHull (polygonizer.hpp:233-237) has an empty body: indices are left as given.
+    template <typename PointT>
+    void concaveHull(const std::vector<PointT>&, std::vector<std::int32_t>&)
+    {
+    }
 
     // Polygonizer::convexHull (polygonizer.cpp:33-91): counter-clockwise hull indices
     template <typename PointT>
@@ -373,8 +438,64 @@ class Polygonizer
     }
 
     detail::Context ctx_;
+    PolygonizerConfiguration config_;
     std::vector<double> xy_;
 };
+
+// Geometry helpers of polygonizer.hpp:158-231, in the same arithmetic (double, same operation order).
+template <typename PointT>
+inline Orientation orientation(const PointT& a, const PointT& b, const PointT& c) noexcept
+{
+    const auto turn = (b.x - a.x) * (c.y - a.y) - (b.y - a.y) * (c.x - a.x);
+    return turn > 0.0 ? Orientation::ANTICLOCKWISE : (turn < 0.0 ? Orientation::CLOCKWISE : Orientation::COLINEAR);
+}
+
+template <typename PointT>
+inline auto crossProduct(const PointT& a, const PointT& b) noexcept
+{
+    return (a.x * b.y) - (b.x * a.y);
+}
+
+// Shoelace area of a polygon given as its vertices in order (0 below three vertices).
+template <typename PointT>
+inline double polygonArea(const std::vector<PointT>& v) noexcept
+{
+    const std::size_t n = v.size();
+    if (n < 3)
+        return 0.0;
+    double twice = 0.0;
+    for (std::size_t i = 0; i + 1 < n; ++i)
+        twice += crossProduct(v[i], v[i + 1]);
+    twice += crossProduct(v[n - 1], v[0]);
+    return std::fabs(twice) * 0.5;
+}
+
+template <typename PointT>
+inline double distanceSquared(const PointT& a, const PointT& b) noexcept
+{
+    const double dx = a.x - b.x;
+    const double dy = a.y - b.y;
+    return dx * dx + dy * dy;
+}
+
+template <typename PointT>
+inline double distance(const PointT& a, const PointT& b) noexcept
+{
+    return std::sqrt(distanceSquared(a, b));
+}
+
+// Area of a rectangle from three consecutive corners (the fourth is not read).
+template <typename PointT>
+inline double areaOfRectangle(const PointT& a, const PointT& b, const PointT& c, const PointT&) noexcept
+{
+    return std::sqrt(distanceSquared(a, b) * distanceSquared(b, c));
+}
+
+template <typename PointT>
+inline double areaOfTriangle(const PointT& a, const PointT& b, const PointT& c) noexcept
+{
+    return std::fabs((a.x * (b.y - c.y) + b.x * (c.y - a.y) + c.x * (a.y - b.y)) * 0.5);
+}
 
 static_assert(sizeof(PointXY) == 16, "PointXY must be two packed doubles (lp_* take n x 2 doubles)");
 static_assert(sizeof(AntipodalPair) == 8, "AntipodalPair must be two int32 (lp_antipodal_pairs layout)");
