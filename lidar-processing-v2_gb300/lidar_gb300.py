@@ -665,6 +665,52 @@ class Server:
             pass
 
 
+class BatchCall:
+    """One lp_process_batch call with its argument arrays built once, for a caller that runs the
+    same scan and result buffers call after call (page-locked buffers refilled in place, as a sensor
+    node reuses its messages): run() is the C call alone, without rebuilding the per-scan structs.
+
+    Binds the caller's arrays themselves, so they must need no conversion: scans float32, N x 4,
+    C-contiguous; rings uint16, 1-D, C-contiguous (or None). Segmenter configs are copied here;
+    the pipeline config is passed by reference on every run.
+    """
+
+    def __init__(self, scans, pipeline=None, seg_configs=None, rings=None, outputs=None):
+        n = len(scans)
+        for a in scans:
+            if (not isinstance(a, np.ndarray) or a.dtype != np.float32 or a.ndim != 2 or a.shape[1] != 4
+                    or not a.flags.c_contiguous):
+                raise ValueError("BatchCall binds its scans: float32 N x 4 C-contiguous arrays")
+        rr = [None if (rings is None or rings[i] is None) else rings[i] for i in range(n)]
+        for r in rr:
+            if r is not None and (not isinstance(r, np.ndarray) or r.dtype != np.uint16 or r.ndim != 1
+                                  or not r.flags.c_contiguous):
+                raise ValueError("BatchCall binds its rings: uint16 1-D C-contiguous arrays")
+        cfgs = seg_configs or [SegmenterConfig.default() for _ in range(n)]
+        bufs = list(outputs) if outputs is not None else []
+        ins = (ScanInput * n)()
+        for i in range(n):
+            ins[i] = ScanInput(scans[i].ctypes.data, None if rr[i] is None else rr[i].ctypes.data, len(scans[i]),
+                               cfgs[i])
+            if outputs is None:
+                bufs.append(ResultBuffers(len(scans[i])))
+            elif len(bufs[i].seg) < len(scans[i]):
+                raise ValueError("output buffers smaller than the scan")
+        self.n = n
+        self.pipeline = pipeline or PipelineConfig.default()
+        self._keep = (list(scans), rr)  # the arrays ins points into
+        self.ins = ins
+        self.outs = (ScanOutput * n)(*[b.out for b in bufs])
+        self.bufs = bufs
+
+    def run(self, ctx, raw=True):
+        st = library().lp_process_batch(ctx.handle, ctypes.byref(self.pipeline), self.ins, self.outs, self.n)
+        for i in range(self.n):
+            self.bufs[i].out = self.outs[i]
+        check(st, ctx)
+        return self.bufs if raw else [b.result() for b in self.bufs]
+
+
 def process_batch(ctx, scans, pipeline=None, seg_configs=None, rings=None, outputs=None, raw=False):
     """Run the whole per-scan path on a batch of scans in one launch sequence.
 
@@ -673,23 +719,6 @@ def process_batch(ctx, scans, pipeline=None, seg_configs=None, rings=None, outpu
     fill (reused across calls, e.g. pinned ones) instead of fresh buffers; raw=True returns those
     buffers (arrays filled in place, counts in .out) without building ScanResult objects.
     """
-    pipeline = pipeline or PipelineConfig.default()
-    n = len(scans)
     arrs = [_xyzi(s) for s in scans]
-    rr = [None if (rings is None or rings[i] is None) else np.ascontiguousarray(rings[i], np.uint16)
-          for i in range(n)]
-    cfgs = seg_configs or [SegmenterConfig.default() for _ in range(n)]
-    ins = (ScanInput * n)()
-    bufs = list(outputs) if outputs is not None else []
-    for i in range(n):
-        ins[i] = ScanInput(arrs[i].ctypes.data, None if rr[i] is None else rr[i].ctypes.data, len(arrs[i]), cfgs[i])
-        if outputs is None:
-            bufs.append(ResultBuffers(len(arrs[i])))
-        elif len(bufs[i].seg) < len(arrs[i]):
-            raise ValueError("output buffers smaller than the scan")
-    outs = (ScanOutput * n)(*[b.out for b in bufs])
-    st = library().lp_process_batch(ctx.handle, ctypes.byref(pipeline), ins, outs, n)
-    for i in range(n):
-        bufs[i].out = outs[i]
-    check(st, ctx)
-    return bufs if raw else [b.result() for b in bufs]
+    rr = None if rings is None else [None if r is None else np.ascontiguousarray(r, np.uint16).reshape(-1) for r in rings]
+    return BatchCall(arrs, pipeline, seg_configs, rr, outputs).run(ctx, raw)
