@@ -151,3 +151,44 @@ def test_ransac_index_stream_matches_libstdcxx():
                 b = gen.bounded(n)
             got += [a, b]
         assert got == want.tolist(), n
+
+
+# --------------------------------------------------------------------------- PCA covariance error
+def test_pca_covariance_error(built):
+    """The PCA box's 2x2 covariance as the FP64 oracle forms it (mean, then centred sums in vertex
+    order, divided by n - 1; the device forms the same sums in the same order) against exact
+    rational arithmetic, on the 40 golden polygons' hulls and on car-sized footprints with float32
+    coordinates 5-80 m from the sensor. Error relative to the larger diagonal entry: 2.8e-16 at
+    most on these inputs (one rounding), checked below 1e-14."""
+    from fractions import Fraction
+
+    g = load(os.path.join(T.GOLDEN, "polygons.npz"))
+    off = np.concatenate([[0], np.cumsum(g["sizes"])])
+    hoff = np.concatenate([[0], np.cumsum(g["hull_sizes"])])
+    polys = []
+    for t in range(len(g["sizes"])):
+        pts = g["points"][off[t]:off[t + 1]]
+        polys.append(pts[g["hulls"][hoff[t]:hoff[t + 1]]])
+    rng = np.random.default_rng(11)
+    for _ in range(40):
+        r, az, yaw = rng.uniform(5, 80), rng.uniform(0, 2 * np.pi), rng.uniform(0, np.pi)
+        u = rng.uniform(-2.25, 2.25, 60)
+        v = rng.uniform(-0.9, 0.9, 60)
+        x = r * np.cos(az) + u * np.cos(yaw) - v * np.sin(yaw)
+        y = r * np.sin(az) + u * np.sin(yaw) + v * np.cos(yaw)
+        xy = np.stack([x, y], 1).astype(np.float32).astype(np.float64)
+        polys.append(xy[T.o_hull(xy)])
+    worst = 0.0
+    for hp in polys:
+        n = len(hp)
+        if n < 3:
+            continue
+        _, cov = T.o_pca(hp)
+        xs = [Fraction(float(v)) for v in hp[:, 0]]
+        ys = [Fraction(float(v)) for v in hp[:, 1]]
+        mx, my = sum(xs) / n, sum(ys) / n
+        exact = [sum((a - mx) ** 2 for a in xs) / (n - 1), sum((a - mx) * (b - my) for a, b in zip(xs, ys)) / (n - 1),
+                 sum((b - my) ** 2 for b in ys) / (n - 1)]
+        scale = max(abs(exact[0]), abs(exact[2]))
+        worst = max(worst, max(float(abs(Fraction(float(c)) - e) / scale) for c, e in zip(cov, exact)))
+    assert worst < 1e-14, worst
