@@ -192,3 +192,43 @@ def test_pca_covariance_error(built):
         scale = max(abs(exact[0]), abs(exact[2]))
         worst = max(worst, max(float(abs(Fraction(float(c)) - e) / scale) for c, e in zip(cov, exact)))
     assert worst < 1e-14, worst
+
+
+# ------------------------------------------------------- whole workload against the reference's code
+def test_workload_matches_reference_code(built):
+    """The oracle (host-libm mode) against the reference's own classes built from its sources
+    (oracle/_ref) on all 64 scans of the benchmark workload: segmentation and cluster labels,
+    cluster counts, z ranges and hull offsets identical; hull index sequences identical except
+    where a cluster holds two points with the same (x, y) (the reference's std::sort leaves their
+    order to the library; the hull's point sequence is identical there too); calipers boxes
+    identical and PCA corners within 1e-9 m, both being functions of the hull's points."""
+    if not os.path.exists(T.REF_PATH):
+        pytest.skip("reference build absent (oracle/build_ref.sh needs the reference tree)")
+    from concurrent.futures import ThreadPoolExecutor
+
+    pipe = T.lp.PipelineConfig.default()
+    data = [T.synth_scan(3, i) for i in range(64)]
+    T.oracle()
+    T.ref()
+    # the reference build runs on one thread (it crashes when several threads run their own
+    # instances); the oracle is thread-safe
+    ref = [T.r_process(d[0], d[1], d[2], pipe) for d in data]
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        orc = list(ex.map(lambda d: T.o_process(d[0], d[1], d[2], pipe, libm=T.LIBM_HOST), data))
+    ties = 0
+    for i, ((x, _, _), a, b) in enumerate(zip(data, ref, orc)):
+        for k in ("seg_labels", "cluster_labels", "hull_offsets", "z_min", "z_max"):
+            assert np.array_equal(getattr(a, k), getattr(b, k)), (i, k)
+        assert a.n_clusters == b.n_clusters, i
+        obs = x[a.seg_labels == T.lp.OBSTACLE]
+        for c in range(a.n_clusters):
+            lo, hi = a.hull_offsets[c], a.hull_offsets[c + 1]
+            ha, hb = a.hull_indices[lo:hi], b.hull_indices[lo:hi]
+            if not np.array_equal(ha, hb):
+                pts = obs[a.cluster_labels[a.seg_labels == T.lp.OBSTACLE] == c][:, :2]
+                assert len(np.unique(pts, axis=0)) < len(pts), (i, c)
+                assert np.array_equal(pts[ha], pts[hb]), (i, c)
+                ties += 1
+            assert T.boxes_identical(a.obb_calipers[c], b.obb_calipers[c]), (i, c)
+            assert T.box_corner_set_close(a.obb_pca[c], b.obb_pca[c], 1e-9), (i, c)
+    assert ties <= 1, ties  # one cluster of 5,120 with the libstdc++ 13 build here
