@@ -30,9 +30,24 @@
 #include <unordered_map>
 #include <vector>
 
+#include "introsort.h"
+
 namespace
 {
-int g_libm_mode = 0; // 0 = CR, 1 = host libm
+int g_libm_mode = 0;  // 0 = CR, 1 = host libm
+int g_hull_ties = 0;  // 0 = equal (x, y) ordered by index, 1 = in libstdc++ std::sort's order
+
+// convexHull's sort comparator, polygonizer.cpp:51-59 (PointXY: double, epsilon = DBL_EPSILON)
+struct RefHullLess
+{
+    const double* xy;
+    bool operator()(int32_t i, int32_t j) const
+    {
+        return xy[2 * i] < xy[2 * j] ||
+               (std::fabs(xy[2 * i] - xy[2 * j]) < std::numeric_limits<double>::epsilon() &&
+                xy[2 * i + 1] < xy[2 * j + 1]);
+    }
+};
 
 constexpr float DEG_TO_RAD = static_cast<float>(M_PI / 180.0); // segmenter.hpp:135
 constexpr float TWO_M_PIf = static_cast<float>(2.0 * M_PI);    // segmenter.hpp:136
@@ -111,6 +126,31 @@ extern "C" {
 void lpo_set_libm_mode(int mode)
 {
     g_libm_mode = mode;
+}
+// Order of hull points with the same (x, y): 0 by index (the GPU's rule), 1 as the reference's
+// std::sort leaves them (libstdc++'s introsort restated in introsort.h, with its comparator).
+void lpo_set_hull_ties(int mode)
+{
+    g_hull_ties = mode;
+}
+// The reference comparator's index sort four ways, for checking the restatement against the
+// library: 0 restated std::sort, 1 std::sort, 2 restated with depth limit 0 (its heapsort path),
+// 3 std::partial_sort(first, last, last) (libstdc++'s heapsort for that path).
+int32_t lpo_debug_sort(const double* xy, uint32_t n, int variant, int32_t* out)
+{
+    std::iota(out, out + n, 0);
+    const RefHullLess less{xy};
+    if (variant == 0)
+        lpo_sort::sort(out, n, less);
+    else if (variant == 1)
+        std::sort(out, out + n, less);
+    else if (variant == 2)
+        lpo_sort::sort(out, n, less, 0);
+    else if (variant == 3)
+        std::partial_sort(out, out + n, out + n, less);
+    else
+        return LP_ERR_BAD_ARG;
+    return LP_OK;
 }
 long lpo_cr_ambiguous_count(void)
 {
@@ -803,7 +843,8 @@ lp_status lpo_cluster(const float* xyz, uint32_t stride, uint32_t n, const lp_cl
 // ---------------------------------------------------------------------------------------------
 
 // convexHull, polygonizer.cpp:33-91. Sort key: (x, y); points with identical (x, y) are ordered
-// by index (the reference's std::sort leaves their order to the sort implementation).
+// by index (the reference's std::sort leaves their order to the sort implementation), or, with
+// lpo_set_hull_ties(1), exactly as libstdc++'s std::sort leaves them.
 lp_status lpo_convex_hull(const double* xy, uint32_t n, int32_t* out, uint32_t* n_out)
 {
     if (n < 3)
@@ -815,13 +856,16 @@ lp_status lpo_convex_hull(const double* xy, uint32_t n, int32_t* out, uint32_t* 
     }
     std::vector<int32_t> idx(n);
     std::iota(idx.begin(), idx.end(), 0);
-    std::sort(idx.begin(), idx.end(), [xy](int32_t i, int32_t j) {
-        if (xy[2 * i] != xy[2 * j])
-            return xy[2 * i] < xy[2 * j];
-        if (xy[2 * i + 1] != xy[2 * j + 1])
-            return xy[2 * i + 1] < xy[2 * j + 1];
-        return i < j;
-    });
+    if (g_hull_ties == 1)
+        lpo_sort::sort(idx.data(), n, RefHullLess{xy});
+    else
+        std::sort(idx.begin(), idx.end(), [xy](int32_t i, int32_t j) {
+            if (xy[2 * i] != xy[2 * j])
+                return xy[2 * i] < xy[2 * j];
+            if (xy[2 * i + 1] != xy[2 * j + 1])
+                return xy[2 * i + 1] < xy[2 * j + 1];
+            return i < j;
+        });
     auto ccwOrColinear = [xy](int32_t a, int32_t b, int32_t c) {
         return (xy[2 * b] - xy[2 * a]) * (xy[2 * c + 1] - xy[2 * a + 1]) -
                    (xy[2 * b + 1] - xy[2 * a + 1]) * (xy[2 * c] - xy[2 * a]) <=

@@ -22,6 +22,7 @@ REF_PATH = os.path.join(REPO, "oracle", "_ref", "libref.so")
 GOLDEN = os.path.join(REPO, "tests", "golden")
 
 LIBM_CR, LIBM_HOST = 0, 1
+TIES_INDEX, TIES_LIBSTDCXX = 0, 1  # order of hull points with equal (x, y)
 DROR_EXACT, DROR_KDTREE = 0, 1
 
 _oracle = None
@@ -36,6 +37,8 @@ def oracle():
         P, c = ctypes.c_void_p, ctypes
         sig = {
             "lpo_set_libm_mode": (None, [c.c_int]),
+            "lpo_set_hull_ties": (None, [c.c_int]),
+            "lpo_debug_sort": (c.c_int32, [P, c.c_uint32, c.c_int, P]),
             "lpo_cr_ambiguous_count": (c.c_long, []),
             "lpo_math": (c.c_float, [c.c_int, c.c_float, c.c_float]),
             "lpo_add_ring_info": (c.c_int32, [P, c.c_uint32, c.c_uint16, P]),
@@ -53,6 +56,13 @@ def oracle():
             f.restype, f.argtypes = r, a
         _oracle = o
     return _oracle
+
+
+def o_debug_sort(xy, variant):
+    a = np.ascontiguousarray(xy, np.float64)
+    out = np.zeros(len(a), np.int32)
+    assert oracle().lpo_debug_sort(ptr(a), len(a), variant, ptr(out)) == 0
+    return out
 
 
 def have_ref():
@@ -161,10 +171,11 @@ def o_cluster(pts, cfg, libm=LIBM_CR):
     return out
 
 
-def o_hull(xy):
+def o_hull(xy, ties=TIES_INDEX):
     a = np.ascontiguousarray(xy, np.float64)
     out = np.zeros(len(a) + 1, np.int32)
     n = ctypes.c_uint32()
+    oracle().lpo_set_hull_ties(ties)
     oracle().lpo_convex_hull(ptr(a), len(a), ptr(out), ctypes.byref(n))
     return out[: n.value].copy()
 
@@ -193,8 +204,9 @@ def o_antipodal(hp):
     return out[: n.value].copy()
 
 
-def o_process(xyzi, ring, seg_cfg, pipeline, libm=LIBM_CR, dror_mode=DROR_EXACT):
+def o_process(xyzi, ring, seg_cfg, pipeline, libm=LIBM_CR, dror_mode=DROR_EXACT, ties=TIES_INDEX):
     oracle().lpo_set_libm_mode(libm)
+    oracle().lpo_set_hull_ties(ties)
     b = lp.ResultBuffers(len(xyzi))
     scan = lp.ScanInput(xyzi.ctypes.data, None if ring is None else ring.ctypes.data, len(xyzi), seg_cfg)
     st = oracle().lpo_process_scan(ctypes.byref(pipeline), ctypes.byref(scan), dror_mode, ctypes.byref(b.out))

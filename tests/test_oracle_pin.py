@@ -201,7 +201,8 @@ def test_workload_matches_reference_code(built):
     cluster counts, z ranges and hull offsets identical; hull index sequences identical except
     where a cluster holds two points with the same (x, y) (the reference's std::sort leaves their
     order to the library; the hull's point sequence is identical there too); calipers boxes
-    identical and PCA corners within 1e-9 m, both being functions of the hull's points."""
+    identical and PCA corners within 1e-9 m, both being functions of the hull's points. With the
+    oracle's libstdc++ tie order the hull index sequences are identical everywhere."""
     if not os.path.exists(T.REF_PATH):
         pytest.skip("reference build absent (oracle/build_ref.sh needs the reference tree)")
     from concurrent.futures import ThreadPoolExecutor
@@ -215,6 +216,12 @@ def test_workload_matches_reference_code(built):
     ref = [T.r_process(d[0], d[1], d[2], pipe) for d in data]
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
         orc = list(ex.map(lambda d: T.o_process(d[0], d[1], d[2], pipe, libm=T.LIBM_HOST), data))
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        orc_lib = list(ex.map(lambda d: T.o_process(d[0], d[1], d[2], pipe, libm=T.LIBM_HOST,
+                                                    ties=T.TIES_LIBSTDCXX), data))
+    T.oracle().lpo_set_hull_ties(T.TIES_INDEX)
+    for i, (a, c) in enumerate(zip(ref, orc_lib)):
+        assert np.array_equal(a.hull_indices, c.hull_indices), i
     ties = 0
     for i, ((x, _, _), a, b) in enumerate(zip(data, ref, orc)):
         for k in ("seg_labels", "cluster_labels", "hull_offsets", "z_min", "z_max"):
@@ -232,3 +239,44 @@ def test_workload_matches_reference_code(built):
             assert T.boxes_identical(a.obb_calipers[c], b.obb_calipers[c]), (i, c)
             assert T.box_corner_set_close(a.obb_pca[c], b.obb_pca[c], 1e-9), (i, c)
     assert ties <= 1, ties  # one cluster of 5,120 with the libstdc++ 13 build here
+
+
+# ------------------------------------------------- std::sort restatement (order of equivalent points)
+def tie_heavy_inputs():
+    rng = np.random.default_rng(21)
+    sizes = [0, 1, 2, 3, 15, 16, 17, 18, 31, 32, 33, 63, 64, 65, 100, 257, 1000, 3000]
+    for n in sizes:
+        for distinct in (1, 2, 3, 7, 50, 10_000):
+            xy = rng.integers(0, distinct, size=(n, 2)).astype(np.float64) * 0.25
+            yield xy
+            yield xy[np.lexsort((xy[:, 1], xy[:, 0]))]          # sorted
+            yield xy[np.lexsort((xy[:, 1], xy[:, 0]))][::-1]    # reverse sorted
+    for n in (40, 200, 2000):  # organ pipe and saw-tooth in x with duplicated y
+        x = np.concatenate([np.arange(n // 2), np.arange(n // 2)[::-1]]).astype(np.float64)
+        yield np.stack([x, np.zeros_like(x)], 1)
+        x = (np.arange(n) % 7).astype(np.float64)
+        yield np.stack([x, (np.arange(n) % 3).astype(np.float64)], 1)
+
+
+def test_introsort_restatement_matches_std_sort(built):
+    """The restated libstdc++ introsort (oracle/introsort.h) leaves the reference comparator's
+    equivalent elements exactly where std::sort does, and its heapsort path matches libstdc++'s."""
+    count = 0
+    for xy in tie_heavy_inputs():
+        assert np.array_equal(T.o_debug_sort(xy, 0), T.o_debug_sort(xy, 1)), len(xy)
+        if len(xy) > 16:  # shorter ranges never reach the introsort loop, so never its heapsort
+            assert np.array_equal(T.o_debug_sort(xy, 2), T.o_debug_sort(xy, 3)), len(xy)
+        count += 1
+    assert count > 300
+
+
+def test_hull_tie_mode_matches_reference_hull(built):
+    """With libstdc++ tie order the oracle's hull equals the reference's convexHull index for
+    index, duplicates included."""
+    if not os.path.exists(T.REF_PATH):
+        pytest.skip("reference build absent (oracle/build_ref.sh needs the reference tree)")
+    rng = np.random.default_rng(8)
+    for t in range(200):
+        n = int(rng.integers(3, 400))
+        xy = rng.integers(0, int(rng.integers(2, 30)), size=(n, 2)).astype(np.float64) * 0.5
+        assert np.array_equal(T.o_hull(xy, ties=T.TIES_LIBSTDCXX), T.r_hull(xy)), t
