@@ -169,6 +169,34 @@ def cpu_baseline(data, budget_s=20.0, threads=None):
                       f"restatement of the reference path, {threads} threads, {dt:.1f} s"}
 
 
+def e2e_leg(lp, ctx, pipe, xs, rings, cfgs, steps):
+    """End to end through the C ABI with host buffers: the scans sit in page-locked host memory and
+    every step copies them in, runs the whole path and copies every result back out into page-locked
+    result buffers reused from step to step (as a sensor node reuses its messages; the call's
+    argument structs are built once, as a C++ caller keeps its lp_scan_input array). Returns the
+    mean seconds per step (the first step untimed) and the bytes copied in and out per step."""
+    pin_x = [lp.pinned_copy(x) for x in xs]
+    pin_r = [lp.pinned_copy(r) for r in rings]
+    bufs = [lp.ResultBuffers(len(x), pinned=True) for x in xs]
+    call = lp.BatchCall(pin_x, pipe, cfgs, pin_r, outputs=bufs)
+    times = []
+    for it in range(max(3, steps // 2) + 1):
+        t1 = time.perf_counter()
+        call.run(ctx)
+        dt = time.perf_counter() - t1
+        if it > 0:
+            times.append(dt)
+    h2d = sum(x.nbytes + r.nbytes for x, r in zip(pin_x, pin_r))
+    # per scan: noise u8 + seg u32 + cluster i32 labels; hull offsets and indices; z range; two boxes
+    d2h = sum(len(b.seg) * 9 + 4 * (b.out.n_clusters + 1 + b.out.n_hull_indices) + 8 * b.out.n_clusters
+              + 2 * 72 * b.out.n_clusters for b in bufs)
+    return float(np.mean(times)), int(h2d), int(d2h)
+
+
+def leg_error(exc):
+    return f"{type(exc).__name__}: {exc}"
+
+
 def kernel_profile(batch):
     prof = batch.profile()
     agg = {}
@@ -431,44 +459,39 @@ def main():
     achieved = alg_bytes / (top_ms / 1e3) / 1e9
     total_ms = sum(a[1] for a in agg2.values())
 
-    plain = []
+    plain, plain_err = [], None
     if not args.no_plain:
         # plain form: one scan per launch sequence, device-resident, no graph
-        for i in range(min(ns, 32)):
-            pb = lp.PreparedBatch(ctx, [xs[i]], pipe, [cfgs[i]], [rings[i]])
-            pb.execute()
-            pb.synchronize()
-            plain.append(pb.time(3, flush_l2=True))
-            pb.close()
+        try:
+            for i in range(min(ns, 32)):
+                pb = lp.PreparedBatch(ctx, [xs[i]], pipe, [cfgs[i]], [rings[i]])
+                pb.execute()
+                pb.synchronize()
+                plain.append(pb.time(3, flush_l2=True))
+                pb.close()
+        except Exception as exc:  # reported in the line; the batched figures stand
+            plain, plain_err = [], leg_error(exc)
     plain_ms = float(np.mean(plain)) if plain else None
 
     e2e = None
     if not args.no_e2e:
-        # end to end through the C ABI with host buffers: the scans sit in page-locked host memory
-        # and every step copies them in, runs the whole path and copies every result back out into
-        # page-locked result buffers reused from step to step (as a sensor node reuses its messages;
-        # the call's argument structs are built once, as a C++ caller keeps its lp_scan_input array)
-        pin_x = [lp.pinned_copy(x) for x in xs]
-        pin_r = [lp.pinned_copy(r) for r in rings]
-        bufs = [lp.ResultBuffers(len(x), pinned=True) for x in xs]
-        call = lp.BatchCall(pin_x, pipe, cfgs, pin_r, outputs=bufs)
-        e2e_times = []
-        for it in range(max(3, args.steps // 2) + 1):
-            t1 = time.perf_counter()
-            call.run(ctx)
-            dt = time.perf_counter() - t1
-            if it > 0:
-                e2e_times.append(dt)
-        e2e_rate = replica_rate(dist, world, ns, float(np.mean(e2e_times)))
-        h2d = sum(x.nbytes + r.nbytes for x, r in zip(pin_x, pin_r))
-        d2h = sum(len(b.seg) * 9 + 4 * (b.out.n_clusters + 1 + b.out.n_hull_indices) + 8 * b.out.n_clusters
-                  + 2 * 72 * b.out.n_clusters for b in bufs)
-        e2e = {"value": e2e_rate, "unit": "scans/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
+        e2e_err, e2e_s, h2d, d2h = None, float("inf"), 0, 0
+        try:
+            e2e_s, h2d, d2h = e2e_leg(lp, ctx, pipe, xs, rings, cfgs, args.steps)
+        except Exception as exc:  # reported in the line; the device-resident figures stand
+            e2e_err = leg_error(exc)
+        e2e_rate = replica_rate(dist, world, ns, e2e_s)
+        if e2e_err is None and e2e_rate > 0:
+            e2e = {"value": e2e_rate, "unit": "scans/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+        else:
+            e2e = {"error": e2e_err or "failed on another rank", "unit": "scans/s"}
 
     cb = None
     if rank == 0 and not args.no_cpu:
-        cb = cpu_baseline(data, budget_s=15.0)
+        try:
+            cb = cpu_baseline(data, budget_s=15.0)
+        except Exception as exc:  # reported in the line
+            cb = {"error": leg_error(exc)}
 
     if rank == 0:
         line = {
@@ -480,7 +503,7 @@ def main():
                        "l2": "inputs larger than L2 (133 MB XYZI, multi-GB working set)",
                        "graph": "captured CUDA graph per batch"},
             "points_per_s": world * npts * args.steps / (dev_ms_max / 1e3),
-            "plain": None if not plain else {
+            "plain": ({"error": plain_err} if plain_err else None) if not plain else {
                 "ms_per_scan": plain_ms, "scans_per_s": 1e3 / plain_ms, "p50_ms": float(np.percentile(plain, 50)),
                 "p99_ms": float(np.percentile(plain, 99)), "scans": len(plain)},
             "batched_over_plain": None if not plain else (value / world) / (1e3 / plain_ms),

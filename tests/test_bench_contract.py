@@ -1,0 +1,112 @@
+"""bench.py's JSON line on CPU: main() run against stand-ins for the device objects (context,
+prepared batch, the shared library's page-locked allocator and lp_process_batch) carries every key
+of the benchmark contract with consistent values, and a failing optional leg is reported in the
+line instead of losing it."""
+import contextlib
+import ctypes
+import io
+import json
+import sys
+
+import numpy as np
+
+import lp_testlib as T
+from test_host_marshalling import PinningLibrary
+
+lp = T.lp
+
+
+class FakeContext:
+    handle = None
+
+    def __init__(self, device=0):
+        self.device = device
+
+    def close(self):
+        pass
+
+
+class FakeResult:
+    def __init__(self, n):
+        self.n_obstacles = n // 2
+        self.n_clusters = 3
+        self.cluster_labels = np.full(n, -1, np.int32)
+        self.cluster_labels[: n // 4] = 0
+        self.hull_indices = np.arange(9, dtype=np.int32)
+
+
+class FakeBatch:
+    def __init__(self, ctx, xs, pipe, cfgs, rings):
+        self.xs = xs
+
+    def execute(self):
+        pass
+
+    def synchronize(self):
+        pass
+
+    def capture_graph(self):
+        pass
+
+    def close(self):
+        pass
+
+    def download(self):
+        return [FakeResult(len(x)) for x in self.xs]
+
+    def profile(self):
+        return [("k_bin", 0.05), ("k_scan", 0.01), ("k_jcp_rows", 0.40), ("k_hull", 0.30), ("k_scan", 0.01)]
+
+    def time(self, iters, flush_l2=False):
+        return 2.5
+
+
+def run_main(monkeypatch, lib, argv):
+    sys.path.insert(0, T.REPO)
+    import bench
+
+    monkeypatch.setattr(lp, "library", lambda: lib)
+    monkeypatch.setattr(lp, "Context", FakeContext)
+    monkeypatch.setattr(lp, "PreparedBatch", FakeBatch)
+    monkeypatch.setattr(sys, "argv", ["bench.py"] + argv)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    out = io.StringIO()
+    with contextlib.redirect_stdout(out):
+        bench.main()
+    return json.loads(out.getvalue().strip().splitlines()[-1])
+
+
+def test_bench_line_carries_the_contract(monkeypatch):
+    line = run_main(monkeypatch, PinningLibrary(), ["--steps", "3", "--warmup", "3", "--scans", "4", "--no-cpu"])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "e2e", "gpu_launches", "roofline", "clocks", "cpu_baseline"):
+        assert key in line, key
+    assert line["n_gpus"] == 1 and line["steps"] == 3 and line["warmup"] == 3
+    assert line["higher_is_better"] is True and line["scaling"] == "weak" and line["vs_baseline"] is None
+    assert abs(line["value"] - 4 * 3 / (3 * 2.5e-3)) < 1e-6  # scans over the summed event time
+    assert abs(line["ms_per_step"] - 2.5) < 1e-9
+    assert line["config"]["workload"] == "batch4_mixed"
+    e = line["e2e"]
+    assert e["unit"] == "scans/s" and e["value"] > 0 and e["h2d_bytes_per_step"] > 0 and e["d2h_bytes_per_step"] > 0
+    # the stand-in profile has four of our kernels; k_scan counts three launches (tile sums, look-back, apply)
+    assert line["gpu_launches"] == (3 + 3 * 2) * 3
+    r = line["roofline"]
+    assert r["kernel"] == "k_jcp_rows" and r["bound"] == "hbm" and r["unit"] == "GB/s"
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-12
+    assert r["traffic"] is not None  # read from the ncu summary under profiles/
+    assert set(line["clocks"]) >= {"sm_mhz", "sm_max_mhz", "reasons"}
+    assert line["plain"]["scans"] == 4
+
+
+class FailingLibrary(PinningLibrary):
+    def lp_process_batch(self, *a):
+        raise RuntimeError("stand-in failure")
+
+
+def test_failed_end_to_end_leg_is_reported(monkeypatch):
+    line = run_main(monkeypatch, FailingLibrary(), ["--steps", "3", "--warmup", "3", "--scans", "4", "--no-cpu",
+                                                    "--no-plain"])
+    assert line["e2e"] == {"error": "RuntimeError: stand-in failure", "unit": "scans/s"}
+    assert line["value"] > 0 and line["plain"] is None
+    assert ctypes.sizeof(lp.ScanOutput) > 0

@@ -115,3 +115,44 @@ def test_batch_call_refuses_inputs_it_would_copy(rec, bad):
     with pytest.raises(ValueError):
         lp.BatchCall(xs, None, cfgs, rs)
     assert not rec.calls
+
+
+class PinningLibrary(RecordingLibrary):
+    """Also hands out 'page-locked' blocks (plain host memory here) as lp_host_alloc would."""
+
+    def __init__(self):
+        super().__init__()
+        self.blocks = []
+
+    def lp_host_alloc(self, nbytes, out):
+        b = ctypes.create_string_buffer(int(nbytes) + 256)
+        self.blocks.append(b)
+        ctypes.cast(out, ctypes.POINTER(ctypes.c_void_p))[0] = (ctypes.addressof(b) + 255) // 256 * 256
+        return 0
+
+    def lp_host_free(self, p):
+        pass
+
+
+def test_bench_end_to_end_leg(monkeypatch):
+    """bench.py's end-to-end leg: page-locked copies of the scans and rings, one bound call run
+    once untimed plus max(3, steps // 2) timed steps, and the bytes it reports per step."""
+    import os
+    import sys
+
+    sys.path.insert(0, T.REPO)
+    import bench
+
+    lib = PinningLibrary()
+    monkeypatch.setattr(lp, "library", lambda: lib)
+    xs, rs, cfgs = scans()
+    secs, h2d, d2h = bench.e2e_leg(lp, FakeContext(), lp.PipelineConfig.default(), xs, rs, cfgs, steps=8)
+    assert len(lib.calls) == 1 + 4 and secs >= 0.0
+    ins = lib.calls[0][4]
+    assert [i[2] for i in ins] == [5, 0, 17]
+    assert all(i[0] != addr(x) for i, x in zip(ins, xs))  # the page-locked copies, not the originals
+    assert h2d == sum(x.nbytes + r.nbytes for x, r in zip(xs, rs))
+    # counts the stand-in reports: clusters 0, 1, 2 and hull indices 0, 3, 6
+    want = sum(9 * len(x) + 4 * (k + 1 + 3 * k) + 8 * k + 144 * k for k, x in enumerate(xs))
+    assert d2h == want
+    assert os.path.basename(bench.__file__) == "bench.py"
