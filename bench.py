@@ -133,6 +133,10 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def workload_name(nscans):
+    return "batch64_mixed" if nscans == 64 else f"batch{nscans}_mixed"
+
+
 def make_workload(nscans):
     import lp_testlib as T
 
@@ -218,7 +222,8 @@ def run_reference_arm(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "scans/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batch64_mixed", "scans": args.scans, "generator_seed": "1000*3+scan"},
+            "config": {"workload": workload_name(args.scans), "scans": args.scans,
+                       "points": int(sum(len(d[0]) for d in data)), "generator_seed": "1000*3+scan"},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "scans/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -498,7 +503,7 @@ def main():
             "metric": METRIC, "value": value, "unit": "scans/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batch64_mixed" if ns == 64 else f"batch{ns}_mixed", "scans": ns, "points": npts,
+            "config": {"workload": workload_name(ns), "scans": ns, "points": npts,
                        "obstacles": n_obs, "clusters": n_clusters, "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (133 MB XYZI, multi-GB working set)",
                        "graph": "captured CUDA graph per batch"},

@@ -110,3 +110,32 @@ def test_failed_end_to_end_leg_is_reported(monkeypatch):
     assert line["e2e"] == {"error": "RuntimeError: stand-in failure", "unit": "scans/s"}
     assert line["value"] > 0 and line["plain"] is None
     assert ctypes.sizeof(lp.ScanOutput) > 0
+
+
+def test_reference_arm_line(monkeypatch):
+    """--impl reference on rank 0: the CPU baseline's rate as the line's value, its record (with the
+    single-thread leg) under cpu_baseline, and an e2e entry with no host-device bytes."""
+    sys.path.insert(0, T.REPO)
+    import bench
+
+    calls = []
+
+    def fake_baseline(data, budget_s=20.0, threads=None):
+        calls.append((len(data), budget_s, threads))
+        return {"value": 70.0 if threads is None else 25.0, "unit": "scans/s", "cores": threads or 16,
+                "kind": "port", "sample": "stand-in"}
+
+    monkeypatch.setattr(bench, "cpu_baseline", fake_baseline)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "4", "--warmup", "3", "--scans", "2"])
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    out = io.StringIO()
+    with contextlib.redirect_stdout(out):
+        bench.main()
+    line = json.loads(out.getvalue().strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] == 70.0 and line["unit"] == "scans/s"
+    assert line["metric"] == bench.METRIC and line["higher_is_better"] is True
+    assert line["cpu_baseline"]["single_thread"]["cores"] == 1
+    assert line["e2e"] == {"value": 70.0, "unit": "scans/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert calls == [(2, 20.0, None), (2, 20.0, 1)]
+    assert line["config"]["workload"] == "batch2_mixed" and line["config"]["points"] > 0
