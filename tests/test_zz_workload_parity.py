@@ -15,6 +15,42 @@ lp = T.lp
 pytestmark = pytest.mark.gpu
 
 
+def first_cluster(mask):
+    idx = np.nonzero(mask)[0]
+    return int(idx[0]) if len(idx) else -1
+
+
+def differences(g, w):
+    """Which outputs of one scan differ, with counts and the first differing point or cluster."""
+    d = []
+    for name in ("seg_labels", "cluster_labels"):
+        a, b = getattr(g, name), getattr(w, name)
+        if not np.array_equal(a, b):
+            ne = np.nonzero(a != b)[0]
+            d.append(f"{name} {len(ne)} points from {int(ne[0])} (gpu {int(a[ne[0]])} oracle {int(b[ne[0]])})")
+    if g.n_clusters != w.n_clusters:
+        d.append(f"n_clusters gpu {g.n_clusters} oracle {w.n_clusters}")
+        return ", ".join(d)
+    k = g.n_clusters
+    if not np.array_equal(g.hull_offsets, w.hull_offsets):
+        c = first_cluster(g.hull_offsets != w.hull_offsets)
+        d.append(f"hull_offsets from cluster {c - 1}")
+    elif not np.array_equal(g.hull_indices, w.hull_indices):
+        c = int(np.searchsorted(w.hull_offsets, first_cluster(g.hull_indices != w.hull_indices), side="right")) - 1
+        d.append(f"hull_indices from cluster {c} (size {int(w.hull_offsets[c + 1] - w.hull_offsets[c])} vertices)")
+    if not (np.array_equal(g.z_min, w.z_min) and np.array_equal(g.z_max, w.z_max)):
+        d.append(f"z range from cluster {first_cluster((g.z_min != w.z_min) | (g.z_max != w.z_max))}")
+    cal = [c for c in range(k) if not T.boxes_identical(g.obb_calipers[c], w.obb_calipers[c])]
+    if cal:
+        a, b = g.obb_calipers[cal[0]], w.obb_calipers[cal[0]]
+        d.append(f"calipers boxes of {len(cal)} clusters from {cal[0]} (area gpu {a.area!r} oracle {b.area!r}, "
+                 f"angle gpu {a.angle_rad!r} oracle {b.angle_rad!r})")
+    pca = [c for c in range(k) if not T.box_corner_set_close(g.obb_pca[c], w.obb_pca[c], 1e-4)]
+    if pca:
+        d.append(f"pca boxes of {len(pca)} clusters from {pca[0]}")
+    return ", ".join(d)
+
+
 def test_full_workload_equals_oracle(ctx):
     data = [T.synth_scan(3, i) for i in range(64)]
     assert sum(len(d[0]) for d in data) > 8_000_000
@@ -28,15 +64,10 @@ def test_full_workload_equals_oracle(ctx):
     T.oracle()
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
         want = list(ex.map(lambda d: T.o_process(d[0], d[1], d[2], pipe), data))
-    bad = []
+    bad = {}
     for i, (g, w) in enumerate(zip(got, want)):
-        same = (np.array_equal(g.seg_labels, w.seg_labels) and np.array_equal(g.cluster_labels, w.cluster_labels)
-                and g.n_clusters == w.n_clusters and np.array_equal(g.hull_offsets, w.hull_offsets)
-                and np.array_equal(g.hull_indices, w.hull_indices) and np.array_equal(g.z_min, w.z_min)
-                and np.array_equal(g.z_max, w.z_max)
-                and all(T.boxes_identical(x, y) for x, y in zip(g.obb_calipers, w.obb_calipers))
-                and all(T.box_corner_set_close(x, y, 1e-4) for x, y in zip(g.obb_pca, w.obb_pca)))
-        if not same:
-            bad.append(i)
-    assert not bad, f"scans differing from the oracle: {bad}"
+        d = differences(g, w)
+        if d:
+            bad[i] = d
+    assert not bad, "scans differing from the oracle: " + "; ".join(f"scan {i}: {d}" for i, d in bad.items())
     assert sum(w.n_clusters for w in want) > 1000
