@@ -71,3 +71,18 @@ def test_full_workload_equals_oracle(ctx):
             bad[i] = d
     assert not bad, "scans differing from the oracle: " + "; ".join(f"scan {i}: {d}" for i, d in bad.items())
     assert sum(w.n_clusters for w in want) > 1000
+
+
+def test_diverging_scans_alone(ctx):
+    """Scans 20, 56 and 61 of the workload differed from the oracle inside the 64-scan batch. Each
+    is run here as a one-scan batch, which tells a divergence of the scan itself from one that
+    depends on the batch around it."""
+    pipe = lp.PipelineConfig.default()
+    bad = {}
+    for i in (20, 56, 61):
+        x, ring, cfg = T.synth_scan(3, i)
+        g = lp.process_batch(ctx, [x], pipe, [cfg], [ring])[0]
+        d = differences(g, T.o_process(x, ring, cfg, pipe))
+        if d:
+            bad[i] = d
+    assert not bad, "alone, differing from the oracle: " + "; ".join(f"scan {i}: {d}" for i, d in bad.items())
