@@ -574,6 +574,9 @@ __device__ __forceinline__ void extents_screened(const double2* P, const float2*
 // extents are kept by one lane; the winner's corners come from them, negated for the reverse
 // direction (exact), so they are the reference's. The skip test (edge length < 1e-6) is screened
 // in FP32 too (|float len^2 - len^2| < 2^-21 len^2) and evaluated in FP64 only near 1e-12.
+// Only the edges the walk visits take part (an unvisited edge's area is +inf): a pair walk that
+// misses a vertex never looks at its edges, and a contender set made only of unvisited edges
+// would leave no box where the reference keeps one.
 // Up to 32 contenders (one per lane) are handled; more fall back to calipers_warp.
 __device__ void calipers_fast(const double2* P, const float2* Pf, int n, const int2* pairs, int npairs, float* ea,
                               float r2, lp_bounding_box* out)
@@ -593,13 +596,26 @@ __device__ void calipers_fast(const double2* P, const float2* Pf, int n, const i
     }
     const float ox = Pf[0].x, oy = Pf[0].y;
     const float e = 1e-4f * r2 + 1e-30f;
+    // Only edges the walk visits can hold the reference's box: on a near-degenerate hull the pair
+    // walk can miss a vertex, and with it an edge that may have the smallest area. Mark the
+    // visited edges (ea[j] = 0, the edge mapping of `visit` below) before choosing contenders.
+    for (int j = static_cast<int>(lane); j < n; j += 32)
+        ea[j] = -1.0f;
+    __syncwarp();
+    for (int v = static_cast<int>(lane); v < 4 * npairs; v += 32)
+    {
+        const int2 pr = pairs[v >> 2];
+        const int index = ((v >> 1) & 1) ? pr.y : pr.x;
+        ea[(v & 1) ? index : ((index == 0) ? n - 1 : index - 1)] = 0.0f; // offset +1: edge index; -1: index - 1
+    }
+    __syncwarp();
     float amin = INFINITY;
     for (int j = static_cast<int>(lane); j < n; j += 32)
     {
         const int j1 = (j + 1 == n) ? 0 : j + 1;
         const float fx = Pf[j1].x - Pf[j].x, fy = Pf[j1].y - Pf[j].y;
         const float fl2 = fx * fx + fy * fy;
-        bool skip = fl2 < 0.9999e-12f;
+        bool skip = fl2 < 0.9999e-12f || ea[j] != 0.0f; // unvisited edges never compete
         if (!skip && !(fl2 > 1.0001e-12f))
         {
             const double dx = P[j1].x - P[j].x, dy = P[j1].y - P[j].y;
