@@ -98,15 +98,16 @@ def build_synth():
 def build_oracle():
     src = os.path.join(REPO, "oracle", "lp_oracle.cpp")
     lib = os.path.join(REPO, "oracle", "liblp_oracle.so")
-    if _stale(lib, [src, os.path.join(INCLUDE, "lidar_gb300.h")]):
+    headers = [os.path.join(REPO, "oracle", f) for f in ("eigen_svd2.h", "introsort.h")]
+    if _stale(lib, [src, os.path.join(INCLUDE, "lidar_gb300.h")] + headers):
         _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-I" + INCLUDE, src, "-o", lib])
     ref_script = os.path.join(REPO, "oracle", "build_ref.sh")
     ref_lib = os.path.join(REPO, "oracle", "_ref", "libref.so")
-    ref_root = os.environ.get("REF_ROOT", "/root/reference")
-    if os.path.isdir(os.path.join(ref_root, "lidar_processing_lib")):
-        shims = [os.path.join(dp, f) for dp, _, fs in os.walk(os.path.join(REPO, "oracle", "shim")) for f in fs]
-        if _stale(ref_lib, shims + [os.path.join(REPO, "oracle", "ref_capi.cpp"), ref_script]):
-            _run(["bash", ref_script])
+    # the recipe finds the reference tree itself (REF_ROOT) and builds nothing where it is absent
+    shims = [os.path.join(dp, f) for dp, _, fs in os.walk(os.path.join(REPO, "oracle", "shim")) for f in fs]
+    extra = [os.path.join(REPO, "oracle", f) for f in ("ref_capi.cpp", "ring_ref_prelude.h", "ring_ref_capi.inc")]
+    if _stale(ref_lib, shims + headers + extra + [ref_script]):
+        _run(["bash", ref_script])
     return lib
 
 

@@ -30,6 +30,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "eigen_svd2.h"
 #include "introsort.h"
 
 namespace
@@ -1020,8 +1021,15 @@ lp_status lpo_bounding_box_rotating_calipers(const double* P, uint32_t nu, lp_bo
     return LP_OK;
 }
 
+// V of Eigen's JacobiSVD of a 2x2 matrix (row-major a[4] -> v[4]), for the oracle's own tests.
+extern "C" int32_t lpo_jacobi_svd2(const double* a, double* v)
+{
+    return eigen_svd2::jacobi_svd2_v(a[0], a[1], a[2], a[3], v) ? 0 : 1;
+}
+
 // boundingBoxPrincipalComponentAnalysis, polygonizer.cpp:280-362, in FP64: mean, centred
-// X^T X / (n - 1), 2x2 symmetric eigenvectors (largest first), rotate, min/max, corners back.
+// X^T X / (n - 1) (:321-322), V of Eigen's JacobiSVD of that covariance (:325-331, restated in
+// eigen_svd2.h), rotate (:334), min/max (:337-340), corners back (:343-347).
 lp_status lpo_bounding_box_pca(const double* P, uint32_t n, lp_bounding_box* box, double* cov_out)
 {
     std::memset(box, 0, sizeof(*box));
@@ -1052,10 +1060,12 @@ lp_status lpo_bounding_box_pca(const double* P, uint32_t n, lp_bounding_box* box
         cov_out[1] = sxy;
         cov_out[2] = syy;
     }
-    // principal axis angle of [[sxx, sxy], [sxy, syy]]
-    const double theta = 0.5 * std::atan2(2.0 * sxy, sxx - syy);
-    const double v00 = std::cos(theta), v10 = std::sin(theta);
-    const double v01 = -v10, v11 = v00;
+    // principal components of [[sxx, sxy], [sxy, syy]]: V of the JacobiSVD (an invalid SVD, on a
+    // non-finite covariance, leaves the box invalid as at :326-330)
+    double V[4];
+    if (!eigen_svd2::jacobi_svd2_v(sxx, sxy, sxy, syy, V))
+        return LP_OK;
+    const double v00 = V[0], v01 = V[1], v10 = V[2], v11 = V[3];
     double mnx = std::numeric_limits<double>::max(), mxx = std::numeric_limits<double>::lowest();
     double mny = mnx, mxy = mxx;
     for (uint32_t i = 0; i < n; ++i)

@@ -1,12 +1,14 @@
 """Generates the golden fixtures in this directory from the REFERENCE build (oracle/_ref/libref.so,
 the reference library's own sources compiled by oracle/build_ref.sh).
 
-Run where the reference tree exists:  python tests/golden/make_golden.py [reference data dir]
+Run where the reference tree exists:  python tests/golden/make_golden.py <reference data dir>
+(the reference's data/ directory of .pcd frames).
 
 Inputs are sector crops of two reference frames (data/*.pcd) and of a synthetic scan, random
-polygons, and RANSAC index-stream parameters. Every output is produced by the reference code
-(segmentation, clustering, DROR, hull, antipodal pairs, calipers, PCA); ring indices are the
-oracle's restatement of the ROS-only Dataloader::addRingInfo with the host libm.
+polygons, two near-collinear hulls of the 64-scan workload, and RANSAC index-stream parameters.
+Every output is produced by the reference code (ring indices, segmentation, clustering, DROR,
+hull, antipodal pairs, calipers, PCA); ring indices come from the reference's own
+Dataloader::addRingInfo, extracted from its ROS node by oracle/build_ref.sh.
 """
 import os
 import sys
@@ -81,6 +83,49 @@ def polygons():
     print("polygons", len(sets))
 
 
+def thin_hulls():
+    """Hulls of cluster 64 of workload scan 20 and cluster 57 of scan 56 (64-scan mixed workload,
+    seeds 3000 + scan): near-collinear polygons, 6-8 cm long and under a micrometre wide, with
+    the reference's PCA boxes."""
+    pipe = lp.PipelineConfig.default()
+    hulls, boxes = [], []
+    for scan, cl in ((20, 64), (56, 57)):
+        x, ring, cfg = T.synth_scan(3, scan)
+        r = T.r_process(x, ring, cfg, pipe)
+        members = np.nonzero(r.cluster_labels == cl)[0]
+        h = r.hull_indices[r.hull_offsets[cl]:r.hull_offsets[cl + 1]]
+        hp = x[members, :2].astype(np.float64)[h]
+        b = T.r_pca(hp)
+        hulls.append(hp)
+        boxes.append([*b.corners_array().ravel(), b.area, b.angle_rad, b.is_valid])
+    np.savez_compressed(os.path.join(HERE, "thin_hulls.npz"), sizes=np.array([len(h) for h in hulls]),
+                        points=np.concatenate(hulls), pca=np.array(boxes))
+    print("thin hulls", len(hulls))
+
+
+def rle(r):
+    """(first positions, values) of the runs of a ring array."""
+    pos = np.concatenate([[0], np.flatnonzero(np.diff(r.astype(np.int32))) + 1])
+    return pos, r[pos]
+
+
+def ring_streams():
+    """The reference's Dataloader::addRingInfo on seeded synthetic scans (the generator is in the
+    repository, so only the output is stored, run-length encoded): the single-scan and dense
+    configurations, 32/64/128-ring scans of the mixed workload (the reference starts at ring 63
+    whatever the sensor) and a shuffled scan (quadrant changes at random)."""
+    cases = [(1, 0, False), (2, 0, False), (3, 1, False), (3, 2, False), (3, 5, False), (1, 0, True)]
+    out = {"cases": np.array([[w, s, int(sh)] for w, s, sh in cases], np.int32)}
+    for k, (w, sidx, sh) in enumerate(cases):
+        x = T.synth_scan(w, sidx)[0]
+        if sh:
+            x = np.ascontiguousarray(x[np.random.default_rng(11).permutation(len(x))])
+        pos, val = rle(T.r_ring(x))
+        out[f"pos_{k}"], out[f"val_{k}"], out[f"n_{k}"] = pos, val, np.array(len(x))
+    np.savez_compressed(os.path.join(HERE, "ring_streams.npz"), **out)
+    print("ring streams", len(cases))
+
+
 def ransac_stream():
     import ctypes
 
@@ -99,18 +144,22 @@ def ransac_stream():
 
 def main():
     assert T.have_ref(), "oracle/_ref/libref.so missing: run oracle/build_ref.sh where the reference exists"
-    data = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/data"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <reference data dir>")
+    data = sys.argv[1]
     cfg = lp.SegmenterConfig.default()
     for name, fname, lo, hi in (("kitti_000_sector", "0000000000.pcd", 0.0, 40.0),
                                 ("kitti_100_sector", "0000000100.pcd", 200.0, 235.0)):
         full = T.read_pcd(os.path.join(data, fname))
-        ring = T.o_ring(full, libm=T.LIBM_HOST)
+        ring = T.r_ring(full)
         keep = sector(full, lo, hi)
         scan_case(name, np.ascontiguousarray(full[keep]), np.ascontiguousarray(ring[keep]), cfg)
     x, ring, scfg = T.synth_scan(1, 0)
     keep = sector(x, 90.0, 130.0)
     scan_case("synth_w1_sector", np.ascontiguousarray(x[keep]), np.ascontiguousarray(ring[keep]), scfg)
     polygons()
+    thin_hulls()
+    ring_streams()
     ransac_stream()
 
 

@@ -49,6 +49,7 @@ def oracle():
             "lpo_antipodal_pairs": (c.c_int32, [P, c.c_uint32, P, c.c_uint32, P]),
             "lpo_bounding_box_rotating_calipers": (c.c_int32, [P, c.c_uint32, P]),
             "lpo_bounding_box_pca": (c.c_int32, [P, c.c_uint32, P, P]),
+            "lpo_jacobi_svd2": (c.c_int32, [P, P]),
             "lpo_process_scan": (c.c_int32, [P, P, c.c_int, P]),
         }
         for k, (r, a) in sig.items():
@@ -83,6 +84,7 @@ def ref():
             "lpr_bounding_box_rotating_calipers": (c.c_int32, [P, c.c_uint32, P]),
             "lpr_bounding_box_pca": (c.c_int32, [P, c.c_uint32, P]),
             "lpr_process_scan": (c.c_int32, [P, P, P]),
+            "lpr_add_ring_info": (c.c_int32, [P, c.c_uint32, P]),
         }
         for k, (rr, a) in sig.items():
             f = getattr(r, k)
@@ -195,6 +197,13 @@ def o_pca(hp):
     return b, cov
 
 
+def o_svd2(a):
+    """V (2x2) of the oracle's restatement of Eigen's JacobiSVD, or None for an invalid input."""
+    m = np.ascontiguousarray(a, np.float64).reshape(4)
+    v = np.zeros(4, np.float64)
+    return v.reshape(2, 2) if oracle().lpo_jacobi_svd2(ptr(m), ptr(v)) == 0 else None
+
+
 def o_antipodal(hp):
     a = np.ascontiguousarray(hp, np.float64)
     cap = 4 * len(a) + 8
@@ -221,6 +230,14 @@ def r_segment(xyzi, ring, cfg, image=False):
     st = ref().lpr_segment(ptr(xyzi), ptr(ring), len(xyzi), ctypes.byref(cfg), ptr(lab), ptr(img))
     assert st == 0, st
     return (lab, img) if image else lab
+
+
+def r_ring(xyzi):
+    """Ring indices from the reference's own Dataloader::addRingInfo (start ring 63)."""
+    a = np.ascontiguousarray(xyzi, np.float32)
+    out = np.zeros(len(a), np.uint16)
+    assert ref().lpr_add_ring_info(ptr(a), len(a), ptr(out)) == 0
+    return out
 
 
 def r_noise(pts, cfg):

@@ -280,3 +280,80 @@ def test_hull_tie_mode_matches_reference_hull(built):
         n = int(rng.integers(3, 400))
         xy = rng.integers(0, int(rng.integers(2, 30)), size=(n, 2)).astype(np.float64) * 0.5
         assert np.array_equal(T.o_hull(xy, ties=T.TIES_LIBSTDCXX), T.r_hull(xy)), t
+
+
+def ring_runs(r):
+    pos = np.concatenate([[0], np.flatnonzero(np.diff(r.astype(np.int32))) + 1])
+    return pos, r[pos]
+
+
+def test_ring_pinned_to_reference_dataloader(built):
+    """The oracle's ring partition (start ring 63, host libm) equals the reference's own
+    Dataloader::addRingInfo output on the committed seeded scans, including 32- and 128-ring
+    sensors (where the reference still counts down from 63) and a shuffled scan."""
+    g = np.load(os.path.join(T.GOLDEN, "ring_streams.npz"))
+    for k, (w, s, shuffled) in enumerate(g["cases"]):
+        x = T.synth_scan(int(w), int(s))[0]
+        if shuffled:
+            x = np.ascontiguousarray(x[np.random.default_rng(11).permutation(len(x))])
+        assert len(x) == int(g[f"n_{k}"])
+        pos, val = ring_runs(T.o_ring(x, first_ring=63, libm=T.LIBM_HOST))
+        assert np.array_equal(pos, g[f"pos_{k}"]) and np.array_equal(val, g[f"val_{k}"]), (w, s, shuffled)
+
+
+def test_ring_oracle_matches_reference_code_on_sector_fixtures(built):
+    """Where the reference build is present, the extracted Dataloader::addRingInfo and the oracle
+    agree on the fixtures' point sequences (crops, so the rings restart at 63)."""
+    if not T.have_ref():
+        pytest.skip("reference build not present")
+    for path in CASES:
+        x = load(path)["xyzi"]
+        assert np.array_equal(T.r_ring(x), T.o_ring(x, first_ring=63, libm=T.LIBM_HOST)), path
+
+
+def test_thin_hulls_pca_pinned(built):
+    """Two near-collinear hulls of the 64-scan workload (6-8 cm long, under a micrometre wide):
+    the oracle's PCA box equals the reference's (JacobiSVD restated from Eigen 3.4)."""
+    g = np.load(os.path.join(T.GOLDEN, "thin_hulls.npz"))
+    off = np.concatenate([[0], np.cumsum(g["sizes"])])
+    for t in range(len(g["sizes"])):
+        hp = g["points"][off[t]:off[t + 1]]
+        b, _ = T.o_pca(hp)
+        want = box_from(g["pca"][t])
+        assert np.array_equal(b.corners_array(), want.corners_array()) and b.area == want.area, t
+
+
+def svd_check(a, v):
+    """V orthonormal, columns eigenvectors of the symmetric a, eigenvalues descending."""
+    assert np.allclose(v.T @ v, np.eye(2), atol=1e-15)
+    lam = np.array([v[:, 0] @ a @ v[:, 0], v[:, 1] @ a @ v[:, 1]])
+    scale = np.abs(a).max()
+    assert np.allclose(a @ v, v * lam, atol=4e-16 * scale)
+    assert lam[0] >= lam[1] - 4e-16 * scale
+
+
+def test_jacobi_svd2_restatement(built):
+    """Eigen's JacobiSVD of a 2x2 covariance as the oracle restates it: a diagonal input keeps its
+    axes (columns swapped when the second value is larger), an off-diagonal entry at or below
+    2 eps max|diagonal| (after scaling) is not rotated, however close to isotropic the matrix is,
+    one just above it is rotated; equal singular values keep their columns; a non-finite input is
+    invalid; random symmetric matrices give orthonormal eigenvectors with descending values."""
+    eps = np.finfo(np.float64).eps
+    assert np.array_equal(T.o_svd2([[3.0, 0.0], [0.0, 1.0]]), np.eye(2))
+    assert np.array_equal(T.o_svd2([[1.0, 0.0], [0.0, 3.0]]), [[0.0, 1.0], [1.0, 0.0]])
+    assert np.array_equal(T.o_svd2([[2.0, 0.0], [0.0, 2.0]]), np.eye(2))
+    assert np.array_equal(T.o_svd2([[0.0, 0.0], [0.0, 0.0]]), np.eye(2))
+    # near-isotropic, off-diagonal at the threshold: no rotation (a closed-form angle gives 45 deg)
+    assert np.array_equal(T.o_svd2([[1.0, 2 * eps], [2 * eps, 1.0]]), np.eye(2))
+    assert np.array_equal(T.o_svd2([[1.0, 1e-20], [1e-20, 1.0 - 1e-15]]), np.eye(2))
+    # just above it: a 45-degree rotation
+    v = T.o_svd2([[1.0, 4 * eps], [4 * eps, 1.0]])
+    assert np.allclose(np.abs(v), np.sqrt(0.5), atol=1e-12)
+    assert T.o_svd2([[np.nan, 0.0], [0.0, 1.0]]) is None
+    assert T.o_svd2([[np.inf, 0.0], [0.0, 1.0]]) is None
+    rng = np.random.default_rng(5)
+    for _ in range(2000):
+        sxx, syy = rng.uniform(0, 10, 2) ** rng.uniform(-3, 3, 2)
+        sxy = rng.normal() * np.sqrt(sxx * syy) * rng.uniform(0, 1) ** 4
+        a = np.array([[sxx, sxy], [sxy, syy]])
+        svd_check(a, T.o_svd2(a))
