@@ -196,10 +196,13 @@ lp_status lp_convex_hull(lp_context* ctx, const double* xy, uint32_t n, int32_t*
  * GPU which loads the library keeps until the process exits; n above LP_NOALLOC_HULL_MAX_POINTS
  * is rejected with LP_ERR_CAPACITY before anything runs. The first call on a device looks up that
  * array's device address (once per device, with the device current), so make that first call
- * before any stream capture. The work is enqueued on `stream` (a cudaStream_t, NULL for the
- * default stream) and the call returns without waiting. All calls share the one array: calls
- * whose kernels overlap on the GPU (other threads, other streams) race and must be serialised
- * by the caller. */
+ * before any stream capture. That address is kept for the life of the process: after a
+ * cudaDeviceReset (or any teardown of the device's primary context) the library reloads and the
+ * kept address is stale, so this entry point must not be called on that device again. The work
+ * is enqueued on `stream` (a cudaStream_t, NULL for the default stream) and the call returns
+ * without waiting; the status reports this call's own launch (LP_ERR_CUDA if it was refused).
+ * All calls share the one array: calls whose kernels overlap on the GPU (other threads, other
+ * streams) race and must be serialised by the caller. */
 #define LP_NOALLOC_HULL_MAX_POINTS 65536u
 lp_status lp_convex_hull_noalloc(const double* d_xy, uint32_t n, int32_t* d_indices_out, uint32_t* d_n_out,
                                  void* stream);

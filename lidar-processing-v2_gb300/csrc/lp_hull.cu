@@ -297,8 +297,90 @@ __device__ void calipers_warp(const double2* P, int n, const int2* pairs, int np
         *out = box;
 }
 
-// PCA box (polygonizer.cpp:280-362) in FP64: mean, centred X^T X / (n - 1), principal axis
-// angle of the 2x2 covariance, rotate, min/max, corners back to the original frame.
+// Principal components of the 2x2 covariance as the reference gets them: V of Eigen 3.4's
+// JacobiSVD (svd_.compute, polygonizer.cpp:326), in binary64 and in that library's operation order
+// (this file is compiled without multiply-add contraction), so the axes are bit-identical to the
+// host's. Steps: divide by the largest |coefficient|; while an off-diagonal entry exceeds
+// max(DBL_MIN, 2 eps max|diagonal|), a left rotation symmetrises the (1, 0) block and a Jacobi
+// rotation diagonalises it (W rotated on both sides, V on the right); columns ordered by
+// descending |diagonal| with a strict comparison. Below the threshold nothing rotates, so a
+// near-diagonal covariance keeps the identity axes. Sweeps stop after 64 (one or two in practice;
+// the library loops until the test passes). Returns false for a non-finite covariance (the
+// library's InvalidInput: the reference's box stays invalid, :327-330).
+struct Rot2
+{
+    double c, s;
+};
+
+__device__ __forceinline__ void rot2_apply(double& x0, double& x1, double& y0, double& y1, Rot2 r)
+{
+    if (r.c == 1.0 && r.s == 0.0)
+        return;
+    const double a0 = x0, a1 = x1, b0 = y0, b1 = y1;
+    x0 = r.c * a0 + r.s * b0;
+    x1 = r.c * a1 + r.s * b1;
+    y0 = -r.s * a0 + r.c * b0;
+    y1 = -r.s * a1 + r.c * b1;
+}
+
+__device__ bool pca_axes(double sxx, double sxy, double syy, double& v00, double& v01, double& v10, double& v11)
+{
+    if (!(isfinite(sxx) && isfinite(sxy) && isfinite(syy)))
+        return false;
+    double scale = fmax(fmax(fabs(sxx), fabs(sxy)), fmax(fabs(sxy), fabs(syy)));
+    if (scale == 0.0)
+        scale = 1.0;
+    double w00 = sxx / scale, w01 = sxy / scale, w10 = sxy / scale, w11 = syy / scale;
+    v00 = 1.0, v01 = 0.0, v10 = 0.0, v11 = 1.0;
+    const double precision = 2.0 * DBL_EPSILON;
+    double max_diag = fmax(fabs(w00), fabs(w11));
+    for (int sweep = 0; sweep < 64; ++sweep)
+    {
+        const double threshold = fmax(DBL_MIN, precision * max_diag);
+        if (!(fabs(w10) > threshold || fabs(w01) > threshold))
+            break;
+        // block of the index pair (1, 0): m = [[W11, W10], [W01, W00]]
+        double m00 = w11, m01 = w10, m10 = w01, m11 = w00;
+        Rot2 r1{1.0, 0.0};
+        const double t = m00 + m11, d = m10 - m01;
+        if (!(fabs(d) < DBL_MIN))
+        {
+            const double u = t / d;
+            const double tmp = sqrt(1.0 + u * u);
+            r1 = Rot2{u / tmp, 1.0 / tmp};
+        }
+        rot2_apply(m00, m01, m10, m11, r1);
+        Rot2 rr{1.0, 0.0}; // the Jacobi rotation of [[m00, m01], [m01, m11]]
+        const double deno = 2.0 * fabs(m01);
+        if (!(deno < DBL_MIN))
+        {
+            const double tau = (m00 - m11) / deno;
+            const double w = sqrt(tau * tau + 1.0);
+            const double tt = tau > 0.0 ? 1.0 / (tau + w) : 1.0 / (tau - w);
+            const double sign_t = tt > 0.0 ? 1.0 : -1.0;
+            const double n = 1.0 / sqrt(tt * tt + 1.0);
+            rr = Rot2{n, -sign_t * (m01 / fabs(m01)) * fabs(tt) * n};
+        }
+        const Rot2 rl{r1.c * rr.c - r1.s * -rr.s, r1.c * -rr.s + r1.s * rr.c}; // r1 composed with rr^T
+        const Rot2 rt{rr.c, -rr.s};
+        rot2_apply(w10, w11, w00, w01, rl); // rows 1 and 0 of W
+        rot2_apply(w01, w11, w00, w10, rt); // columns 1 and 0 of W
+        rot2_apply(v01, v11, v00, v10, rt); // columns 1 and 0 of V
+        max_diag = fmax(max_diag, fmax(fabs(w11), fabs(w00)));
+    }
+    if (fabs(w11) * scale > fabs(w00) * scale)
+    {
+        const double a = v00, b = v10;
+        v00 = v01;
+        v10 = v11;
+        v01 = a;
+        v11 = b;
+    }
+    return true;
+}
+
+// PCA box (polygonizer.cpp:280-362) in FP64 by one thread: mean, centred X^T X / (n - 1), the
+// JacobiSVD axes, rotate, min/max, corners back to the original frame.
 __device__ void pca_box(const double2* P, int n, lp_bounding_box* out)
 {
     lp_bounding_box box;
@@ -328,30 +410,31 @@ __device__ void pca_box(const double2* P, int n, lp_bounding_box* out)
         sxx /= (n - 1);
         sxy /= (n - 1);
         syy /= (n - 1);
-        const double theta = 0.5 * atan2(2.0 * sxy, sxx - syy);
-        const double v00 = cos(theta), v10 = sin(theta);
-        const double v01 = -v10, v11 = v00;
-        double mnx = DBL_MAX, mxx = -DBL_MAX, mny = DBL_MAX, mxy = -DBL_MAX;
-        for (int i = 0; i < n; ++i)
+        double v00, v01, v10, v11;
+        if (pca_axes(sxx, sxy, syy, v00, v01, v10, v11))
         {
-            const double dx = P[i].x - mx, dy = P[i].y - my;
-            const double rx = dx * v00 + dy * v10;
-            const double ry = dx * v01 + dy * v11;
-            mnx = fmin(mnx, rx);
-            mxx = fmax(mxx, rx);
-            mny = fmin(mny, ry);
-            mxy = fmax(mxy, ry);
+            double mnx = DBL_MAX, mxx = -DBL_MAX, mny = DBL_MAX, mxy = -DBL_MAX;
+            for (int i = 0; i < n; ++i)
+            {
+                const double dx = P[i].x - mx, dy = P[i].y - my;
+                const double rx = dx * v00 + dy * v10;
+                const double ry = dx * v01 + dy * v11;
+                mnx = fmin(mnx, rx);
+                mxx = fmax(mxx, rx);
+                mny = fmin(mny, ry);
+                mxy = fmax(mxy, ry);
+            }
+            const double xs[4] = {mnx, mxx, mxx, mnx};
+            const double ys[4] = {mny, mny, mxy, mxy};
+            for (int k = 0; k < 4; ++k)
+            {
+                box.corners[k][0] = xs[k] * v00 + ys[k] * v01 + mx;
+                box.corners[k][1] = xs[k] * v10 + ys[k] * v11 + my;
+            }
+            box.area = __double2float_rn((mxx - mnx) * (mxy - mny));
+            box.angle_rad = __double2float_rn(atan2(v10, v00));
+            box.is_valid = 1;
         }
-        const double xs[4] = {mnx, mxx, mxx, mnx};
-        const double ys[4] = {mny, mny, mxy, mxy};
-        for (int k = 0; k < 4; ++k)
-        {
-            box.corners[k][0] = xs[k] * v00 + ys[k] * v01 + mx;
-            box.corners[k][1] = xs[k] * v10 + ys[k] * v11 + my;
-        }
-        box.area = __double2float_rn((mxx - mnx) * (mxy - mny));
-        box.angle_rad = __double2float_rn(atan2(v10, v00));
-        box.is_valid = 1;
     }
     *out = box;
 }
@@ -413,11 +496,11 @@ __device__ __forceinline__ void sum_xy_fp64(const double2* P, int n, double& sx,
     }
 }
 
-// PCA box by one warp. The mean and the covariance sums run in FP64 in the reference's order (the
-// principal angle is ill-conditioned exactly where those sums nearly cancel, so they are kept
-// bit-identical); a = sxx - syy and b = 2 sxy are formed in FP64 too. From there the angle, the
-// rotation and the extents use FP32 (relative error ~1e-7 of the cluster extent, far inside the
-// tolerance the box is held to), the corners add the FP64 mean back.
+// PCA box by one warp, every step in FP64 in the reference's order: the mean, the covariance sums
+// (the principal axis is ill-conditioned exactly where they nearly cancel), the JacobiSVD axes
+// (pca_axes, evaluated by every lane alike), the rotated extents (lanes stride over the vertices;
+// min and max do not depend on order) and the corners. The box equals the single-thread pca_box
+// bit for bit.
 __device__ void pca_box_warp(const double2* P, int n, lp_bounding_box* out)
 {
     const uint32_t lane = lane_id();
@@ -460,35 +543,39 @@ __device__ void pca_box_warp(const double2* P, int n, lp_bounding_box* out)
         const double cq = acc / static_cast<double>(n - 1);
         const double sxx = __shfl_sync(0xffffffffu, cq, 0), sxy = __shfl_sync(0xffffffffu, cq, 1),
                      syy = __shfl_sync(0xffffffffu, cq, 2);
-        const float theta = 0.5f * lpm::cr_atan2f(__double2float_rn(2.0 * sxy), __double2float_rn(sxx - syy));
-        float v10, v00;
-        sincosf(theta, &v10, &v00);
-        const float v01 = -v10, v11 = v00;
-        float mnx = FLT_MAX, mxx = -FLT_MAX, mny = FLT_MAX, mxy = -FLT_MAX;
-        for (int i = static_cast<int>(lane); i < n; i += 32)
+        double v00, v01, v10, v11;
+        if (pca_axes(sxx, sxy, syy, v00, v01, v10, v11))
         {
-            const float dx = __double2float_rn(P[i].x - mx), dy = __double2float_rn(P[i].y - my);
-            const float rx = dx * v00 + dy * v10;
-            const float ry = dx * v01 + dy * v11;
-            mnx = fminf(mnx, rx);
-            mxx = fmaxf(mxx, rx);
-            mny = fminf(mny, ry);
-            mxy = fmaxf(mxy, ry);
+            double mnx = DBL_MAX, mxx = -DBL_MAX, mny = DBL_MAX, mxy = -DBL_MAX;
+            for (int i = static_cast<int>(lane); i < n; i += 32)
+            {
+                const double dx = P[i].x - mx, dy = P[i].y - my;
+                const double rx = dx * v00 + dy * v10;
+                const double ry = dx * v01 + dy * v11;
+                mnx = fmin(mnx, rx);
+                mxx = fmax(mxx, rx);
+                mny = fmin(mny, ry);
+                mxy = fmax(mxy, ry);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                mnx = fmin(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+                mxx = fmax(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+                mny = fmin(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+                mxy = fmax(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+            }
+            const double xs[4] = {mnx, mxx, mxx, mnx};
+            const double ys[4] = {mny, mny, mxy, mxy};
+            for (int k = 0; k < 4; ++k)
+            {
+                box.corners[k][0] = xs[k] * v00 + ys[k] * v01 + mx;
+                box.corners[k][1] = xs[k] * v10 + ys[k] * v11 + my;
+            }
+            box.area = __double2float_rn((mxx - mnx) * (mxy - mny));
+            box.angle_rad = __double2float_rn(atan2(v10, v00));
+            box.is_valid = 1;
         }
-        mnx = warp_min_f(mnx);
-        mxx = warp_max_f(mxx);
-        mny = warp_min_f(mny);
-        mxy = warp_max_f(mxy);
-        const float xs[4] = {mnx, mxx, mxx, mnx};
-        const float ys[4] = {mny, mny, mxy, mxy};
-        for (int k = 0; k < 4; ++k)
-        {
-            box.corners[k][0] = static_cast<double>(xs[k] * v00 + ys[k] * v01) + mx;
-            box.corners[k][1] = static_cast<double>(xs[k] * v10 + ys[k] * v11) + my;
-        }
-        box.area = (mxx - mnx) * (mxy - mny);
-        box.angle_rad = theta; // atan2(sin t, cos t) = t for t in (-pi/2, pi/2]
-        box.is_valid = 1;
     }
     if (lane == 0)
         *out = box;
@@ -2087,9 +2174,13 @@ extern "C" lp_status lp_convex_hull_noalloc(const double* d_xy, uint32_t n, int3
         scratch = g_noalloc_ptr[dev];
     }
     const cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // the status is this launch's own (cudaLaunchKernel's return value), so an error left behind
+    // by some other code in the process is neither reported as this call's nor cleared
+    cudaError_t e;
     if (n < 3)
     {
-        k_hull_noalloc_small<<<1, 32, 0, st>>>(n, d_indices_out, d_n_out);
+        void* args[] = {&n, &d_indices_out, &d_n_out};
+        e = cudaLaunchKernel(reinterpret_cast<const void*>(&k_hull_noalloc_small), dim3(1), dim3(32), args, 0, st);
     }
     else
     {
@@ -2097,8 +2188,10 @@ extern "C" lp_status lp_convex_hull_noalloc(const double* d_xy, uint32_t n, int3
         // previous call's contents never leak into this one
         auto* sort_buf = reinterpret_cast<lpg::HPt<double>*>(scratch);
         int* stack = reinterpret_cast<int*>(static_cast<unsigned char*>(scratch) + kNoallocSortBytes);
-        lpg::k_hull_single<<<1, lpg::kHullThreads, 0, st>>>(reinterpret_cast<const double2*>(d_xy), n, sort_buf, stack,
-                                                          d_indices_out, d_n_out);
+        const double2* xy = reinterpret_cast<const double2*>(d_xy);
+        void* args[] = {&xy, &n, &sort_buf, &stack, &d_indices_out, &d_n_out};
+        e = cudaLaunchKernel(reinterpret_cast<const void*>(&lpg::k_hull_single), dim3(1), dim3(lpg::kHullThreads), args,
+                             0, st);
     }
-    return cudaGetLastError() == cudaSuccess ? LP_OK : LP_ERR_CUDA;
+    return e == cudaSuccess ? LP_OK : LP_ERR_CUDA;
 }

@@ -4,6 +4,7 @@ the synthetic scan generator, a PCD reader and comparison helpers."""
 from __future__ import annotations
 
 import ctypes
+import itertools
 import os
 import sys
 
@@ -298,26 +299,36 @@ def r_process(xyzi, ring, seg_cfg, pipeline):
 
 # --------------------------------------------------------------------------------- comparisons
 def box_corner_set_close(b1, b2, tol=1e-4):
-    """Corners of two boxes describe the same rectangle within tol (any corner order)."""
+    """Corners of two boxes describe the same rectangle within tol: some one-to-one assignment of
+    the corners (any order) keeps every pair within tol. All 24 assignments are tried; a greedy
+    nearest-corner match would fail on boxes narrower than the tolerance, whose corners pair up
+    ambiguously."""
     if bool(b1.is_valid) != bool(b2.is_valid):
         return False
     if not b1.is_valid:
         return True
     c1, c2 = b1.corners_array(), b2.corners_array()
-    used = set()
-    for p in c1:
-        d = np.abs(c2 - p).max(axis=1)
-        j = int(np.argmin(d))
-        if d[j] > tol or j in used:
-            return False
-        used.add(j)
-    return True
+    d = np.abs(c1[:, None, :] - c2[None, :, :]).max(axis=2)  # d[i, j]: corner i of b1 to corner j of b2
+    return any(max(d[i, p[i]] for i in range(4)) <= tol for p in itertools.permutations(range(4)))
 
 
 def boxes_identical(b1, b2):
     return (b1.is_valid == b2.is_valid and (not b1.is_valid or (
         np.array_equal(b1.corners_array(), b2.corners_array()) and b1.area == b2.area
         and b1.angle_rad == b2.angle_rad)))
+
+
+def pca_boxes_equal(b1, b2):
+    """PCA boxes computed by the same binary64 steps: validity, corners (in order) and area
+    identical; the angle (binary64 atan2 of the axis, rounded to float) within one float ulp,
+    since the device's and the host's atan2 may differ in the last binary64 bit."""
+    if bool(b1.is_valid) != bool(b2.is_valid):
+        return False
+    if not b1.is_valid:
+        return True
+    ulp = float(np.spacing(np.float32(abs(b2.angle_rad))))
+    return (np.array_equal(b1.corners_array(), b2.corners_array()) and b1.area == b2.area
+            and abs(b1.angle_rad - b2.angle_rad) <= ulp)
 
 
 def same_partition(a, b):

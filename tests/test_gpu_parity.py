@@ -1,7 +1,8 @@
 """GPU parity: every stage through the C ABI against the CPU oracle (correctly rounded libm mode)
 on seeded synthetic scans and the committed reference fixtures. Integer outputs (labels,
-partitions, hull index sequences, masks) must be identical; calipers boxes identical; PCA box
-corners within 1e-4 m as a set."""
+partitions, hull index sequences, masks) must be identical; calipers boxes identical; PCA boxes
+within the reference contract (corners within 1e-4 m as a set) and, beyond it, identical in
+corners and area (the device follows the oracle's binary64 steps; angle within one float ulp)."""
 import ctypes
 import glob
 import os
@@ -167,7 +168,35 @@ def test_polygons(ctx):
         if len(hp) >= 2:
             assert np.array_equal(poly.findAntipodalPairsOfConvexHull(hp), T.o_antipodal(hp))
         assert T.boxes_identical(poly.boundingBoxRotatingCalipers(hp), T.o_calipers(hp))
-        assert T.box_corner_set_close(poly.boundingBoxPrincipalComponentAnalysis(hp), T.o_pca(hp)[0], 1e-4)
+        pb = poly.boundingBoxPrincipalComponentAnalysis(hp)
+        assert T.box_corner_set_close(pb, T.o_pca(hp)[0], 1e-4)
+        assert T.pca_boxes_equal(pb, T.o_pca(hp)[0])
+
+
+def test_pca_thin_hulls(ctx):
+    """The two near-collinear hulls of the 64-scan workload (tests/golden/thin_hulls.npz, 6-8 cm
+    long and under a micrometre wide) through lp_bounding_box_pca: the reference's box."""
+    g = np.load(os.path.join(T.GOLDEN, "thin_hulls.npz"))
+    off = np.concatenate([[0], np.cumsum(g["sizes"])])
+    poly = lp.Polygonizer(ctx)
+    for t in range(len(g["sizes"])):
+        hp = np.ascontiguousarray(g["points"][off[t]:off[t + 1]])
+        pb = poly.boundingBoxPrincipalComponentAnalysis(hp)
+        assert T.pca_boxes_equal(pb, T.o_pca(hp)[0]), t
+        assert np.array_equal(pb.corners_array(), g["pca"][t][:8].reshape(4, 2)), t
+
+
+def test_pca_workload_scans_exact(ctx):
+    """Scans 20 and 56 of the 64-scan workload, whose thin clusters 64 and 57 once gave PCA boxes
+    beyond 1e-4 m: every PCA box of both scans (warp path of the hull kernel) equals the oracle's."""
+    pipe = lp.PipelineConfig.default()
+    for s in (20, 56):
+        x, ring, cfg = T.synth_scan(3, s)
+        got = lp.process_batch(ctx, [x], pipe, [cfg], [ring])[0]
+        want = T.o_process(x, ring, cfg, pipe)
+        assert got.n_clusters == want.n_clusters
+        bad = [c for c in range(want.n_clusters) if not T.pca_boxes_equal(got.obb_pca[c], want.obb_pca[c])]
+        assert not bad, (s, bad[:5])
 
 
 @pytest.mark.parametrize("w,s", [(1, 0), (3, 0)])
@@ -238,6 +267,7 @@ def compare_scan(got, want, label=""):
         assert T.boxes_identical(a, b), label
     for a, b in zip(got.obb_pca, want.obb_pca):
         assert T.box_corner_set_close(a, b, 1e-4), label
+        assert T.pca_boxes_equal(a, b), label
 
 
 def test_pipeline_batch_mixed(ctx):

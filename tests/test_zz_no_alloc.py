@@ -1,7 +1,8 @@
 """lp_convex_hull_noalloc: the hull entry point for callers that cannot allocate device memory
 (its working memory is a static device array inside the library). Checked through the C ABI
-against lp_convex_hull on two calls in a row, a large then a small polygon, so that leftovers of
-the first call in the shared array would show. The caller's buffers are device tensors."""
+against the oracle's convexHull and against lp_convex_hull on two calls in a row, a large then a
+small polygon, so that leftovers of the first call in the shared array would show. The caller's
+buffers are device tensors."""
 import ctypes
 
 import numpy as np
@@ -30,7 +31,8 @@ def test_noalloc_hull_matches_lp_convex_hull(ctx):
     for n in (40000, 700):  # two calls in a row: the second reuses the array the first filled
         pts = (rng.normal(size=(n, 2)) * 8.0).astype(np.float32).astype(np.float64)
         pts[: n // 10] = np.round(pts[: n // 10], 1)  # duplicates and collinear runs
-        want = poly.convexHull(pts)
+        want = T.o_hull(pts)
+        assert np.array_equal(poly.convexHull(pts), want)
         d_xy = torch.from_numpy(pts).cuda()
         d_out = torch.full((n + 1,), -7, dtype=torch.int32, device="cuda")
         d_n = torch.zeros(1, dtype=torch.int32, device="cuda")

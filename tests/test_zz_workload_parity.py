@@ -2,7 +2,7 @@
 (8.3 M points, seeds 1000*3 + scan), run as one prepared batch (four concurrent parts) replayed from
 its captured CUDA graph, equals the oracle scan by scan: segmentation and cluster labels, cluster
 counts, hull index sequences and z ranges identical, calipers boxes identical, PCA box corners
-within 1e-4 m. The oracle runs one scan per host thread. A scan that differs is run again as a
+within 1e-4 m and identical to the oracle's (same binary64 steps). The oracle runs one scan per host thread. A scan that differs is run again as a
 one-scan batch, and the failure message says whether its divergence repeats there."""
 import os
 from concurrent.futures import ThreadPoolExecutor
@@ -49,6 +49,9 @@ def differences(g, w):
     pca = [c for c in range(k) if not T.box_corner_set_close(g.obb_pca[c], w.obb_pca[c], 1e-4)]
     if pca:
         d.append(f"pca boxes of {len(pca)} clusters from {pca[0]}")
+    exact = [c for c in range(k) if not T.pca_boxes_equal(g.obb_pca[c], w.obb_pca[c])]
+    if exact and not pca:
+        d.append(f"pca boxes of {len(exact)} clusters within 1e-4 m but not identical, from {exact[0]}")
     return ", ".join(d)
 
 
