@@ -334,7 +334,7 @@ def run_dror(args):
     res = batch.download()
     noise_pts = int(sum(int(r.noise_labels.sum()) for r in res))
     _, agg = kernel_profile(batch)
-    dror_kernels = [k for k in agg if k.startswith("k_dror")]
+    dror_kernels = [k for k in agg if k.startswith("k_kt_")]
     dror_ms = sum(agg[k][1] for k in dror_kernels)
     total_ms = sum(a[1] for a in agg.values())
     batch.capture_graph()

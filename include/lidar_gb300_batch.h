@@ -48,6 +48,12 @@ lp_status lp_batch_profile(lp_context* ctx, lp_batch* batch, char* names, uint32
 lp_status lp_host_alloc(uint64_t bytes, void** out);
 void lp_host_free(void* p);
 
+/* The kd-tree the outlier filter builds on the device for the cloud xyz (n points, stride floats
+ * apart): per node position, x, y, z and the subtree size (as uint32 bits), n x 4 floats into
+ * nodes_out. It equals the reference's KDTree::rebuild (kdtree.hpp:161-214) node for node; used by
+ * the parity tests. No counterpart in the reference. */
+lp_status lp_debug_kdtree(lp_context* ctx, const float* xyz, uint32_t stride, uint32_t n,
+                          const lp_noise_remover_config* cfg, float* nodes_out);
 /* Device evaluation of the library's correctly rounded binary32 functions (kind 0 atan2(a, b),
  * 1 atan(a), 2 exp(a), 3 the reference's atan2 approximation; 4, 5, 6 the same three functions
  * without their float-float first stage); used by the parity tests. */

@@ -100,7 +100,7 @@ lp_status plan(lp_context* ctx, lp_batch& B)
     hb = BatchHost{};
     hb.nscan = static_cast<int>(R.scans.size());
     hb.any_noise = (R.stages & ST_NOISE) != 0;
-    uint64_t pt = 0, pix = 0, row = 0, tile = 0, slice = 0, cell = 0, nearc = 0, hash = 0, cl = 0, dh = 0;
+    uint64_t pt = 0, pix = 0, row = 0, tile = 0, slice = 0, cell = 0, nearc = 0, hash = 0, cl = 0;
     const bool seg = (R.stages & ST_SEG) != 0;
     for (const ScanIn& in : R.scans)
     {
@@ -173,17 +173,14 @@ lp_status plan(lp_context* ctx, lp_batch& B)
         sd.dror_s2 = std::pow(static_cast<double>(R.nr.radius_multiplier_m_per_m), 2.0); // noise_remover.cpp:49-52
         sd.dror_rmin2 = R.nr.min_search_radius_m * R.nr.min_search_radius_m;
         sd.dror_k = R.nr.min_neighbours;
-        sd.dhash_off = static_cast<uint32_t>(dh);
-        sd.dhash_cap = next_pow2(std::max(64u, 4u * in.n)); // cells <= 3n band insertions
         pt += in.n;
         tile += div_up(std::max(in.n, 1u), 1024u);
         hash += sd.hash_cap;
         cl += sd.cluster_cap;
-        dh += sd.dhash_cap;
         hb.scans.push_back(sd);
     }
     const uint64_t lim = 0x7fffffffull;
-    if (pt > lim / 4 || pix > lim / 8 || hash > lim || cell > lim || dh > lim || cl > lim)
+    if (pt > lim / 8 || pix > lim / 8 || hash > lim || cell > lim || cl > lim)
         return fail(ctx, LP_ERR_CAPACITY, "batch too large for 32-bit indexing; split it");
     hb.ntiles = static_cast<uint32_t>(tile);
     hb.nslices = static_cast<uint32_t>(slice);
@@ -199,7 +196,6 @@ lp_status plan(lp_context* ctx, lp_batch& B)
     b.nrows = static_cast<uint32_t>(row);
     b.nhash = static_cast<uint32_t>(hash);
     b.ncl = static_cast<uint32_t>(cl);
-    b.ndhash = static_cast<uint32_t>(dh);
     return LP_OK;
 }
 
@@ -225,7 +221,7 @@ size_t carve(lp_batch& B, char* base)
     put(b.state, S);
     put(b.io, S);
     put(b.io_ret, S);
-    const uint32_t maxlen = std::max({N, b.npix, b.nhash, b.ncell, b.ndhash, b.ncl, b.ntiles, b.nnear}) + 2;
+    const uint32_t maxlen = std::max({N, b.npix, b.nhash, b.ncell, b.ncl, b.ntiles, b.nnear}) + 2;
     put(B.scan_sums, div_up(maxlen, static_cast<uint32_t>(kScanTile)) + 4);
     float4* src;
     put(src, N);
@@ -244,13 +240,23 @@ size_t carve(lp_batch& B, char* base)
         put(b.src_pos, N + 1);
         put(b.pts, N);
         put(b.pt_src, N);
-        put(b.dkey, b.ndhash);
-        put(b.dcnt, b.ndhash + 1);
-        put(b.dstart, b.ndhash + 1);
-        put(b.dslot, 3ull * N); // up to three band insertions per point
-        put(b.drank, 3ull * N);
-        put(b.dorder, 3ull * N);
-        put(b.dr2, N);
+        // kd-tree replay (lp_kdtree.cu): leftover pool of kKtPoolPerPoint entries per point (the
+        // searches leave about 4 per point; a fuller pool is reported as a capacity error)
+        b.kpool_cap = static_cast<uint32_t>(std::min<uint64_t>(static_cast<uint64_t>(kKtPoolPerPoint) * N + 64, 0x7fffffffull));
+        put(b.kt, N);
+        put(b.kbb, 2ull * N);
+        put(b.kscr, 2ull * N);
+        put(b.kown, N);
+        put(b.kshort, N + 1);
+        put(b.klo_n, N + 1);
+        put(b.klo_off, N + 1);
+        put(b.klo_at, N);
+        put(b.kpool, b.kpool_cap);
+        put(b.kflat, b.kpool_cap);
+        put(b.kq, N);
+        put(b.kc, N);
+        put(b.kpiece, 2ull * N + 2ull * S);
+        put(b.kctr, 4);
     }
     else
     {
@@ -433,8 +439,6 @@ lp_status execute(lp_context* ctx, lp_batch& B)
     launch_state_init(L, b, noise ? 1 : 0);
     if (noise)
     {
-        LP_CUDA(ctx, cudaMemsetAsync(b.dkey, 0xff, static_cast<size_t>(b.ndhash) * 8, st));
-        LP_CUDA(ctx, cudaMemsetAsync(b.dcnt, 0, (static_cast<size_t>(b.ndhash) + 1) * 4, st));
         launch_noise(L, b, B.hb, R.nr);
         if (R.stages & (ST_SEG | ST_CLUSTER | ST_ALL_OBS | ST_RING))
             launch_noise_compaction(L, b, B.hb);
@@ -1189,6 +1193,30 @@ lp_status lp_noise_remove(lp_context* ctx, const float* xyz, uint32_t stride, ui
     B.run.scans.push_back(in);
     LP_TRY(run_once(ctx, B));
     LP_TRY(copy_d2h(ctx, labels_out, B.b.noise, n));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LP_OK;
+}
+
+lp_status lp_debug_kdtree(lp_context* ctx, const float* xyz, uint32_t stride, uint32_t n,
+                          const lp_noise_remover_config* cfg, float* nodes_out)
+{
+    if (!ctx || !cfg || (n && (!xyz || !nodes_out)) || stride < 3)
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument or stride < 3");
+    if (n == 0)
+        return LP_OK;
+    LP_TRY(ensure_device(ctx));
+    lp_batch& B = cached(ctx);
+    B.run = Run{};
+    B.run.stages = ST_NOISE;
+    B.run.nr = *cfg;
+    ScanIn in;
+    in.xyzi = xyz;
+    in.stride = stride;
+    in.n = n;
+    B.run.scans.push_back(in);
+    LP_TRY(run_once(ctx, B));
+    LP_CUDA(ctx, cudaMemcpyAsync(nodes_out, B.b.kt, static_cast<size_t>(n) * sizeof(float4), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
     LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return LP_OK;
 }

@@ -38,6 +38,7 @@ enum : uint8_t
 
 // Jump-convolution weight record of a queued pixel: 24 fresh weights, their sum, padding to a
 // multiple of 16 bytes (vector loads).
+constexpr uint32_t kKtPoolPerPoint = 8; // leftover search entries per point the DROR pool holds
 constexpr uint32_t kJwStride = 28;
 // Per image row of the jump convolution: lastq[3], pad, 24 stale weights, 24 stale label infos
 // (kJrowNoUpdate: the row leaves the slot as it was; kJrowDynamic | pixel: the final colour of
@@ -182,15 +183,22 @@ struct BatchDev
     int2* hs_pairs;       // antipodal pairs, at 4 * cl_start + 16 * cluster
     uint32_t* queue;      // [0] clusters in the batch, [1] hull work-queue head
 
-    // ---- DROR --------------------------------------------------------------------------------
-    uint32_t ndhash;           // grid-cell hash slots
-    unsigned long long* dkey;  // per slot: packed cell coordinates or ~0
-    uint32_t* dcnt;            // per slot: points in the cell (ndhash + 1)
-    uint32_t* dstart;          // exclusive scan of dcnt
-    uint32_t* dslot;           // per input point: hash slot
-    uint32_t* drank;           // per input point: arrival rank in its cell
-    uint32_t* dorder;          // input points grouped by cell
-    float* dr2;                // per input point: squared search radius
+    // ---- DROR (reference kd-tree replay, lp_kdtree.cu) ------------------------------------------
+    float4* kt;                // per input point: tree node record by position (x, y, z, subtree size bits)
+    float4* kbb;               // 2 per input point: subtree box (lo, hi) by node position
+    uint32_t* kscr;            // 2 per input point: candidate positions of the parallel partition
+    uint32_t* kown;            // per point: count of its own search (capped at min_neighbours)
+    uint32_t* kshort;          // per point (+1): 1 if its own search fell short -> exclusive scan
+    uint32_t* klo_n;           // per point (+1): entries its search left behind
+    uint32_t* klo_off;         // exclusive scan of klo_n: their place in kflat
+    uint32_t* klo_at;          // per point: their place in kpool
+    uint32_t* kpool;           // leftover entries as searches produce them (kpool_cap)
+    uint32_t* kflat;           // the points' leftovers in point order (kpool_cap)
+    uint32_t kpool_cap;
+    uint32_t* kq;              // short points in order
+    uint4* kc;                 // per short point: count, stop entry, left entries (pool at, count)
+    uint2* kpiece;             // per scan: stack of pieces (2 n + 2 per scan)
+    uint32_t* kctr;            // [0] pool head
 
     // ---- outputs per input point ---------------------------------------------------------------
     uint32_t* out_seg;

@@ -2086,6 +2086,7 @@ void launch_polygons(Launcher& L, const BatchDev& b, const BatchHost& hb, int co
 
 void init_kernel_attributes()
 {
+    init_kdtree_attributes();
     cudaFuncSetAttribute(k_hull, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kHullDynSmem));
 }
 

@@ -65,7 +65,6 @@ struct ScanDev
     double dror_s2;
     float dror_rmin2;
     uint32_t dror_k;
-    uint32_t dhash_off, dhash_cap;
 };
 
 // Dynamic per-scan values produced on the device.
@@ -73,8 +72,7 @@ struct ScanState
 {
     uint32_t err;
     uint32_t n_pts;     // points entering segmentation (after noise removal)
-    uint32_t dmax_r2_bits;
-    float dcell;        // DROR grid cell edge
+    uint32_t reserved_dror[2];
     // RANSAC (segmenter.cpp:321-479)
     uint32_t n_cand, cand_off;
     int32_t ransac_ok;

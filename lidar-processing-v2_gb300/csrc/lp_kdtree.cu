@@ -1,0 +1,950 @@
+// lp_kdtree.cu — dynamic-radius outlier removal exactly as the reference's kd-tree search leaves it.
+//
+// Reference: NoiseRemover::filter (lidar_processing_lib/src/noise_remover.cpp:38-68) over
+// KDTree::rebuild (kdtree.hpp:161-214) and KDTree::radius_search_k_nearest (kdtree.hpp:339-397).
+// Per point, in input order: squared radius r2 = max(float(s2 * double(x*x + y*y)), rmin^2); a
+// depth-first search from the root counts nodes with d0 + (d1 + d2) <= r2 (dk = (q_k - p_k)^2 in
+// binary32, query first) and stops at min_neighbours; fewer found means NOISE. The search's stack
+// is a member of the tree and is not cleared when the search stops early: the next point's search
+// pushes the root on top of what is left, and once its own subtrees are exhausted it carries on
+// through the subtrees earlier searches left behind, counting points there again. A point with
+// fewer than min_neighbours true neighbours can therefore still reach the count. This file
+// reproduces that sequence exactly (every scan starts with an empty stack, as a new NoiseRemover):
+//
+//   1. Tree (k_kt_level): the reference builds its tree by std::nth_element on the middle of
+//      each range (x, y, z by depth); which of several points with equal coordinates lands on
+//      which side depends on that library routine's swaps. The build replays libstdc++'s
+//      introselect step for step (median of three, unguarded Hoare partition, insertion sort at
+//      three elements, heap selection at the depth limit). Large ranges: one CTA per range, the
+//      Hoare partition replayed in parallel (the t-th element >= pivot from the left is swapped
+//      with the t-th element <= pivot from the right while the first lies left of the second);
+//      ranges of at most kKtSmall points finish their whole subtree in shared memory. Node
+//      children follow from the range arithmetic alone, so a node record is its point and its
+//      subtree size; subtree boxes (k_kt_box_level) serve the skip test of steps 3 and 4.
+//   2. Own search (k_kt_own, one thread per point): the point's search from the root, in the
+//      reference's push order, until min_neighbours or exhaustion. A point that reaches the
+//      count leaves the rest of its stack behind: those entries go to a pool, then into one
+//      array in point order (k_kt_flat). Points that exhaust their own search ("short" points)
+//      are listed in order (k_kt_short).
+//   3. Own segment (k_kt_segment, one thread per short point): the stack a short point meets is
+//      the leftovers of the points since the previous short point (a contiguous piece of the
+//      array, newest on top) above whatever the previous short point left. The point walks its
+//      piece from the top; an entry whose subtree box is farther than the radius is consumed
+//      without a match (skipped); the others are searched exactly. Reaching the count there
+//      decides the point (VALID) and records where it stopped and the entries it left.
+//   4. Chain (k_kt_chain, one CTA per scan): the short points in order, with the stack below the
+//      pieces as a list of pieces; a point not decided in step 3 consumes pieces from the top,
+//      its threads testing and searching the entries of a piece in parallel, an ordered prefix
+//      of their counts finding the entry where the count is reached. Exhausting the stack means
+//      NOISE and an empty stack for the next point.
+// The result equals the reference's sequential search bit for bit (same binary32 expressions,
+// same visiting order, same stop points); the tree's node positions equal the reference's.
+#include "lp_batch.cuh"
+#include "lp_common.cuh"
+#include "lp_stages.hpp"
+
+namespace lpg
+{
+namespace
+{
+constexpr uint32_t kKtSmall = 2048;    // ranges built in shared memory by one CTA
+constexpr uint32_t kKtSeqMax = 64;     // ranges built by one thread (introselect as written)
+constexpr int kKtThreads = 512;        // tree build CTAs
+constexpr int kKtItems = 8;            // elements per thread per tile of the parallel partition
+constexpr int kKtStack = 64;           // search stack entries (>= tree depth + 1 for 2^62 points)
+constexpr int kChainThreads = 256;
+constexpr uint32_t kNone = 0xffffffffu;
+
+// Stack entries: node position (scan-local) << 2 | axis.
+__device__ __forceinline__ uint32_t kt_entry(uint32_t m, int ax)
+{
+    return (m << 2) | static_cast<uint32_t>(ax);
+}
+
+__device__ __forceinline__ float kt_coord(const float4& r, int ax)
+{
+    return ax == 0 ? r.x : (ax == 1 ? r.y : r.z);
+}
+
+__device__ __forceinline__ float kt_radius2(const ScanDev& sd, const float4& p)
+{
+    // noise_remover.cpp:55-57: float products and sum, widened, scaled, narrowed, floored
+    const double rho2 = static_cast<double>((p.x * p.x) + (p.y * p.y));
+    return fmaxf(__double2float_rn(sd.dror_s2 * rho2), sd.dror_rmin2);
+}
+
+__device__ __forceinline__ uint32_t floor_log2_u(uint32_t v)
+{
+    return 31u - static_cast<uint32_t>(__clz(v));
+}
+
+// Range of node slot j (0 <= j < 2^level) of the implicit tree over [0, n): the bits of j from the
+// top choose left (0) or right (1) at each level. Returns false where the range does not exist.
+// *plen receives the parent's length (n for the root).
+__device__ __forceinline__ bool kt_range(uint32_t n, int level, uint32_t j, uint32_t& b, uint32_t& e, uint32_t* plen)
+{
+    b = 0;
+    e = n;
+    uint32_t parent = n;
+    for (int l = level - 1; l >= 0; --l)
+    {
+        if (e <= b)
+            return false;
+        const uint32_t mid = b + (e - b) / 2;
+        parent = e - b;
+        if ((j >> l) & 1u)
+            b = mid + 1;
+        else
+            e = mid;
+    }
+    if (plen)
+        *plen = parent;
+    return e > b;
+}
+
+// ---------------------------------------------------------------------------------------------
+// libstdc++ introselect, one thread (std::nth_element as GCC's <bits/stl_algo.h> performs it).
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void kt_swap(float4* a, uint32_t i, uint32_t j)
+{
+    const float4 t = a[i];
+    a[i] = a[j];
+    a[j] = t;
+}
+
+// The median of a[first + 1], a[mid], a[last - 1] is swapped into a[first].
+__device__ void kt_median_to_first(float4* a, uint32_t first, uint32_t last, int ax)
+{
+    const uint32_t x = first + 1, y = first + (last - first) / 2, z = last - 1;
+    const float vx = kt_coord(a[x], ax), vy = kt_coord(a[y], ax), vz = kt_coord(a[z], ax);
+    uint32_t m;
+    if (vx < vy)
+        m = (vy < vz) ? y : ((vx < vz) ? z : x);
+    else
+        m = (vx < vz) ? x : ((vy < vz) ? z : y);
+    kt_swap(a, first, m);
+}
+
+// Unguarded Hoare partition of [first + 1, last) around a[first]; returns the cut. The median of
+// three guarantees an element >= pivot and one <= pivot inside the range, which stop the scans;
+// the explicit bounds only keep a malformed input (NaN coordinates) inside the range.
+__device__ uint32_t kt_partition_seq(float4* a, uint32_t first, uint32_t last, int ax)
+{
+    const float p = kt_coord(a[first], ax);
+    uint32_t lo = first + 1, hi = last;
+    for (;;)
+    {
+        while (lo + 1 < last && kt_coord(a[lo], ax) < p)
+            ++lo;
+        --hi;
+        while (hi > first && p < kt_coord(a[hi], ax))
+            --hi;
+        if (!(lo < hi))
+            return lo;
+        kt_swap(a, lo, hi);
+        ++lo;
+    }
+}
+
+__device__ void kt_insertion(float4* a, uint32_t first, uint32_t last, int ax)
+{
+    if (first == last)
+        return;
+    for (uint32_t i = first + 1; i < last; ++i)
+    {
+        const float4 v = a[i];
+        const float kv = kt_coord(v, ax);
+        if (kv < kt_coord(a[first], ax))
+        {
+            for (uint32_t j = i; j > first; --j)
+                a[j] = a[j - 1];
+            a[first] = v;
+        }
+        else
+        {
+            uint32_t j = i;
+            while (j > first + 1 && kv < kt_coord(a[j - 1], ax))
+            {
+                a[j] = a[j - 1];
+                --j;
+            }
+            a[j] = v;
+        }
+    }
+}
+
+// Max-heap sift of value v from `hole` in a[base, base + len) (std::__adjust_heap + __push_heap).
+__device__ void kt_sift(float4* a, uint32_t base, uint32_t hole, uint32_t len, float4 v, int ax)
+{
+    const uint32_t top = hole;
+    uint32_t child = hole;
+    while (len >= 2 && child < (len - 1) / 2)
+    {
+        child = 2 * (child + 1);
+        if (kt_coord(a[base + child], ax) < kt_coord(a[base + child - 1], ax))
+            --child;
+        a[base + hole] = a[base + child];
+        hole = child;
+    }
+    if ((len & 1u) == 0 && len >= 2 && child == (len - 2) / 2)
+    {
+        child = 2 * (child + 1);
+        a[base + hole] = a[base + child - 1];
+        hole = child - 1;
+    }
+    const float kv = kt_coord(v, ax);
+    uint32_t parent = (hole - 1) / 2;
+    while (hole > top && kt_coord(a[base + parent], ax) < kv)
+    {
+        a[base + hole] = a[base + parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    a[base + hole] = v;
+}
+
+// std::__heap_select(first, middle, last) then the swap of first and nth (introselect at the depth
+// limit): a max-heap of [first, nth], every later element smaller than its top replaces it.
+__device__ void kt_heap_select(float4* a, uint32_t first, uint32_t nth, uint32_t last, int ax)
+{
+    const uint32_t mid = nth - first + 1;
+    if (mid >= 2)
+        for (uint32_t parent = (mid - 2) / 2;; --parent)
+        {
+            kt_sift(a, first, parent, mid, a[first + parent], ax);
+            if (parent == 0)
+                break;
+        }
+    for (uint32_t i = first + mid; i < last; ++i)
+        if (kt_coord(a[i], ax) < kt_coord(a[first], ax))
+        {
+            const float4 v = a[i];
+            a[i] = a[first];
+            kt_sift(a, first, 0, mid, v, ax);
+        }
+    kt_swap(a, first, nth);
+}
+
+// Continues an introselect of nth in [first, last) with `depth` rounds left, on one thread.
+__device__ void kt_select_seq(float4* a, uint32_t first, uint32_t nth, uint32_t last, int depth, int ax)
+{
+    while (last - first > 3)
+    {
+        if (depth == 0)
+        {
+            kt_heap_select(a, first, nth, last, ax);
+            return;
+        }
+        --depth;
+        kt_median_to_first(a, first, last, ax);
+        const uint32_t cut = kt_partition_seq(a, first, last, ax);
+        if (cut <= nth)
+            first = cut;
+        else
+            last = cut;
+    }
+    kt_insertion(a, first, last, ax);
+}
+
+// ---------------------------------------------------------------------------------------------
+// One partition round by a whole CTA: median of three into a[first], then the unguarded Hoare
+// partition of [first + 1, last) replayed in parallel. With L_t the t-th position (from the
+// left) holding a value >= pivot and R_t the t-th (from the right) holding a value <= pivot, the
+// sequential loop swaps L_t with R_t for every t with L_t < R_t (T such pairs; these pairs are
+// disjoint) and then stops at min(L_{T+1}, R_T) (L_1 when T = 0): the left scan meets either the
+// next original candidate or the element it swapped to R_T. ge/le receive the candidate
+// positions in ascending order (le reversed gives R). Returns the cut.
+// ---------------------------------------------------------------------------------------------
+struct KtShared
+{
+    float tile[kKtThreads * kKtItems];
+    uint32_t warp_sum[kKtThreads / 32];
+    uint32_t bcast[4];
+};
+
+__device__ uint32_t kt_round_block(float4* a, uint32_t first, uint32_t last, int ax, uint32_t* ge, uint32_t* le,
+                                   KtShared& sh)
+{
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t nwarps = blockDim.x >> 5;
+    if (tid == 0)
+        kt_median_to_first(a, first, last, ax);
+    __syncthreads();
+    const float p = kt_coord(a[first], ax);
+    const uint32_t lo = first + 1, n = last - lo;
+    const uint32_t tile = blockDim.x * kKtItems;
+    uint32_t nge = 0, nle = 0;
+    for (uint32_t base = 0; base < n; base += tile)
+    {
+        const uint32_t cnt = min(tile, n - base);
+        for (uint32_t k = tid; k < cnt; k += blockDim.x)
+            sh.tile[k] = kt_coord(a[lo + base + k], ax);
+        __syncthreads();
+        uint32_t fge = 0, fle = 0, cge = 0, cle = 0;
+#pragma unroll
+        for (int k = 0; k < kKtItems; ++k)
+        {
+            const uint32_t idx = tid * kKtItems + k;
+            if (idx < cnt)
+            {
+                const float v = sh.tile[idx];
+                if (!(v < p))
+                {
+                    fge |= 1u << k;
+                    ++cge;
+                }
+                if (!(p < v))
+                {
+                    fle |= 1u << k;
+                    ++cle;
+                }
+            }
+        }
+        // block exclusive scan of (cge | cle << 16)
+        const uint32_t packed = cge | (cle << 16);
+        uint32_t incl = packed;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= static_cast<uint32_t>(o))
+                incl += t;
+        }
+        if (lane == 31)
+            sh.warp_sum[warp] = incl;
+        __syncthreads();
+        uint32_t wpre = 0, total = 0;
+        for (uint32_t w = 0; w < nwarps; ++w)
+        {
+            const uint32_t s = sh.warp_sum[w];
+            if (w < warp)
+                wpre += s;
+            total += s;
+        }
+        const uint32_t ex = incl - packed + wpre;
+        uint32_t og = nge + (ex & 0xffffu), ol = nle + (ex >> 16);
+#pragma unroll
+        for (int k = 0; k < kKtItems; ++k)
+        {
+            const uint32_t pos = lo + base + tid * kKtItems + k;
+            if (fge & (1u << k))
+                ge[og++] = pos;
+            if (fle & (1u << k))
+                le[ol++] = pos;
+        }
+        nge += total & 0xffffu;
+        nle += total >> 16;
+        __syncthreads();
+    }
+    // T: the largest t with ge[t - 1] < le[nle - t] (monotone in t)
+    if (tid == 0)
+    {
+        uint32_t lo_t = 0, hi_t = min(nge, nle);
+        while (lo_t < hi_t)
+        {
+            const uint32_t mid = (lo_t + hi_t + 1) / 2;
+            if (ge[mid - 1] < le[nle - mid])
+                lo_t = mid;
+            else
+                hi_t = mid - 1;
+        }
+        const uint32_t T = lo_t;
+        uint32_t cut;
+        if (T == 0)
+            cut = ge[0];
+        else
+            cut = min(T < nge ? ge[T] : 0xffffffffu, le[nle - T]);
+        sh.bcast[0] = T;
+        sh.bcast[1] = cut;
+    }
+    __syncthreads();
+    const uint32_t T = sh.bcast[0], cut = sh.bcast[1];
+    for (uint32_t t = tid; t < T; t += blockDim.x)
+        kt_swap(a, ge[t], le[nle - 1 - t]);
+    __syncthreads();
+    return cut;
+}
+
+// Introselect of nth in [first, last) by a whole CTA; rounds on ranges of at most kKtSeqMax
+// elements (and the depth-limit fallback) run on thread 0.
+__device__ void kt_select_block(float4* a, uint32_t first, uint32_t nth, uint32_t last, int ax, uint32_t* ge,
+                                uint32_t* le, KtShared& sh)
+{
+    int depth = 2 * static_cast<int>(floor_log2_u(last - first));
+    while (last - first > kKtSeqMax && depth > 0)
+    {
+        --depth;
+        const uint32_t cut = kt_round_block(a, first, last, ax, ge, le, sh);
+        if (cut <= nth)
+            first = cut;
+        else
+            last = cut;
+    }
+    if (threadIdx.x == 0)
+        kt_select_seq(a, first, nth, last, depth, ax);
+    __syncthreads();
+}
+
+// Subtree of [b0, e0) (at depth d0 of the tree, at most kKtSmall points) built in shared memory;
+// node records get their subtree size in .w; subtree boxes are written bottom-up.
+__device__ void kt_build_small(float4* g, float4* box, uint32_t b0, uint32_t e0, int d0, float4* s, uint32_t* ge,
+                               uint32_t* le, KtShared& sh)
+{
+    const uint32_t n = e0 - b0;
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+        s[k] = g[b0 + k];
+    __syncthreads();
+    // the longest range at depth d has floor(n / 2^d) points (a range of L splits into floor(L/2)
+    // and ceil(L/2) - 1), so depths 0 .. floor(log2 n) hold ranges
+    const int maxd = static_cast<int>(floor_log2_u(n));
+    for (int d = 0; d <= maxd; ++d)
+    {
+        const uint32_t slots = 1u << d;
+        // ranges above kKtSeqMax: the whole CTA, one after the other
+        if ((n >> d) > kKtSeqMax)
+            for (uint32_t j = 0; j < slots; ++j)
+            {
+                uint32_t b, e;
+                if (kt_range(n, d, j, b, e, nullptr) && e - b > kKtSeqMax)
+                    kt_select_block(s, b, b + (e - b) / 2, e, (d0 + d) % 3, ge, le, sh);
+            }
+        // the rest: one thread each
+        for (uint32_t j = threadIdx.x; j < slots; j += blockDim.x)
+        {
+            uint32_t b, e;
+            if (kt_range(n, d, j, b, e, nullptr) && e - b <= kKtSeqMax && e - b > 1)
+                kt_select_seq(s, b, b + (e - b) / 2, e, 2 * static_cast<int>(floor_log2_u(e - b)), (d0 + d) % 3);
+        }
+        __syncthreads();
+    }
+    // subtree sizes and boxes, deepest level first
+    for (int d = maxd; d >= 0; --d)
+    {
+        const uint32_t slots = 1u << d;
+        for (uint32_t j = threadIdx.x; j < slots; j += blockDim.x)
+        {
+            uint32_t b, e;
+            if (!kt_range(n, d, j, b, e, nullptr))
+                continue;
+            const uint32_t m = b + (e - b) / 2;
+            float4 p = s[m];
+            p.w = __uint_as_float(e - b);
+            s[m] = p;
+            float4 lo = make_float4(p.x, p.y, p.z, 0.0f), hi = lo;
+            if (m > b)
+            {
+                const uint32_t c = b0 + b + (m - b) / 2;
+                const float4 cl = box[2 * c], ch = box[2 * c + 1];
+                lo = make_float4(fminf(lo.x, cl.x), fminf(lo.y, cl.y), fminf(lo.z, cl.z), 0.0f);
+                hi = make_float4(fmaxf(hi.x, ch.x), fmaxf(hi.y, ch.y), fmaxf(hi.z, ch.z), 0.0f);
+            }
+            if (m + 1 < e)
+            {
+                const uint32_t c = b0 + m + 1 + (e - m - 1) / 2;
+                const float4 cl = box[2 * c], ch = box[2 * c + 1];
+                lo = make_float4(fminf(lo.x, cl.x), fminf(lo.y, cl.y), fminf(lo.z, cl.z), 0.0f);
+                hi = make_float4(fmaxf(hi.x, ch.x), fmaxf(hi.y, ch.y), fmaxf(hi.z, ch.z), 0.0f);
+            }
+            box[2 * (b0 + m)] = lo;
+            box[2 * (b0 + m) + 1] = hi;
+        }
+        __syncthreads();
+    }
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+        g[b0 + k] = s[k];
+}
+
+__global__ void k_kt_load(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0)
+    {
+        b.klo_n[b.nsrc] = 0; // the scanned arrays' last slots (totals after the scans)
+        b.kshort[b.nsrc] = 0;
+        b.kctr[0] = 0;
+    }
+    if (i >= b.nsrc)
+        return;
+    const float4 p = b.src[i];
+    b.kt[i] = make_float4(p.x, p.y, p.z, 0.0f);
+}
+
+// One level of the build: CTA (scan, slot j). Ranges above kKtSmall are put in order around their
+// middle here; a range of at most kKtSmall whose parent was larger (or the root) builds its whole
+// subtree in shared memory.
+__global__ void __launch_bounds__(kKtThreads) k_kt_level(BatchDev b, int level, uint32_t slots)
+{
+    extern __shared__ float4 kt_smem[];
+    __shared__ KtShared sh;
+    const uint32_t s = blockIdx.x / slots, j = blockIdx.x % slots;
+    if (s >= static_cast<uint32_t>(b.nscan))
+        return;
+    const ScanDev& sd = b.scans[s];
+    uint32_t lb, le, plen;
+    if (!kt_range(sd.n_src, level, j, lb, le, &plen))
+        return;
+    float4* g = b.kt + sd.src_off;
+    float4* box = b.kbb + 2ull * sd.src_off;
+    uint32_t* ge = b.kscr + 2ull * sd.src_off + 2ull * lb;
+    uint32_t* lq = ge + (le - lb);
+    const uint32_t len = le - lb;
+    if (len > kKtSmall)
+    {
+        const uint32_t nth = lb + len / 2;
+        kt_select_block(g, lb, nth, le, level % 3, ge, lq, sh);
+        if (threadIdx.x == 0)
+        {
+            float4 p = g[nth];
+            p.w = __uint_as_float(len);
+            g[nth] = p;
+        }
+    }
+    else if (level == 0 || plen > kKtSmall)
+    {
+        kt_build_small(g, box, lb, le, level, kt_smem, ge, lq, sh);
+    }
+}
+
+// Boxes of the nodes above the shared-memory subtrees, one level at a time from the bottom.
+__global__ void k_kt_box_level(BatchDev b, int level, uint32_t slots)
+{
+    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const uint32_t s = static_cast<uint32_t>(t / slots), j = static_cast<uint32_t>(t % slots);
+    if (s >= static_cast<uint32_t>(b.nscan))
+        return;
+    const ScanDev& sd = b.scans[s];
+    uint32_t lb, le;
+    if (!kt_range(sd.n_src, level, j, lb, le, nullptr) || le - lb <= kKtSmall)
+        return;
+    const float4* g = b.kt + sd.src_off;
+    float4* box = b.kbb + 2ull * sd.src_off;
+    const uint32_t m = lb + (le - lb) / 2;
+    const float4 p = g[m];
+    float4 lo = make_float4(p.x, p.y, p.z, 0.0f), hi = lo;
+    const uint32_t cs[2] = {lb + (m - lb) / 2, m + 1 + (le - m - 1) / 2};
+    const bool has[2] = {m > lb, m + 1 < le};
+    for (int k = 0; k < 2; ++k)
+        if (has[k])
+        {
+            const float4 cl = box[2 * cs[k]], ch = box[2 * cs[k] + 1];
+            lo = make_float4(fminf(lo.x, cl.x), fminf(lo.y, cl.y), fminf(lo.z, cl.z), 0.0f);
+            hi = make_float4(fmaxf(hi.x, ch.x), fmaxf(hi.y, ch.y), fmaxf(hi.z, ch.z), 0.0f);
+        }
+    box[2 * m] = lo;
+    box[2 * m + 1] = hi;
+}
+
+// ---------------------------------------------------------------------------------------------
+// The reference's search (kdtree.hpp:355-388) from the entries on stk[0, sp): pop, count the node
+// when within r2 (stopping at k), push both children when the splitting plane is within the
+// radius (right first, so the left is searched first) or else the side of the query. Empty
+// children are not pushed: the reference pushes and pops them without effect. Returns the count;
+// after an early stop stk[0, sp) holds the entries left behind.
+// ---------------------------------------------------------------------------------------------
+__device__ uint32_t kt_search(const float4* __restrict__ g, uint32_t n, float qx, float qy, float qz, float r2,
+                              uint32_t k, uint32_t found, uint32_t* stk, int& sp, bool& overflow)
+{
+    while (sp > 0)
+    {
+        const uint32_t e = stk[--sp];
+        const uint32_t m = e >> 2;
+        const int ax = static_cast<int>(e & 3u);
+        if (m >= n || ax > 2)
+        {
+            overflow = true; // not a node of this tree: reported, never followed
+            return found;
+        }
+        const float4 nd = g[m];
+        const float d0 = (qx - nd.x) * (qx - nd.x);
+        const float d1 = (qy - nd.y) * (qy - nd.y);
+        const float d2 = (qz - nd.z) * (qz - nd.z);
+        if (d0 + (d1 + d2) <= r2)
+        {
+            if (++found >= k)
+                return found;
+        }
+        const uint32_t len = __float_as_uint(nd.w);
+        if (len == 0 || m < len / 2 || m - len / 2 + len > n)
+        {
+            overflow = true; // a subtree size the build did not leave: reported, never followed
+            return found;
+        }
+        const uint32_t lb = m - len / 2;
+        const uint32_t llen = m - lb, rlen = len - llen - 1;
+        const int nx = (ax == 2) ? 0 : ax + 1;
+        const float q = (ax == 0) ? qx : ((ax == 1) ? qy : qz);
+        const float delta = kt_coord(nd, ax) - q;
+        const bool push_r = (delta * delta <= r2) ? true : !(delta > 0);
+        const bool push_l = (delta * delta <= r2) ? true : (delta > 0);
+        if (sp + 2 > kKtStack)
+        {
+            overflow = true;
+            return found;
+        }
+        if (push_r && rlen)
+            stk[sp++] = kt_entry(m + 1 + rlen / 2, nx);
+        if (push_l && llen)
+            stk[sp++] = kt_entry(lb + llen / 2, nx);
+    }
+    return found;
+}
+
+// A subtree whose box lies farther than the radius holds no match: the reference's search
+// through it ends without counting anything. The box distance is taken in binary64 against the
+// radius with a relative margin of 1e-5, well above the binary32 rounding of the reference's
+// distance (a few units in 2^-24), so no subtree that could hold a match is skipped.
+__device__ __forceinline__ bool kt_may_hit(const float4* __restrict__ box, uint32_t m, float qx, float qy, float qz,
+                                           float r2)
+{
+    const float4 lo = box[2 * m], hi = box[2 * m + 1];
+    auto gap = [](float q, float l, float h) -> double {
+        if (q < l)
+            return static_cast<double>(l) - static_cast<double>(q);
+        if (q > h)
+            return static_cast<double>(q) - static_cast<double>(h);
+        return 0.0;
+    };
+    const double gx = gap(qx, lo.x, hi.x), gy = gap(qy, lo.y, hi.y), gz = gap(qz, lo.z, hi.z);
+    return gx * gx + gy * gy + gz * gz <= static_cast<double>(r2) * (1.0 + 1e-5) + 1e-30;
+}
+
+__device__ __forceinline__ int kt_scan_of(const BatchDev& b, uint32_t i)
+{
+    return find_scan(b.nscan, i, [&](int s) { return b.scans[s].src_off; });
+}
+
+// Pool allocation of `count` entries, one atomic per group of converged lanes (the lanes loop
+// over the group's members alike, so every shuffle has all of them); kNone when the pool is full.
+__device__ __forceinline__ uint32_t kt_pool_alloc(uint32_t* head, uint32_t cap, uint32_t count)
+{
+    const uint32_t active = __activemask();
+    const uint32_t lane = lane_id();
+    uint32_t pre = 0, total = 0;
+    for (uint32_t l = 0; l < 32; ++l)
+        if ((active >> l) & 1u)
+        {
+            const uint32_t c = __shfl_sync(active, count, l);
+            total += c;
+            if (l < lane)
+                pre += c;
+        }
+    const uint32_t leader = static_cast<uint32_t>(__ffs(static_cast<int>(active)) - 1);
+    uint32_t base = 0;
+    if (lane == leader && total)
+        base = atomicAdd(head, total);
+    base = __shfl_sync(active, base, leader);
+    if (base > cap || cap - base < total)
+        return kNone;
+    return base + pre;
+}
+
+// Step 2: every point's own search; VALID points' leftovers into the pool.
+__global__ void k_kt_own(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.nsrc)
+        return;
+    const int s = kt_scan_of(b, i);
+    const ScanDev& sd = b.scans[s];
+    const float4 q = b.src[i];
+    const float r2 = kt_radius2(sd, q);
+    uint32_t stk[kKtStack];
+    int sp = 0;
+    bool overflow = false;
+    stk[sp++] = kt_entry(sd.n_src / 2, 0);
+    const float4* g = b.kt + sd.src_off;
+    const uint32_t k = sd.dror_k;
+    const uint32_t found = kt_search(g, sd.n_src, q.x, q.y, q.z, r2, k, 0, stk, sp, overflow);
+    if (overflow)
+        raise_err(&b.state[s], ERR_INTERNAL);
+    const bool valid = found >= k;
+    b.kown[i] = found;
+    b.kshort[i] = valid ? 0u : 1u;
+    uint32_t nleft = valid ? static_cast<uint32_t>(sp) : 0u;
+    const uint32_t at = kt_pool_alloc(b.kctr, b.kpool_cap, nleft);
+    if (at == kNone)
+    {
+        raise_err(&b.state[s], ERR_HASH_FULL); // leftover pool full: reported, scan invalid
+        nleft = 0;
+    }
+    b.klo_n[i] = nleft;
+    b.klo_at[i] = (at == kNone) ? 0u : at;
+    for (uint32_t t = 0; t < nleft; ++t)
+        b.kpool[at + t] = stk[t];
+    if (valid)
+        b.noise[i] = LP_NOISE_VALID;
+}
+
+// Leftovers into one array in point order (klo_off: exclusive scan of the counts).
+__global__ void k_kt_flat(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.nsrc)
+        return;
+    const uint32_t n = b.klo_off[i + 1] - b.klo_off[i];
+    const uint32_t at = b.klo_at[i], to = b.klo_off[i];
+    for (uint32_t t = 0; t < n; ++t)
+        b.kflat[to + t] = b.kpool[at + t];
+}
+
+// The short points in order (kshort: exclusive scan of the flags).
+__global__ void k_kt_short(BatchDev b)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.nsrc)
+        return;
+    if (b.kshort[i + 1] != b.kshort[i])
+        b.kq[b.kshort[i]] = i;
+}
+
+// First entry (flat index) of the piece a short point meets on top of the stack: the leftovers of
+// the points after the previous short point of its scan.
+__device__ __forceinline__ uint32_t kt_segment_lo(const BatchDev& b, const ScanDev& sd, uint32_t t)
+{
+    const uint32_t first = b.kshort[sd.src_off];
+    const uint32_t prev = (t > first) ? b.kq[t - 1] + 1 : sd.src_off;
+    return b.klo_off[prev];
+}
+
+// Step 3: each short point through its own piece.
+__global__ void k_kt_segment(BatchDev b)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nshort = b.kshort[b.nsrc];
+    if (t >= nshort)
+        return;
+    const uint32_t i = b.kq[t];
+    const int s = kt_scan_of(b, i);
+    const ScanDev& sd = b.scans[s];
+    const float4 q = b.src[i];
+    const float r2 = kt_radius2(sd, q);
+    const float4* g = b.kt + sd.src_off;
+    const float4* box = b.kbb + 2ull * sd.src_off;
+    const uint32_t k = sd.dror_k;
+    uint32_t found = b.kown[i];
+    const uint32_t lo = kt_segment_lo(b, sd, t), hi = b.klo_off[i];
+    uint4 res = make_uint4(0u, kNone, 0u, 0u); // found, stop entry, partial leftover at, count
+    uint32_t stk[kKtStack];
+    bool overflow = false;
+    for (uint32_t x = hi; x > lo; --x)
+    {
+        const uint32_t e = b.kflat[x - 1];
+        if (!kt_may_hit(box, e >> 2, q.x, q.y, q.z, r2))
+            continue;
+        int sp = 0;
+        stk[sp++] = e;
+        found = kt_search(g, sd.n_src, q.x, q.y, q.z, r2, k, found, stk, sp, overflow);
+        if (found >= k)
+        {
+            uint32_t at = kt_pool_alloc(b.kctr, b.kpool_cap, static_cast<uint32_t>(sp));
+            if (at == kNone)
+            {
+                raise_err(&b.state[s], ERR_HASH_FULL);
+                at = 0;
+                sp = 0;
+            }
+            for (int u = 0; u < sp; ++u)
+                b.kpool[at + u] = stk[u];
+            res = make_uint4(found, x - 1, at, static_cast<uint32_t>(sp));
+            b.noise[i] = LP_NOISE_VALID;
+            break;
+        }
+    }
+    if (overflow)
+        raise_err(&b.state[s], ERR_INTERNAL);
+    res.x = found;
+    b.kc[t] = res;
+}
+
+// Step 4: one CTA per scan walks its short points in order over the stack of pieces. A piece
+// (lo, hi) holds entries [lo, hi) of the flat array (bit 31 of lo clear) or of the pool (set),
+// consumed from hi - 1 down.
+__global__ void __launch_bounds__(kChainThreads) k_kt_chain(BatchDev b)
+{
+    __shared__ uint32_t s_cnt[kChainThreads];
+    __shared__ uint32_t s_top;
+    __shared__ uint2 s_piece;
+    __shared__ uint32_t s_found, s_hit, s_hit_found;
+    const int s = blockIdx.x;
+    if (s >= b.nscan)
+        return;
+    const ScanDev& sd = b.scans[s];
+    ScanState* st = &b.state[s];
+    const uint32_t tid = threadIdx.x;
+    const float4* g = b.kt + sd.src_off;
+    const float4* box = b.kbb + 2ull * sd.src_off;
+    const uint32_t k = sd.dror_k;
+    uint2* pieces = b.kpiece + 2ull * sd.src_off + 2ull * static_cast<uint32_t>(s);
+    const uint32_t cap = 2u * sd.n_src + 2u;
+    const uint32_t t0 = b.kshort[sd.src_off], t1 = b.kshort[sd.src_off + sd.n_src];
+    if (tid == 0)
+        s_top = 0;
+    __syncthreads();
+    uint32_t stk[kKtStack];
+    bool overflow = false;
+    for (uint32_t t = t0; t < t1; ++t)
+    {
+        const uint32_t i = b.kq[t];
+        const uint4 c = b.kc[t];
+        if (c.y != kNone)
+        {
+            // decided in its own piece: what is left of the piece below the stop, then the entries
+            // the stopping search left, go on top of the stack
+            if (tid == 0)
+            {
+                const uint32_t lo = kt_segment_lo(b, sd, t);
+                if (c.y > lo && s_top < cap)
+                    pieces[s_top++] = make_uint2(lo, c.y);
+                if (c.w && s_top < cap)
+                    pieces[s_top++] = make_uint2(c.z | 0x80000000u, c.z + c.w);
+                if (s_top >= cap)
+                    raise_err(st, ERR_INTERNAL);
+            }
+            __syncthreads();
+            continue;
+        }
+        const float4 q = b.src[i];
+        const float r2 = kt_radius2(sd, q);
+        if (tid == 0)
+        {
+            s_found = c.x;
+            s_hit = kNone;
+        }
+        __syncthreads();
+        while (s_top > 0 && s_hit == kNone)
+        {
+            if (tid == 0)
+                s_piece = pieces[s_top - 1];
+            __syncthreads();
+            const uint2 pc = s_piece;
+            const bool in_pool = (pc.x & 0x80000000u) != 0;
+            const uint32_t lo = pc.x & 0x7fffffffu, hi = pc.y;
+            const uint32_t* arr = in_pool ? b.kpool : b.kflat;
+            const uint32_t chunk = min(hi - lo, static_cast<uint32_t>(blockDim.x));
+            uint32_t cnt = 0;
+            if (tid < chunk)
+            {
+                const uint32_t e = arr[hi - 1 - tid];
+                if (kt_may_hit(box, e >> 2, q.x, q.y, q.z, r2))
+                {
+                    int sp = 0;
+                    stk[sp++] = e;
+                    cnt = kt_search(g, sd.n_src, q.x, q.y, q.z, r2, k, 0, stk, sp, overflow);
+                }
+            }
+            s_cnt[tid] = cnt;
+            __syncthreads();
+            if (tid == 0)
+            {
+                // ordered prefix from the top: the first entry at which the count is reached
+                uint32_t f = s_found, hit = kNone;
+                for (uint32_t u = 0; u < chunk; ++u)
+                {
+                    if (s_cnt[u] && f + s_cnt[u] >= k)
+                    {
+                        hit = u;
+                        break;
+                    }
+                    f += s_cnt[u];
+                }
+                if (hit == kNone)
+                {
+                    s_found = f;
+                    if (hi - chunk > lo)
+                        pieces[s_top - 1].y = hi - chunk;
+                    else
+                        --s_top;
+                }
+                else
+                {
+                    s_hit = hit;
+                    s_hit_found = f;
+                }
+            }
+            __syncthreads();
+            if (s_hit != kNone && tid == 0)
+            {
+                // the stopping search again, from the count before it, to keep what it leaves
+                const uint32_t x = hi - 1 - s_hit;
+                int sp = 0;
+                stk[sp++] = arr[x];
+                kt_search(g, sd.n_src, q.x, q.y, q.z, r2, k, s_hit_found, stk, sp, overflow);
+                if (x > lo)
+                    pieces[s_top - 1].y = x;
+                else
+                    --s_top;
+                if (sp > 0)
+                {
+                    uint32_t at = kt_pool_alloc(b.kctr, b.kpool_cap, static_cast<uint32_t>(sp));
+                    if (at == kNone)
+                    {
+                        raise_err(st, ERR_HASH_FULL);
+                        sp = 0;
+                        at = 0;
+                    }
+                    for (int u = 0; u < sp; ++u)
+                        b.kpool[at + u] = stk[u];
+                    if (sp > 0)
+                    {
+                        if (s_top < cap)
+                            pieces[s_top++] = make_uint2(at | 0x80000000u, at + static_cast<uint32_t>(sp));
+                        else
+                            raise_err(st, ERR_INTERNAL);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        if (tid == 0)
+            b.noise[i] = (s_hit != kNone) ? LP_NOISE_VALID : LP_NOISE_NOISE;
+        __syncthreads();
+    }
+    if (overflow)
+        raise_err(st, ERR_INTERNAL);
+}
+} // namespace
+
+size_t kt_build_smem_bytes()
+{
+    return static_cast<size_t>(kKtSmall) * sizeof(float4);
+}
+
+void init_kdtree_attributes()
+{
+    cudaFuncSetAttribute(k_kt_level, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kt_build_smem_bytes()));
+}
+
+void launch_noise(Launcher& L, const BatchDev& b, const BatchHost& hb, const lp_noise_remover_config& cfg)
+{
+    (void)cfg;
+    const uint32_t T = 256;
+    uint32_t nmax = 0;
+    for (const ScanDev& sd : hb.scans)
+        nmax = std::max(nmax, sd.n_src);
+    if (nmax == 0)
+        return;
+    LP_LAUNCH(L, k_kt_load, div_up(b.nsrc, T), T, b);
+    // levels until every range of the deepest level is at most kKtSmall (then built in shared memory)
+    int levels = 1;
+    while ((nmax >> (levels - 1)) > kKtSmall)
+        ++levels;
+    const uint32_t S = static_cast<uint32_t>(b.nscan);
+    for (int l = 0; l < levels; ++l)
+    {
+        const uint32_t slots = 1u << l;
+        LP_LAUNCH_SMEM(L, k_kt_level, S * slots, kKtThreads, kt_build_smem_bytes(), b, l, slots);
+    }
+    for (int l = levels - 2; l >= 0; --l)
+    {
+        const uint32_t slots = 1u << l;
+        LP_LAUNCH(L, k_kt_box_level, div_up(S * slots, 128u), 128, b, l, slots);
+    }
+    LP_LAUNCH(L, k_kt_own, div_up(b.nsrc, 128u), 128, b);
+    L.scan(b.klo_n, b.klo_off, b.nsrc + 1);
+    L.scan(b.kshort, b.kshort, b.nsrc + 1);
+    LP_LAUNCH(L, k_kt_flat, div_up(b.nsrc, T), T, b);
+    LP_LAUNCH(L, k_kt_short, div_up(b.nsrc, T), T, b);
+    LP_LAUNCH(L, k_kt_segment, div_up(b.nsrc, 128u), 128, b);
+    LP_LAUNCH(L, k_kt_chain, S, kChainThreads, b);
+}
+} // namespace lpg

@@ -115,6 +115,7 @@ struct Launcher
 
 // One-time kernel attributes (dynamic shared memory opt-in); called when a context is created.
 void init_kernel_attributes();
+void init_kdtree_attributes(); // lp_kdtree.cu
 // Direct host I/O (lp_io.cu): inputs from and results into the caller's page-locked buffers.
 void launch_io_in(Launcher& L, const BatchDev& b, const IoScan* io);
 void launch_io_out(Launcher& L, const BatchDev& b, const IoScan* io, uint32_t* ret, int with_hull, int with_obb,

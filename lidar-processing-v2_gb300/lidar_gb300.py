@@ -447,6 +447,21 @@ class Segmenter:
         return self._image
 
 
+def debug_kdtree(ctx, xyz, config=None):
+    """The outlier filter's device kd-tree for the cloud xyz: per node position x, y, z (float32,
+    n x 3) and subtree sizes (uint32, n), as lp_debug_kdtree returns them."""
+    a = np.ascontiguousarray(xyz, np.float32)
+    n = len(a)
+    out = np.zeros((n, 4), np.float32)
+    cfg = config or NoiseRemoverConfig.default()
+    lib = library()
+    lib.lp_debug_kdtree.restype = ctypes.c_int32
+    lib.lp_debug_kdtree.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.c_void_p, ctypes.c_void_p]
+    check(lib.lp_debug_kdtree(ctx.handle, ptr(a), a.shape[1], n, ctypes.byref(cfg), ptr(out)), ctx)
+    return np.ascontiguousarray(out[:, :3]), out[:, 3].view(np.uint32).copy()
+
+
 class NoiseRemover:
     """NoiseRemover (noise_remover.hpp:56-86): filter(points) -> VALID/NOISE per point."""
 

@@ -13,6 +13,13 @@
 // Every comparison is made between the same elements in the same sequence as that implementation,
 // so the result equals std::sort's for any comparator, including ones that are not strict weak
 // orders. `less(a, b)` compares two element values.
+//
+// nth_element below restates libstdc++'s introselect (std::nth_element), which the reference's
+// KDTree::rebuild (kdtree.hpp:186-188) calls once per tree node: the same pivot and partition
+// steps, narrowed to the side holding the nth position until at most three elements remain
+// (insertion sort), with depth limit 2 * floor(log2 n) after which a heap selection of the nth
+// element takes over. Elements that compare equal to the nth one end up on either side in the
+// order this sequence of swaps leaves them, which decides the tree's shape when coordinates tie.
 #pragma once
 
 #include <cstddef>
@@ -159,6 +166,57 @@ void insertion_sort(T* a, std::ptrdiff_t len, Less& less)
         else
             insert_unguarded(a, i, less);
     }
+}
+
+// Heap selection (the introselect's fallback at the depth limit): a max-heap of the first `mid`
+// elements, then every later element smaller than the heap's top replaces it.
+template <class T, class Less>
+void heap_select(T* a, std::ptrdiff_t mid, std::ptrdiff_t len, Less& less)
+{
+    if (mid >= 2)
+        for (std::ptrdiff_t parent = (mid - 2) / 2;; --parent)
+        {
+            sift(a, parent, mid, a[parent], less);
+            if (parent == 0)
+                break;
+        }
+    for (std::ptrdiff_t i = mid; i < len; ++i)
+        if (less(a[i], a[0]))
+        {
+            const T v = a[i];
+            a[i] = a[0];
+            sift(a, 0, mid, v, less);
+        }
+}
+
+inline int floor_log2(std::size_t n);
+
+// std::nth_element(a, a + nth, a + n, less) as libstdc++ performs it.
+template <class T, class Less>
+void nth_element(T* a, std::size_t n, std::size_t nth, Less less, int depth_override = -1)
+{
+    if (n == 0 || nth >= n)
+        return;
+    std::ptrdiff_t first = 0, last = static_cast<std::ptrdiff_t>(n);
+    const std::ptrdiff_t k = static_cast<std::ptrdiff_t>(nth);
+    int depth = depth_override >= 0 ? depth_override : 2 * floor_log2(n);
+    while (last - first > 3)
+    {
+        if (depth == 0)
+        {
+            heap_select(a + first, k - first + 1, last - first, less);
+            std::swap(a[first], a[k]);
+            return;
+        }
+        --depth;
+        median_to_front(a + first, last - first, less);
+        const std::ptrdiff_t cut = first + partition(a + first, last - first, less);
+        if (cut <= k)
+            first = cut;
+        else
+            last = cut;
+    }
+    insertion_sort(a + first, last - first, less);
 }
 
 inline int floor_log2(std::size_t n)

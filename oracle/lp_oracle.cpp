@@ -602,6 +602,91 @@ inline float drorRadius2(const float* p, double s2, float rmin2)
 }
 } // namespace
 
+// KDTree::rebuild (kdtree.hpp:161-214): nodes_ holds the points in input order; a stack of
+// (begin, end, parent link, depth) ranges, each put in order around its middle position by
+// std::nth_element on the depth's axis (x, y, z in turn), the middle becoming the node and the two
+// sides its subtrees. Returns the root position; node positions are the array's.
+struct KdNode
+{
+    float p[3];
+    uint32_t index;
+    int32_t left, right;
+};
+
+int32_t kdBuild(const float* P, uint32_t n, std::vector<KdNode>& nodes)
+{
+    nodes.resize(n);
+    for (uint32_t i = 0; i < n; ++i)
+        nodes[i] = {{P[3 * i], P[3 * i + 1], P[3 * i + 2]}, i, -1, -1};
+    struct Build
+    {
+        uint32_t b, e;
+        int32_t parent; // -1 root
+        int side;       // 0 left, 1 right
+        uint32_t depth;
+    };
+    int32_t root = -1;
+    std::vector<Build> bs;
+    bs.push_back({0, n, -1, 0, 0});
+    while (!bs.empty())
+    {
+        const Build t = bs.back();
+        bs.pop_back();
+        if (t.b >= t.e)
+            continue;
+        const uint32_t axis = t.depth % 3;
+        const uint32_t mid = t.b + (t.e - t.b) / 2;
+        std::nth_element(nodes.begin() + t.b, nodes.begin() + mid, nodes.begin() + t.e,
+                         [axis](const KdNode& x, const KdNode& y) { return x.p[axis] < y.p[axis]; });
+        if (t.parent < 0)
+            root = static_cast<int32_t>(mid);
+        else if (t.side == 0)
+            nodes[t.parent].left = static_cast<int32_t>(mid);
+        else
+            nodes[t.parent].right = static_cast<int32_t>(mid);
+        if (mid > t.b)
+            bs.push_back({t.b, mid, static_cast<int32_t>(mid), 0, t.depth + 1});
+        if (mid + 1 < t.e)
+            bs.push_back({mid + 1, t.e, static_cast<int32_t>(mid), 1, t.depth + 1});
+    }
+    return root;
+}
+
+// The kd-tree's points by node position (n x 3 floats), for checking a tree built elsewhere.
+int32_t lpo_kdtree_positions(const float* xyz, uint32_t n, float* out_xyz)
+{
+    std::vector<KdNode> nodes;
+    kdBuild(xyz, n, nodes);
+    for (uint32_t i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d)
+            out_xyz[3 * i + d] = nodes[i].p[d];
+    return 0;
+}
+
+// std::nth_element (host library) or its restatement (lpo_sort::nth_element) on float keys:
+// the resulting order of the input indices. depth_override >= 0 forces the restatement's depth
+// limit (0: heap selection at once).
+int32_t lpo_debug_nth(const float* v, uint32_t n, uint32_t nth, int32_t restated, int32_t depth_override,
+                      int32_t* order_out)
+{
+    struct Key
+    {
+        float v;
+        int32_t i;
+    };
+    std::vector<Key> a(n);
+    for (uint32_t i = 0; i < n; ++i)
+        a[i] = {v[i], static_cast<int32_t>(i)};
+    auto less = [](const Key& x, const Key& y) { return x.v < y.v; };
+    if (restated)
+        lpo_sort::nth_element(a.data(), n, nth, less, depth_override);
+    else
+        std::nth_element(a.begin(), a.begin() + nth, a.end(), less);
+    for (uint32_t i = 0; i < n; ++i)
+        order_out[i] = a[i].i;
+    return 0;
+}
+
 lp_status lpo_noise_remove(const float* xyz, uint32_t stride, uint32_t n,
                            const lp_noise_remover_config* cfg, int mode, uint8_t* out)
 {
@@ -653,46 +738,8 @@ lp_status lpo_noise_remove(const float* xyz, uint32_t stride, uint32_t n,
         return LP_OK;
     }
     // mode 1: reference kd-tree with the persistent traversal stack
-    struct Node
-    {
-        float p[3];
-        uint32_t index;
-        int32_t left, right;
-    };
-    std::vector<Node> nodes(n);
-    for (uint32_t i = 0; i < n; ++i)
-        nodes[i] = {{P[3 * i], P[3 * i + 1], P[3 * i + 2]}, i, -1, -1};
-    struct Build
-    {
-        uint32_t b, e;
-        int32_t parent; // -1 root
-        int side;       // 0 left, 1 right
-        uint32_t depth;
-    };
-    int32_t root = -1;
-    std::vector<Build> bs;
-    bs.push_back({0, n, -1, 0, 0});
-    while (!bs.empty())
-    {
-        const Build t = bs.back();
-        bs.pop_back();
-        if (t.b >= t.e)
-            continue;
-        const uint32_t axis = t.depth % 3;
-        const uint32_t mid = t.b + (t.e - t.b) / 2;
-        std::nth_element(nodes.begin() + t.b, nodes.begin() + mid, nodes.begin() + t.e,
-                         [axis](const Node& x, const Node& y) { return x.p[axis] < y.p[axis]; });
-        if (t.parent < 0)
-            root = static_cast<int32_t>(mid);
-        else if (t.side == 0)
-            nodes[t.parent].left = static_cast<int32_t>(mid);
-        else
-            nodes[t.parent].right = static_cast<int32_t>(mid);
-        if (mid > t.b)
-            bs.push_back({t.b, mid, static_cast<int32_t>(mid), 0, t.depth + 1});
-        if (mid + 1 < t.e)
-            bs.push_back({mid + 1, t.e, static_cast<int32_t>(mid), 1, t.depth + 1});
-    }
+    std::vector<KdNode> nodes;
+    const int32_t root = kdBuild(P.data(), n, nodes);
     struct Entry
     {
         int32_t node;
@@ -711,7 +758,7 @@ lp_status lpo_noise_remove(const float* xyz, uint32_t stride, uint32_t n,
             stack.pop_back();
             if (e.node < 0)
                 continue;
-            const Node& nd = nodes[e.node];
+            const KdNode& nd = nodes[e.node];
             if (drorDist(q, nd.p) <= r2)
             {
                 if (++found >= k)

@@ -24,7 +24,7 @@ GOLDEN = os.path.join(REPO, "tests", "golden")
 
 LIBM_CR, LIBM_HOST = 0, 1
 TIES_INDEX, TIES_LIBSTDCXX = 0, 1  # order of hull points with equal (x, y)
-DROR_EXACT, DROR_KDTREE = 0, 1
+DROR_EXACT, DROR_KDTREE = 0, 1  # exact radius counting / the reference's kd-tree search (its stack kept)
 
 _oracle = None
 _ref = None
@@ -51,6 +51,8 @@ def oracle():
             "lpo_bounding_box_rotating_calipers": (c.c_int32, [P, c.c_uint32, P]),
             "lpo_bounding_box_pca": (c.c_int32, [P, c.c_uint32, P, P]),
             "lpo_jacobi_svd2": (c.c_int32, [P, P]),
+            "lpo_kdtree_positions": (c.c_int32, [P, c.c_uint32, P]),
+            "lpo_debug_nth": (c.c_int32, [P, c.c_uint32, c.c_uint32, c.c_int32, c.c_int32, P]),
             "lpo_process_scan": (c.c_int32, [P, P, c.c_int, P]),
         }
         for k, (r, a) in sig.items():
@@ -155,7 +157,7 @@ def o_segment(xyzi, ring, cfg, libm=LIBM_CR, image=False):
     return (lab, img) if image else lab
 
 
-def o_noise(pts, cfg, mode=DROR_EXACT):
+def o_noise(pts, cfg, mode=DROR_KDTREE):
     a = np.ascontiguousarray(pts, np.float32)
     out = np.zeros(len(a), np.uint8)
     st = oracle().lpo_noise_remove(ptr(a), a.shape[1], len(a), ctypes.byref(cfg), mode, ptr(out))
@@ -205,6 +207,21 @@ def o_svd2(a):
     return v.reshape(2, 2) if oracle().lpo_jacobi_svd2(ptr(m), ptr(v)) == 0 else None
 
 
+def o_kdtree_positions(xyz):
+    """The reference kd-tree's points by node position (std::nth_element build), n x 3 float32."""
+    a = np.ascontiguousarray(np.asarray(xyz, np.float32)[:, :3])
+    out = np.zeros_like(a)
+    oracle().lpo_kdtree_positions(ptr(a), len(a), ptr(out))
+    return out
+
+
+def o_debug_nth(v, nth, restated, depth_override=-1):
+    a = np.ascontiguousarray(v, np.float32)
+    out = np.zeros(len(a), np.int32)
+    oracle().lpo_debug_nth(ptr(a), len(a), nth, int(restated), depth_override, ptr(out))
+    return out
+
+
 def o_antipodal(hp):
     a = np.ascontiguousarray(hp, np.float64)
     cap = 4 * len(a) + 8
@@ -214,7 +231,7 @@ def o_antipodal(hp):
     return out[: n.value].copy()
 
 
-def o_process(xyzi, ring, seg_cfg, pipeline, libm=LIBM_CR, dror_mode=DROR_EXACT, ties=TIES_INDEX):
+def o_process(xyzi, ring, seg_cfg, pipeline, libm=LIBM_CR, dror_mode=DROR_KDTREE, ties=TIES_INDEX):
     oracle().lpo_set_libm_mode(libm)
     oracle().lpo_set_hull_ties(ties)
     b = lp.ResultBuffers(len(xyzi))

@@ -30,12 +30,6 @@ def test_headers_declare_the_reference_replacements():
         assert fn in names
 
 
-def test_integration_guide_names_every_entry_point():
-    guide = open(os.path.join(T.REPO, "INTEGRATION.md")).read()
-    missing = sorted(n for n in declared_functions() if f"`{n}`" not in guide)
-    assert not missing, missing
-
-
 def test_library_exports_every_declared_symbol(built):
     lib = ctypes.CDLL(T.lp.LIB_PATH)
     missing = [n for n in sorted(declared_functions()) if not hasattr(lib, n)]

@@ -141,6 +141,63 @@ def test_cluster_voxel_capacity(ctx):
         T.o_cluster(pts, lp.ClustererConfig(0.05, 0.25, 0.25, 3))
 
 
+def kdtree_clouds():
+    """Clouds for the tree build: tiny sizes around the build's thresholds (3, 64, 2048 points),
+    coordinates with many ties (the tree then depends on nth_element's swaps), a dense scan."""
+    rng = np.random.default_rng(17)
+    out = []
+    for n in (1, 2, 3, 4, 5, 64, 65, 66, 2047, 2048, 2049, 4097, 5000, 70000):
+        out.append((f"uniform{n}", rng.uniform(-50, 50, size=(n, 3)).astype(np.float32)))
+    for n in (300, 9000, 150000):
+        out.append((f"ties{n}", np.round(rng.normal(size=(n, 3)) * 4.0, 0).astype(np.float32)))
+    x = T.synth_scan(1, 0)[0]
+    out.append(("scan", np.ascontiguousarray(x[:, :3])))
+    return out
+
+
+@pytest.mark.parametrize("name,pts", kdtree_clouds(), ids=lambda v: v if isinstance(v, str) else "")
+def test_kdtree_build_matches_reference(ctx, name, pts):
+    """The device kd-tree equals the reference's KDTree::rebuild (std::nth_element per node) node
+    for node, including where coordinates tie; subtree sizes follow the range arithmetic."""
+    nodes, sizes = lp.debug_kdtree(ctx, pts)
+    want = T.o_kdtree_positions(pts)
+    assert np.array_equal(nodes.view(np.uint32), want.view(np.uint32)), name
+    n = len(pts)
+    expect = np.zeros(n, np.uint32)
+    todo = [(0, n)]
+    while todo:
+        b, e = todo.pop()
+        if e <= b:
+            continue
+        m = b + (e - b) // 2
+        expect[m] = e - b
+        todo += [(b, m), (m + 1, e)]
+    assert np.array_equal(sizes, expect), name
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(T.GOLDEN, "*_sector.npz"))), ids=os.path.basename)
+def test_noise_removal_reference_fixtures(ctx, path):
+    """DROR masks equal the reference's own NoiseRemover output (made by the reference build) on
+    the fixtures' clouds, in input order and shuffled, default and dense configurations."""
+    g = np.load(path)
+    x = np.ascontiguousarray(g["xyzi"][:, :3])
+    perm = g["dror_perm"]
+    for tag, c in (("default", lp.NoiseRemoverConfig.default()),
+                   ("dense", lp.NoiseRemoverConfig(3 * 0.17 * np.pi / 180.0, 0.1, 3))):
+        nr = lp.NoiseRemover(ctx, c)
+        assert np.array_equal(nr.filter(x), g["dror_" + tag]), tag
+        assert np.array_equal(nr.filter(np.ascontiguousarray(x[perm])), g["dror_shuffled_" + tag]), tag
+
+
+def test_noise_removal_organized_scan(ctx):
+    """A whole organised scan in ring order (long runs of neighbouring queries: deep leftover
+    stacks): the mask equals the reference kd-tree's, which here differs from exact counting."""
+    x = np.ascontiguousarray(T.synth_scan(1, 0)[0][:, :3])
+    c = lp.NoiseRemoverConfig.default()
+    got = lp.NoiseRemover(ctx, c).filter(x)
+    assert np.array_equal(got, T.o_noise(x, c, T.DROR_KDTREE))
+
+
 @pytest.mark.parametrize("cfg", [lp.NoiseRemoverConfig.default(), lp.NoiseRemoverConfig(3 * 0.17 * np.pi / 180, 0.1, 3)],
                          ids=["default", "dense"])
 def test_noise_removal_exact(ctx, cfg):
@@ -150,7 +207,7 @@ def test_noise_removal_exact(ctx, cfg):
     pts = np.ascontiguousarray(np.concatenate([x[:, :3], clutter]).astype(np.float32))
     pts = np.ascontiguousarray(pts[rng.permutation(len(pts))])
     got = lp.NoiseRemover(ctx, cfg).filter(pts)
-    assert np.array_equal(got, T.o_noise(pts, cfg, T.DROR_EXACT))
+    assert np.array_equal(got, T.o_noise(pts, cfg, T.DROR_KDTREE))
     assert got.sum() > 0
 
 
@@ -294,7 +351,7 @@ def test_pipeline_with_noise_removal(ctx):
                                      noise=lp.NoiseRemoverConfig(3 * 0.17 * np.pi / 180, 0.1, 3))
     res = lp.process_batch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
     for (x, ring, cfg), r in zip(data, res):
-        want = T.o_process(x, ring, cfg, pipe, dror_mode=T.DROR_EXACT)
+        want = T.o_process(x, ring, cfg, pipe, dror_mode=T.DROR_KDTREE)
         assert np.array_equal(r.noise_labels, want.noise_labels)
         compare_scan(r, want)
 
@@ -454,7 +511,7 @@ def test_prepared_batch_split_noise(ctx):
         assert np.array_equal(g.noise_labels, r.noise_labels), i
         compare_scan(g, r, f"scan {i}")
     for (x, ring, cfg), g in list(zip(data, got))[:2]:
-        want = T.o_process(x, ring, cfg, pipe, dror_mode=T.DROR_EXACT)
+        want = T.o_process(x, ring, cfg, pipe, dror_mode=T.DROR_KDTREE)
         assert np.array_equal(g.noise_labels, want.noise_labels)
         compare_scan(g, want)
     b.close()
