@@ -8,8 +8,11 @@ metric through the C ABI with host buffers (H2D + D2H inside the timed region). 
 scan per launch sequence) is timed on the same scans for the batched/plain ratio, and the CPU
 oracle (a restatement of the reference path) on a bounded sample of the same workload.
 
+The line also carries a serving sub-record (six sensors at 10 Hz with bursts, >= 3,000 scans,
+p50/p99/p99.9 latency) and an outlier-filter sub-record (32 x 1M-point scans, DROR stage roofline).
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-  small profiling case: python bench.py --steps 2 --warmup 1 --scans 16 --no-cpu --no-plain --no-e2e
+  small profiling case: python bench.py --steps 2 --warmup 1 --scans 16 --no-cpu --no-plain --no-e2e --no-serve --no-dror
 Multi-GPU (torchrun): replicas, one independent batch per rank (scans do not shard a step).
 """
 import argparse
@@ -138,9 +141,9 @@ def workload_name(nscans):
 
 
 def make_workload(nscans):
-    import lp_testlib as T
+    import lidar_gb300 as lp
 
-    return [T.synth_scan(WORKLOAD, i) for i in range(nscans)]
+    return [lp.synth_scan(WORKLOAD, i) for i in range(nscans)]
 
 
 def cpu_baseline(data, budget_s=20.0, threads=None):
@@ -229,15 +232,15 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line))
 
 
-def run_serve(args):
+def serve_leg(duration):
     """Serving workload: six sensors at 10 Hz (periods ~ N(100 ms, 10 ms)), the rate doubled
     during the first second of every 5 s, scans of 32/64/128 rings x 1024-4096 bins (synthetic
-    workload 5), a 20 GB admission budget. Latency = submission -> results in host buffers."""
-    import lp_testlib as T
+    workload 5), a 20 GB admission budget. Latency = submission -> results in host buffers.
+    Returns the record (latency percentiles, rates, clocks)."""
     import lidar_gb300 as lp
 
     sensors, per_sensor = 6, 8
-    pool = [[T.synth_scan(5, s * per_sensor + k) for k in range(per_sensor)] for s in range(sensors)]
+    pool = [[lp.synth_scan(5, s * per_sensor + k) for k in range(per_sensor)] for s in range(sensors)]
     pipe = lp.PipelineConfig.default()
     server = lp.Server(0, pipe, memory_budget_bytes=20 << 30, max_batch_scans=16, slots=3)
     rng = np.random.default_rng(5000)
@@ -245,7 +248,7 @@ def run_serve(args):
     for s in range(sensors):
         t = float(rng.uniform(0.0, 0.1))
         k = 0
-        while t < args.duration:
+        while t < duration:
             events.append((t, s, k))
             k += 1
             period = float(rng.normal(0.100, 0.010))
@@ -255,68 +258,71 @@ def run_serve(args):
     events.sort()
     done = {}
     stop = threading.Event()
+    warm = sensors * per_sensor
+    t_end = [time.perf_counter() + 1e9]
 
     def poller():
         while not stop.is_set() or len(done) < len(events) + warm:
             for d, _ in server.poll(wait_us=2000):
                 done[int(d.tag)] = (d.latency_ms, d.queue_ms, d.batch_scans, d.status)
-            if stop.is_set() and time.perf_counter() - t_end > 30:
+            if stop.is_set() and time.perf_counter() - t_end[0] > 30:
                 break
 
     # warm-up: every pool scan once
-    warm = 0
     for s in range(sensors):
         for k in range(per_sensor):
             x, ring, cfg = pool[s][k]
-            server.submit(x, ring, cfg, 1_000_000 + warm)
-            warm += 1
-    t_end = time.perf_counter() + 1e9
+            server.submit(x, ring, cfg, 1_000_000 + s * per_sensor + k)
     th = threading.Thread(target=poller, daemon=True)
     th.start()
-    while sum(1 for t in done if t >= 1_000_000) < warm:
+    while sum(1 for t in list(done) if t >= 1_000_000) < warm:
         time.sleep(0.01)
-    t0 = time.perf_counter()
-    for i, (t, s, k) in enumerate(events):
-        dt = t0 + t - time.perf_counter()
-        if dt > 0:
-            time.sleep(dt)
-        x, ring, cfg = pool[s][k % per_sensor]
-        server.submit(x, ring, cfg, i)
-    t_end = time.perf_counter()
-    stop.set()
-    th.join(timeout=60)
+    with ClockSampler(0) as clocks:
+        t0 = time.perf_counter()
+        for i, (t, s, k) in enumerate(events):
+            dt = t0 + t - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            x, ring, cfg = pool[s][k % per_sensor]
+            server.submit(x, ring, cfg, i)
+        t_end[0] = time.perf_counter()
+        stop.set()
+        th.join(timeout=60)
     stats = server.stats()
     server.close()
     lat = np.array([done[i][0] for i in range(len(events)) if i in done])
     bs = np.array([done[i][2] for i in range(len(events)) if i in done])
     ok = sum(1 for i in range(len(events)) if i in done and done[i][3] == 0)
     pts = [len(pool[s][k % per_sensor][0]) for _, s, k in events]
-    line = {"metric": "serving latency p99 ms/scan (6 sensors x 10 Hz, continuous batching)",
-            "value": float(np.percentile(lat, 99)), "unit": "ms", "higher_is_better": False, "n_gpus": 1,
-            "data": "synthetic", "dtype": "f32",
-            "config": {"workload": "serve_6x10Hz_mixed", "sensors": sensors, "duration_s": args.duration,
-                       "burst": "rate x2 during the first 1 s of every 5 s", "memory_budget_gb": 20,
-                       "slots": 3, "max_batch_scans": 16},
-            "scans": int(len(lat)), "ok": int(ok), "offered_scans_per_s": len(events) / args.duration,
-            "achieved_scans_per_s": len(lat) / max(t_end - t0, 1e-9),
+    return {"workload": "serve_6x10Hz_mixed", "sensors": sensors, "duration_s": duration,
+            "burst": "rate x2 during the first 1 s of every 5 s", "memory_budget_gb": 20,
+            "scans": int(len(lat)), "ok": int(ok), "offered_scans_per_s": len(events) / duration,
+            "achieved_scans_per_s": len(lat) / max(t_end[0] - t0, 1e-9),
             "points_per_scan": {"min": int(min(pts)), "max": int(max(pts)), "mean": float(np.mean(pts))},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "p99.9": float(np.percentile(lat, 99.9)), "max": float(lat.max())},
             "batch_scans": {"mean": float(bs.mean()), "max": int(bs.max())},
-            "server": stats}
+            "server": stats, "clocks": clocks.summary()}
+
+
+def run_serve(args):
+    r = serve_leg(args.duration)
+    line = {"metric": "serving latency p99 ms/scan (6 sensors x 10 Hz, continuous batching)",
+            "value": r["latency_ms"]["p99"], "unit": "ms", "higher_is_better": False, "n_gpus": 1,
+            "data": "synthetic", "dtype": "f32", "config": {"workload": r["workload"]}, **r}
     print(json.dumps(line))
 
 
-def run_dror(args):
+def dror_leg(steps, warmup, distinct=4, ns=32):
     """Outlier-filter workload: 32 unorganised scans of 1.0 M points (128-ring geometry at 16384
     bins, 950k returns + 50k clutter within 15 m, shuffled; synthetic workload 4) per launch. DROR
-    with multiplier 3 x 0.17 deg (rad), min neighbours 3, min radius 0.1 m on the input, then the
-    unorganised segmentation, clustering and hulls. Distinct scans: --dror-unique (each repeated)."""
-    import lp_testlib as T
+    with multiplier 3 x 0.17 deg (rad), min neighbours 3, min radius 0.1 m on the input (the
+    reference's kd-tree search replayed), then the unorganised segmentation, clustering and hulls.
+    `distinct` generated scans are repeated to `ns` (32 in the workload; fewer for a profiling case).
+    Returns the record (stage time, roofline)."""
     import lidar_gb300 as lp
 
-    uniq = [T.synth_scan(4, i) for i in range(args.dror_unique)]
-    ns = 32
+    uniq = [lp.synth_scan(4, i) for i in range(min(distinct, ns))]
     data = [uniq[i % len(uniq)] for i in range(ns)]
     xs = [d[0] for d in data]
     cfgs = []
@@ -338,31 +344,60 @@ def run_dror(args):
     dror_ms = sum(agg[k][1] for k in dror_kernels)
     total_ms = sum(a[1] for a in agg.values())
     batch.capture_graph()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch.execute()
     batch.synchronize()
     with ClockSampler(0) as clocks:
-        step_ms = [batch.time(1, flush_l2=False) for _ in range(args.steps)]
+        step_ms = [batch.time(1, flush_l2=False) for _ in range(steps)]
     ms = float(np.mean(step_ms))
     peak, peak_kind = measured_peaks()
+    if not dror_ms > 0:
+        raise RuntimeError("no outlier-filter kernel in the batch profile")
     dror_gbs = 17.0 * npts / (dror_ms / 1e3) / 1e9
     top = max(agg.items(), key=lambda kv: kv[1][1])
-    line = {"metric": "scans/s (32 x 1.0M-point unorganised scans, DROR + pipeline)", "value": ns / (ms / 1e3),
-            "unit": "scans/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-            "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "dror32x1M", "scans": ns, "distinct_scans": len(uniq), "points": npts,
-                       "dror": "multiplier 3*0.17deg, min_neighbours 3, min radius 0.1 m"},
-            "ms_per_step": ms, "points_per_s": npts / (ms / 1e3), "noise_points": noise_pts,
-            "dror_stage": {"ms": dror_ms, "kernels": dror_kernels, "points_per_s": npts / (dror_ms / 1e3),
-                           "roofline": {"bound": "hbm", "achieved": dror_gbs, "peak": peak, "unit": "GB/s",
-                                        "frac": dror_gbs / peak, "algorithmic_bytes_per_point": 17,
-                                        "peak_source": peak_kind},
-                           "share_of_step": dror_ms / total_ms},
-            "top_kernel": {"name": top[0], "share": top[1][1] / total_ms},
-            "clocks": clocks.summary()}
-    print(json.dumps(line))
     batch.close()
     ctx.close()
+    return {"workload": f"dror{ns}x1M", "scans": ns, "distinct_scans": len(uniq), "points": npts,
+            "dror": "multiplier 3*0.17deg, min_neighbours 3, min radius 0.1 m; the reference kd-tree search",
+            "scans_per_s": ns / (ms / 1e3), "ms_per_step": ms, "points_per_s": npts / (ms / 1e3),
+            "noise_points": noise_pts,
+            "dror_stage": {"ms": dror_ms, "kernels": {k: round(agg[k][1], 3) for k in dror_kernels},
+                           "points_per_s": npts / (dror_ms / 1e3), "share_of_step": dror_ms / total_ms,
+                           "roofline": {"bound": "hbm", "achieved": dror_gbs, "peak": peak, "unit": "GB/s",
+                                        "frac": dror_gbs / peak, "algorithmic_bytes_per_point": 17,
+                                        "peak_source": peak_kind}},
+            "top_kernel": {"name": top[0], "share": top[1][1] / total_ms},
+            "clocks": clocks.summary()}
+
+
+def run_dror(args):
+    r = dror_leg(args.steps, args.warmup, args.dror_unique, args.dror_scans)
+    line = {"metric": f"scans/s ({args.dror_scans} x 1.0M-point unorganised scans, DROR + pipeline)", "value": r["scans_per_s"],
+            "unit": "scans/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic", "config": {"workload": r["workload"]}, **r}
+    print(json.dumps(line))
+
+
+# Kernels of the segmentation stage (ring partition, polar grid, RECM, RANSAC, projection, dilation,
+# jump convolution, label write-back); prefix scans count with the stage of the kernel before them.
+SEG_KERNELS = {"k_quadrant", "k_ring_count", "k_ring_apply", "k_bin", "k_scatter", "k_cell_small", "k_cell_large",
+               "k_chain", "k_near", "k_ransac_draw", "k_ransac_inliers", "k_ransac_select", "k_label_depth",
+               "k_project_key", "k_pixel", "k_dilate_rows", "k_jcp_weights", "k_jcp_rowrec", "k_jcp_rows",
+               "k_populate"}
+
+
+def stage_ms(prof, kernels):
+    """Summed event time of the named kernels and of the prefix scans launched right after them."""
+    tot, prev = 0.0, None
+    for name, ms in prof:
+        if name == "k_scan":
+            if prev in kernels:
+                tot += ms
+            continue
+        prev = name
+        if name in kernels:
+            tot += ms
+    return tot
 
 
 def traffic_bytes(kernel, alg_bytes):
@@ -382,7 +417,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--serve", action="store_true", help="multi-sensor serving workload instead of the batch bench")
     ap.add_argument("--dror", action="store_true", help="32 x 1M-point outlier-filter workload")
-    ap.add_argument("--dror-unique", type=int, default=4, help="distinct generated scans in --dror (repeated to 32)")
+    ap.add_argument("--dror-unique", type=int, default=4, help="distinct generated scans in --dror (repeated)")
+    ap.add_argument("--dror-scans", type=int, default=32, help="scans per batch in --dror (32 for the workload)")
     ap.add_argument("--duration", type=float, default=60.0, help="seconds of simulated sensor stream (--serve)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -392,6 +428,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-scan-per-launch form")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end run")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving sub-record")
+    ap.add_argument("--no-dror", action="store_true", help="skip the outlier-filter sub-record")
+    ap.add_argument("--serve-duration", type=float, default=52.0,
+                    help="seconds of sensor stream in the serving sub-record (>= 3,000 scans at 60 scans/s)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     dist = dist_init(world)
@@ -449,7 +489,7 @@ def main():
     value = replica_rate(dist, world, ns * args.steps, dev_ms / 1e3)
 
     # the dominant kernel's launch timed with events on the context stream (roofline)
-    _, agg2 = kernel_profile(batch)
+    prof2, agg2 = kernel_profile(batch)
     # a batch of 16 or more scans runs as concurrent parts: the kernel launches once per part, each
     # launch on its part's share of the work (per-launch figures are batch totals / launches)
     top_launches = agg2[top_name][0]
@@ -463,6 +503,10 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (top_ms / 1e3) / 1e9
     total_ms = sum(a[1] for a in agg2.values())
+    # segmentation stage (projection + RECM + RANSAC + JCP): 20 B per input point over the summed
+    # event time of its kernels in the batch (parts profiled one after the other)
+    seg_ms = stage_ms(prof2, SEG_KERNELS)
+    seg_gbs = 20.0 * npts / (seg_ms / 1e3) / 1e9 if seg_ms > 0 else 0.0
 
     plain, plain_err = [], None
     if not args.no_plain:
@@ -472,7 +516,7 @@ def main():
                 pb = lp.PreparedBatch(ctx, [xs[i]], pipe, [cfgs[i]], [rings[i]])
                 pb.execute()
                 pb.synchronize()
-                plain.append(pb.time(3, flush_l2=True))
+                plain.append(pb.time(3, flush_l2=False))
                 pb.close()
         except Exception as exc:  # reported in the line; the batched figures stand
             plain, plain_err = [], leg_error(exc)
@@ -498,6 +542,20 @@ def main():
         except Exception as exc:  # reported in the line
             cb = {"error": leg_error(exc)}
 
+    batch.close()
+    ctx.close()
+    serve = dror = None
+    if rank == 0 and not args.no_serve:
+        try:
+            serve = serve_leg(args.serve_duration)
+        except Exception as exc:  # reported in the line
+            serve = {"error": leg_error(exc)}
+    if rank == 0 and not args.no_dror:
+        try:
+            dror = dror_leg(5, 3)
+        except Exception as exc:  # reported in the line
+            dror = {"error": leg_error(exc)}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "scans/s", "n_gpus": world, "steps": args.steps,
@@ -517,15 +575,18 @@ def main():
             "gpu_launches": int(kernels_per_step * args.steps),
             "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic_bytes(top_name, alg_bytes),
-                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": int(alg_bytes), "launch_ms": top_ms},
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": int(alg_bytes), "launch_ms": top_ms,
+                         "stage": {"name": "segmentation (projection, RECM, RANSAC, jump convolution)",
+                                   "ms": seg_ms, "algorithmic_bytes": 20 * npts, "achieved": seg_gbs,
+                                   "frac": seg_gbs / peak}},
             "kernel_share": {k: round(v[1] / total_ms, 4) for k, v in sorted(agg2.items(), key=lambda kv: -kv[1][1])[:10]},
             "clocks": clocks.summary(),
             "cpu_baseline": cb,
+            "serve": serve,
+            "dror": dror,
             "wall_s": wall,
         }
         print(json.dumps(line))
-    batch.close()
-    ctx.close()
     barrier(dist)
 
 

@@ -255,6 +255,10 @@ size_t carve(lp_batch& B, char* base)
         put(b.kflat, b.kpool_cap);
         put(b.kq, N);
         put(b.kc, N);
+        put(b.kcflag, N + 1);
+        put(b.kcand, N);
+        put(b.kspec, N);
+        put(b.kspec_n, N);
         put(b.kpiece, 2ull * N + 2ull * S);
         put(b.kctr, 4);
     }

@@ -197,6 +197,10 @@ struct BatchDev
     uint32_t kpool_cap;
     uint32_t* kq;              // short points in order
     uint4* kc;                 // per short point: count, stop entry, left entries (pool at, count)
+    uint32_t* kcflag;          // per short point (+1): 1 if step 3 left it undecided -> exclusive scan
+    uint32_t* kcand;           // those candidates (short indices) in order
+    uint4* kspec;              // per candidate: count, stop short index, stop entry | kind << 31, left at
+    uint32_t* kspec_n;         // per candidate: entries the stopping search left
     uint2* kpiece;             // per scan: stack of pieces (2 n + 2 per scan)
     uint32_t* kctr;            // [0] pool head
 

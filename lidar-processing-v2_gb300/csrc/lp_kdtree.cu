@@ -32,11 +32,14 @@
 //      piece from the top; an entry whose subtree box is farther than the radius is consumed
 //      without a match (skipped); the others are searched exactly. Reaching the count there
 //      decides the point (VALID) and records where it stopped and the entries it left.
-//   4. Chain (k_kt_chain, one CTA per scan): the short points in order, with the stack below the
-//      pieces as a list of pieces; a point not decided in step 3 consumes pieces from the top,
-//      its threads testing and searching the entries of a piece in parallel, an ordered prefix
-//      of their counts finding the entry where the count is reached. Exhausting the stack means
-//      NOISE and an empty stack for the next point.
+//   4. Candidates (short points step 3 did not decide) in two steps. k_kt_spec, one thread per
+//      candidate: the walk through the pieces pushed since the previous candidate, as if nothing
+//      lay below them, which is exact whenever the previous candidate emptied the stack (running
+//      out of entries is NOISE). k_kt_chain, one warp per scan: the candidates in order with R,
+//      what earlier walks left below those pieces; a stopped walk adds its remainder to R, one
+//      that ran out continues into R (the lanes searching 32 entries at a time, an ordered prefix
+//      of their counts finding the stop). While R is empty, runs of candidates whose walks ran
+//      out are NOISE at once.
 // The result equals the reference's sequential search bit for bit (same binary32 expressions,
 // same visiting order, same stop points); the tree's node positions equal the reference's.
 #include "lp_batch.cuh"
@@ -52,7 +55,6 @@ constexpr uint32_t kKtSeqMax = 64;     // ranges built by one thread (introselec
 constexpr int kKtThreads = 512;        // tree build CTAs
 constexpr int kKtItems = 8;            // elements per thread per tile of the parallel partition
 constexpr int kKtStack = 64;           // search stack entries (>= tree depth + 1 for 2^62 points)
-constexpr int kChainThreads = 256;
 constexpr uint32_t kNone = 0xffffffffu;
 
 // Stack entries: node position (scan-local) << 2 | axis.
@@ -756,75 +758,211 @@ __global__ void k_kt_segment(BatchDev b)
     b.kc[t] = res;
 }
 
-// Step 4: one CTA per scan walks its short points in order over the stack of pieces. A piece
-// (lo, hi) holds entries [lo, hi) of the flat array (bit 31 of lo clear) or of the pool (set),
-// consumed from hi - 1 down.
-__global__ void __launch_bounds__(kChainThreads) k_kt_chain(BatchDev b)
+// Candidates: short points not decided in their own piece (flag -> exclusive scan -> list).
+__global__ void k_kt_cand_flag(BatchDev b)
 {
-    __shared__ uint32_t s_cnt[kChainThreads];
-    __shared__ uint32_t s_top;
-    __shared__ uint2 s_piece;
-    __shared__ uint32_t s_found, s_hit, s_hit_found;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nshort = b.kshort[b.nsrc];
+    if (t == 0)
+        b.kcflag[nshort] = 0;
+    if (t < nshort)
+        b.kcflag[t] = (b.kc[t].y == kNone) ? 1u : 0u;
+}
+
+__global__ void k_kt_cand_list(BatchDev b)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < b.kshort[b.nsrc] && b.kcflag[t + 1] != b.kcflag[t])
+        b.kcand[b.kcflag[t]] = t;
+}
+
+// Walks the pieces the short points (tp, t) of a scan pushed (all decided in their own piece:
+// the rest of their piece below the stop, then the entries the stopping search left, on top),
+// newest first, for query q from count `found`. Stops where the count reaches k and returns the
+// stop: short index u, kind (1: the left entries, 0: the piece rest) and entry index; the entries
+// that stopping search left go to the pool.
+struct KtStop
+{
+    uint32_t u, kind, x, at, n;
+};
+
+__device__ bool kt_walk_pushed(const BatchDev& b, const ScanDev& sd, const float4* g, const float4* box, uint32_t tp1,
+                               uint32_t t, float qx, float qy, float qz, float r2, uint32_t k, uint32_t& found,
+                               KtStop& stop, uint32_t* stk, bool& overflow, bool& pool_full)
+{
+    for (uint32_t u = t; u > tp1;)
+    {
+        --u;
+        const uint4 c = b.kc[u];
+        for (int kind = 1; kind >= 0; --kind)
+        {
+            const uint32_t lo = kind ? c.z : kt_segment_lo(b, sd, u);
+            const uint32_t hi = kind ? c.z + c.w : c.y;
+            const uint32_t* arr = kind ? b.kpool : b.kflat;
+            for (uint32_t x = hi; x > lo; --x)
+            {
+                const uint32_t e = arr[x - 1];
+                if (!kt_may_hit(box, e >> 2, qx, qy, qz, r2))
+                    continue;
+                int sp = 0;
+                stk[sp++] = e;
+                found = kt_search(g, sd.n_src, qx, qy, qz, r2, k, found, stk, sp, overflow);
+                if (found >= k)
+                {
+                    uint32_t at = kt_pool_alloc(b.kctr, b.kpool_cap, static_cast<uint32_t>(sp));
+                    if (at == kNone)
+                    {
+                        pool_full = true;
+                        at = 0;
+                        sp = 0;
+                    }
+                    for (int v = 0; v < sp; ++v)
+                        b.kpool[at + v] = stk[v];
+                    stop = KtStop{u, static_cast<uint32_t>(kind), x - 1, at, static_cast<uint32_t>(sp)};
+                    return true;
+                }
+            }
+        }
+    }
+    return false;
+}
+
+// Step 4a: every candidate walks the pieces pushed since the previous candidate, as if nothing
+// lay below them (true when the previous candidate exhausted the stack).
+__global__ void k_kt_spec(BatchDev b)
+{
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t ncand = b.kcflag[b.kshort[b.nsrc]];
+    if (c >= ncand)
+        return;
+    const uint32_t t = b.kcand[c];
+    const uint32_t i = b.kq[t];
+    const int s = kt_scan_of(b, i);
+    const ScanDev& sd = b.scans[s];
+    const uint32_t t_first = b.kshort[sd.src_off];
+    const uint32_t c_first = b.kcflag[t_first];
+    const uint32_t tp1 = (c > c_first) ? b.kcand[c - 1] + 1 : t_first; // first pushing short point
+    const float4 q = b.src[i];
+    const float r2 = kt_radius2(sd, q);
+    uint32_t found = b.kc[t].x;
+    uint32_t stk[kKtStack];
+    bool overflow = false, pool_full = false;
+    KtStop stop{kNone, 0, 0, 0, 0};
+    kt_walk_pushed(b, sd, b.kt + sd.src_off, b.kbb + 2ull * sd.src_off, tp1, t, q.x, q.y, q.z, r2, sd.dror_k, found,
+                   stop, stk, overflow, pool_full);
+    if (overflow)
+        raise_err(&b.state[s], ERR_INTERNAL);
+    if (pool_full)
+        raise_err(&b.state[s], ERR_HASH_FULL);
+    b.kspec[c] = make_uint4(found, stop.u, stop.x | (stop.kind << 31), stop.at);
+    b.kspec_n[c] = stop.n;
+}
+
+// Step 4b: one warp per scan applies the candidates' walks in order. R, the stack below the pieces
+// pushed since the previous candidate, is a list of pieces (lo, hi): entries [lo, hi) of the flat
+// array (bit 31 of lo clear) or of the pool (set), consumed from hi - 1 down. A candidate whose
+// walk stopped adds what its walk left on top of R. One whose walk ran out continues into R
+// (32 entries at a time, the lanes searching their entries in full and an ordered prefix of the
+// counts finding the stop); running out of R too means NOISE and an empty R. While R is empty, a
+// run of candidates whose walks ran out is NOISE as a whole (ballot over 32 at a time).
+__global__ void __launch_bounds__(32) k_kt_chain(BatchDev b)
+{
     const int s = blockIdx.x;
     if (s >= b.nscan)
         return;
     const ScanDev& sd = b.scans[s];
     ScanState* st = &b.state[s];
-    const uint32_t tid = threadIdx.x;
+    const uint32_t lane = threadIdx.x;
     const float4* g = b.kt + sd.src_off;
     const float4* box = b.kbb + 2ull * sd.src_off;
     const uint32_t k = sd.dror_k;
-    uint2* pieces = b.kpiece + 2ull * sd.src_off + 2ull * static_cast<uint32_t>(s);
+    uint2* R = b.kpiece + 2ull * sd.src_off + 2ull * static_cast<uint32_t>(s);
     const uint32_t cap = 2u * sd.n_src + 2u;
-    const uint32_t t0 = b.kshort[sd.src_off], t1 = b.kshort[sd.src_off + sd.n_src];
-    if (tid == 0)
-        s_top = 0;
-    __syncthreads();
+    const uint32_t t_first = b.kshort[sd.src_off], t_end = b.kshort[sd.src_off + sd.n_src];
+    const uint32_t c0 = b.kcflag[t_first], c1 = b.kcflag[t_end];
+    uint32_t top = 0; // pieces in R (lane-uniform)
+    bool overflow = false, pool_full = false, full = false;
     uint32_t stk[kKtStack];
-    bool overflow = false;
-    for (uint32_t t = t0; t < t1; ++t)
-    {
-        const uint32_t i = b.kq[t];
-        const uint4 c = b.kc[t];
-        if (c.y != kNone)
+    auto push = [&](uint32_t lo, uint32_t hi) {
+        if (hi > (lo & 0x7fffffffu))
         {
-            // decided in its own piece: what is left of the piece below the stop, then the entries
-            // the stopping search left, go on top of the stack
-            if (tid == 0)
+            if (top < cap)
             {
-                const uint32_t lo = kt_segment_lo(b, sd, t);
-                if (c.y > lo && s_top < cap)
-                    pieces[s_top++] = make_uint2(lo, c.y);
-                if (c.w && s_top < cap)
-                    pieces[s_top++] = make_uint2(c.z | 0x80000000u, c.z + c.w);
-                if (s_top >= cap)
-                    raise_err(st, ERR_INTERNAL);
+                if (lane == 0)
+                    R[top] = make_uint2(lo, hi);
+                ++top;
             }
-            __syncthreads();
+            else
+                full = true;
+        }
+    };
+    uint32_t c = c0;
+    while (c < c1)
+    {
+        if (top == 0)
+        {
+            const uint32_t cc = c + lane;
+            const bool live = cc < c1;
+            const bool hit = live && b.kspec[cc].y != kNone;
+            const uint32_t hits = __ballot_sync(0xffffffffu, hit);
+            const uint32_t h = hits ? static_cast<uint32_t>(__ffs(static_cast<int>(hits)) - 1) : 32u;
+            if (live && lane < h)
+                b.noise[b.kq[b.kcand[cc]]] = LP_NOISE_NOISE;
+            c += h;
+            if (h == 32u || c >= c1)
+                continue;
+        }
+        const uint4 sp4 = b.kspec[c];
+        const uint32_t t = b.kcand[c];
+        const uint32_t i = b.kq[t];
+        if (sp4.y != kNone)
+        {
+            // the walk stopped at short point u: R gains the pieces of the pushing points below u,
+            // then the rest of u's pieces below the stop, then the entries the stopping search left
+            const uint32_t tp1 = (c > c0) ? b.kcand[c - 1] + 1 : t_first;
+            const uint32_t hu = sp4.y, hx = sp4.z & 0x7fffffffu, hkind = sp4.z >> 31;
+            for (uint32_t u = tp1; u <= hu; ++u)
+            {
+                const uint4 cu = b.kc[u];
+                const uint32_t lo = kt_segment_lo(b, sd, u);
+                if (u < hu)
+                {
+                    push(lo, cu.y);
+                    push(cu.z | 0x80000000u, cu.z + cu.w);
+                }
+                else if (hkind == 1)
+                {
+                    push(lo, cu.y);
+                    push(cu.z | 0x80000000u, hx);
+                }
+                else
+                {
+                    push(lo, hx);
+                }
+            }
+            push(sp4.w | 0x80000000u, sp4.w + b.kspec_n[c]);
+            if (lane == 0)
+                b.noise[i] = LP_NOISE_VALID;
+            ++c;
+            __syncwarp(); // lane 0's pieces are read by every lane next
             continue;
         }
+        // the walk ran out with R non-empty: continue into R
         const float4 q = b.src[i];
         const float r2 = kt_radius2(sd, q);
-        if (tid == 0)
+        uint32_t found = sp4.x;
+        bool hit = false;
+        while (top > 0 && !hit)
         {
-            s_found = c.x;
-            s_hit = kNone;
-        }
-        __syncthreads();
-        while (s_top > 0 && s_hit == kNone)
-        {
-            if (tid == 0)
-                s_piece = pieces[s_top - 1];
-            __syncthreads();
-            const uint2 pc = s_piece;
+            const uint2 pc = R[top - 1];
             const bool in_pool = (pc.x & 0x80000000u) != 0;
             const uint32_t lo = pc.x & 0x7fffffffu, hi = pc.y;
             const uint32_t* arr = in_pool ? b.kpool : b.kflat;
-            const uint32_t chunk = min(hi - lo, static_cast<uint32_t>(blockDim.x));
+            const uint32_t chunk = min(hi - lo, 32u);
             uint32_t cnt = 0;
-            if (tid < chunk)
+            if (lane < chunk)
             {
-                const uint32_t e = arr[hi - 1 - tid];
+                const uint32_t e = arr[hi - 1 - lane];
                 if (kt_may_hit(box, e >> 2, q.x, q.y, q.z, r2))
                 {
                     int sp = 0;
@@ -832,74 +970,68 @@ __global__ void __launch_bounds__(kChainThreads) k_kt_chain(BatchDev b)
                     cnt = kt_search(g, sd.n_src, q.x, q.y, q.z, r2, k, 0, stk, sp, overflow);
                 }
             }
-            s_cnt[tid] = cnt;
-            __syncthreads();
-            if (tid == 0)
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
             {
-                // ordered prefix from the top: the first entry at which the count is reached
-                uint32_t f = s_found, hit = kNone;
-                for (uint32_t u = 0; u < chunk; ++u)
-                {
-                    if (s_cnt[u] && f + s_cnt[u] >= k)
-                    {
-                        hit = u;
-                        break;
-                    }
-                    f += s_cnt[u];
-                }
-                if (hit == kNone)
-                {
-                    s_found = f;
-                    if (hi - chunk > lo)
-                        pieces[s_top - 1].y = hi - chunk;
-                    else
-                        --s_top;
-                }
-                else
-                {
-                    s_hit = hit;
-                    s_hit_found = f;
-                }
+                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= static_cast<uint32_t>(o))
+                    incl += v;
             }
-            __syncthreads();
-            if (s_hit != kNone && tid == 0)
+            const uint32_t reach = __ballot_sync(0xffffffffu, lane < chunk && cnt > 0 && found + incl >= k);
+            if (reach)
             {
-                // the stopping search again, from the count before it, to keep what it leaves
-                const uint32_t x = hi - 1 - s_hit;
+                const uint32_t hl = static_cast<uint32_t>(__ffs(static_cast<int>(reach)) - 1);
+                const uint32_t before = found + __shfl_sync(0xffffffffu, incl - cnt, hl);
+                const uint32_t x = hi - 1 - hl;
+                // the stopping search again on lane 0, from the count before it, for what it leaves
                 int sp = 0;
-                stk[sp++] = arr[x];
-                kt_search(g, sd.n_src, q.x, q.y, q.z, r2, k, s_hit_found, stk, sp, overflow);
-                if (x > lo)
-                    pieces[s_top - 1].y = x;
-                else
-                    --s_top;
-                if (sp > 0)
+                uint32_t at = 0;
+                if (lane == 0)
                 {
-                    uint32_t at = kt_pool_alloc(b.kctr, b.kpool_cap, static_cast<uint32_t>(sp));
+                    stk[sp++] = arr[x];
+                    kt_search(g, sd.n_src, q.x, q.y, q.z, r2, k, before, stk, sp, overflow);
+                    at = kt_pool_alloc(b.kctr, b.kpool_cap, static_cast<uint32_t>(sp));
                     if (at == kNone)
                     {
-                        raise_err(st, ERR_HASH_FULL);
-                        sp = 0;
+                        pool_full = true;
                         at = 0;
+                        sp = 0;
                     }
-                    for (int u = 0; u < sp; ++u)
-                        b.kpool[at + u] = stk[u];
-                    if (sp > 0)
-                    {
-                        if (s_top < cap)
-                            pieces[s_top++] = make_uint2(at | 0x80000000u, at + static_cast<uint32_t>(sp));
-                        else
-                            raise_err(st, ERR_INTERNAL);
-                    }
+                    for (int v = 0; v < sp; ++v)
+                        b.kpool[at + v] = stk[v];
                 }
+                sp = __shfl_sync(0xffffffffu, sp, 0);
+                at = __shfl_sync(0xffffffffu, at, 0);
+                // R: the piece keeps its entries below the stop, then the left entries go on top
+                --top;
+                push(pc.x, x);
+                push(at | 0x80000000u, at + static_cast<uint32_t>(sp));
+                hit = true;
             }
-            __syncthreads();
+            else
+            {
+                found += __shfl_sync(0xffffffffu, incl, 31);
+                if (hi - chunk > lo)
+                {
+                    if (lane == 0)
+                        R[top - 1].y = hi - chunk;
+                }
+                else
+                    --top;
+            }
+            __syncwarp();
         }
-        if (tid == 0)
-            b.noise[i] = (s_hit != kNone) ? LP_NOISE_VALID : LP_NOISE_NOISE;
-        __syncthreads();
+        if (lane == 0)
+            b.noise[i] = hit ? LP_NOISE_VALID : LP_NOISE_NOISE;
+        ++c;
+        __syncwarp();
     }
-    if (overflow)
+    if (__any_sync(0xffffffffu, overflow) && lane == 0)
+        raise_err(st, ERR_INTERNAL);
+    if (__any_sync(0xffffffffu, pool_full) && lane == 0)
+        raise_err(st, ERR_HASH_FULL);
+    if (full && lane == 0)
         raise_err(st, ERR_INTERNAL);
 }
 } // namespace
@@ -945,6 +1077,10 @@ void launch_noise(Launcher& L, const BatchDev& b, const BatchHost& hb, const lp_
     LP_LAUNCH(L, k_kt_flat, div_up(b.nsrc, T), T, b);
     LP_LAUNCH(L, k_kt_short, div_up(b.nsrc, T), T, b);
     LP_LAUNCH(L, k_kt_segment, div_up(b.nsrc, 128u), 128, b);
-    LP_LAUNCH(L, k_kt_chain, S, kChainThreads, b);
+    LP_LAUNCH(L, k_kt_cand_flag, div_up(b.nsrc + 1, T), T, b);
+    L.scan(b.kcflag, b.kcflag, b.nsrc + 1);
+    LP_LAUNCH(L, k_kt_cand_list, div_up(b.nsrc, T), T, b);
+    LP_LAUNCH(L, k_kt_spec, div_up(b.nsrc, 128u), 128, b);
+    LP_LAUNCH(L, k_kt_chain, S, 32, b);
 }
 } // namespace lpg

@@ -447,6 +447,46 @@ class Segmenter:
         return self._image
 
 
+# ------------------------------------------------------------------ seeded synthetic scans
+_synth = None
+
+
+def _synth_lib():
+    """liblp_synth.so: the seeded synthetic scan generator the benchmarks and tests draw from
+    (spinning 32/64/128-ring sensor, ray-cast ground, boxes, cylinders, wall; workloads 1-5)."""
+    global _synth
+    if _synth is None:
+        s = ctypes.CDLL(SYNTH_PATH)
+        P = ctypes.c_void_p
+        s.lp_synth_capacity.restype = ctypes.c_uint32
+        s.lp_synth_capacity.argtypes = [ctypes.c_int32, ctypes.c_int32]
+        s.lp_synth_scan.restype = ctypes.c_uint32
+        s.lp_synth_scan.argtypes = [ctypes.c_int32, ctypes.c_int32, P, P, ctypes.c_uint32]
+        s.lp_synth_shape.restype = None
+        s.lp_synth_shape.argtypes = [ctypes.c_int32, ctypes.c_int32, P, P, P, P]
+        _synth = s
+    return _synth
+
+
+def synth_shape(workload, scan):
+    """(rings, azimuth bins, elevation up deg, elevation down deg) of a seeded synthetic scan."""
+    r, w, up, dn = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_float(), ctypes.c_float()
+    _synth_lib().lp_synth_shape(workload, scan, ctypes.byref(r), ctypes.byref(w), ctypes.byref(up), ctypes.byref(dn))
+    return r.value, w.value, up.value, dn.value
+
+
+def synth_scan(workload, scan):
+    """(xyzi float32 N x 4, true ring uint16, SegmenterConfig) of seeded synthetic scan `scan` of
+    workload 1-5 (seed 1000 * workload + scan)."""
+    cap = _synth_lib().lp_synth_capacity(workload, scan)
+    x = np.zeros((cap, 4), np.float32)
+    r = np.zeros(cap, np.uint16)
+    n = _synth_lib().lp_synth_scan(workload, scan, ptr(x), ptr(r), cap)
+    rings, bins, up, dn = synth_shape(workload, scan)
+    cfg = SegmenterConfig.default(image_height=rings, image_width=bins, elevation_up_deg=up, elevation_down_deg=dn)
+    return np.ascontiguousarray(x[:n]), np.ascontiguousarray(r[:n]), cfg
+
+
 def debug_kdtree(ctx, xyz, config=None):
     """The outlier filter's device kd-tree for the cloud xyz: per node position x, y, z (float32,
     n x 3) and subtree sizes (uint32, n), as lp_debug_kdtree returns them."""

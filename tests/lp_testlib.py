@@ -1,6 +1,6 @@
 """Test helpers: bindings of the CPU oracle (oracle/liblp_oracle.so), of the reference build
-(oracle/_ref/libref.so, present only where the reference tree was available at build time), of
-the synthetic scan generator, a PCD reader and comparison helpers."""
+(oracle/_ref/libref.so, present only where the reference tree was available at build time), the
+package's synthetic scan generator, a PCD reader and comparison helpers."""
 from __future__ import annotations
 
 import ctypes
@@ -28,7 +28,6 @@ DROR_EXACT, DROR_KDTREE = 0, 1  # exact radius counting / the reference's kd-tre
 
 _oracle = None
 _ref = None
-_synth = None
 
 
 def oracle():
@@ -97,36 +96,8 @@ def ref():
 
 
 # ---------------------------------------------------------------------------- synthetic scans
-def synth():
-    global _synth
-    if _synth is None:
-        s = ctypes.CDLL(lp.SYNTH_PATH)
-        P, c = ctypes.c_void_p, ctypes
-        s.lp_synth_capacity.restype = c.c_uint32
-        s.lp_synth_capacity.argtypes = [c.c_int32, c.c_int32]
-        s.lp_synth_scan.restype = c.c_uint32
-        s.lp_synth_scan.argtypes = [c.c_int32, c.c_int32, P, P, c.c_uint32]
-        s.lp_synth_shape.restype = None
-        s.lp_synth_shape.argtypes = [c.c_int32, c.c_int32, P, P, P, P]
-        _synth = s
-    return _synth
-
-
-def synth_shape(workload, scan):
-    r, w, up, dn = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_float(), ctypes.c_float()
-    synth().lp_synth_shape(workload, scan, ctypes.byref(r), ctypes.byref(w), ctypes.byref(up), ctypes.byref(dn))
-    return r.value, w.value, up.value, dn.value
-
-
-def synth_scan(workload, scan):
-    """(xyzi float32 N x 4, true ring uint16, SegmenterConfig) of a seeded synthetic scan."""
-    cap = synth().lp_synth_capacity(workload, scan)
-    x = np.zeros((cap, 4), np.float32)
-    r = np.zeros(cap, np.uint16)
-    n = synth().lp_synth_scan(workload, scan, ptr(x), ptr(r), cap)
-    rings, bins, up, dn = synth_shape(workload, scan)
-    cfg = lp.SegmenterConfig.default(image_height=rings, image_width=bins, elevation_up_deg=up, elevation_down_deg=dn)
-    return np.ascontiguousarray(x[:n]), np.ascontiguousarray(r[:n]), cfg
+synth_shape = lp.synth_shape  # the package's seeded generator (liblp_synth.so)
+synth_scan = lp.synth_scan
 
 
 # ------------------------------------------------------------------------------------------ I/O

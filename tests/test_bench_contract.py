@@ -78,7 +78,8 @@ def run_main(monkeypatch, lib, argv):
 
 
 def test_bench_line_carries_the_contract(monkeypatch):
-    line = run_main(monkeypatch, PinningLibrary(), ["--steps", "3", "--warmup", "3", "--scans", "4", "--no-cpu"])
+    line = run_main(monkeypatch, PinningLibrary(), ["--steps", "3", "--warmup", "3", "--scans", "4", "--no-cpu",
+                                                    "--no-serve", "--no-dror"])
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
                 "vs_baseline", "dtype", "data", "config", "e2e", "gpu_launches", "roofline", "clocks", "cpu_baseline"):
         assert key in line, key
@@ -97,6 +98,32 @@ def test_bench_line_carries_the_contract(monkeypatch):
     assert r["traffic"] is not None  # read from the ncu summary under profiles/
     assert set(line["clocks"]) >= {"sm_mhz", "sm_max_mhz", "reasons"}
     assert line["plain"]["scans"] == 4
+    st = r["stage"]  # segmentation stage: k_bin, the prefix scan after it and k_jcp_rows in the stand-in profile
+    assert abs(st["ms"] - 0.46) < 1e-12 and st["algorithmic_bytes"] == 20 * sum(len(x) for x in bench_points())
+    assert abs(st["frac"] - st["achieved"] / r["peak"]) < 1e-12
+
+
+def bench_points():
+    import bench
+    return [d[0] for d in bench.make_workload(4)]
+
+
+def test_serving_and_outlier_sub_records(monkeypatch):
+    """The default line carries the serving and outlier-filter sub-records as their legs return
+    them; a failing leg is reported in its sub-record."""
+    sys.path.insert(0, T.REPO)
+    import bench
+
+    monkeypatch.setattr(bench, "serve_leg", lambda duration: {"latency_ms": {"p99": 2.0}, "duration_s": duration})
+
+    def broken(steps, warmup):
+        raise RuntimeError("stand-in outlier failure")
+
+    monkeypatch.setattr(bench, "dror_leg", broken)
+    line = run_main(monkeypatch, PinningLibrary(), ["--steps", "3", "--warmup", "3", "--scans", "4", "--no-cpu",
+                                                    "--no-plain"])
+    assert line["serve"] == {"latency_ms": {"p99": 2.0}, "duration_s": 52.0}
+    assert line["dror"] == {"error": "RuntimeError: stand-in outlier failure"}
 
 
 class FailingLibrary(PinningLibrary):
@@ -106,7 +133,7 @@ class FailingLibrary(PinningLibrary):
 
 def test_failed_end_to_end_leg_is_reported(monkeypatch):
     line = run_main(monkeypatch, FailingLibrary(), ["--steps", "3", "--warmup", "3", "--scans", "4", "--no-cpu",
-                                                    "--no-plain"])
+                                                    "--no-plain", "--no-serve", "--no-dror"])
     assert line["e2e"] == {"error": "RuntimeError: stand-in failure", "unit": "scans/s"}
     assert line["value"] > 0 and line["plain"] is None
     assert ctypes.sizeof(lp.ScanOutput) > 0
