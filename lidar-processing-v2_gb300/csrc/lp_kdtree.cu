@@ -42,15 +42,21 @@
 //      out are NOISE at once.
 // The result equals the reference's sequential search bit for bit (same binary32 expressions,
 // same visiting order, same stop points); the tree's node positions equal the reference's.
+#include <cooperative_groups.h>
+
 #include "lp_batch.cuh"
 #include "lp_common.cuh"
 #include "lp_stages.hpp"
+
+namespace cg = cooperative_groups;
 
 namespace lpg
 {
 namespace
 {
 constexpr uint32_t kKtSmall = 2048;    // ranges built in shared memory by one CTA
+constexpr uint32_t kKtHuge = 65536;    // ranges partitioned by a cluster of kKtCluster CTAs
+constexpr int kKtCluster = 8;
 constexpr uint32_t kKtSeqMax = 64;     // ranges built by one thread (introselect as written)
 constexpr int kKtThreads = 512;        // tree build CTAs
 constexpr int kKtItems = 8;            // elements per thread per tile of the parallel partition
@@ -387,30 +393,101 @@ __device__ void kt_select_block(float4* a, uint32_t first, uint32_t nth, uint32_
     __syncthreads();
 }
 
+// One partition round by one warp on a[first, last) in shared memory (the parallel Hoare replay of
+// kt_round_block, 32 elements per step with ballots); ge/le hold the candidate positions.
+__device__ uint32_t kt_round_warp(float4* a, uint32_t first, uint32_t last, int ax, uint16_t* ge, uint16_t* le)
+{
+    const uint32_t lane = lane_id();
+    if (lane == 0)
+        kt_median_to_first(a, first, last, ax);
+    __syncwarp();
+    const float p = kt_coord(a[first], ax);
+    const uint32_t lo = first + 1, n = last - lo;
+    const uint32_t below = (1u << lane) - 1u;
+    uint32_t nge = 0, nle = 0;
+    for (uint32_t base = 0; base < n; base += 32)
+    {
+        const uint32_t idx = base + lane;
+        bool g = false, l = false;
+        if (idx < n)
+        {
+            const float v = kt_coord(a[lo + idx], ax);
+            g = !(v < p);
+            l = !(p < v);
+        }
+        const uint32_t bg = __ballot_sync(0xffffffffu, g), bl = __ballot_sync(0xffffffffu, l);
+        if (g)
+            ge[nge + __popc(bg & below)] = static_cast<uint16_t>(lo + idx);
+        if (l)
+            le[nle + __popc(bl & below)] = static_cast<uint16_t>(lo + idx);
+        nge += __popc(bg);
+        nle += __popc(bl);
+    }
+    __syncwarp();
+    uint32_t T = 0, cut = 0;
+    if (lane == 0)
+    {
+        uint32_t lo_t = 0, hi_t = min(nge, nle);
+        while (lo_t < hi_t)
+        {
+            const uint32_t mid = (lo_t + hi_t + 1) / 2;
+            if (ge[mid - 1] < le[nle - mid])
+                lo_t = mid;
+            else
+                hi_t = mid - 1;
+        }
+        T = lo_t;
+        cut = (T == 0) ? ge[0] : min(T < nge ? static_cast<uint32_t>(ge[T]) : 0xffffffffu, static_cast<uint32_t>(le[nle - T]));
+    }
+    T = __shfl_sync(0xffffffffu, T, 0);
+    cut = __shfl_sync(0xffffffffu, cut, 0);
+    for (uint32_t t = lane; t < T; t += 32)
+        kt_swap(a, ge[t], le[nle - 1 - t]);
+    __syncwarp();
+    return cut;
+}
+
+__device__ void kt_select_warp(float4* a, uint32_t first, uint32_t nth, uint32_t last, int ax, uint16_t* ge,
+                               uint16_t* le)
+{
+    int depth = 2 * static_cast<int>(floor_log2_u(last - first));
+    while (last - first > kKtSeqMax && depth > 0)
+    {
+        --depth;
+        const uint32_t cut = kt_round_warp(a, first, last, ax, ge, le);
+        if (cut <= nth)
+            first = cut;
+        else
+            last = cut;
+    }
+    if (lane_id() == 0)
+        kt_select_seq(a, first, nth, last, depth, ax);
+    __syncwarp();
+}
+
 // Subtree of [b0, e0) (at depth d0 of the tree, at most kKtSmall points) built in shared memory;
 // node records get their subtree size in .w; subtree boxes are written bottom-up.
-__device__ void kt_build_small(float4* g, float4* box, uint32_t b0, uint32_t e0, int d0, float4* s, uint32_t* ge,
-                               uint32_t* le, KtShared& sh)
+__device__ void kt_build_small(float4* g, float4* box, uint32_t b0, uint32_t e0, int d0, float4* s, uint16_t* lists)
 {
     const uint32_t n = e0 - b0;
+    const uint32_t warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     for (uint32_t k = threadIdx.x; k < n; k += blockDim.x)
         s[k] = g[b0 + k];
     __syncthreads();
     // the longest range at depth d has floor(n / 2^d) points (a range of L splits into floor(L/2)
-    // and ceil(L/2) - 1), so depths 0 .. floor(log2 n) hold ranges
+    // and ceil(L/2) - 1), so depths 0 .. floor(log2 n) hold ranges. Ranges above kKtSeqMax: one warp
+    // each (positions of range [b, e) in lists[2b, 2e)); the rest: one thread each.
     const int maxd = static_cast<int>(floor_log2_u(n));
     for (int d = 0; d <= maxd; ++d)
     {
         const uint32_t slots = 1u << d;
-        // ranges above kKtSeqMax: the whole CTA, one after the other
         if ((n >> d) > kKtSeqMax)
-            for (uint32_t j = 0; j < slots; ++j)
+            for (uint32_t j = warp; j < slots; j += nwarps)
             {
                 uint32_t b, e;
                 if (kt_range(n, d, j, b, e, nullptr) && e - b > kKtSeqMax)
-                    kt_select_block(s, b, b + (e - b) / 2, e, (d0 + d) % 3, ge, le, sh);
+                    kt_select_warp(s, b, b + (e - b) / 2, e, (d0 + d) % 3, lists + 2 * b, lists + 2 * b + (e - b));
             }
-        // the rest: one thread each
         for (uint32_t j = threadIdx.x; j < slots; j += blockDim.x)
         {
             uint32_t b, e;
@@ -456,6 +533,214 @@ __device__ void kt_build_small(float4* g, float4* box, uint32_t b0, uint32_t e0,
         g[b0 + k] = s[k];
 }
 
+// One partition round by a cluster of kKtCluster CTAs on a[first, last) (the median of three into
+// a[first] by rank 0, then the same parallel Hoare replay as kt_round_block): every CTA takes a
+// slice of [first + 1, last), counts its candidates, learns the counts of the slices before it
+// through distributed shared memory and writes its positions in order; rank 0 finds T and the cut;
+// the swaps are spread over the whole cluster. Cluster barriers order the global-memory steps.
+struct KtClusterShared
+{
+    uint32_t warp_sum[kKtThreads / 32];
+    uint32_t cnt[2]; // this CTA's ge, le counts
+    uint32_t res[2]; // rank 0: T, cut
+};
+
+__device__ uint32_t block_sum(uint32_t v, uint32_t* warp_sum)
+{
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0)
+        warp_sum[warp] = v;
+    __syncthreads();
+    uint32_t t = 0;
+    for (uint32_t w = 0; w < nwarps; ++w)
+        t += warp_sum[w];
+    return t;
+}
+
+__device__ uint32_t kt_round_cluster(float4* a, uint32_t first, uint32_t last, int ax, uint32_t* ge, uint32_t* le,
+                                     KtClusterShared& sh, cg::cluster_group& cluster)
+{
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const uint32_t rank = cluster.block_rank();
+    if (rank == 0 && tid == 0)
+        kt_median_to_first(a, first, last, ax);
+    cluster.sync();
+    const float p = kt_coord(a[first], ax);
+    const uint32_t lo = first + 1, n = last - lo;
+    const uint32_t cs = (n + kKtCluster - 1) / kKtCluster;
+    const uint32_t c0 = min(n, rank * cs), c1 = min(n, c0 + cs);
+    // pass 1: this slice's counts
+    uint32_t cge = 0, cle = 0;
+    for (uint32_t k = c0 + tid; k < c1; k += blockDim.x)
+    {
+        const float v = kt_coord(a[lo + k], ax);
+        cge += !(v < p) ? 1u : 0u;
+        cle += !(p < v) ? 1u : 0u;
+    }
+    const uint32_t tge = block_sum(cge, sh.warp_sum);
+    const uint32_t tle = block_sum(cle, sh.warp_sum);
+    if (tid == 0)
+    {
+        sh.cnt[0] = tge;
+        sh.cnt[1] = tle;
+    }
+    cluster.sync();
+    uint32_t base_ge = 0, base_le = 0, nge = 0, nle = 0;
+    for (uint32_t r = 0; r < static_cast<uint32_t>(kKtCluster); ++r)
+    {
+        const uint32_t* rc = cluster.map_shared_rank(&sh.cnt[0], r);
+        const uint32_t g0 = rc[0], l0 = rc[1];
+        if (r < rank)
+        {
+            base_ge += g0;
+            base_le += l0;
+        }
+        nge += g0;
+        nle += l0;
+    }
+    // pass 2: ordered positions of this slice, a tile of blockDim x kKtItems at a time
+    const uint32_t tile = blockDim.x * kKtItems;
+    uint32_t og_run = base_ge, ol_run = base_le;
+    for (uint32_t t0 = c0; t0 < c1; t0 += tile)
+    {
+        uint32_t fge = 0, fle = 0, ng = 0, nl = 0;
+#pragma unroll
+        for (int k = 0; k < kKtItems; ++k)
+        {
+            const uint32_t idx = t0 + tid * kKtItems + k;
+            if (idx < c1)
+            {
+                const float v = kt_coord(a[lo + idx], ax);
+                if (!(v < p))
+                {
+                    fge |= 1u << k;
+                    ++ng;
+                }
+                if (!(p < v))
+                {
+                    fle |= 1u << k;
+                    ++nl;
+                }
+            }
+        }
+        const uint32_t pk = ng | (nl << 16);
+        uint32_t incl = pk;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= static_cast<uint32_t>(o))
+                incl += v;
+        }
+        __syncthreads();
+        if (lane == 31)
+            sh.warp_sum[warp] = incl;
+        __syncthreads();
+        uint32_t wpre = 0, total = 0;
+        for (uint32_t w = 0; w < nwarps; ++w)
+        {
+            const uint32_t v = sh.warp_sum[w];
+            if (w < warp)
+                wpre += v;
+            total += v;
+        }
+        const uint32_t ex = incl - pk + wpre;
+        uint32_t og = og_run + (ex & 0xffffu), ol = ol_run + (ex >> 16);
+#pragma unroll
+        for (int k = 0; k < kKtItems; ++k)
+        {
+            const uint32_t pos = lo + t0 + tid * kKtItems + k;
+            if (fge & (1u << k))
+                ge[og++] = pos;
+            if (fle & (1u << k))
+                le[ol++] = pos;
+        }
+        og_run += total & 0xffffu;
+        ol_run += total >> 16;
+    }
+    cluster.sync();
+    if (rank == 0 && tid == 0)
+    {
+        uint32_t lo_t = 0, hi_t = min(nge, nle);
+        while (lo_t < hi_t)
+        {
+            const uint32_t mid = (lo_t + hi_t + 1) / 2;
+            if (ge[mid - 1] < le[nle - mid])
+                lo_t = mid;
+            else
+                hi_t = mid - 1;
+        }
+        const uint32_t T = lo_t;
+        sh.res[0] = T;
+        sh.res[1] = (T == 0) ? ge[0] : min(T < nge ? ge[T] : 0xffffffffu, le[nle - T]);
+    }
+    cluster.sync();
+    const uint32_t* r0 = cluster.map_shared_rank(&sh.res[0], 0);
+    const uint32_t T = r0[0], cut = r0[1];
+    const uint32_t nthreads = blockDim.x * kKtCluster;
+    for (uint32_t t = rank * blockDim.x + tid; t < T; t += nthreads)
+        kt_swap(a, ge[t], le[nle - 1 - t]);
+    cluster.sync();
+    return cut;
+}
+
+// Levels whose ranges exceed kKtHuge: a cluster per range runs the introselect rounds while the
+// range is above kKtHuge, then its rank 0 finishes it as a single CTA would.
+__global__ void __cluster_dims__(kKtCluster, 1, 1) __launch_bounds__(kKtThreads)
+    k_kt_level_huge(BatchDev b, int level, uint32_t slots)
+{
+    __shared__ KtClusterShared csh;
+    __shared__ KtShared sh;
+    cg::cluster_group cluster = cg::this_cluster();
+    const uint32_t range = blockIdx.x / kKtCluster;
+    const uint32_t s = range / slots, j = range % slots;
+    if (s >= static_cast<uint32_t>(b.nscan))
+        return; // uniform over the cluster
+    const ScanDev& sd = b.scans[s];
+    uint32_t lb, le;
+    if (!kt_range(sd.n_src, level, j, lb, le, nullptr) || le - lb <= kKtHuge)
+        return; // uniform over the cluster
+    float4* g = b.kt + sd.src_off;
+    uint32_t* ge = b.kscr + 2ull * sd.src_off + 2ull * lb;
+    uint32_t* lq = ge + (le - lb);
+    const uint32_t len = le - lb, nth = lb + len / 2;
+    uint32_t first = lb, last = le;
+    int depth = 2 * static_cast<int>(floor_log2_u(len));
+    while (last - first > kKtHuge && depth > 0)
+    {
+        --depth;
+        const uint32_t cut = kt_round_cluster(g, first, last, level % 3, ge, lq, csh, cluster);
+        if (cut <= nth)
+            first = cut;
+        else
+            last = cut;
+    }
+    if (cluster.block_rank() == 0)
+    {
+        // the rest of the introselect on one CTA (the same rounds kt_select_block runs)
+        while (last - first > kKtSeqMax && depth > 0)
+        {
+            --depth;
+            const uint32_t cut = kt_round_block(g, first, last, level % 3, ge, lq, sh);
+            if (cut <= nth)
+                first = cut;
+            else
+                last = cut;
+        }
+        if (threadIdx.x == 0)
+        {
+            kt_select_seq(g, first, nth, last, depth, level % 3);
+            float4 p = g[nth];
+            p.w = __uint_as_float(len);
+            g[nth] = p;
+        }
+    }
+    cluster.sync(); // no CTA leaves while another may read its shared memory
+}
+
 __global__ void k_kt_load(BatchDev b)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -490,6 +775,8 @@ __global__ void __launch_bounds__(kKtThreads) k_kt_level(BatchDev b, int level, 
     uint32_t* ge = b.kscr + 2ull * sd.src_off + 2ull * lb;
     uint32_t* lq = ge + (le - lb);
     const uint32_t len = le - lb;
+    if (len > kKtHuge)
+        return; // k_kt_level_huge
     if (len > kKtSmall)
     {
         const uint32_t nth = lb + len / 2;
@@ -503,7 +790,7 @@ __global__ void __launch_bounds__(kKtThreads) k_kt_level(BatchDev b, int level, 
     }
     else if (level == 0 || plen > kKtSmall)
     {
-        kt_build_small(g, box, lb, le, level, kt_smem, ge, lq, sh);
+        kt_build_small(g, box, lb, le, level, kt_smem, reinterpret_cast<uint16_t*>(kt_smem + kKtSmall));
     }
 }
 
@@ -1038,7 +1325,8 @@ __global__ void __launch_bounds__(32) k_kt_chain(BatchDev b)
 
 size_t kt_build_smem_bytes()
 {
-    return static_cast<size_t>(kKtSmall) * sizeof(float4);
+    // the subtree's records, then two uint16 candidate lists per point
+    return static_cast<size_t>(kKtSmall) * sizeof(float4) + static_cast<size_t>(kKtSmall) * 2 * sizeof(uint16_t);
 }
 
 void init_kdtree_attributes()
@@ -1064,6 +1352,8 @@ void launch_noise(Launcher& L, const BatchDev& b, const BatchHost& hb, const lp_
     for (int l = 0; l < levels; ++l)
     {
         const uint32_t slots = 1u << l;
+        if ((nmax >> l) > kKtHuge)
+            LP_LAUNCH(L, k_kt_level_huge, S * slots * kKtCluster, kKtThreads, b, l, slots);
         LP_LAUNCH_SMEM(L, k_kt_level, S * slots, kKtThreads, kt_build_smem_bytes(), b, l, slots);
     }
     for (int l = levels - 2; l >= 0; --l)
