@@ -165,6 +165,53 @@ typedef struct lp_xyzrgb
 lp_status lp_split_clouds(lp_context* ctx, const float* xyzi, const uint32_t* labels, uint32_t n, lp_xyzrgb* ground,
                           lp_xyzrgb* obstacle, lp_xyzrgb* unsegmented, uint32_t* counts);
 
+/* The processor's per-cluster products after the hulls (processor.cpp:609-797), from one scan's
+ * pipeline outputs: the clustered cloud, the vehicle gates and the boundary marker geometry.
+ * - clustered cloud (processor.cpp:627-658): every clustered point, grouped by cluster label in
+ *   label order, input order within a label, coloured per label with three std::rand() % 256
+ *   draws (r, g, b). The reference never seeds rand(), so the draws continue glibc's default
+ *   stream; rand_draws says how many the process made before this scan (0 after start-up; each
+ *   scan with K clusters makes 3K).
+ * - vehicle gates (processor.cpp:675-771; perform_polygon_simplification, false in the reference):
+ *   a cluster of more than 150 points with a hull of at least 3 vertices, height (z range) and
+ *   hull-area volume inside the vehicle table's limits (processor.hpp:60-192), is boxed by
+ *   rotating calipers over ALL its points in input order (as the reference calls it), and
+ *   classified by the first vehicle type whose length, width, height, volume and area bounds it
+ *   meets when the hull fills more than 0.4 of the box.
+ * - boundary markers (convertPolygonPointsToMarker, processor.cpp:241-343): LINE_LIST points of the
+ *   polygon (the box corners for a classified cluster, else the hull) at z_min and z_max and the
+ *   vertical edges, 6 per polygon vertex; none for a polygon of fewer than 3 points. */
+typedef struct lp_object_config
+{
+    int32_t vehicle_gates; /* 1: evaluate the vehicle gates */
+    uint32_t reserved;
+    uint64_t rand_draws;   /* std::rand() calls made in the process before this scan */
+} lp_object_config;
+
+typedef struct lp_object_output
+{
+    lp_xyzrgb* clustered_cloud;  /* optional; capacity >= clustered points (labels >= 0) */
+    int32_t* vehicle_class;      /* optional, n_clusters: vehicle type 0-4 (compact car, sedan, SUV,
+                                    truck, minivan), -1 where the cluster is not boxed */
+    lp_bounding_box* gate_boxes; /* optional, n_clusters: the gate's calipers box (invalid where the
+                                    gate did not reach it) */
+    uint32_t* marker_offsets;    /* optional, n_clusters + 1: first marker point of each cluster */
+    double* marker_points;       /* optional, marker_capacity x 3 doubles (x, y, z) */
+    uint32_t marker_capacity;
+    /* Written by the library. */
+    uint32_t n_clustered;
+    uint32_t n_marker_points;
+} lp_object_output;
+
+/* xyzi: n x 4 floats; cluster_labels: n (LP_INVALID_CLUSTER for unclustered points); hull_offsets
+ * (n_clusters + 1), hull_indices (local to each cluster), z_min, z_max (n_clusters): the outputs of
+ * lp_process_scan for that cloud. All buffers are host memory. LP_ERR_CAPACITY when the marker
+ * points exceed marker_capacity (n_marker_points then says how many are needed). */
+lp_status lp_cluster_objects(lp_context* ctx, const float* xyzi, const int32_t* cluster_labels, uint32_t n,
+                             uint32_t n_clusters, const uint32_t* hull_offsets, const int32_t* hull_indices,
+                             const float* z_min, const float* z_max, const lp_object_config* cfg,
+                             lp_object_output* out);
+
 /* Ground segmentation. xyzi: n x 4 floats (x, y, z, intensity). ring: per-point ring index, or
  * NULL for a cloud without a ring field (the height index then comes from the elevation angle,
  * as for pcl::PointXYZ/XYZI). labels_out: n uint32 (LP_LABEL_*). image_bgr_out: optional

@@ -1129,6 +1129,212 @@ lp_status lp_split_clouds(lp_context* ctx, const float* xyzi, const uint32_t* la
     return LP_OK;
 }
 
+namespace
+{
+// processor.hpp:60-192: vehicle types widened by the tolerances, their volume and area bounds and
+// the overall limits, in the same binary64 expressions (host code is built without contraction).
+VehicleTableDev vehicle_table()
+{
+    VehicleTableDev t{};
+    const double base[5][6] = {{4.3, 4.6, 1.6, 1.9, 1.4, 1.5},
+                                {4.6, 5.0, 1.6, 1.9, 1.4, 1.5},
+                                {4.6, 5.2, 1.7, 2.1, 1.7, 1.8},
+                                {5.2, 5.8, 1.9, 2.2, 1.8, 2.0},
+                                {4.9, 5.2, 1.7, 2.1, 1.7, 1.8}};
+    const double lt = 0.8, wt = 0.5, ht = 0.5;
+    for (int v = 0; v < 5; ++v)
+    {
+        t.dims[v][0] = base[v][0] - lt;
+        t.dims[v][1] = base[v][1] + lt;
+        t.dims[v][2] = base[v][2] - wt;
+        t.dims[v][3] = base[v][3] + wt;
+        t.dims[v][4] = base[v][4] - ht;
+        t.dims[v][5] = base[v][5] + ht;
+        t.bounds[v][0] = t.dims[v][0] * t.dims[v][2] * t.dims[v][4];
+        t.bounds[v][1] = t.dims[v][1] * t.dims[v][3] * t.dims[v][5];
+        t.bounds[v][2] = t.dims[v][0] * t.dims[v][2];
+        t.bounds[v][3] = t.dims[v][1] * t.dims[v][3];
+    }
+    t.min_h = std::numeric_limits<double>::max();
+    t.max_h = std::numeric_limits<double>::lowest();
+    t.min_v = std::numeric_limits<double>::max();
+    t.max_v = std::numeric_limits<double>::lowest();
+    for (int v = 0; v < 5; ++v)
+    {
+        t.min_h = std::min(t.min_h, t.dims[v][4]);
+        t.max_h = std::max(t.max_h, t.dims[v][5]);
+        t.min_v = std::min(t.min_v, t.bounds[v][0]);
+        t.max_v = std::max(t.max_v, t.bounds[v][1]);
+    }
+    return t;
+}
+
+// glibc rand() (TYPE_3 additive feedback generator, the state rand() uses when never seeded):
+// r[0] = 1, r[i] = 16807 r[i-1] mod (2^31 - 1) for i < 31, r[31..33] = r[0..2], then
+// r[i] = r[i-31] + r[i-3] mod 2^32 with 310 values discarded; rand() returns r[i] >> 1. The window
+// holds the last 34 values; `draws` values are skipped (advanced from the context's cached window
+// when it lies behind).
+void rand_step(RandWindow& w)
+{
+    w.r[w.pos] = w.r[(w.pos + 3u) % 34u] + w.r[(w.pos + 31u) % 34u];
+    w.pos = (w.pos + 1u) % 34u;
+}
+
+RandWindow rand_window(lp_context* ctx, uint64_t draws)
+{
+    if (!ctx->rand_valid || draws < ctx->rand_at)
+    {
+        RandWindow w{};
+        int64_t word = 1;
+        w.r[0] = 1u;
+        for (int k = 1; k < 31; ++k)
+        {
+            const int64_t hi = word / 127773, lo = word % 127773;
+            word = 16807 * lo - 2836 * hi;
+            if (word < 0)
+                word += 2147483647;
+            w.r[k] = static_cast<uint32_t>(word);
+        }
+        for (int k = 31; k < 34; ++k)
+            w.r[k] = w.r[k - 31];
+        w.pos = 0; // slot of r[34] (index 34 mod 34)
+        for (int k = 0; k < 310; ++k)
+            rand_step(w);
+        ctx->rand_window = w;
+        ctx->rand_at = 0;
+        ctx->rand_valid = true;
+    }
+    for (; ctx->rand_at < draws; ++ctx->rand_at)
+        rand_step(ctx->rand_window);
+    return ctx->rand_window;
+}
+} // namespace
+
+lp_status lp_cluster_objects(lp_context* ctx, const float* xyzi, const int32_t* cluster_labels, uint32_t n,
+                             uint32_t n_clusters, const uint32_t* hull_offsets, const int32_t* hull_indices,
+                             const float* z_min, const float* z_max, const lp_object_config* cfg,
+                             lp_object_output* out)
+{
+    if (!ctx || !cfg || !out || (n && (!xyzi || !cluster_labels)) ||
+        (n_clusters && (!hull_offsets || !z_min || !z_max)))
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument");
+    out->n_clustered = 0;
+    out->n_marker_points = 0;
+    const uint32_t K = n_clusters;
+    if (K && out->marker_offsets)
+        std::memset(out->marker_offsets, 0, (static_cast<size_t>(K) + 1) * 4);
+    if (K == 0)
+    {
+        if (out->marker_offsets)
+            out->marker_offsets[0] = 0;
+        return LP_OK;
+    }
+    if (hull_offsets[0] != 0)
+        return fail(ctx, LP_ERR_BAD_ARG, "hull_offsets[0] must be 0");
+    for (uint32_t l = 0; l < K; ++l)
+        if (hull_offsets[l + 1] < hull_offsets[l])
+            return fail(ctx, LP_ERR_BAD_ARG, "hull_offsets must not decrease");
+    const uint32_t H = hull_offsets[K];
+    if (H && !hull_indices)
+        return fail(ctx, LP_ERR_BAD_ARG, "null hull_indices");
+    if (n > 0x7fffffffu / 8u)
+        return fail(ctx, LP_ERR_CAPACITY, "cloud too large for 32-bit indexing");
+    const uint32_t ntiles = obj_tiles(n);
+    const uint64_t cells = static_cast<uint64_t>(K) * ntiles + 1;
+    if (cells > 0x7fffffffull)
+        return fail(ctx, LP_ERR_CAPACITY, "too many clusters for the cloud's size");
+    const uint64_t mcap = 6ull * (static_cast<uint64_t>(H) + 4ull * K); // a polygon has max(h, 4) points
+    if (mcap > 0x7fffffffull)
+        return fail(ctx, LP_ERR_CAPACITY, "marker geometry too large");
+    LP_TRY(ensure_device(ctx));
+    auto al = [](size_t v) { return (v + 255) & ~static_cast<size_t>(255); };
+    const size_t N = n;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o += al(std::max<size_t>(bytes, 1));
+        return at;
+    };
+    const size_t o_pts = take(N * 16), o_lab = take(N * 4), o_cnt = take(cells * 4),
+                 o_sums = take(8 * (cells / 2048 + 4)), o_err = take(4), o_col = take(static_cast<size_t>(K) * 4),
+                 o_cloff = take((K + 1ull) * 4), o_cloud = take(N * sizeof(lp_xyzrgb)), o_hoff = take((K + 1ull) * 4),
+                 o_hidx = take(static_cast<size_t>(H) * 4), o_zmin = take(K * 4ull), o_zmax = take(K * 4ull),
+                 o_cls = take(K * 4ull), o_box = take(K * sizeof(lp_bounding_box)), o_P = take(N * 16),
+                 o_Pf = take(N * 8), o_ea = take(N * 4), o_pairs = take((4ull * N + 16ull * K) * 8),
+                 o_state = take(sizeof(ScanState)), o_moff = take((K + 1ull) * 4), o_mpts = take(mcap * 24);
+    char* m = nullptr;
+    LP_TRY(scratch(ctx, o, &m));
+    const cudaStream_t st = ctx->stream;
+    if (n)
+    {
+        LP_CUDA(ctx, cudaMemcpyAsync(m + o_pts, xyzi, N * 16, cudaMemcpyHostToDevice, st));
+        LP_CUDA(ctx, cudaMemcpyAsync(m + o_lab, cluster_labels, N * 4, cudaMemcpyHostToDevice, st));
+    }
+    LP_CUDA(ctx, cudaMemcpyAsync(m + o_hoff, hull_offsets, (K + 1ull) * 4, cudaMemcpyHostToDevice, st));
+    if (H)
+        LP_CUDA(ctx, cudaMemcpyAsync(m + o_hidx, hull_indices, static_cast<size_t>(H) * 4, cudaMemcpyHostToDevice, st));
+    LP_CUDA(ctx, cudaMemcpyAsync(m + o_zmin, z_min, K * 4ull, cudaMemcpyHostToDevice, st));
+    LP_CUDA(ctx, cudaMemcpyAsync(m + o_zmax, z_max, K * 4ull, cudaMemcpyHostToDevice, st));
+    LP_CUDA(ctx, cudaMemsetAsync(m + o_cnt, 0, cells * 4, st));
+    LP_CUDA(ctx, cudaMemsetAsync(m + o_err, 0, 4, st));
+    LP_CUDA(ctx, cudaMemsetAsync(m + o_state, 0, sizeof(ScanState), st));
+    const RandWindow w = rand_window(ctx, cfg->rand_draws);
+    uint32_t* err = reinterpret_cast<uint32_t*>(m + o_err);
+    uint32_t* sums = reinterpret_cast<uint32_t*>(m + o_sums);
+    auto* cloud = reinterpret_cast<lp_xyzrgb*>(m + o_cloud);
+    launch_objects_cloud(st, reinterpret_cast<const float4*>(m + o_pts), reinterpret_cast<const int32_t*>(m + o_lab), n, K,
+                         reinterpret_cast<uint32_t*>(m + o_cnt), sums, err, w, reinterpret_cast<uchar4*>(m + o_col),
+                         reinterpret_cast<uint32_t*>(m + o_cloff), cloud, ctx->launches);
+    ObjDev od{};
+    od.K = K;
+    od.cl_off = reinterpret_cast<const uint32_t*>(m + o_cloff);
+    od.hull_off = reinterpret_cast<const uint32_t*>(m + o_hoff);
+    od.hull_idx = reinterpret_cast<const int32_t*>(m + o_hidx);
+    od.zmin = reinterpret_cast<const float*>(m + o_zmin);
+    od.zmax = reinterpret_cast<const float*>(m + o_zmax);
+    od.cls = reinterpret_cast<int32_t*>(m + o_cls);
+    od.boxes = reinterpret_cast<lp_bounding_box*>(m + o_box);
+    od.cloud = cloud;
+    od.moff = reinterpret_cast<uint32_t*>(m + o_moff);
+    od.mpts = reinterpret_cast<double*>(m + o_mpts);
+    od.mcap = static_cast<uint32_t>(mcap);
+    static const VehicleTableDev vt = vehicle_table();
+    launch_objects_gates(st, od, vt, cfg->vehicle_gates, reinterpret_cast<double2*>(m + o_P),
+                         reinterpret_cast<float2*>(m + o_Pf), reinterpret_cast<float*>(m + o_ea),
+                         reinterpret_cast<int2*>(m + o_pairs), reinterpret_cast<ScanState*>(m + o_state),
+                         ctx->launches);
+    launch_objects_markers(st, od, sums, ctx->launches);
+    LP_CUDA(ctx, cudaGetLastError());
+    uint32_t h_err = 0, h_nc = 0, h_nm = 0;
+    ScanState h_state{};
+    LP_CUDA(ctx, cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, st));
+    LP_CUDA(ctx, cudaMemcpyAsync(&h_nc, m + o_cloff + 4ull * K, 4, cudaMemcpyDeviceToHost, st));
+    LP_CUDA(ctx, cudaMemcpyAsync(&h_nm, m + o_moff + 4ull * K, 4, cudaMemcpyDeviceToHost, st));
+    LP_CUDA(ctx, cudaMemcpyAsync(&h_state, m + o_state, sizeof(ScanState), cudaMemcpyDeviceToHost, st));
+    LP_CUDA(ctx, cudaStreamSynchronize(st));
+    if (h_err)
+        return fail(ctx, LP_ERR_BAD_ARG, "a cluster label is not below n_clusters");
+    if (h_state.err)
+        return fail(ctx, LP_ERR_INTERNAL, "vehicle gate: calipers pair capacity exceeded");
+    out->n_clustered = h_nc;
+    out->n_marker_points = h_nm;
+    if (out->clustered_cloud && h_nc)
+        LP_CUDA(ctx, cudaMemcpyAsync(out->clustered_cloud, cloud, h_nc * sizeof(lp_xyzrgb), cudaMemcpyDeviceToHost, st));
+    if (out->vehicle_class)
+        LP_CUDA(ctx, cudaMemcpyAsync(out->vehicle_class, m + o_cls, K * 4ull, cudaMemcpyDeviceToHost, st));
+    if (out->gate_boxes)
+        LP_CUDA(ctx, cudaMemcpyAsync(out->gate_boxes, m + o_box, K * sizeof(lp_bounding_box), cudaMemcpyDeviceToHost, st));
+    if (out->marker_offsets)
+        LP_CUDA(ctx, cudaMemcpyAsync(out->marker_offsets, m + o_moff, (K + 1ull) * 4, cudaMemcpyDeviceToHost, st));
+    const bool fits = h_nm <= out->marker_capacity;
+    if (out->marker_points && h_nm && fits)
+        LP_CUDA(ctx, cudaMemcpyAsync(out->marker_points, m + o_mpts, h_nm * 24ull, cudaMemcpyDeviceToHost, st));
+    LP_CUDA(ctx, cudaStreamSynchronize(st));
+    if (out->marker_points && !fits)
+        return fail(ctx, LP_ERR_CAPACITY, "marker_capacity below n_marker_points");
+    return LP_OK;
+}
+
 lp_status lp_add_ring_info(lp_context* ctx, const float* xyzi, uint32_t n, uint16_t first_ring, uint16_t* ring_out)
 {
     if (!ctx || (n && (!xyzi || !ring_out)))

@@ -2071,6 +2071,98 @@ __global__ void k_boxes_single(const double2* P, uint32_t n, int2* pairs, int ca
 }
 } // namespace
 
+namespace
+{
+// The vehicle gates (processor.cpp:679-755), one warp per cluster. Lane 0 checks the hull size, the
+// point count, the height against the table's limits and the volume of the hull area (polygonArea,
+// polygonizer.hpp:186-198, binary64 in hull order); a cluster that passes is boxed by rotating
+// calipers over all its points in input order, which is what the reference passes
+// (polygonizer_points_), with the same routine the hulls' boxes use; lane 0 then checks the hull's
+// share of the box (> 0.4) and the box's edges against the vehicle types in order.
+__global__ void k_obj_gate(ObjDev o, VehicleTableDev vt, int enabled, double2* P, float2* Pf, float* ea, int2* pairs,
+                           ScanState* st)
+{
+    const uint32_t l = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
+    if (l >= o.K)
+        return;
+    const uint32_t lane = lane_id();
+    const uint32_t off = o.cl_off[l], nc = o.cl_off[l + 1] - off;
+    const uint32_t h0 = o.hull_off[l], h = o.hull_off[l + 1] - h0;
+    const double height = static_cast<double>(o.zmax[l]) - static_cast<double>(o.zmin[l]);
+    double area = 0.0, volume = 0.0;
+    int pass = 0;
+    if (lane == 0)
+    {
+        lp_bounding_box none;
+        for (int k = 0; k < 4; ++k)
+            none.corners[k][0] = none.corners[k][1] = 0.0;
+        none.area = 0.0f;
+        none.angle_rad = 0.0f;
+        none.is_valid = 0;
+        o.boxes[l] = none;
+        o.cls[l] = -1;
+        if (enabled && h >= 3 && nc > 150 && height > vt.min_h && height < vt.max_h)
+        {
+            auto vx = [&](uint32_t k) { return static_cast<double>(o.cloud[off + static_cast<uint32_t>(o.hull_idx[h0 + k])].x); };
+            auto vy = [&](uint32_t k) { return static_cast<double>(o.cloud[off + static_cast<uint32_t>(o.hull_idx[h0 + k])].y); };
+            double a = 0.0;
+            for (uint32_t k = 0; k + 1 < h; ++k)
+                a += (vx(k) * vy(k + 1)) - (vx(k + 1) * vy(k));
+            a += (vx(h - 1) * vy(0)) - (vx(0) * vy(h - 1));
+            area = fabs(a) * 0.5;
+            volume = area * height;
+            pass = (volume > vt.min_v && volume < vt.max_v) ? 1 : 0;
+        }
+    }
+    pass = __shfl_sync(0xffffffffu, pass, 0);
+    if (!pass)
+        return;
+    area = __shfl_sync(0xffffffffu, area, 0);
+    volume = __shfl_sync(0xffffffffu, volume, 0);
+    for (uint32_t k = lane; k < nc; k += 32)
+    {
+        const lp_xyzrgb& p = o.cloud[off + k];
+        P[off + k] = make_double2(static_cast<double>(p.x), static_cast<double>(p.y));
+        Pf[off + k] = make_float2(p.x, p.y);
+    }
+    __syncwarp();
+    calipers_box(st, P + off, Pf + off, ea + off, static_cast<int>(nc), pairs + 4ull * off + 16ull * l, &o.boxes[l]);
+    __syncwarp();
+    if (lane != 0)
+        return;
+    const lp_bounding_box box = o.boxes[l];
+    if (!box.is_valid || !(area / static_cast<double>(box.area) > 0.4))
+        return;
+    auto dist = [&](int a, int c) {
+        const double dx = box.corners[a][0] - box.corners[c][0];
+        const double dy = box.corners[a][1] - box.corners[c][1];
+        return sqrt(dx * dx + dy * dy);
+    };
+    const double e1 = dist(0, 1), e2 = dist(1, 2);
+    const double len = fmax(e1, e2), wid = fmin(e1, e2);
+    for (int v = 0; v < 5; ++v)
+    {
+        const double* d = vt.dims[v];
+        const double* bb = vt.bounds[v];
+        if (len > d[0] && len < d[1] && wid > d[2] && wid < d[3] && height > d[4] && height < d[5] && volume > bb[0] &&
+            volume < bb[1] && area > bb[2] && area < bb[3])
+        {
+            o.cls[l] = v;
+            break;
+        }
+    }
+}
+} // namespace
+
+void launch_objects_gates(cudaStream_t st, const ObjDev& o, const VehicleTableDev& vt, int enabled, double2* P,
+                          float2* Pf, float* ea, int2* pairs, ScanState* state, uint64_t& launches)
+{
+    if (o.K == 0)
+        return;
+    k_obj_gate<<<div_up(o.K, 4u), 128, 0, st>>>(o, vt, enabled, P, Pf, ea, pairs, state);
+    launches += 1;
+}
+
 void launch_polygons(Launcher& L, const BatchDev& b, const BatchHost& hb, int compute_obb)
 {
     (void)hb;

@@ -60,6 +60,11 @@ struct lp_context
     size_t split_cap = 0;
     void* flush = nullptr; // buffer larger than L2 for cache flushing between timed runs
     size_t flush_bytes = 0;
+    // lp_cluster_objects: glibc rand() positioned at the last call's first draw (advanced, not
+    // recomputed, when the next call's offset lies ahead)
+    uint64_t rand_at = 0;
+    bool rand_valid = false;
+    lpg::RandWindow rand_window{};
 };
 
 struct lp_batch

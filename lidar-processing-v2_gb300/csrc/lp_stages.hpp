@@ -128,6 +128,41 @@ void launch_unpack_pointcloud2(cudaStream_t st, const uint8_t* data, uint32_t wi
 // The processor's ground / obstacle / unsegmented clouds (lp_split.cu): out holds 3 x n records.
 void launch_split_clouds(cudaStream_t st, const float4* pts, const uint32_t* labels, uint32_t n, lp_xyzrgb* out,
                          uint32_t* counts, uint32_t* sums, uint64_t& launches);
+// Per-cluster products after the hulls (lp_objects.cu, k_obj_gate in lp_hull.cu).
+struct RandWindow // glibc rand()'s last 34 values; pos: the slot the next value replaces
+{
+    uint32_t r[34];
+    uint32_t pos;
+};
+struct VehicleTableDev // processor.hpp:60-192 in binary64: min/max length, width, height; bounds
+{
+    double dims[5][6];
+    double bounds[5][4]; // min/max volume, min/max area
+    double min_h, max_h, min_v, max_v;
+};
+struct ObjDev
+{
+    uint32_t K;
+    const uint32_t* cl_off;   // K + 1: first cloud slot of each cluster
+    const uint32_t* hull_off; // K + 1
+    const int32_t* hull_idx;  // local indices
+    const float* zmin;
+    const float* zmax;
+    int32_t* cls;             // K: vehicle type or -1
+    lp_bounding_box* boxes;   // K: the gate's calipers boxes
+    const lp_xyzrgb* cloud;   // the clustered cloud
+    uint32_t* moff;           // K + 1: marker points per cluster -> exclusive scan
+    double* mpts;             // marker points (3 doubles each)
+    uint32_t mcap;
+};
+uint32_t obj_tiles(uint32_t n);
+void launch_objects_cloud(cudaStream_t st, const float4* pts, const int32_t* labels, uint32_t n, uint32_t K,
+                          uint32_t* cnt, uint32_t* sums, uint32_t* err, const RandWindow& w, uchar4* colour,
+                          uint32_t* cl_off, lp_xyzrgb* cloud, uint64_t& launches);
+void launch_objects_gates(cudaStream_t st, const ObjDev& o, const VehicleTableDev& vt, int enabled, double2* P,
+                          float2* Pf, float* ea, int2* pairs, ScanState* state, uint64_t& launches);
+void launch_objects_markers(cudaStream_t st, const ObjDev& o, uint32_t* sums, uint64_t& launches);
+
 // Streaming multiprocessors of the current device (persistent grids are sized by it).
 int sm_count();
 

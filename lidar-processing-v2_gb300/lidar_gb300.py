@@ -270,6 +270,7 @@ def _declare(lib):
         "lp_kernel_launch_count": (c.c_uint64, [P]),
         "lp_add_ring_info": (c.c_int32, [P, P, c.c_uint32, c.c_uint16, P]),
         "lp_split_clouds": (c.c_int32, [P, P, P, c.c_uint32, P, P, P, P]),
+        "lp_cluster_objects": (c.c_int32, [P, P, P, c.c_uint32, c.c_uint32, P, P, P, P, P, P]),
         "lp_unpack_pointcloud2": (c.c_int32, [P, P, c.c_uint32, c.c_uint32, c.c_uint32, c.c_uint32, P, P, P]),
         "lp_segment": (c.c_int32, [P, P, P, c.c_uint32, P, P, P]),
         "lp_noise_remove": (c.c_int32, [P, P, c.c_uint32, c.c_uint32, P, P]),
@@ -418,6 +419,67 @@ def split_clouds(ctx, cloud, labels):
     check(library().lp_split_clouds(ctx.handle, ptr(a), ptr(lab), len(a), ptr(outs[0]), ptr(outs[1]), ptr(outs[2]),
                                     ptr(counts)), ctx)
     return tuple(o[:k] for o, k in zip(outs, counts))
+
+
+class ObjectConfig(ctypes.Structure):
+    """lp_object_config: the vehicle gates on or off and the std::rand() draws made before."""
+
+    _fields_ = [("vehicle_gates", ctypes.c_int32), ("reserved", ctypes.c_uint32), ("rand_draws", ctypes.c_uint64)]
+
+
+class ObjectOutput(ctypes.Structure):
+    _fields_ = [
+        ("clustered_cloud", ctypes.c_void_p),
+        ("vehicle_class", ctypes.c_void_p),
+        ("gate_boxes", ctypes.c_void_p),
+        ("marker_offsets", ctypes.c_void_p),
+        ("marker_points", ctypes.c_void_p),
+        ("marker_capacity", ctypes.c_uint32),
+        ("n_clustered", ctypes.c_uint32),
+        ("n_marker_points", ctypes.c_uint32),
+    ]
+
+
+class ClusterObjects:
+    """The processor's per-cluster products of one scan (processor.cpp:609-797): the clustered cloud
+    (XYZRGB records by label, colours from std::rand()), the vehicle class per cluster (-1 when not
+    boxed), the gate's calipers boxes, and the boundary marker points (n x 3 float64, offsets per
+    cluster)."""
+
+    def __init__(self, cloud, vehicle_class, gate_boxes, marker_offsets, marker_points):
+        self.cloud = cloud
+        self.vehicle_class = vehicle_class
+        self.gate_boxes = gate_boxes
+        self.marker_offsets = marker_offsets
+        self.marker_points = marker_points
+
+
+def object_buffers(n, n_clusters, hull_offsets):
+    """Output buffers of lp_cluster_objects sized for n points and the given hulls."""
+    K = int(n_clusters)
+    mcap = 6 * (int(hull_offsets[K]) + 4 * K) if K else 0
+    bufs = (np.zeros(max(n, 1), XYZRGB), np.full(max(K, 1), -7, np.int32), (BoundingBox * max(K, 1))(),
+            np.zeros(K + 1, np.uint32), np.zeros((max(mcap, 1), 3), np.float64))
+    out = ObjectOutput(ptr(bufs[0]), ptr(bufs[1]), ctypes.cast(bufs[2], ctypes.c_void_p).value, ptr(bufs[3]),
+                       ptr(bufs[4]), mcap, 0, 0)
+    return out, bufs
+
+
+def cluster_objects(ctx, cloud, result, vehicle_gates=False, rand_draws=0):
+    """lp_cluster_objects over one scan's pipeline result (cluster labels, hulls, z ranges)."""
+    a = _xyzi(cloud)
+    lab = np.ascontiguousarray(result.cluster_labels, np.int32)
+    K = int(result.n_clusters)
+    hoff = np.ascontiguousarray(result.hull_offsets[: K + 1], np.uint32)
+    hidx = np.ascontiguousarray(result.hull_indices, np.int32)
+    zmin = np.ascontiguousarray(result.z_min[:K], np.float32)
+    zmax = np.ascontiguousarray(result.z_max[:K], np.float32)
+    cfg = ObjectConfig(1 if vehicle_gates else 0, 0, rand_draws)
+    out, bufs = object_buffers(len(a), K, hoff)
+    check(library().lp_cluster_objects(ctx.handle, ptr(a), ptr(lab), len(a), K, ptr(hoff), ptr(hidx), ptr(zmin),
+                                       ptr(zmax), ctypes.byref(cfg), ctypes.byref(out)), ctx)
+    return ClusterObjects(bufs[0][: out.n_clustered].copy(), bufs[1][:K].copy(), list(bufs[2])[:K],
+                          bufs[3].copy(), bufs[4][: out.n_marker_points].copy())
 
 
 class Segmenter:

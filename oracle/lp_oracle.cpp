@@ -1286,3 +1286,241 @@ void lpo_ransac_draws(uint32_t n, uint32_t iters, uint32_t* out)
     }
 }
 }
+
+extern "C" {
+// ---------------------------------------------------------------------------------------------
+// The processor's per-cluster loop after the hulls: Processor::run, processor.cpp:609-797 (the
+// clustered cloud with std::rand() colours, the vehicle gates, convertPolygonPointsToMarker).
+// ---------------------------------------------------------------------------------------------
+
+// glibc's rand() (random_r, TYPE_3 additive feedback generator), restated from its published
+// algorithm: state r[0] = seed (1 when never seeded), r[i] = 16807 r[i-1] mod (2^31 - 1) for
+// i = 1..30, r[31..33] = r[0..2], then r[i] = r[i-31] + r[i-3] mod 2^32; output k is r[k+344] >> 1
+// (the first 310 values after r[33] are discarded by the seeding).
+struct GlibcRand
+{
+    uint32_t w[34];
+    uint64_t i = 34; // index of the next r[i]
+    explicit GlibcRand(uint32_t seed = 1)
+    {
+        int32_t r[34];
+        r[0] = static_cast<int32_t>(seed);
+        for (int k = 1; k < 31; ++k)
+        {
+            const int64_t hi = r[k - 1] / 127773, lo = r[k - 1] % 127773;
+            int64_t word = 16807 * lo - 2836 * hi;
+            if (word < 0)
+                word += 2147483647;
+            r[k] = static_cast<int32_t>(word);
+        }
+        for (int k = 31; k < 34; ++k)
+            r[k] = r[k - 31];
+        for (int k = 0; k < 34; ++k)
+            w[k] = static_cast<uint32_t>(r[k]);
+        for (int k = 0; k < 310; ++k)
+            step();
+    }
+    uint32_t step()
+    {
+        // ring of the last 34 values: r[i] = r[i-31] + r[i-3]
+        const uint32_t v = w[(i - 31) % 34] + w[(i - 3) % 34];
+        w[i % 34] = v;
+        ++i;
+        return v;
+    }
+    int32_t next() { return static_cast<int32_t>(step() >> 1); }
+};
+
+int32_t lpo_glibc_rand(uint64_t skip, uint32_t count, int32_t* out)
+{
+    GlibcRand g;
+    for (uint64_t k = 0; k < skip; ++k)
+        g.step();
+    for (uint32_t k = 0; k < count; ++k)
+        out[k] = g.next();
+    return 0;
+}
+
+namespace
+{
+// processor.hpp:60-192: the vehicle table widened by the tolerances, its volume and area bounds and
+// the overall limits, in the same binary64 expressions.
+struct VehicleTable
+{
+    double dims[5][6]; // min/max length, width, height
+    double bounds[5][4]; // min/max volume, area
+    double min_h, max_h, min_v, max_v;
+    VehicleTable()
+    {
+        const double base[5][6] = {{4.3, 4.6, 1.6, 1.9, 1.4, 1.5},
+                                    {4.6, 5.0, 1.6, 1.9, 1.4, 1.5},
+                                    {4.6, 5.2, 1.7, 2.1, 1.7, 1.8},
+                                    {5.2, 5.8, 1.9, 2.2, 1.8, 2.0},
+                                    {4.9, 5.2, 1.7, 2.1, 1.7, 1.8}};
+        const double lt = 0.8, wt = 0.5, ht = 0.5;
+        for (int v = 0; v < 5; ++v)
+        {
+            dims[v][0] = base[v][0] - lt;
+            dims[v][1] = base[v][1] + lt;
+            dims[v][2] = base[v][2] - wt;
+            dims[v][3] = base[v][3] + wt;
+            dims[v][4] = base[v][4] - ht;
+            dims[v][5] = base[v][5] + ht;
+        }
+        for (int v = 0; v < 5; ++v)
+        {
+            bounds[v][0] = dims[v][0] * dims[v][2] * dims[v][4];
+            bounds[v][1] = dims[v][1] * dims[v][3] * dims[v][5];
+            bounds[v][2] = dims[v][0] * dims[v][2];
+            bounds[v][3] = dims[v][1] * dims[v][3];
+        }
+        min_h = std::numeric_limits<double>::max();
+        max_h = std::numeric_limits<double>::lowest();
+        min_v = std::numeric_limits<double>::max();
+        max_v = std::numeric_limits<double>::lowest();
+        for (int v = 0; v < 5; ++v)
+        {
+            if (dims[v][4] < min_h)
+                min_h = dims[v][4];
+            if (dims[v][5] > max_h)
+                max_h = dims[v][5];
+            if (bounds[v][0] < min_v)
+                min_v = bounds[v][0];
+            if (bounds[v][1] > max_v)
+                max_v = bounds[v][1];
+        }
+    }
+};
+} // namespace
+
+lp_status lpo_cluster_objects(const float* xyzi, const int32_t* labels, uint32_t n, uint32_t K,
+                              const uint32_t* hull_offsets, const int32_t* hull_indices, const float* zmin_in,
+                              const float* zmax_in, const lp_object_config* cfg, lp_object_output* out)
+{
+    static const VehicleTable vt;
+    GlibcRand g;
+    for (uint64_t k = 0; k < cfg->rand_draws; ++k)
+        g.step();
+    uint32_t cpos = 0, mpos = 0;
+    bool overflow = false;
+    std::vector<std::vector<uint32_t>> members(K);
+    for (uint32_t i = 0; i < n; ++i)
+        if (labels[i] >= 0 && static_cast<uint32_t>(labels[i]) < K)
+            members[labels[i]].push_back(i);
+    std::vector<double> pts;
+    for (uint32_t l = 0; l < K; ++l)
+    {
+        const uint8_t r = static_cast<uint8_t>(g.next() % 256), gg = static_cast<uint8_t>(g.next() % 256),
+                      b = static_cast<uint8_t>(g.next() % 256);
+        pts.clear();
+        double z_min = std::numeric_limits<double>::max(), z_max = std::numeric_limits<double>::lowest();
+        for (uint32_t i : members[l])
+        {
+            if (out->clustered_cloud)
+                out->clustered_cloud[cpos] = lp_xyzrgb{xyzi[4 * i], xyzi[4 * i + 1], xyzi[4 * i + 2], r, gg, b, 255};
+            ++cpos;
+            pts.push_back(xyzi[4 * i]);
+            pts.push_back(xyzi[4 * i + 1]);
+            const double z = xyzi[4 * i + 2];
+            if (z < z_min)
+                z_min = z;
+            if (z > z_max)
+                z_max = z;
+        }
+        (void)zmin_in;
+        (void)zmax_in;
+        // polygon points in hull order
+        std::vector<double> poly;
+        for (uint32_t k = hull_offsets[l]; k < hull_offsets[l + 1]; ++k)
+        {
+            const uint32_t i = members[l][hull_indices[k]];
+            poly.push_back(xyzi[4 * i]);
+            poly.push_back(xyzi[4 * i + 1]);
+        }
+        int32_t cls = -1;
+        lp_bounding_box gbox;
+        std::memset(&gbox, 0, sizeof(gbox));
+        const double height = z_max - z_min;
+        const uint32_t np = static_cast<uint32_t>(poly.size() / 2);
+        if (cfg->vehicle_gates && np >= 3 && members[l].size() > 150 && height > vt.min_h && height < vt.max_h)
+        {
+            // polygonArea (polygonizer.hpp:186-198)
+            double area = 0.0;
+            for (uint32_t k = 0; k + 1 < np; ++k)
+                area += (poly[2 * k] * poly[2 * k + 3]) - (poly[2 * k + 2] * poly[2 * k + 1]);
+            area += (poly[2 * (np - 1)] * poly[1]) - (poly[0] * poly[2 * (np - 1) + 1]);
+            const double polygon_area = std::fabs(area) * 0.5;
+            const double polygon_volume = polygon_area * height;
+            if (polygon_volume > vt.min_v && polygon_volume < vt.max_v)
+            {
+                lpo_bounding_box_rotating_calipers(pts.data(), static_cast<uint32_t>(members[l].size()), &gbox);
+                if (gbox.is_valid && polygon_area / gbox.area > 0.4)
+                {
+                    auto dist = [&](int a, int c) {
+                        const double dx = gbox.corners[a][0] - gbox.corners[c][0];
+                        const double dy = gbox.corners[a][1] - gbox.corners[c][1];
+                        return std::sqrt(dx * dx + dy * dy);
+                    };
+                    const double e1 = dist(0, 1), e2 = dist(1, 2);
+                    const double L = std::max(e1, e2), W = std::min(e1, e2);
+                    for (int v = 0; v < 5; ++v)
+                    {
+                        const double* d = vt.dims[v];
+                        const double* bb = vt.bounds[v];
+                        if (L > d[0] && L < d[1] && W > d[2] && W < d[3] && height > d[4] && height < d[5] &&
+                            polygon_volume > bb[0] && polygon_volume < bb[1] && polygon_area > bb[2] &&
+                            polygon_area < bb[3])
+                        {
+                            cls = v;
+                            poly.assign({gbox.corners[0][0], gbox.corners[0][1], gbox.corners[1][0], gbox.corners[1][1],
+                                         gbox.corners[2][0], gbox.corners[2][1], gbox.corners[3][0], gbox.corners[3][1]});
+                            break;
+                        }
+                    }
+                }
+            }
+        }
+        if (out->vehicle_class)
+            out->vehicle_class[l] = cls;
+        if (out->gate_boxes)
+            out->gate_boxes[l] = gbox;
+        if (out->marker_offsets)
+            out->marker_offsets[l] = mpos;
+        const uint32_t m = static_cast<uint32_t>(poly.size() / 2);
+        if (m >= 3)
+        {
+            auto put = [&](double x, double y, double z) {
+                if (out->marker_points && mpos < out->marker_capacity)
+                {
+                    out->marker_points[3 * static_cast<size_t>(mpos)] = x;
+                    out->marker_points[3 * static_cast<size_t>(mpos) + 1] = y;
+                    out->marker_points[3 * static_cast<size_t>(mpos) + 2] = z;
+                }
+                else if (out->marker_points)
+                    overflow = true;
+                ++mpos;
+            };
+            for (const double z : {z_min, z_max})
+            {
+                for (uint32_t k = 1; k < m; ++k)
+                {
+                    put(poly[2 * (k - 1)], poly[2 * (k - 1) + 1], z);
+                    put(poly[2 * k], poly[2 * k + 1], z);
+                }
+                put(poly[2 * (m - 1)], poly[2 * (m - 1) + 1], z);
+                put(poly[0], poly[1], z);
+            }
+            for (uint32_t k = 0; k < m; ++k)
+            {
+                put(poly[2 * k], poly[2 * k + 1], z_min);
+                put(poly[2 * k], poly[2 * k + 1], z_max);
+            }
+        }
+    }
+    if (out->marker_offsets)
+        out->marker_offsets[K] = mpos;
+    out->n_clustered = cpos;
+    out->n_marker_points = mpos;
+    return overflow ? LP_ERR_CAPACITY : LP_OK;
+}
+}

@@ -51,6 +51,8 @@ def oracle():
             "lpo_bounding_box_pca": (c.c_int32, [P, c.c_uint32, P, P]),
             "lpo_jacobi_svd2": (c.c_int32, [P, P]),
             "lpo_kdtree_positions": (c.c_int32, [P, c.c_uint32, P]),
+            "lpo_glibc_rand": (c.c_int32, [c.c_uint64, c.c_uint32, P]),
+            "lpo_cluster_objects": (c.c_int32, [P, P, c.c_uint32, c.c_uint32, P, P, P, P, P, P]),
             "lpo_debug_nth": (c.c_int32, [P, c.c_uint32, c.c_uint32, c.c_int32, c.c_int32, P]),
             "lpo_process_scan": (c.c_int32, [P, P, c.c_int, P]),
         }
@@ -191,6 +193,30 @@ def o_debug_nth(v, nth, restated, depth_override=-1):
     out = np.zeros(len(a), np.int32)
     oracle().lpo_debug_nth(ptr(a), len(a), nth, int(restated), depth_override, ptr(out))
     return out
+
+
+def o_glibc_rand(skip, count):
+    out = np.zeros(count, np.int32)
+    oracle().lpo_glibc_rand(skip, count, ptr(out))
+    return out
+
+
+def o_cluster_objects(cloud, result, vehicle_gates=False, rand_draws=0):
+    """The oracle's restatement of the processor's per-cluster loop (processor.cpp:609-797)."""
+    a = np.ascontiguousarray(np.asarray(cloud, np.float32)[:, :4])
+    lab = np.ascontiguousarray(result.cluster_labels, np.int32)
+    K = int(result.n_clusters)
+    hoff = np.ascontiguousarray(result.hull_offsets[: K + 1], np.uint32)
+    hidx = np.ascontiguousarray(result.hull_indices, np.int32)
+    zmin = np.ascontiguousarray(result.z_min[:K], np.float32)
+    zmax = np.ascontiguousarray(result.z_max[:K], np.float32)
+    cfg = lp.ObjectConfig(1 if vehicle_gates else 0, 0, rand_draws)
+    out, bufs = lp.object_buffers(len(a), K, hoff)
+    st = oracle().lpo_cluster_objects(ptr(a), ptr(lab), len(a), K, ptr(hoff), ptr(hidx), ptr(zmin), ptr(zmax),
+                                      ctypes.byref(cfg), ctypes.byref(out))
+    assert st == 0, st
+    return lp.ClusterObjects(bufs[0][: out.n_clustered].copy(), bufs[1][:K].copy(), list(bufs[2])[:K],
+                             bufs[3].copy(), bufs[4][: out.n_marker_points].copy())
 
 
 def o_antipodal(hp):

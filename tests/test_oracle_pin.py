@@ -357,3 +357,14 @@ def test_jacobi_svd2_restatement(built):
         sxy = rng.normal() * np.sqrt(sxx * syy) * rng.uniform(0, 1) ** 4
         a = np.array([[sxx, sxy], [sxy, syy]])
         svd_check(a, T.o_svd2(a))
+
+
+def test_glibc_rand_restatement_matches_libc():
+    """The oracle's restatement of glibc's rand() (the stream the processor's cluster colours draw
+    from, processor.cpp:630-632, never seeded) equals the host C library's rand() after srand(1)."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    libc.srand(1)
+    seq = np.array([libc.rand() for _ in range(5000)], np.int32)
+    assert np.array_equal(T.o_glibc_rand(0, 5000), seq)
+    assert np.array_equal(T.o_glibc_rand(4321, 100), seq[4321:4421])
