@@ -54,6 +54,12 @@ void lp_host_free(void* p);
  * the parity tests. No counterpart in the reference. */
 lp_status lp_debug_kdtree(lp_context* ctx, const float* xyz, uint32_t stride, uint32_t n,
                           const lp_noise_remover_config* cfg, float* nodes_out);
+/* Bounded waits giving up: kind 0 runs the device-wide prefix scan on a tile whose predecessor
+ * never publishes (its ticket counter starts past tile 0), kind 1 waits on an mbarrier that never
+ * completes; each polls `limit` times, then records the failure as the library's kernels do.
+ * Returns LP_ERR_TIMEOUT with *gave_up != 0 when the wait gave up (the expected outcome), leaving
+ * the context usable. For the failure-path tests; no counterpart in the reference. */
+lp_status lp_debug_wait_timeout(lp_context* ctx, int32_t kind, uint32_t limit, uint32_t* gave_up);
 /* Device evaluation of the library's correctly rounded binary32 functions (kind 0 atan2(a, b),
  * 1 atan(a), 2 exp(a), 3 the reference's atan2 approximation; 4, 5, 6 the same three functions
  * without their float-float first stage); used by the parity tests. */
@@ -74,7 +80,10 @@ typedef struct lp_server lp_server;
 
 typedef struct lp_server_config
 {
-    uint64_t memory_budget_bytes; /* device memory reserved for in-flight batches (split over slots) */
+    uint64_t memory_budget_bytes; /* device memory reserved once for in-flight batches: one pool from
+                                     which each admitted batch takes exactly its planned bytes; a scan
+                                     that does not fit the memory free now waits, one larger than the
+                                     whole budget is refused (LP_ERR_CAPACITY) */
     uint32_t max_batch_scans;     /* most scans one batch admits */
     uint32_t slots;               /* batches that can be on the GPU at once (each has its own stream) */
 } lp_server_config;

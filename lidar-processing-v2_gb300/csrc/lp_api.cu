@@ -1872,6 +1872,23 @@ lp_status lp_batch_profile(lp_context* ctx, lp_batch* B, char* names, uint32_t n
 
 // Evaluates the device's correctly rounded binary32 functions (kind 0 atan2, 1 atan, 2 exp,
 // 3 the reference's atan2 approximation) on host arrays; used by the parity tests.
+lp_status lp_debug_wait_timeout(lp_context* ctx, int32_t kind, uint32_t limit, uint32_t* gave_up)
+{
+    if (!ctx || !gave_up || (kind != 0 && kind != 1) || limit == 0)
+        return fail(ctx, LP_ERR_BAD_ARG, "kind 0 or 1, limit > 0, non-null result");
+    *gave_up = 0;
+    LP_TRY(ensure_device(ctx));
+    char* m = nullptr;
+    LP_TRY(scratch(ctx, 256, &m));
+    uint32_t* err = reinterpret_cast<uint32_t*>(m + 64);
+    LP_CUDA(ctx, cudaMemsetAsync(m, 0, 256, ctx->stream));
+    launch_debug_wait_timeout(ctx->stream, kind, limit, reinterpret_cast<unsigned long long*>(m), err, ctx->launches);
+    LP_CUDA(ctx, cudaGetLastError());
+    LP_CUDA(ctx, cudaMemcpyAsync(gave_up, err, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    LP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return *gave_up ? LP_ERR_TIMEOUT : LP_OK;
+}
+
 lp_status lp_debug_math(lp_context* ctx, int32_t kind, const float* a, const float* b, uint32_t n, float* out)
 {
     if (!ctx || !a || !out)

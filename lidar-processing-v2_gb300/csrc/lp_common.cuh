@@ -250,7 +250,7 @@ __device__ __forceinline__ void st_status(unsigned long long* p, unsigned long l
 // Exclusive prefix of the tile `tile` whose own total is `total` (warp 0 of the block; the
 // result is valid in every lane).
 __device__ __forceinline__ uint32_t lb_tile_prefix(unsigned long long* tiles, uint32_t tile, uint32_t total,
-                                                   uint32_t* err)
+                                                   uint32_t* err, uint32_t poll_limit)
 {
     const uint32_t lane = lane_id();
     if (tile == 0)
@@ -272,7 +272,7 @@ __device__ __forceinline__ uint32_t lb_tile_prefix(unsigned long long* tiles, ui
             uint32_t polls = 0;
             do
                 w = ld_status(&tiles[t]);
-            while ((w >> 62) == 0u && ++polls < (1u << 24));
+            while ((w >> 62) == 0u && ++polls < poll_limit);
             if ((w >> 62) == 0u)
             {
                 ok = false;
@@ -293,8 +293,11 @@ __device__ __forceinline__ uint32_t lb_tile_prefix(unsigned long long* tiles, ui
     return prefix;
 }
 
+constexpr uint32_t kLbPollLimit = 1u << 24; // polls of a predecessor's word before giving up
+
 template <class Src, class Dst>
-__global__ void __launch_bounds__(kLbThreads) k_scan_lb(Src src, Dst dst, unsigned long long* state, uint32_t* err)
+__global__ void __launch_bounds__(kLbThreads) k_scan_lb(Src src, Dst dst, unsigned long long* state, uint32_t* err,
+                                                        uint32_t poll_limit)
 {
     __shared__ uint32_t s_warp[kLbThreads / 32];
     __shared__ uint32_t s_tile;
@@ -326,7 +329,7 @@ __global__ void __launch_bounds__(kLbThreads) k_scan_lb(Src src, Dst dst, unsign
         const uint32_t wv = (lane < kLbThreads / 32) ? s_warp[lane] : 0u;
         const uint32_t wi = warp_incl_scan(wv);
         const uint32_t total = __shfl_sync(0xffffffffu, wi, 31);
-        const uint32_t prefix = lb_tile_prefix(state + 1, tile, total, err);
+        const uint32_t prefix = lb_tile_prefix(state + 1, tile, total, err, poll_limit);
         if (lane < kLbThreads / 32)
             s_warp[lane] = prefix + wi - wv;
     }
@@ -350,7 +353,7 @@ void scan_lookback(cudaStream_t st, Src src, Dst dst, uint32_t n, uint32_t* sums
     const uint32_t nt = div_up(n, kLbTile);
     unsigned long long* state = reinterpret_cast<unsigned long long*>(sums);
     cudaMemsetAsync(state, 0, (static_cast<size_t>(nt) + 1) * sizeof(unsigned long long), st);
-    k_scan_lb<<<nt, kLbThreads, 0, st>>>(src, dst, state, err);
+    k_scan_lb<<<nt, kLbThreads, 0, st>>>(src, dst, state, err, kLbPollLimit);
 }
 
 // Plain u32 arrays as scan source and destination (vector accesses when 16-byte aligned).

@@ -1422,6 +1422,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
     __shared__ uint32_t mrow[kRowCache];
     __shared__ unsigned long long mbar[2];
     __shared__ int32_t st_row[2], st_coff[2];
+    __shared__ int32_t st_pend[2]; // a copy into the buffer is in flight (issued, not yet waited for)
     const int s = blockIdx.x;
     const ScanDev& sd = b.scans[s];
     const int32_t H = sd.H, W = sd.W;
@@ -1435,6 +1436,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
         mbar_init(&mbar[0], 1u);
         mbar_init(&mbar[1], 1u);
         st_row[0] = st_row[1] = -1;
+        st_pend[0] = st_pend[1] = 0;
     }
     __syncthreads();
     // thread 0: copy row hh into buffer bf (queue entries widened to 16-byte bounds)
@@ -1454,6 +1456,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                  &mbar[bf]);
         st_row[bf] = hh;
         st_coff[bf] = static_cast<int32_t>((c0 - ca) / 2);
+        st_pend[bf] = 1;
     };
     auto stageable = [&](int32_t hh) { return cache && mrow[hh] > 0 && mrow[hh] <= kStageRec; };
     auto next_row = [&](int32_t hh) {
@@ -1504,13 +1507,20 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
             const bool landed = mbar_wait(&mbar[cur], parity[cur], 1u << 22);
             if (!__syncthreads_and(landed))
             {
-                // report, give the copy a last bounded chance to drain, stop
+                // report, then give every copy still in flight (this row's and the next row's,
+                // issued above) a last bounded wait before the CTA leaves its shared memory
                 if (threadIdx.x == 0)
                     raise_err(&b.state[s], ERR_INTERNAL);
-                mbar_wait(&mbar[cur], parity[cur], 1u << 24);
+                for (int bf = 0; bf < 2; ++bf)
+                    if (st_pend[bf])
+                        mbar_wait(&mbar[bf], parity[bf], 1u << 24);
                 return;
             }
             parity[cur] ^= 1u;
+            // landed for every thread, so no thread reads st_pend in this row; thread 0 alone
+            // writes it (here and in issue), so clearing needs no further barrier
+            if (threadIdx.x == 0)
+                st_pend[cur] = 0;
         }
         // the row's record (from the parallel pass): lastq and the stale-buffer update
         const uint32_t* rrec = staged ? reinterpret_cast<const uint32_t*>(stage + cur * kStageBytes + kStageRecBytes + kStageColBytes)

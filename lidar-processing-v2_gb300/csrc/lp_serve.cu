@@ -1,20 +1,24 @@
 // lp_serve.cu — serving loop with continuous batching (lp_server_*, lidar_gb300_batch.h).
 //
 // Sensors submit scans as they arrive; one worker thread turns the pending queue into batches.
-// Each batch runs in a slot: its own CUDA stream and a device region reserved up front, so
-// several batches are on the GPU at once (upload of one, kernels of another, download of a
-// third) and slots never allocate or free while others run. Admission is by memory: a batch is
-// formed from the oldest pending scans while its planned layout fits the slot's region (the
-// regions together are the server's device-memory budget); scans that arrive while the slots
-// are busy wait and are admitted as soon as a slot frees up. A host callback on the slot's
-// stream wakes the worker when a batch finishes; the worker then copies results into the
-// caller's buffers and records the latency from submission to results in host memory.
-// Every scan's results are the same whatever batch it lands in (kernels keep scans apart).
+// Each batch runs in a slot (its own CUDA stream and context), so several batches are on the GPU
+// at once (upload of one, kernels of another, download of a third). Device memory is one pool of
+// the server's budget, reserved once at creation: nothing allocates or frees device memory while
+// batches run. Admission is by the memory free in the pool right now: a batch is formed from the
+// oldest pending scans, shrunk until its planned layout fits the largest free region, and takes
+// exactly that many bytes; its region returns to the pool (merged with free neighbours) when the
+// batch is harvested. A scan that fits the budget but not the memory free now waits at the head
+// of the queue (first in, first out) until running batches return theirs; only a scan larger
+// than the whole budget is refused (LP_ERR_CAPACITY). A host callback on the slot's stream wakes
+// the worker when a batch finishes; the worker then copies results into the caller's buffers and
+// records the latency from submission to results in host memory. Every scan's results are the
+// same whatever batch it lands in (kernels keep scans apart).
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <thread>
@@ -42,7 +46,8 @@ struct Request
 struct Slot
 {
     lp_context* ctx = nullptr;
-    lp_batch batch;
+    lp_batch batch; // mem / cap: the slot's region of the pool while a batch runs
+    size_t region = 0; // offset of that region in the pool
     std::vector<Request> reqs;
     std::vector<lp_scan_output> outs;
     bool busy = false;
@@ -66,6 +71,11 @@ struct lp_server
     bool stop = false;
     lp_server_stats stats{};
     std::string error;
+    // the device-memory pool and its free regions (offset -> bytes), 256-byte granules
+    char* pool = nullptr;
+    size_t pool_bytes = 0;
+    std::map<size_t, size_t> free_regions;
+    bool blocked = false; // the queue's head waits for memory: retry after a harvest
 };
 
 namespace
@@ -78,8 +88,60 @@ void CUDART_CB on_batch_done(void* p)
     s->server->cv.notify_all();
 }
 
-// Builds the batch of the given requests into the slot; returns false when it does not fit.
-lp_status plan_fits(Slot& slot, const lp_pipeline_config& cfg, const std::vector<Request>& reqs, size_t cap, bool& fits)
+constexpr size_t kGranule = 256;
+
+size_t round_up(size_t v)
+{
+    return (v + kGranule - 1) & ~(kGranule - 1);
+}
+
+// Largest free region of the pool (0 when none).
+size_t largest_free(const lp_server* sv)
+{
+    size_t best = 0;
+    for (const auto& r : sv->free_regions)
+        best = std::max(best, r.second);
+    return best;
+}
+
+// First free region of at least `bytes`; returns its offset (SIZE_MAX when none).
+size_t pool_take(lp_server* sv, size_t bytes)
+{
+    for (auto it = sv->free_regions.begin(); it != sv->free_regions.end(); ++it)
+        if (it->second >= bytes)
+        {
+            const size_t off = it->first, len = it->second;
+            sv->free_regions.erase(it);
+            if (len > bytes)
+                sv->free_regions.emplace(off + bytes, len - bytes);
+            return off;
+        }
+    return SIZE_MAX;
+}
+
+// Returns a region to the pool, merged with adjacent free regions.
+void pool_give(lp_server* sv, size_t off, size_t bytes)
+{
+    auto next = sv->free_regions.lower_bound(off);
+    if (next != sv->free_regions.end() && off + bytes == next->first)
+    {
+        bytes += next->second;
+        next = sv->free_regions.erase(next);
+    }
+    if (next != sv->free_regions.begin())
+    {
+        auto prev = std::prev(next);
+        if (prev->first + prev->second == off)
+        {
+            prev->second += bytes;
+            return;
+        }
+    }
+    sv->free_regions.emplace(off, bytes);
+}
+
+// Plans the batch of the given requests in the slot; `bytes` receives its device footprint.
+lp_status plan_bytes(Slot& slot, const lp_pipeline_config& cfg, const std::vector<Request>& reqs, size_t& bytes)
 {
     std::vector<lp_scan_input> ins;
     ins.reserve(reqs.size());
@@ -91,7 +153,7 @@ lp_status plan_fits(Slot& slot, const lp_pipeline_config& cfg, const std::vector
     st = lprt::plan(slot.ctx, slot.batch);
     if (st != LP_OK)
         return st;
-    fits = lprt::measure(slot.batch) <= cap;
+    bytes = round_up(lprt::measure(slot.batch));
     return LP_OK;
 }
 
@@ -128,14 +190,21 @@ void harvest(lp_server* sv, Slot& slot)
     }
     slot.reqs.clear();
     slot.outs.clear();
+    std::lock_guard<std::mutex> lk(sv->m);
+    pool_give(sv, slot.region, slot.batch.cap);
+    slot.batch.mem = nullptr;
+    slot.batch.cap = 0;
     slot.busy = false;
     slot.done.store(false);
+    sv->blocked = false; // memory came back: the queue's head may fit now
 }
 
-// Takes the oldest pending scans that fit into the slot and starts them. Called with the lock held.
+// Takes the oldest pending scans whose batch fits the largest free region of the pool and starts
+// them in the slot. The head scan waits (stays first in the queue) when even alone it does not
+// fit the memory free now; it is refused only when it exceeds the whole pool. Called with the
+// lock held.
 void admit(lp_server* sv, Slot& slot, std::unique_lock<std::mutex>& lk)
 {
-    const size_t cap = slot.batch.cap;
     std::vector<Request> take;
     const size_t maxb = std::max<uint32_t>(1u, sv->scfg.max_batch_scans);
     while (!sv->pending.empty() && take.size() < maxb)
@@ -143,28 +212,51 @@ void admit(lp_server* sv, Slot& slot, std::unique_lock<std::mutex>& lk)
         take.push_back(sv->pending.front());
         sv->pending.pop_front();
     }
+    const size_t avail = largest_free(sv);
     lk.unlock();
-    // shrink the batch until its planned layout fits the slot's region
-    bool fits = false;
+    // shrink the batch until its planned layout fits the largest free region
+    size_t bytes = 0;
     lp_status st = LP_OK;
     std::vector<Request> back;
     while (!take.empty())
     {
-        st = plan_fits(slot, sv->cfg, take, cap, fits);
-        if (st != LP_OK || fits || take.size() == 1)
+        st = plan_bytes(slot, sv->cfg, take, bytes);
+        if (st != LP_OK || bytes <= avail || take.size() == 1)
             break;
         back.insert(back.begin(), take.back());
         take.pop_back();
     }
-    if (!take.empty() && (st != LP_OK || !fits))
+    bool wait = false;
+    if (!take.empty() && st != LP_OK)
     {
-        // a single scan larger than a slot (or malformed): fail it, keep the rest pending
-        finish_request(sv, take.front(), st != LP_OK ? st : LP_ERR_CAPACITY, now_s(), 1);
+        // malformed: fail it, keep the rest pending
+        finish_request(sv, take.front(), st, now_s(), 1);
         back.insert(back.begin(), take.begin() + 1, take.end());
+        take.clear();
+    }
+    else if (!take.empty() && bytes > avail)
+    {
+        if (bytes > sv->pool_bytes)
+        {
+            // larger than the whole budget: it can never run
+            finish_request(sv, take.front(), LP_ERR_CAPACITY, now_s(), 1);
+            back.insert(back.begin(), take.begin() + 1, take.end());
+        }
+        else
+        {
+            back.insert(back.begin(), take.begin(), take.end()); // wait for memory, first in line
+            wait = true;
+        }
         take.clear();
     }
     if (!take.empty())
     {
+        lk.lock();
+        const size_t off = pool_take(sv, bytes);
+        lk.unlock();
+        slot.region = off;
+        slot.batch.mem = sv->pool + off;
+        slot.batch.cap = bytes;
         slot.reqs = take;
         slot.outs.clear();
         for (const Request& r : take)
@@ -184,6 +276,11 @@ void admit(lp_server* sv, Slot& slot, std::unique_lock<std::mutex>& lk)
             for (const Request& r : take)
                 finish_request(sv, r, st, slot.t_start, static_cast<uint32_t>(take.size()));
             slot.reqs.clear();
+            lk.lock();
+            pool_give(sv, slot.region, slot.batch.cap);
+            lk.unlock();
+            slot.batch.mem = nullptr;
+            slot.batch.cap = 0;
         }
         else
         {
@@ -191,6 +288,8 @@ void admit(lp_server* sv, Slot& slot, std::unique_lock<std::mutex>& lk)
         }
     }
     lk.lock();
+    if (wait)
+        sv->blocked = true;
     if (!take.empty() && slot.busy)
     {
         sv->stats.batches += 1;
@@ -218,7 +317,7 @@ void worker_loop(lp_server* sv)
         bool idle_slot = false;
         for (auto& s : sv->slots)
             idle_slot |= !s->busy;
-        if (!any_done && (sv->pending.empty() || !idle_slot))
+        if (!any_done && (sv->pending.empty() || !idle_slot || sv->blocked))
         {
             sv->cv.wait_for(lk, std::chrono::microseconds(500));
             continue;
@@ -231,7 +330,7 @@ void worker_loop(lp_server* sv)
                 lk.lock();
             }
         for (auto& s : sv->slots)
-            if (!s->busy && !sv->pending.empty())
+            if (!s->busy && !sv->pending.empty() && !sv->blocked)
                 admit(sv, *s, lk);
     }
 }
@@ -255,31 +354,32 @@ lp_status lp_server_create(int32_t device, const lp_pipeline_config* cfg, const 
     sv->device = device;
     sv->cfg = *cfg;
     sv->scfg = *scfg;
-    const size_t per_slot = static_cast<size_t>(scfg->memory_budget_bytes / scfg->slots);
+    // one pool of the whole budget, reserved once; batches take regions of it as they are admitted
+    const size_t pool = static_cast<size_t>(scfg->memory_budget_bytes) & ~(kGranule - 1);
+    if (pool == 0)
+        return LP_ERR_BAD_ARG;
+    if (cudaSetDevice(device) != cudaSuccess || cudaMalloc(reinterpret_cast<void**>(&sv->pool), pool) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return LP_ERR_CAPACITY;
+    }
+    sv->pool_bytes = pool;
+    sv->free_regions.emplace(0, pool);
     for (uint32_t i = 0; i < scfg->slots; ++i)
     {
         auto s = std::make_unique<Slot>();
         s->server = sv.get();
         lp_status st = lp_context_create(device, &s->ctx);
         if (st != LP_OK)
-            return st;
-        // the slot's region is reserved once; batches are admitted only when they fit it
-        if (cudaMalloc(reinterpret_cast<void**>(&s->batch.mem), per_slot) != cudaSuccess)
         {
-            cudaGetLastError();
-            lp_context_destroy(s->ctx);
             for (auto& o : sv->slots)
-            {
-                cudaFree(o->batch.mem);
-                o->batch.mem = nullptr;
                 lp_context_destroy(o->ctx);
-            }
-            return LP_ERR_CAPACITY;
+            cudaFree(sv->pool);
+            return st;
         }
-        s->batch.cap = per_slot;
         sv->slots.push_back(std::move(s));
     }
-    sv->stats.device_bytes = static_cast<uint64_t>(per_slot) * scfg->slots;
+    sv->stats.device_bytes = static_cast<uint64_t>(pool);
     lp_server* raw = sv.release();
     raw->worker = std::thread(worker_loop, raw);
     *out = raw;
@@ -343,10 +443,11 @@ void lp_server_destroy(lp_server* sv)
         cudaStreamSynchronize(s->ctx->stream);
         if (s->batch.graph)
             cudaGraphExecDestroy(s->batch.graph);
-        cudaFree(s->batch.mem);
-        s->batch.mem = nullptr;
+        s->batch.mem = nullptr; // a region of the pool, not its own allocation
+        s->batch.cap = 0;
         lp_context_destroy(s->ctx);
     }
+    cudaFree(sv->pool);
     delete sv;
 }
 

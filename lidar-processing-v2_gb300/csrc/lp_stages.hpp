@@ -11,6 +11,8 @@ namespace lpg
 {
 void scan_exclusive(cudaStream_t st, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* sums, uint32_t* err,
                     uint64_t& launches);
+void launch_debug_wait_timeout(cudaStream_t st, int kind, uint32_t limit, unsigned long long* state, uint32_t* err,
+                               uint64_t& launches);
 
 // One timed launch (profiling mode only).
 struct LaunchRecord

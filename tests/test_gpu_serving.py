@@ -1,5 +1,7 @@
 """Serving loop (lp_server_*): scans submitted while others are on the GPU are batched together,
-and every scan's results are identical to the same scan processed alone."""
+every scan's results equal the oracle's and the same scan processed alone, and admission is by the
+memory free in the server's pool: a scan that does not fit the memory free now waits and then
+completes exactly; only a scan larger than the whole budget is refused."""
 import time
 
 import numpy as np
@@ -40,25 +42,72 @@ def test_served_results_equal_alone(ctx):
         assert d.status == lp.LP_OK and d.latency_ms > 0
         alone = lp.process_batch(ctx, [x], pipe, [cfg], [ring])[0]
         compare_scan(r, alone, f"scan {i} (batch of {d.batch_scans})")
+        compare_scan(r, T.o_process(x, ring, cfg, pipe), f"scan {i} against the oracle")
 
 
-def test_served_small_budget_splits_batches(ctx):
-    """A budget that holds only one scan per slot forces single-scan batches; results unchanged."""
-    data = [T.synth_scan(5, i) for i in range(20, 26)]
-    pipe = lp.PipelineConfig.default()
-    server = lp.Server(0, pipe, memory_budget_bytes=2 * (600 << 20), max_batch_scans=8, slots=2)
+def scan_bytes(ctx, x, ring, cfg, pipe):
+    b = lp.PreparedBatch(ctx, [x], pipe, [cfg], [ring])
     try:
+        return b.device_bytes
+    finally:
+        b.close()
+
+
+def test_large_scan_waits_for_memory_then_completes(ctx):
+    """A pool that holds the largest scan but not that scan beside a running batch: the large scan,
+    submitted right behind a batch of small ones, waits for their memory instead of being refused,
+    then completes; every result equals the oracle."""
+    pipe = lp.PipelineConfig.default()
+    small = [T.synth_scan(5, i) for i in range(30, 34)]
+    sizes = [(len(d[0]), k) for k, d in enumerate(T.synth_scan(5, i) for i in range(34, 48))]
+    big = T.synth_scan(5, 34 + max(sizes)[1])
+    need_big = scan_bytes(ctx, *big, pipe)
+    need_small = scan_bytes(ctx, *small[0], pipe)
+    budget = need_big + need_small // 2  # the big scan alone fits; beside any small batch it does not
+    server = lp.Server(0, pipe, memory_budget_bytes=budget, max_batch_scans=4, slots=2)
+    try:
+        data = small + [big]
         for i, (x, ring, cfg) in enumerate(data):
             server.submit(x, ring, cfg, i)
         got = drain(server, len(data))
         stats = server.stats()
     finally:
         server.close()
-    assert len(got) == len(data)
+    assert len(got) == len(data) and stats["failed"] == 0, stats
+    assert stats["batches"] >= 2, stats
+    d_big, r_big = got[len(data) - 1]
+    assert d_big.status == lp.LP_OK
+    # it could only start once a batch ahead of it had finished and returned its memory
+    first_done = min(got[i][0].latency_ms for i in range(len(small)))
+    assert d_big.queue_ms >= 0.5 * first_done, (d_big.queue_ms, first_done)
     for i, (x, ring, cfg) in enumerate(data):
         d, r = got[i]
-        if d.status == lp.LP_OK:
-            compare_scan(r, lp.process_batch(ctx, [x], pipe, [cfg], [ring])[0], f"scan {i}")
+        assert d.status == lp.LP_OK
+        compare_scan(r, T.o_process(x, ring, cfg, pipe), f"scan {i}")
+
+
+def test_scan_larger_than_budget_is_refused(ctx):
+    """Only a scan that exceeds the whole budget is refused; the scans around it still run."""
+    pipe = lp.PipelineConfig.default()
+    data = [T.synth_scan(5, i) for i in range(20, 24)]
+    need = max(scan_bytes(ctx, *d, pipe) for d in data)
+    big = T.synth_scan(5, 46)  # 322,827 points
+    server = lp.Server(0, pipe, memory_budget_bytes=need + (need >> 3), max_batch_scans=8, slots=2)
+    try:
+        order = data[:2] + [big] + data[2:]
+        for i, (x, ring, cfg) in enumerate(order):
+            server.submit(x, ring, cfg, i)
+        got = drain(server, len(order))
+        stats = server.stats()
+    finally:
+        server.close()
+    assert len(got) == len(order) and stats["completed"] == len(order)
+    too_big = scan_bytes(ctx, *big, pipe) > need + (need >> 3)
+    assert too_big
+    for i, (x, ring, cfg) in enumerate(order):
+        d, r = got[i]
+        if i == 2 and too_big:
+            assert d.status == lp.LP_ERR_CAPACITY
         else:
-            assert d.status == lp.LP_ERR_CAPACITY  # a scan larger than a slot is refused, not run
-    assert stats["completed"] == len(data)
+            assert d.status == lp.LP_OK
+            compare_scan(r, T.o_process(x, ring, cfg, pipe), f"scan {i}")
