@@ -349,6 +349,7 @@ size_t carve(lp_batch& B, char* base)
         put(b.hs_pts, static_cast<size_t>(N) + 8);
         put(b.hs_pairs, static_cast<size_t>(4) * N + 16ull * b.ncl + 16);
         put(b.queue, 8);
+        put(b.tie_list, b.ncl + 1);
     }
     return c.off + 4096;
 }

@@ -181,7 +181,8 @@ struct BatchDev
     int32_t* hs_stack;    // monotone-chain stack, at 2 * cl_start + 2 * cluster
     double2* hs_pts;      // hull vertices as FP64, at cl_start
     int2* hs_pairs;       // antipodal pairs, at 4 * cl_start + 16 * cluster
-    uint32_t* queue;      // [0] clusters in the batch, [1] hull work-queue head
+    uint32_t* queue;      // [0] clusters in the batch, [1] hull work-queue head, [4] tie clusters
+    uint32_t* tie_list;   // clusters whose hull has a vertex with an identical point (reference tie order)
 
     // ---- DROR (reference kd-tree replay, lp_kdtree.cu) ------------------------------------------
     float4* kt;                // per input point: tree node record by position (x, y, z, subtree size bits)

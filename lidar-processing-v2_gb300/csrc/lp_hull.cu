@@ -21,6 +21,7 @@
 #include <cfloat>
 #include <mutex>
 
+#include "lp_introsort.cuh"
 #include "lp_batch.cuh"
 #include "lp_common.cuh"
 #include "lp_math.cuh"
@@ -1481,6 +1482,20 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
     }
     __syncthreads();
     const int h = sm.nhull;
+    {
+        // a hull vertex with an identical candidate next to it: the reference's pick among them
+        // follows std::sort's order (k_hull_ties replays it)
+        bool tie = false;
+        for (int j = threadIdx.x; j < h; j += blockDim.x)
+        {
+            const int q = H[j];
+            const HPt<float> c = C[q];
+            tie |= (q > 0 && C[q - 1].x == c.x && C[q - 1].y == c.y) ||
+                   (q + 1 < static_cast<int>(m) && C[q + 1].x == c.x && C[q + 1].y == c.y);
+        }
+        if (__syncthreads_or(tie) && threadIdx.x == 0)
+            b.tie_list[atomicAdd(&b.queue[5], 1u)] = g;
+    }
 
     // 5 + 6. Local index of each hull vertex (the number of members before it in input order) and
     //        the boxes. They only read the hull: warps 0 and 1 compute the calipers and PCA boxes
@@ -1907,6 +1922,18 @@ __device__ void hull_one_warp(const BatchDev& b, WarpSmem& ws, const float2* dir
         h = monotone_chain(C, static_cast<int>(m), H);
     h = __shfl_sync(0xffffffffu, h, 0);
     __syncwarp();
+    {
+        bool tie = false;
+        for (int j = static_cast<int>(lane); j < h; j += 32)
+        {
+            const int q = H[j];
+            const HPt<float> c = C[q];
+            tie |= (q > 0 && C[q - 1].x == c.x && C[q - 1].y == c.y) ||
+                   (q + 1 < static_cast<int>(m) && C[q + 1].x == c.x && C[q + 1].y == c.y);
+        }
+        if (__any_sync(0xffffffffu, tie) && lane == 0)
+            b.tie_list[atomicAdd(&b.queue[5], 1u)] = g;
+    }
     for (int j = 0; j < h; ++j)
     {
         const uint32_t key = C[H[j]].key;
@@ -2013,6 +2040,149 @@ __global__ void __launch_bounds__(kHullThreads) k_hull(BatchDev b, int compute_o
 }
 
 // Dense hull output: hull_cnt holds the exclusive scan (hull offsets over the batch).
+// ---------------------------------------------------------------------------------------------
+// The reference's order among identical points (Polygonizer::convexHull, polygonizer.cpp:51-59):
+// std::sort orders the point indices by x, then (|dx| < DBL_EPSILON) y, and leaves points that
+// compare equal in whatever order its introsort produced. The monotone chain keeps, of a run of
+// identical points, the first in that order at the leftmost vertex and on the upper chain, and
+// the last on the lower chain up to the rightmost vertex. The hull kernels order ties by input
+// index; where a hull vertex has an identical point, the whole cluster's std::sort is replayed
+// (lp_introsort.cuh) and each vertex re-picked from its run.
+// ---------------------------------------------------------------------------------------------
+template <typename T>
+struct HRec
+{
+    T x, y;
+    uint32_t idx;
+};
+
+template <typename T>
+struct HullLess // the reference's sort comparator on its binary64 PointXY
+{
+    __device__ __forceinline__ bool operator()(const HRec<T>& a, const HRec<T>& b) const
+    {
+        const double ax = static_cast<double>(a.x), bx = static_cast<double>(b.x);
+        return ax < bx || (fabs(ax - bx) < DBL_EPSILON && static_cast<double>(a.y) < static_cast<double>(b.y));
+    }
+};
+
+// The same comparator on binary32 coordinates widened to binary64, decided in binary32 where that
+// is exact: equal finite x compare by y (|dx| = 0; infinite x give inf - inf = NaN, not below
+// DBL_EPSILON); distinct x of which one is at least 2^-20 in magnitude differ by at least 2^-44, so
+// only x both below 2^-20 need the binary64 difference.
+template <>
+struct HullLess<float>
+{
+    __device__ __forceinline__ bool operator()(const HRec<float>& a, const HRec<float>& b) const
+    {
+        if (a.x < b.x)
+            return true;
+        if (a.x == b.x)
+            return fabsf(a.x) < INFINITY && a.y < b.y;
+        if (fabsf(a.x) < 0x1p-20f && fabsf(b.x) < 0x1p-20f)
+            return fabs(static_cast<double>(a.x) - static_cast<double>(b.x)) < DBL_EPSILON && a.y < b.y;
+        return false;
+    }
+};
+
+template <typename T>
+struct IdxLess
+{
+    __device__ __forceinline__ bool operator()(const HRec<T>& a, const HRec<T>& b) const { return a.idx < b.idx; }
+};
+
+// rec: the n points in input order (idx = position). hull (h local indices, in input-order ties)
+// is rewritten with the reference's picks; vxy(j): the coordinates of hull vertex j (read before
+// hull[j] is rewritten); ge/le: n entries each.
+template <typename T, class VertexXY>
+__device__ void hull_repair_ties(HRec<T>* rec, uint32_t n, int32_t* hull, int h, VertexXY vxy, uint32_t* ge,
+                                 uint32_t* le, isort::SortShared& ss)
+{
+    __shared__ int s_jr;
+    isort::cta_sort(rec, n, HullLess<T>{}, ge, le, ss);
+    if (threadIdx.x == 0)
+    {
+        // the rightmost vertex ends the lower chain: the lexicographic maximum, its last occurrence
+        // (a cloud of identical points has the hull [first, last] of one coordinate)
+        int jr = 0;
+        double2 best = vxy(0);
+        for (int j = 1; j < h; ++j)
+        {
+            const double2 v = vxy(j);
+            if (v.x > best.x || (v.x == best.x && v.y >= best.y))
+            {
+                jr = j;
+                best = v;
+            }
+        }
+        s_jr = jr;
+    }
+    __syncthreads();
+    const int jr = s_jr;
+    const HullLess<T> less{};
+    for (int j = threadIdx.x; j < h; j += blockDim.x)
+    {
+        const double2 v = vxy(j);
+        const HRec<T> t{static_cast<T>(v.x), static_cast<T>(v.y), 0u};
+        // equal range of the vertex's point in the sorted records
+        uint32_t lo = 0, hi = n;
+        while (lo < hi)
+        {
+            const uint32_t mid = (lo + hi) / 2;
+            if (less(rec[mid], t))
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        uint32_t lo2 = lo, hi2 = n;
+        while (lo2 < hi2)
+        {
+            const uint32_t mid = (lo2 + hi2) / 2;
+            if (!less(t, rec[mid]))
+                lo2 = mid + 1;
+            else
+                hi2 = mid;
+        }
+        if (lo2 > lo)
+            hull[j] = static_cast<int32_t>(rec[(j == 0 || j > jr) ? lo : lo2 - 1].idx);
+    }
+    __syncthreads();
+}
+
+// Clusters listed by k_hull (a hull vertex with an identical candidate): the members' records in
+// input order (sorted by member key), then the repair. Scratch per cluster: the candidate area
+// (records), the chain stack area (ge / le), the FP64 hull area (vertex coordinates).
+__global__ void __launch_bounds__(kHullThreads) k_hull_ties(BatchDev b)
+{
+    __shared__ isort::SortShared ss;
+    const uint32_t ntie = b.queue[5]; // the tie count (queue[4] is the small-cluster head)
+    for (uint32_t t = blockIdx.x; t < ntie; t += gridDim.x)
+    {
+        const uint32_t g = b.tie_list[t];
+        const uint32_t start = b.cl_start[g], n = b.cl_cnt[g];
+        const int h = static_cast<int>(b.hull_cnt[g + 1] - b.hull_cnt[g]); // scanned: offsets
+        HRec<float>* rec = reinterpret_cast<HRec<float>*>(reinterpret_cast<HPt<float>*>(b.hs_cand) + 2ull * start);
+        uint32_t* ge = reinterpret_cast<uint32_t*>(b.hs_stack + 2ull * start + 2ull * g);
+        uint32_t* le = ge + n;
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+        {
+            const float2 p = b.mxy[start + k];
+            rec[k] = HRec<float>{p.x, p.y, b.members[start + k]};
+        }
+        __syncthreads();
+        isort::cta_sort(rec, n, IdxLess<float>{}, ge, le, ss);
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+            rec[k].idx = k; // local index: position in input order
+        __syncthreads();
+        int32_t* hull = b.hull_tmp + start;
+        double2* hv = b.hs_pts + start; // the vertices' coordinates, kept before the records re-sort
+        for (int j = threadIdx.x; j < h; j += blockDim.x)
+            hv[j] = make_double2(static_cast<double>(rec[hull[j]].x), static_cast<double>(rec[hull[j]].y));
+        __syncthreads();
+        hull_repair_ties(rec, n, hull, h, [=](int j) { return hv[j]; }, ge, le, ss);
+    }
+}
+
 __global__ void k_hull_compact(BatchDev b, const uint32_t* work)
 {
     const uint32_t total = b.queue[2] + b.queue[3];
@@ -2040,13 +2210,33 @@ __global__ void __launch_bounds__(kHullThreads) k_hull_single(const double2* pts
     block_sort_global(scratch, n);
     __syncthreads();
     __shared__ int hn;
+    __shared__ isort::SortShared ss;
     if (threadIdx.x == 0)
         hn = monotone_chain(scratch, static_cast<int>(n), stack);
     __syncthreads();
+    bool tie = false;
     for (int j = threadIdx.x; j < hn; j += blockDim.x)
-        out[j] = static_cast<int32_t>(scratch[stack[j]].key);
+    {
+        const int q = stack[j];
+        const HPt<double> c = scratch[q];
+        out[j] = static_cast<int32_t>(c.key);
+        tie |= (q > 0 && scratch[q - 1].x == c.x && scratch[q - 1].y == c.y) ||
+               (q + 1 < static_cast<int>(n) && scratch[q + 1].x == c.x && scratch[q + 1].y == c.y);
+    }
     if (threadIdx.x == 0)
         *n_out = static_cast<uint32_t>(hn);
+    if (__syncthreads_or(tie))
+    {
+        // a vertex with an identical point: the reference's std::sort order decides which one. The
+        // sort buffer takes the records (24 bytes each, as its entries) and the chain stack (2n + 8
+        // ints, free now) the partition lists; the vertices' coordinates are read from the input.
+        auto* rec = reinterpret_cast<HRec<double>*>(scratch);
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+            rec[i] = HRec<double>{pts[i].x, pts[i].y, i};
+        __syncthreads();
+        uint32_t* ge = reinterpret_cast<uint32_t*>(stack);
+        hull_repair_ties(rec, n, out, hn, [=](int j) { return pts[out[j]]; }, ge, ge + n, ss);
+    }
 }
 
 __global__ void k_boxes_single(const double2* P, uint32_t n, int2* pairs, int cap, int kind, lp_bounding_box* out,
@@ -2173,6 +2363,7 @@ void launch_polygons(Launcher& L, const BatchDev& b, const BatchHost& hb, int co
     LP_LAUNCH_SMEM(L, k_hull, static_cast<uint32_t>(sms * 2), kHullThreads, kHullDynSmem, b, compute_obb,
                    static_cast<const uint32_t*>(work));
     L.scan(b.hull_cnt, b.hull_cnt, b.ncl + 1);
+    LP_LAUNCH(L, k_hull_ties, static_cast<uint32_t>(sms), kHullThreads, b);
     LP_LAUNCH(L, k_hull_compact, static_cast<uint32_t>(sms * 8), 128, b, static_cast<const uint32_t*>(work));
 }
 

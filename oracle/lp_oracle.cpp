@@ -128,8 +128,9 @@ void lpo_set_libm_mode(int mode)
 {
     g_libm_mode = mode;
 }
-// Order of hull points with the same (x, y): 0 by index (the GPU's rule), 1 as the reference's
-// std::sort leaves them (libstdc++'s introsort restated in introsort.h, with its comparator).
+// Order of hull points with the same (x, y): 1 as the reference's std::sort leaves them (libstdc++'s
+// introsort restated in introsort.h, with its comparator; the GPU's order), 0 by input index (kept to
+// show where the order matters).
 void lpo_set_hull_ties(int mode)
 {
     g_hull_ties = mode;

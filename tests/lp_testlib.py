@@ -23,7 +23,7 @@ REF_PATH = os.path.join(REPO, "oracle", "_ref", "libref.so")
 GOLDEN = os.path.join(REPO, "tests", "golden")
 
 LIBM_CR, LIBM_HOST = 0, 1
-TIES_INDEX, TIES_LIBSTDCXX = 0, 1  # order of hull points with equal (x, y)
+TIES_INDEX, TIES_LIBSTDCXX = 0, 1  # order of hull points with equal (x, y): input order / the reference's std::sort
 DROR_EXACT, DROR_KDTREE = 0, 1  # exact radius counting / the reference's kd-tree search (its stack kept)
 
 _oracle = None
@@ -149,7 +149,7 @@ def o_cluster(pts, cfg, libm=LIBM_CR):
     return out
 
 
-def o_hull(xy, ties=TIES_INDEX):
+def o_hull(xy, ties=TIES_LIBSTDCXX):
     a = np.ascontiguousarray(xy, np.float64)
     out = np.zeros(len(a) + 1, np.int32)
     n = ctypes.c_uint32()
@@ -228,7 +228,7 @@ def o_antipodal(hp):
     return out[: n.value].copy()
 
 
-def o_process(xyzi, ring, seg_cfg, pipeline, libm=LIBM_CR, dror_mode=DROR_KDTREE, ties=TIES_INDEX):
+def o_process(xyzi, ring, seg_cfg, pipeline, libm=LIBM_CR, dror_mode=DROR_KDTREE, ties=TIES_LIBSTDCXX):
     oracle().lpo_set_libm_mode(libm)
     oracle().lpo_set_hull_ties(ties)
     b = lp.ResultBuffers(len(xyzi))

@@ -230,6 +230,53 @@ def test_polygons(ctx):
         assert T.pca_boxes_equal(pb, T.o_pca(hp)[0])
 
 
+def test_hull_ties_follow_reference_sort(ctx):
+    """Clouds full of identical points (coordinates rounded to a coarse grid): which of the identical
+    points the hull reports follows the reference's std::sort order (libstdc++ introsort replayed on
+    the device), index for index, up to 40,000 points (ranges partitioned by the whole CTA)."""
+    rng = np.random.default_rng(29)
+    poly = lp.Polygonizer(ctx)
+    differ = 0
+    for t, n in enumerate([5, 17, 40, 300, 2047, 2049, 5000, 40000]):
+        pts = np.round(rng.normal(size=(n, 2)) * 3.0, 0 if t % 2 else 1).astype(np.float32).astype(np.float64)
+        got = poly.convexHull(pts)
+        want = T.o_hull(pts, T.TIES_LIBSTDCXX)
+        assert np.array_equal(got, want), n
+        differ += int(not np.array_equal(want, T.o_hull(pts, T.TIES_INDEX)))
+    assert differ > 0  # the input-order rule would differ on some of these
+    # degenerate clouds: every point identical (the hull is [first, last] of one coordinate), two
+    # distinct points repeated, a vertical line of repeated points
+    for n in [3, 4, 17, 50, 3000]:
+        one = np.repeat(np.array([[1.25, -0.5]]), n, 0)
+        two = np.array([[0.5, 0.5], [2.0, -1.0]])[rng.integers(0, 2, n)]
+        two[:2] = [[0.5, 0.5], [2.0, -1.0]]
+        line = np.stack([np.full(n, 3.0), np.round(rng.normal(size=n) * 2.0)], 1)
+        for pts in (one, two, line):
+            assert np.array_equal(poly.convexHull(pts), T.o_hull(pts, T.TIES_LIBSTDCXX)), n
+
+
+def test_pipeline_hull_ties(ctx):
+    """A scan with copies of half its obstacle points at the same (x, y), 0.5 m higher and one ring
+    up (so each copy wins its own range-image pixel and joins the cluster): clusters hold many
+    identical (x, y), and the hulls follow the reference's std::sort order among them (more than
+    a hundred hull indices differ under an input-order rule)."""
+    x, ring, cfg = T.synth_scan(3, 3)
+    pipe = lp.PipelineConfig.default()
+    base = T.o_process(x, ring, cfg, pipe)
+    obs = np.nonzero(base.seg_labels == lp.OBSTACLE)[0]
+    dup = np.sort(np.random.default_rng(4).choice(obs, size=len(obs) // 2, replace=False))
+    cp = x[dup].copy()
+    cp[:, 2] += 0.5
+    rc = np.maximum(ring[dup].astype(np.int32) - 1, 0).astype(np.uint16)
+    x2 = np.ascontiguousarray(np.concatenate([x, cp]))
+    r2 = np.ascontiguousarray(np.concatenate([ring, rc]))
+    got = lp.process_batch(ctx, [x2], pipe, [cfg], [r2])[0]
+    want = T.o_process(x2, r2, cfg, pipe, ties=T.TIES_LIBSTDCXX)
+    compare_scan(got, want, "copies above the obstacles")
+    other = T.o_process(x2, r2, cfg, pipe, ties=T.TIES_INDEX)
+    assert int((want.hull_indices != other.hull_indices).sum()) > 50
+
+
 def test_pca_thin_hulls(ctx):
     """The two near-collinear hulls of the 64-scan workload (tests/golden/thin_hulls.npz, 6-8 cm
     long and under a micrometre wide) through lp_bounding_box_pca: the reference's box."""
