@@ -2150,20 +2150,29 @@ __device__ void hull_repair_ties(HRec<T>* rec, uint32_t n, int32_t* hull, int h,
 }
 
 // Clusters listed by k_hull (a hull vertex with an identical candidate): the members' records in
-// input order (sorted by member key), then the repair. Scratch per cluster: the candidate area
-// (records), the chain stack area (ge / le), the FP64 hull area (vertex coordinates).
+// input order (sorted by member key), then the repair. The sorts are chains of dependent accesses,
+// so clusters of at most kTieSmemRecs members are sorted in shared memory (records, then the ge / le
+// lists); larger ones use the cluster's scratch: the candidate area (records), the chain stack
+// area (ge / le). The vertices' coordinates go to the FP64 hull area.
+constexpr uint32_t kTieSmemRecs = 4096;
+constexpr size_t kTieDynSmem = static_cast<size_t>(kTieSmemRecs) * (sizeof(HRec<float>) + 8);
+
 __global__ void __launch_bounds__(kHullThreads) k_hull_ties(BatchDev b)
 {
     __shared__ isort::SortShared ss;
+    extern __shared__ __align__(16) unsigned char tsm[];
     const uint32_t ntie = b.queue[5]; // the tie count (queue[4] is the small-cluster head)
     for (uint32_t t = blockIdx.x; t < ntie; t += gridDim.x)
     {
         const uint32_t g = b.tie_list[t];
         const uint32_t start = b.cl_start[g], n = b.cl_cnt[g];
         const int h = static_cast<int>(b.hull_cnt[g + 1] - b.hull_cnt[g]); // scanned: offsets
-        HRec<float>* rec = reinterpret_cast<HRec<float>*>(reinterpret_cast<HPt<float>*>(b.hs_cand) + 2ull * start);
-        uint32_t* ge = reinterpret_cast<uint32_t*>(b.hs_stack + 2ull * start + 2ull * g);
-        uint32_t* le = ge + n;
+        const bool local = n <= kTieSmemRecs;
+        HRec<float>* rec = local ? reinterpret_cast<HRec<float>*>(tsm)
+                                 : reinterpret_cast<HRec<float>*>(reinterpret_cast<HPt<float>*>(b.hs_cand) + 2ull * start);
+        uint32_t* ge = local ? reinterpret_cast<uint32_t*>(tsm + kTieSmemRecs * sizeof(HRec<float>))
+                             : reinterpret_cast<uint32_t*>(b.hs_stack + 2ull * start + 2ull * g);
+        uint32_t* le = ge + (local ? kTieSmemRecs : n);
         for (uint32_t k = threadIdx.x; k < n; k += blockDim.x)
         {
             const float2 p = b.mxy[start + k];
@@ -2363,7 +2372,7 @@ void launch_polygons(Launcher& L, const BatchDev& b, const BatchHost& hb, int co
     LP_LAUNCH_SMEM(L, k_hull, static_cast<uint32_t>(sms * 2), kHullThreads, kHullDynSmem, b, compute_obb,
                    static_cast<const uint32_t*>(work));
     L.scan(b.hull_cnt, b.hull_cnt, b.ncl + 1);
-    LP_LAUNCH(L, k_hull_ties, static_cast<uint32_t>(sms), kHullThreads, b);
+    LP_LAUNCH_SMEM(L, k_hull_ties, static_cast<uint32_t>(sms), kHullThreads, kTieDynSmem, b);
     LP_LAUNCH(L, k_hull_compact, static_cast<uint32_t>(sms * 8), 128, b, static_cast<const uint32_t*>(work));
 }
 
@@ -2371,6 +2380,7 @@ void init_kernel_attributes()
 {
     init_kdtree_attributes();
     cudaFuncSetAttribute(k_hull, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kHullDynSmem));
+    cudaFuncSetAttribute(k_hull_ties, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTieDynSmem));
 }
 
 int sm_count()

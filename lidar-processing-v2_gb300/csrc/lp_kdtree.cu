@@ -35,10 +35,10 @@
 //   4. Candidates (short points step 3 did not decide) in two steps. k_kt_spec, one thread per
 //      candidate: the walk through the pieces pushed since the previous candidate, as if nothing
 //      lay below them, which is exact whenever the previous candidate emptied the stack (running
-//      out of entries is NOISE). k_kt_chain, one warp per scan: the candidates in order with R,
+//      out of entries is NOISE). k_kt_chain, one CTA per scan: the candidates in order with R,
 //      what earlier walks left below those pieces; a stopped walk adds its remainder to R, one
-//      that ran out continues into R (the lanes searching 32 entries at a time, an ordered prefix
-//      of their counts finding the stop). While R is empty, runs of candidates whose walks ran
+//      that ran out continues into R (the threads searching 256 entries at a time, an ordered
+//      prefix of their counts finding the stop). While R is empty, runs of candidates whose walks ran
 //      out are NOISE at once.
 // The result equals the reference's sequential search bit for bit (same binary32 expressions,
 // same visiting order, same stop points); the tree's node positions equal the reference's.
@@ -1145,21 +1145,38 @@ __global__ void k_kt_spec(BatchDev b)
     b.kspec_n[c] = stop.n;
 }
 
-// Step 4b: one warp per scan applies the candidates' walks in order. R, the stack below the pieces
+// Step 4b: one CTA per scan applies the candidates' walks in order. R, the stack below the pieces
 // pushed since the previous candidate, is a list of pieces (lo, hi): entries [lo, hi) of the flat
 // array (bit 31 of lo clear) or of the pool (set), consumed from hi - 1 down. A candidate whose
-// walk stopped adds what its walk left on top of R. One whose walk ran out continues into R
-// (32 entries at a time, the lanes searching their entries in full and an ordered prefix of the
-// counts finding the stop); running out of R too means NOISE and an empty R. While R is empty, a
-// run of candidates whose walks ran out is NOISE as a whole (ballot over 32 at a time).
-__global__ void __launch_bounds__(32) k_kt_chain(BatchDev b)
+// walk stopped adds what its walk left on top of R. One whose walk ran out continues into R,
+// up to kChainThreads entries at a time across the top kChainPieces pieces: every thread searches
+// one entry's subtree in full (these searches, chains of dependent node loads, are the chain's
+// cost, so a round is as wide as the CTA), and an ordered prefix of the counts finds the stop;
+// running out of R too means NOISE and an empty R. While R is empty, a run of candidates whose
+// walks ran out is NOISE as a whole. The candidates' records are staged kChainThreads at a time in
+// shared memory. Control flow is uniform: every thread holds the same R top, count and candidate;
+// thread 0 writes R and the pool, and a barrier precedes every read of them.
+constexpr uint32_t kChainThreads = 256;
+constexpr uint32_t kChainPieces = 32;
+
+__global__ void __launch_bounds__(kChainThreads) k_kt_chain(BatchDev b)
 {
+    __shared__ uint32_t red[kChainThreads / 32];
+    __shared__ uint32_t bc[4];
+    // the window of candidates [w0, w1): walk record, left-entry count, point, its first pushing
+    // short point, query
+    __shared__ uint4 w_spec[kChainThreads];
+    __shared__ uint32_t w_specn[kChainThreads], w_i[kChainThreads], w_tp1[kChainThreads];
+    __shared__ float4 w_q[kChainThreads];
+    // the top pieces of R for one round (index 0 = the top) and their entry-count prefix
+    __shared__ uint2 r_pc[kChainPieces];
+    __shared__ uint32_t r_pre[kChainPieces + 1];
     const int s = blockIdx.x;
     if (s >= b.nscan)
         return;
     const ScanDev& sd = b.scans[s];
     ScanState* st = &b.state[s];
-    const uint32_t lane = threadIdx.x;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const float4* g = b.kt + sd.src_off;
     const float4* box = b.kbb + 2ull * sd.src_off;
     const uint32_t k = sd.dror_k;
@@ -1167,7 +1184,7 @@ __global__ void __launch_bounds__(32) k_kt_chain(BatchDev b)
     const uint32_t cap = 2u * sd.n_src + 2u;
     const uint32_t t_first = b.kshort[sd.src_off], t_end = b.kshort[sd.src_off + sd.n_src];
     const uint32_t c0 = b.kcflag[t_first], c1 = b.kcflag[t_end];
-    uint32_t top = 0; // pieces in R (lane-uniform)
+    uint32_t top = 0; // pieces in R (the same in every thread)
     bool overflow = false, pool_full = false, full = false;
     uint32_t stk[kKtStack];
     auto push = [&](uint32_t lo, uint32_t hi) {
@@ -1175,7 +1192,7 @@ __global__ void __launch_bounds__(32) k_kt_chain(BatchDev b)
         {
             if (top < cap)
             {
-                if (lane == 0)
+                if (tid == 0)
                     R[top] = make_uint2(lo, hi);
                 ++top;
             }
@@ -1183,30 +1200,85 @@ __global__ void __launch_bounds__(32) k_kt_chain(BatchDev b)
                 full = true;
         }
     };
-    uint32_t c = c0;
+    // block-wide minimum and inclusive sum (every thread gets the result)
+    auto block_min = [&](uint32_t v) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0)
+            red[warp] = v;
+        __syncthreads();
+        uint32_t m = red[0];
+        for (uint32_t w = 1; w < nwarps; ++w)
+            m = min(m, red[w]);
+        __syncthreads();
+        return m;
+    };
+    auto block_incl = [&](uint32_t v, uint32_t& total) {
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= static_cast<uint32_t>(o))
+                v += u;
+        }
+        if (lane == 31)
+            red[warp] = v;
+        __syncthreads();
+        uint32_t pre = 0;
+        total = 0;
+        for (uint32_t w = 0; w < nwarps; ++w)
+        {
+            const uint32_t x = red[w];
+            if (w < warp)
+                pre += x;
+            total += x;
+        }
+        __syncthreads();
+        return v + pre;
+    };
+    uint32_t c = c0, w0 = c0, w1 = c0;
     while (c < c1)
     {
+        if (c >= w1)
+        {
+            // stage the next window of candidates (one per thread)
+            w0 = c;
+            w1 = min(c + blockDim.x, c1);
+            const uint32_t cc = c + tid;
+            if (cc < w1)
+            {
+                const uint32_t t = b.kcand[cc];
+                const uint32_t i = b.kq[t];
+                w_spec[tid] = b.kspec[cc];
+                w_specn[tid] = b.kspec_n[cc];
+                w_i[tid] = i;
+                w_tp1[tid] = (cc > c0) ? b.kcand[cc - 1] + 1 : t_first;
+                w_q[tid] = b.src[i];
+            }
+            __syncthreads();
+        }
         if (top == 0)
         {
-            const uint32_t cc = c + lane;
-            const bool live = cc < c1;
-            const bool hit = live && b.kspec[cc].y != kNone;
-            const uint32_t hits = __ballot_sync(0xffffffffu, hit);
-            const uint32_t h = hits ? static_cast<uint32_t>(__ffs(static_cast<int>(hits)) - 1) : 32u;
-            if (live && lane < h)
-                b.noise[b.kq[b.kcand[cc]]] = LP_NOISE_NOISE;
+            // candidates whose walks ran out with R empty are NOISE, up to the first that stopped
+            const uint32_t cc = c + tid;
+            const bool live = cc < w1;
+            const bool hit = live && w_spec[cc - w0].y != kNone;
+            const uint32_t h = min(block_min(hit ? tid : kNone), w1 - c);
+            if (live && tid < h)
+                b.noise[w_i[cc - w0]] = LP_NOISE_NOISE;
             c += h;
-            if (h == 32u || c >= c1)
+            if (c >= w1)
                 continue;
         }
-        const uint4 sp4 = b.kspec[c];
-        const uint32_t t = b.kcand[c];
-        const uint32_t i = b.kq[t];
+        const uint32_t wc = c - w0;
+        const uint4 sp4 = w_spec[wc];
+        const uint32_t i = w_i[wc];
         if (sp4.y != kNone)
         {
             // the walk stopped at short point u: R gains the pieces of the pushing points below u,
             // then the rest of u's pieces below the stop, then the entries the stopping search left
-            const uint32_t tp1 = (c > c0) ? b.kcand[c - 1] + 1 : t_first;
+            const uint32_t tp1 = w_tp1[wc];
             const uint32_t hu = sp4.y, hx = sp4.z & 0x7fffffffu, hkind = sp4.z >> 31;
             for (uint32_t u = tp1; u <= hu; ++u)
             {
@@ -1227,29 +1299,59 @@ __global__ void __launch_bounds__(32) k_kt_chain(BatchDev b)
                     push(lo, hx);
                 }
             }
-            push(sp4.w | 0x80000000u, sp4.w + b.kspec_n[c]);
-            if (lane == 0)
+            push(sp4.w | 0x80000000u, sp4.w + w_specn[wc]);
+            if (tid == 0)
                 b.noise[i] = LP_NOISE_VALID;
             ++c;
-            __syncwarp(); // lane 0's pieces are read by every lane next
+            __syncthreads(); // thread 0's pieces are read by every thread next
             continue;
         }
         // the walk ran out with R non-empty: continue into R
-        const float4 q = b.src[i];
+        const float4 q = w_q[wc];
         const float r2 = kt_radius2(sd, q);
         uint32_t found = sp4.x;
         bool hit = false;
         while (top > 0 && !hit)
         {
-            const uint2 pc = R[top - 1];
-            const bool in_pool = (pc.x & 0x80000000u) != 0;
-            const uint32_t lo = pc.x & 0x7fffffffu, hi = pc.y;
-            const uint32_t* arr = in_pool ? b.kpool : b.kflat;
-            const uint32_t chunk = min(hi - lo, 32u);
-            uint32_t cnt = 0;
-            if (lane < chunk)
+            // the top pieces (warp 0) and how many entries of them this round covers
+            const uint32_t np = min(top, kChainPieces);
+            if (warp == 0)
             {
-                const uint32_t e = arr[hi - 1 - lane];
+                const uint2 pc = (lane < np) ? R[top - 1 - lane] : make_uint2(0u, 0u);
+                const uint32_t sz = (lane < np) ? pc.y - (pc.x & 0x7fffffffu) : 0u;
+                uint32_t incl = sz;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1)
+                {
+                    const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= static_cast<uint32_t>(o))
+                        incl += u;
+                }
+                if (lane < np)
+                    r_pc[lane] = pc;
+                r_pre[lane + 1] = incl;
+                if (lane == 0)
+                    r_pre[0] = 0;
+            }
+            __syncthreads();
+            const uint32_t covered = min(r_pre[np], blockDim.x);
+            uint32_t cnt = 0, my_p = 0;
+            if (tid < covered)
+            {
+                // the piece holding this thread's entry: the last p with r_pre[p] <= tid
+                uint32_t lo_p = 0, hi_p = np - 1;
+                while (lo_p < hi_p)
+                {
+                    const uint32_t mid = (lo_p + hi_p + 1) / 2;
+                    if (r_pre[mid] <= tid)
+                        lo_p = mid;
+                    else
+                        hi_p = mid - 1;
+                }
+                my_p = lo_p;
+                const uint2 pc = r_pc[my_p];
+                const uint32_t* arr = (pc.x & 0x80000000u) ? b.kpool : b.kflat;
+                const uint32_t e = arr[pc.y - 1 - (tid - r_pre[my_p])];
                 if (kt_may_hit(box, e >> 2, q.x, q.y, q.z, r2))
                 {
                     int sp = 0;
@@ -1257,28 +1359,29 @@ __global__ void __launch_bounds__(32) k_kt_chain(BatchDev b)
                     cnt = kt_search(g, sd.n_src, q.x, q.y, q.z, r2, k, 0, stk, sp, overflow);
                 }
             }
-            uint32_t incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1)
+            uint32_t total = 0;
+            const uint32_t incl = block_incl(cnt, total);
+            const bool reach_here = tid < covered && cnt > 0 && found + incl >= k;
+            const uint32_t hl = block_min(reach_here ? tid : kNone);
+            if (hl != kNone)
             {
-                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= static_cast<uint32_t>(o))
-                    incl += v;
-            }
-            const uint32_t reach = __ballot_sync(0xffffffffu, lane < chunk && cnt > 0 && found + incl >= k);
-            if (reach)
-            {
-                const uint32_t hl = static_cast<uint32_t>(__ffs(static_cast<int>(reach)) - 1);
-                const uint32_t before = found + __shfl_sync(0xffffffffu, incl - cnt, hl);
-                const uint32_t x = hi - 1 - hl;
-                // the stopping search again on lane 0, from the count before it, for what it leaves
-                int sp = 0;
-                uint32_t at = 0;
-                if (lane == 0)
+                if (tid == hl)
                 {
+                    bc[0] = found + incl - cnt; // the count before the stopping entry
+                    bc[3] = my_p;
+                }
+                __syncthreads();
+                const uint32_t before = bc[0], p = bc[3];
+                const uint2 pc = r_pc[p];
+                const uint32_t x = pc.y - 1 - (hl - r_pre[p]);
+                const uint32_t* arr = (pc.x & 0x80000000u) ? b.kpool : b.kflat;
+                // the stopping search again on thread 0, from the count before it, for what it leaves
+                if (tid == 0)
+                {
+                    int sp = 0;
                     stk[sp++] = arr[x];
                     kt_search(g, sd.n_src, q.x, q.y, q.z, r2, k, before, stk, sp, overflow);
-                    at = kt_pool_alloc(b.kctr, b.kpool_cap, static_cast<uint32_t>(sp));
+                    uint32_t at = kt_pool_alloc(b.kctr, b.kpool_cap, static_cast<uint32_t>(sp));
                     if (at == kNone)
                     {
                         pool_full = true;
@@ -1287,38 +1390,41 @@ __global__ void __launch_bounds__(32) k_kt_chain(BatchDev b)
                     }
                     for (int v = 0; v < sp; ++v)
                         b.kpool[at + v] = stk[v];
+                    bc[1] = static_cast<uint32_t>(sp);
+                    bc[2] = at;
                 }
-                sp = __shfl_sync(0xffffffffu, sp, 0);
-                at = __shfl_sync(0xffffffffu, at, 0);
-                // R: the piece keeps its entries below the stop, then the left entries go on top
-                --top;
+                __syncthreads();
+                const uint32_t nsp = bc[1], at = bc[2];
+                // R: the pieces above p are consumed, p keeps its entries below the stop, then the
+                // left entries go on top
+                top -= p + 1;
                 push(pc.x, x);
-                push(at | 0x80000000u, at + static_cast<uint32_t>(sp));
+                push(at | 0x80000000u, at + nsp);
                 hit = true;
             }
             else
             {
-                found += __shfl_sync(0xffffffffu, incl, 31);
-                if (hi - chunk > lo)
-                {
-                    if (lane == 0)
-                        R[top - 1].y = hi - chunk;
-                }
-                else
-                    --top;
+                found += total;
+                // pieces fully covered are consumed; the last covered one keeps what lies below
+                uint32_t p = 0;
+                while (p < np && r_pre[p + 1] <= covered)
+                    ++p;
+                top -= p;
+                if (p < np && covered > r_pre[p] && tid == 0)
+                    R[top - 1].y = r_pc[p].y - (covered - r_pre[p]);
             }
-            __syncwarp();
+            __syncthreads();
         }
-        if (lane == 0)
+        if (tid == 0)
             b.noise[i] = hit ? LP_NOISE_VALID : LP_NOISE_NOISE;
         ++c;
-        __syncwarp();
+        __syncthreads();
     }
-    if (__any_sync(0xffffffffu, overflow) && lane == 0)
+    if (__syncthreads_or(overflow) && tid == 0)
         raise_err(st, ERR_INTERNAL);
-    if (__any_sync(0xffffffffu, pool_full) && lane == 0)
+    if (__syncthreads_or(pool_full) && tid == 0)
         raise_err(st, ERR_HASH_FULL);
-    if (full && lane == 0)
+    if (full && tid == 0)
         raise_err(st, ERR_INTERNAL);
 }
 } // namespace
@@ -1371,6 +1477,6 @@ void launch_noise(Launcher& L, const BatchDev& b, const BatchHost& hb, const lp_
     L.scan(b.kcflag, b.kcflag, b.nsrc + 1);
     LP_LAUNCH(L, k_kt_cand_list, div_up(b.nsrc, T), T, b);
     LP_LAUNCH(L, k_kt_spec, div_up(b.nsrc, 128u), 128, b);
-    LP_LAUNCH(L, k_kt_chain, S, 32, b);
+    LP_LAUNCH(L, k_kt_chain, S, kChainThreads, b);
 }
 } // namespace lpg
