@@ -430,6 +430,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end run")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving sub-record")
     ap.add_argument("--no-dror", action="store_true", help="skip the outlier-filter sub-record")
+    ap.add_argument("--no-tune", action="store_true", help="time the default tuning (no autotuner run)")
+    ap.add_argument("--tune-iters", type=int, default=3, help="timed executions per autotuner candidate")
     ap.add_argument("--serve-duration", type=float, default=52.0,
                     help="seconds of sensor stream in the serving sub-record (>= 3,000 scans at 60 scans/s)")
     args = ap.parse_args()
@@ -458,7 +460,22 @@ def main():
     xs, rings, cfgs = [d[0] for d in data], [d[1] for d in data], [d[2] for d in data]
     pipe = lp.PipelineConfig.default()
     npts = sum(len(x) for x in xs)
+    tune = None
+    if not args.no_tune:
+        # the library's autotuner on the workload's bucket; batches created afterwards in this
+        # context (the timed batch, the end-to-end calls) take its choice
+        try:
+            t_tune = time.perf_counter()
+            table = lp.TuningTable()
+            best, rep = lp.autotune(ctx, xs, pipe, cfgs, rings, iters=args.tune_iters, table=table)
+            ctx.set_tuning_table(table)
+            tune = {"bucket": list(lp.tuning_key(xs, cfgs).as_tuple()), "chosen": best.as_dict(),
+                    "default_ms": rep["start_ms"], "tuned_ms": rep["best_ms"], "trials": rep["trials"],
+                    "iters_per_trial": args.tune_iters, "seconds": time.perf_counter() - t_tune}
+        except Exception as exc:  # reported in the line; the default tuning is timed instead
+            tune = {"error": leg_error(exc)}
     batch = lp.PreparedBatch(ctx, xs, pipe, cfgs, rings)
+    batch_tuning = batch.tuning.as_dict()
 
     # per-kernel profile of one un-captured execution (dominant kernel for the roofline)
     batch.execute()
@@ -564,7 +581,8 @@ def main():
             "config": {"workload": workload_name(ns), "scans": ns, "points": npts,
                        "obstacles": n_obs, "clusters": n_clusters, "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (133 MB XYZI, multi-GB working set)",
-                       "graph": "captured CUDA graph per batch"},
+                       "graph": "captured CUDA graph per batch",
+                       "tuning": batch_tuning},
             "points_per_s": world * npts * args.steps / (dev_ms_max / 1e3),
             "plain": ({"error": plain_err} if plain_err else None) if not plain else {
                 "ms_per_scan": plain_ms, "scans_per_s": 1e3 / plain_ms, "p50_ms": float(np.percentile(plain, 50)),
@@ -582,6 +600,7 @@ def main():
             "kernel_share": {k: round(v[1] / total_ms, 4) for k, v in sorted(agg2.items(), key=lambda kv: -kv[1][1])[:10]},
             "clocks": clocks.summary(),
             "cpu_baseline": cb,
+            "autotune": tune,
             "serve": serve,
             "dror": dror,
             "wall_s": wall,

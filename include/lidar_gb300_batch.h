@@ -73,6 +73,74 @@ lp_status lp_debug_math_sweep(lp_context* ctx, int32_t kind, uint64_t first, uin
                               uint64_t* first_bad);
 
 /* ------------------------------------------------------------------------------------------ */
+/* Tuning: batch split and launch shapes chosen at run time, per batch bucket.                 */
+/* No counterpart in the reference (it runs one scan at a time on one CPU thread).             */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct lp_tuning
+{
+    uint32_t parts;            /* concurrent parts of a batch of 16 or more scans (1-8; 0: one per 8
+                                  scans, at most 4); never more than the batch has scans */
+    uint32_t balance_parts;    /* 0: scans dealt round-robin; 1: largest scan first to the part holding
+                                  the fewest points */
+    uint32_t hull_cta_min;     /* clusters of more members take a whole CTA of the hull kernel, smaller
+                                  ones one warp (64-512) */
+    uint32_t hull_ctas_per_sm; /* persistent hull CTAs per SM (1-4) */
+    uint32_t cell_ctas_per_sm; /* polar-cell sort CTAs per SM (1-16) */
+    uint32_t jcp_ctas_per_sm;  /* vote-weight CTAs per SM (1-16) */
+} lp_tuning;
+
+/* A batch's bucket: scan-count class (0: 1 scan, 1: 2-15, 2: 16-31, 3: 32-63, 4: 64 or more), and
+ * the ring-count class (0: up to 32 rings, 1: up to 64, 2: more) and azimuth class (0: up to 1024
+ * bins, 1: up to 2048, 2: more) that hold the most points of the batch. */
+typedef struct lp_tuning_key
+{
+    uint32_t scans_class;
+    uint32_t ring_class;
+    uint32_t azimuth_class;
+} lp_tuning_key;
+
+typedef struct lp_tuning_table lp_tuning_table;
+
+/* The compiled-in defaults (set by sweeps of the 64-scan mixed batch). */
+void lp_tuning_default(lp_tuning* t);
+/* LP_ERR_BAD_ARG unless every field lies in its range. */
+lp_status lp_tuning_validate(const lp_tuning* t);
+lp_status lp_tuning_key_of(const lp_scan_input* scans, uint32_t nscans, lp_tuning_key* out);
+/* Host-side table bucket -> tuning (and the step time it was measured at). */
+lp_status lp_tuning_table_create(lp_tuning_table** out);
+void lp_tuning_table_destroy(lp_tuning_table* table);
+lp_status lp_tuning_table_set(lp_tuning_table* table, const lp_tuning_key* key, const lp_tuning* tuning, float ms);
+/* 1 and the entry when the bucket is in the table; 0 and the defaults when it is not. */
+int32_t lp_tuning_table_get(const lp_tuning_table* table, const lp_tuning_key* key, lp_tuning* out, float* ms);
+uint32_t lp_tuning_table_size(const lp_tuning_table* table);
+/* Plain text, one bucket per line; load adds to (and overrides entries of) the table. */
+lp_status lp_tuning_table_save(const lp_tuning_table* table, const char* path);
+lp_status lp_tuning_table_load(lp_tuning_table* table, const char* path);
+/* The context keeps a copy: batches created afterwards (lp_batch_create, lp_process_batch, the
+ * serving loop) take their bucket's entry, the defaults where there is none. */
+lp_status lp_context_set_tuning_table(lp_context* ctx, const lp_tuning_table* table);
+/* A batch with an explicit tuning, whatever the context's table holds. */
+lp_status lp_batch_create_tuned(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans,
+                                uint32_t nscans, const lp_tuning* tuning, lp_batch** out);
+lp_status lp_batch_get_tuning(const lp_batch* batch, lp_tuning* out);
+
+typedef struct lp_autotune_report
+{
+    uint32_t trials;  /* candidate tunings timed (the starting one included) */
+    float start_ms;   /* device time per execution of the starting tuning */
+    float best_ms;    /* and of the one chosen */
+} lp_autotune_report;
+
+/* Coordinate descent over the tuning fields on these scans: each candidate is a prepared batch
+ * replayed as a CUDA graph, timed with CUDA events over `iters` executions (L2 flushed between
+ * them); a candidate replaces the current choice only if at least 1 % faster. Starts from the
+ * table's entry for the scans' bucket (else the defaults) and stores the choice there. trial_ms /
+ * trial_cfg (trial_cap entries, either may be null) receive every timed candidate in order. */
+lp_status lp_autotune(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans, uint32_t nscans,
+                      uint32_t iters, lp_tuning_table* table, lp_tuning* best, lp_autotune_report* report,
+                      float* trial_ms, lp_tuning* trial_cfg, uint32_t trial_cap);
+
+/* ------------------------------------------------------------------------------------------ */
 /* Serving: scans from several sensors submitted as they arrive, continuous batching.          */
 /* No counterpart in the reference (its processor node handles one scan per callback).         */
 /* ------------------------------------------------------------------------------------------ */
@@ -101,6 +169,7 @@ typedef struct lp_server_stats
 {
     uint64_t submitted, completed, failed, batches, scans_in_batches, max_batch_seen, pending;
     uint64_t device_bytes;
+    uint64_t memory_waits; /* times the queue's head waited for memory to come back */
 } lp_server_stats;
 
 void lp_server_config_default(lp_server_config* cfg);

@@ -24,7 +24,7 @@ BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(REPO, "include")
 
 CUDA_TUS = ["lp_common.cu", "lp_segment.cu", "lp_cluster.cu", "lp_hull.cu", "lp_dror.cu", "lp_kdtree.cu", "lp_api.cu",
-            "lp_serve.cu", "lp_io.cu", "lp_split.cu", "lp_wire.cu", "lp_objects.cu"]
+            "lp_serve.cu", "lp_io.cu", "lp_split.cu", "lp_wire.cu", "lp_objects.cu", "lp_tune.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -184,9 +184,13 @@ lp_status plan(lp_context* ctx, lp_batch& B)
         return fail(ctx, LP_ERR_CAPACITY, "batch too large for 32-bit indexing; split it");
     hb.ntiles = static_cast<uint32_t>(tile);
     hb.nslices = static_cast<uint32_t>(slice);
+    hb.hull_ctas_per_sm = B.tune.hull_ctas_per_sm;
+    hb.cell_ctas_per_sm = B.tune.cell_ctas_per_sm;
+    hb.jcp_ctas_per_sm = B.tune.jcp_ctas_per_sm;
     BatchDev& b = B.b;
     b = BatchDev{};
     b.nscan = hb.nscan;
+    b.hull_cta_min = B.tune.hull_cta_min;
     b.nsrc = static_cast<uint32_t>(pt);
     b.npts = static_cast<uint32_t>(pt);
     b.ntiles = static_cast<uint32_t>(tile);
@@ -563,12 +567,6 @@ void destroy_batch(lp_batch* B)
     delete B;
 }
 
-// Parts a batch of n scans is split into: one below 16 scans, then one per 8 scans, at most 4.
-uint32_t split_parts(uint32_t n)
-{
-    return n < 16u ? 1u : std::min(4u, n / 8u);
-}
-
 // Launches a batch: a split batch forks its parts' streams from the context stream, launches every
 // part on its own stream and joins them back (also the shape a graph capture records).
 lp_status launch_batch(lp_context* ctx, lp_batch& B)
@@ -842,12 +840,13 @@ lp_status run_direct(lp_context* ctx, lp_batch& B, lp_scan_output* outs)
     return direct_finish(ctx, B, outs);
 }
 
-// The direct path for 16 or more scans: concurrent parts (scans dealt round-robin), each on its own
-// stream, ordered after earlier work on the context stream; each part's host reads and writes
-// overlap the other parts' kernels.
+// The direct path for a split batch: concurrent parts (the scans the tuning assigns each), each on
+// its own stream, ordered after earlier work on the context stream; each part's host reads and
+// writes overlap the other parts' kernels.
 lp_status run_direct_split(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans,
-                           lp_scan_output* outs, uint32_t nscans, uint32_t K)
+                           lp_scan_output* outs, uint32_t nscans, const lp_tuning& tune, uint32_t K)
 {
+    const std::vector<std::vector<uint32_t>> where = assign_parts(scans, nscans, K, tune.balance_parts != 0);
     while (ctx->cached_parts.size() < K)
     {
         lp_batch* P = new lp_batch();
@@ -867,8 +866,9 @@ lp_status run_direct_split(lp_context* ctx, const lp_pipeline_config* cfg, const
     for (uint32_t k = 0; k < K && worst == LP_OK; ++k)
     {
         lp_batch& P = *ctx->cached_parts[k];
+        P.tune = tune;
         std::vector<lp_scan_input> in;
-        for (uint32_t i = k; i < nscans; i += K)
+        for (const uint32_t i : where[k])
         {
             in.push_back(scans[i]);
             sub[k].push_back(outs[i]);
@@ -890,11 +890,69 @@ lp_status run_direct_split(lp_context* ctx, const lp_pipeline_config* cfg, const
     {
         const lp_status st = direct_finish(ctx, *ctx->cached_parts[k], sub[k].data());
         for (size_t j = 0; j < sub[k].size(); ++j)
-            outs[k + j * K] = sub[k][j];
+            outs[where[k][j]] = sub[k][j];
         if (st != LP_OK && (worst == LP_OK || worst == LP_ERR_CAPACITY))
             worst = st;
     }
     return worst;
+}
+lp_status create_batch(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans, uint32_t nscans,
+                       const lp_tuning& tune, lp_batch** out)
+{
+    if (!ctx || !out || nscans == 0)
+        return fail(ctx, LP_ERR_BAD_ARG, "null argument or empty batch");
+    *out = nullptr;
+    LP_TRY(ensure_device(ctx));
+    lp_batch* B = new lp_batch();
+    B->tune = tune;
+    const uint32_t K = part_count(tune, nscans);
+    lp_status st = LP_OK;
+    if (K == 1)
+    {
+        st = fill_pipeline(ctx, *B, cfg, scans, nscans);
+        if (st == LP_OK)
+            st = build(ctx, *B);
+        if (st == LP_OK)
+            st = upload(ctx, *B);
+    }
+    else
+    {
+        // scans dealt round-robin (every part gets a similar mix of scan sizes) or by points
+        B->part_scans = assign_parts(scans, nscans, K, tune.balance_parts != 0);
+        for (uint32_t k = 0; k < K && st == LP_OK; ++k)
+        {
+            std::vector<lp_scan_input> sub;
+            for (const uint32_t i : B->part_scans[k])
+                sub.push_back(scans[i]);
+            lp_batch* P = new lp_batch();
+            P->tune = tune;
+            B->parts.push_back(P);
+            if (cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking) != cudaSuccess)
+                st = fail(ctx, LP_ERR_CUDA, "cudaStreamCreateWithFlags");
+            if (st == LP_OK)
+                st = fill_pipeline(ctx, *P, cfg, sub.data(), static_cast<uint32_t>(sub.size()));
+            if (st == LP_OK)
+                st = build(ctx, *P);
+            if (st == LP_OK)
+                st = upload(ctx, *P);
+        }
+        for (uint32_t k = 0; k <= K && st == LP_OK; ++k)
+        {
+            cudaEvent_t e;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                st = fail(ctx, LP_ERR_CUDA, "cudaEventCreateWithFlags");
+            else
+                B->fork_join.push_back(e);
+        }
+    }
+    if (st != LP_OK)
+    {
+        cudaStreamSynchronize(ctx->stream);
+        destroy_batch(B);
+        return st;
+    }
+    *out = B;
+    return LP_OK;
 }
 } // namespace lprt
 
@@ -1603,10 +1661,12 @@ lp_status lp_process_batch(lp_context* ctx, const lp_pipeline_config* cfg, const
     LP_TRY(ensure_device(ctx));
     lp_batch& B = cached(ctx);
     LP_TRY(fill_pipeline(ctx, B, cfg, scans, nscans));
+    const lp_tuning tune = tuning_for(ctx, scans, nscans);
+    B.tune = tune;
     if (direct_io_ok(B, scans, outs))
     {
-        const uint32_t K = split_parts(nscans);
-        return K > 1 ? run_direct_split(ctx, cfg, scans, outs, nscans, K) : run_direct(ctx, B, outs);
+        const uint32_t K = part_count(tune, nscans);
+        return K > 1 ? run_direct_split(ctx, cfg, scans, outs, nscans, tune, K) : run_direct(ctx, B, outs);
     }
     const lp_status st = run_once(ctx, B);
     if (st != LP_OK && st != LP_ERR_CAPACITY)
@@ -1627,56 +1687,22 @@ lp_status lp_process_scan(lp_context* ctx, const lp_pipeline_config* cfg, const 
 lp_status lp_batch_create(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans, uint32_t nscans,
                           lp_batch** out)
 {
-    if (!ctx || !out || nscans == 0)
-        return fail(ctx, LP_ERR_BAD_ARG, "null argument or empty batch");
-    *out = nullptr;
-    LP_TRY(ensure_device(ctx));
-    lp_batch* B = new lp_batch();
-    const uint32_t K = split_parts(nscans);
-    lp_status st = LP_OK;
-    if (K == 1)
-    {
-        st = fill_pipeline(ctx, *B, cfg, scans, nscans);
-        if (st == LP_OK)
-            st = build(ctx, *B);
-        if (st == LP_OK)
-            st = upload(ctx, *B);
-    }
-    else
-    {
-        // scans dealt round-robin, so every part gets a similar mix of scan sizes
-        for (uint32_t k = 0; k < K && st == LP_OK; ++k)
-        {
-            std::vector<lp_scan_input> sub;
-            for (uint32_t i = k; i < nscans; i += K)
-                sub.push_back(scans[i]);
-            lp_batch* P = new lp_batch();
-            B->parts.push_back(P);
-            if (cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking) != cudaSuccess)
-                st = fail(ctx, LP_ERR_CUDA, "cudaStreamCreateWithFlags");
-            if (st == LP_OK)
-                st = fill_pipeline(ctx, *P, cfg, sub.data(), static_cast<uint32_t>(sub.size()));
-            if (st == LP_OK)
-                st = build(ctx, *P);
-            if (st == LP_OK)
-                st = upload(ctx, *P);
-        }
-        for (uint32_t k = 0; k <= K && st == LP_OK; ++k)
-        {
-            cudaEvent_t e;
-            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
-                st = fail(ctx, LP_ERR_CUDA, "cudaEventCreateWithFlags");
-            else
-                B->fork_join.push_back(e);
-        }
-    }
-    if (st != LP_OK)
-    {
-        cudaStreamSynchronize(ctx->stream);
-        destroy_batch(B);
-        return st;
-    }
-    *out = B;
+    return create_batch(ctx, cfg, scans, nscans, tuning_for(ctx, scans, nscans), out);
+}
+
+lp_status lp_batch_create_tuned(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans,
+                                uint32_t nscans, const lp_tuning* tuning, lp_batch** out)
+{
+    if (!tuning || lp_tuning_validate(tuning) != LP_OK)
+        return fail(ctx, LP_ERR_BAD_ARG, "tuning out of range");
+    return create_batch(ctx, cfg, scans, nscans, *tuning, out);
+}
+
+lp_status lp_batch_get_tuning(const lp_batch* batch, lp_tuning* out)
+{
+    if (!batch || !out)
+        return LP_ERR_BAD_ARG;
+    *out = batch->tune;
     return LP_OK;
 }
 
@@ -1749,13 +1775,14 @@ lp_status lp_batch_download(lp_context* ctx, lp_batch* B, lp_scan_output* outs)
         lp_status worst = LP_OK;
         for (size_t k = 0; k < K; ++k)
         {
-            const size_t S = B->parts[k]->run.scans.size();
+            const std::vector<uint32_t>& where = B->part_scans[k];
+            const size_t S = where.size();
             std::vector<lp_scan_output> sub(S);
             for (size_t j = 0; j < S; ++j)
-                sub[j] = outs[j * K + k];
+                sub[j] = outs[where[j]];
             const lp_status st = lp_batch_download(ctx, B->parts[k], sub.data());
             for (size_t j = 0; j < S; ++j)
-                outs[j * K + k] = sub[j];
+                outs[where[j]] = sub[j];
             if (st != LP_OK && (worst == LP_OK || worst == LP_ERR_CAPACITY))
                 worst = st;
         }

@@ -164,6 +164,7 @@ struct BatchDev
 
     // ---- per-cluster ---------------------------------------------------------------------------
     uint32_t ncl;
+    uint32_t hull_cta_min; // clusters of more members take a CTA of the hull kernel (tuning)
     uint32_t* cl_cnt;     // members per cluster
     uint32_t* cl_start;   // exclusive scan of cl_cnt
     uint32_t* cl_fill;

@@ -1979,7 +1979,7 @@ __global__ void k_hull_worklist(BatchDev b, uint32_t* work)
     const int s = find_scan(b.nscan, g, [&](int q) { return b.scans[q].cl_off; });
     if (g - b.scans[s].cl_off >= b.state[s].n_clusters)
         return;
-    if (b.cl_cnt[g] > kBigCluster)
+    if (b.cl_cnt[g] > b.hull_cta_min) // hull_cta_min <= kBigCluster: the warp path's limit
         work[atomicAdd(&b.queue[2], 1u)] = g;
     else
         work[b.ncl - 1u - atomicAdd(&b.queue[3], 1u)] = g;
@@ -2369,7 +2369,7 @@ void launch_polygons(Launcher& L, const BatchDev& b, const BatchHost& hb, int co
     uint32_t* work = b.cl_fill;
     LP_LAUNCH(L, k_hull_worklist, div_up(b.ncl, 256u), 256, b, work);
     const int sms = sm_count();
-    LP_LAUNCH_SMEM(L, k_hull, static_cast<uint32_t>(sms * 2), kHullThreads, kHullDynSmem, b, compute_obb,
+    LP_LAUNCH_SMEM(L, k_hull, static_cast<uint32_t>(sms) * hb.hull_ctas_per_sm, kHullThreads, kHullDynSmem, b, compute_obb,
                    static_cast<const uint32_t*>(work));
     L.scan(b.hull_cnt, b.hull_cnt, b.ncl + 1);
     LP_LAUNCH_SMEM(L, k_hull_ties, static_cast<uint32_t>(sms), kHullThreads, kTieDynSmem, b);

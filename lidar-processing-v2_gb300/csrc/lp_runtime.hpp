@@ -2,6 +2,7 @@
 // (lp_serve.cu): contexts, batches and the plan/upload/execute/download steps of a batch.
 #pragma once
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -35,6 +36,8 @@ struct ScanIn
     int32_t first_ring = 0;
 };
 
+lp_tuning tuning_default(); // lp_tune.cu
+
 struct Run
 {
     uint32_t stages = 0;
@@ -65,6 +68,8 @@ struct lp_context
     uint64_t rand_at = 0;
     bool rand_valid = false;
     lpg::RandWindow rand_window{};
+    // lp_context_set_tuning_table: bucket (lprt::key_index) -> tuning for batches created here
+    std::map<uint32_t, lp_tuning> tuning;
 };
 
 struct lp_batch
@@ -87,7 +92,9 @@ struct lp_batch
     // run concurrently on their streams (fork from and join into the context stream), so one
     // part's latency-bound tails overlap the others' work.
     std::vector<lp_batch*> parts;
-    std::vector<cudaEvent_t> fork_join; // [0] fork, [1 + k] part k done
+    std::vector<std::vector<uint32_t>> part_scans; // the batch's scan indices in part k, in batch order
+    std::vector<cudaEvent_t> fork_join;            // [0] fork, [1 + k] part k done
+    lp_tuning tune = lprt::tuning_default();       // the batch's split and launch shapes
     std::vector<uint32_t> h_nh;         // direct host I/O: hull index count per scan (read back)
 };
 
@@ -107,4 +114,12 @@ lp_status download(lp_context* ctx, lp_batch& B, lp_scan_output* outs);
 lp_status fill_pipeline(lp_context* ctx, lp_batch& B, const lp_pipeline_config* cfg, const lp_scan_input* scans,
                         uint32_t nscans);
 void destroy_batch(lp_batch* B);
+// Tuning (lp_tune.cu): bucket index of a key, the tuning a batch of these scans takes in this
+// context, the number of parts and which scans go to each.
+uint32_t key_index(const lp_tuning_key& k);
+lp_tuning_key key_of(const lp_scan_input* scans, uint32_t nscans);
+lp_tuning tuning_for(const lp_context* ctx, const lp_scan_input* scans, uint32_t nscans);
+uint32_t part_count(const lp_tuning& t, uint32_t nscans);
+std::vector<std::vector<uint32_t>> assign_parts(const lp_scan_input* scans, uint32_t nscans, uint32_t parts,
+                                                bool balance);
 } // namespace lprt

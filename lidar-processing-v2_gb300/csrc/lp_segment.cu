@@ -1879,7 +1879,7 @@ void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, ui
     LP_LAUNCH(L, k_bin, div_up(b.npts, 2u * T), T, b);
     L.scan(b.cell_cnt, b.cell_start, b.ncell + 1);
     LP_LAUNCH(L, k_scatter, div_up(b.npts, T), T, b);
-    LP_LAUNCH(L, k_cell_small, std::min(div_up(b.ncell, 256u), static_cast<uint32_t>(sm_count()) * 8u), 256, b);
+    LP_LAUNCH(L, k_cell_small, std::min(div_up(b.ncell, 256u), static_cast<uint32_t>(sm_count()) * hb.cell_ctas_per_sm), 256, b);
     LP_LAUNCH(L, k_cell_large, static_cast<uint32_t>(sm_count()) * 2u, 512, b);
     LP_LAUNCH(L, k_chain, div_up(hb.nslices, 128u), 128, b, hb.nslices);
     LP_LAUNCH(L, k_near, div_up(b.nnear * 32u, 256u), 256, b, 0);
@@ -1892,7 +1892,7 @@ void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, ui
     LP_LAUNCH(L, k_project_key, div_up(b.npts, T), T, b);
     LP_LAUNCH(L, k_pixel, div_up(b.npix, T), T, b);
     LP_LAUNCH(L, k_dilate_rows, b.nrows, 256, b);
-    LP_LAUNCH(L, k_jcp_weights, static_cast<uint32_t>(sm_count()) * 8u, 256, b);
+    LP_LAUNCH(L, k_jcp_weights, static_cast<uint32_t>(sm_count()) * hb.jcp_ctas_per_sm, 256, b);
     LP_LAUNCH(L, k_jcp_rowrec, div_up(b.nrows * 32u, 256u), 256, b);
     LP_LAUNCH_SMEM(L, k_jcp_rows, static_cast<uint32_t>(b.nscan), 256, 2u * kStageBytes, b);
     LP_LAUNCH(L, k_populate, div_up(b.npix, T), T, b, d_image);

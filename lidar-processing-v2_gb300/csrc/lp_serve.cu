@@ -150,6 +150,7 @@ lp_status plan_bytes(Slot& slot, const lp_pipeline_config& cfg, const std::vecto
     lp_status st = lprt::fill_pipeline(slot.ctx, slot.batch, &cfg, ins.data(), static_cast<uint32_t>(ins.size()));
     if (st != LP_OK)
         return st;
+    slot.batch.tune = lprt::tuning_for(slot.ctx, ins.data(), static_cast<uint32_t>(ins.size())); // launch shapes
     st = lprt::plan(slot.ctx, slot.batch);
     if (st != LP_OK)
         return st;
@@ -289,7 +290,10 @@ void admit(lp_server* sv, Slot& slot, std::unique_lock<std::mutex>& lk)
     }
     lk.lock();
     if (wait)
+    {
         sv->blocked = true;
+        sv->stats.memory_waits += 1;
+    }
     if (!take.empty() && slot.busy)
     {
         sv->stats.batches += 1;

@@ -177,6 +177,10 @@ struct BatchHost
     uint32_t ntiles = 0;
     uint32_t nslices = 0;
     std::vector<ScanDev> scans;
+    // launch shapes (lp_tuning)
+    uint32_t hull_ctas_per_sm = 2;
+    uint32_t cell_ctas_per_sm = 8;
+    uint32_t jcp_ctas_per_sm = 8;
 };
 
 void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, uint8_t* d_image);

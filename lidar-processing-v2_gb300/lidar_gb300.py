@@ -302,6 +302,20 @@ def _declare(lib):
         "lp_server_poll": (c.c_int32, [P, P, c.c_uint32, c.POINTER(c.c_uint32), c.c_uint32]),
         "lp_server_stats_get": (c.c_int32, [P, P]),
         "lp_server_destroy": (None, [P]),
+        "lp_tuning_default": (None, [P]),
+        "lp_tuning_validate": (c.c_int32, [P]),
+        "lp_tuning_key_of": (c.c_int32, [P, c.c_uint32, P]),
+        "lp_tuning_table_create": (c.c_int32, [c.POINTER(P)]),
+        "lp_tuning_table_destroy": (None, [P]),
+        "lp_tuning_table_set": (c.c_int32, [P, P, P, c.c_float]),
+        "lp_tuning_table_get": (c.c_int32, [P, P, P, c.POINTER(c.c_float)]),
+        "lp_tuning_table_size": (c.c_uint32, [P]),
+        "lp_tuning_table_save": (c.c_int32, [P, c.c_char_p]),
+        "lp_tuning_table_load": (c.c_int32, [P, c.c_char_p]),
+        "lp_context_set_tuning_table": (c.c_int32, [P, P]),
+        "lp_batch_create_tuned": (c.c_int32, [P, P, P, c.c_uint32, P, c.POINTER(P)]),
+        "lp_batch_get_tuning": (c.c_int32, [P, P]),
+        "lp_autotune": (c.c_int32, [P, P, P, c.c_uint32, c.c_uint32, P, P, P, P, P, c.c_uint32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -362,6 +376,11 @@ class Context:
             self.close()
         except Exception:
             pass
+
+    def set_tuning_table(self, table):
+        """Batches created in this context afterwards take their bucket's entry of `table` (a TuningTable;
+        None clears)."""
+        check(library().lp_context_set_tuning_table(self.handle, table.handle if table is not None else None), self)
 
     @property
     def launches(self):
@@ -638,12 +657,120 @@ class Polygonizer:
         return b
 
 
+class Tuning(ctypes.Structure):
+    """lp_tuning: a batch's split into concurrent parts and its launch shapes (results never
+    depend on it)."""
+    _fields_ = [("parts", ctypes.c_uint32), ("balance_parts", ctypes.c_uint32), ("hull_cta_min", ctypes.c_uint32),
+                ("hull_ctas_per_sm", ctypes.c_uint32), ("cell_ctas_per_sm", ctypes.c_uint32),
+                ("jcp_ctas_per_sm", ctypes.c_uint32)]
+
+    @staticmethod
+    def default(**kw):
+        t = Tuning()
+        library().lp_tuning_default(ctypes.byref(t))
+        for k, v in kw.items():
+            setattr(t, k, v)
+        return t
+
+    def valid(self):
+        return library().lp_tuning_validate(ctypes.byref(self)) == LP_OK
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
+class TuningKey(ctypes.Structure):
+    _fields_ = [("scans_class", ctypes.c_uint32), ("ring_class", ctypes.c_uint32), ("azimuth_class", ctypes.c_uint32)]
+
+    def as_tuple(self):
+        return (int(self.scans_class), int(self.ring_class), int(self.azimuth_class))
+
+
+class AutotuneReport(ctypes.Structure):
+    _fields_ = [("trials", ctypes.c_uint32), ("start_ms", ctypes.c_float), ("best_ms", ctypes.c_float)]
+
+
+def _scan_inputs(scans, seg_configs=None, rings=None):
+    """(ScanInput array, arrays kept alive) for a list of clouds."""
+    n = len(scans)
+    arrs = [_xyzi(s) for s in scans]
+    rs = [None if (rings is None or rings[i] is None) else np.ascontiguousarray(rings[i], np.uint16) for i in range(n)]
+    cfgs = seg_configs or [SegmenterConfig.default() for _ in range(n)]
+    ins = (ScanInput * n)()
+    for i in range(n):
+        ins[i] = ScanInput(arrs[i].ctypes.data, None if rs[i] is None else rs[i].ctypes.data, len(arrs[i]), cfgs[i])
+    return ins, (arrs, rs)
+
+
+def tuning_key(scans, seg_configs=None):
+    ins, keep = _scan_inputs(scans, seg_configs)
+    k = TuningKey()
+    check(library().lp_tuning_key_of(ins, len(scans), ctypes.byref(k)))
+    return k
+
+
+class TuningTable:
+    """Host table bucket -> tuning (lp_tuning_table)."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(library().lp_tuning_table_create(ctypes.byref(h)))
+        self.handle = h
+
+    def set(self, key, tuning, ms=0.0):
+        check(library().lp_tuning_table_set(self.handle, ctypes.byref(key), ctypes.byref(tuning), ms))
+
+    def get(self, key):
+        """(found, Tuning, ms): the defaults and found=False when the bucket has no entry."""
+        t = Tuning()
+        ms = ctypes.c_float()
+        found = library().lp_tuning_table_get(self.handle, ctypes.byref(key), ctypes.byref(t), ctypes.byref(ms))
+        return bool(found), t, float(ms.value)
+
+    def __len__(self):
+        return int(library().lp_tuning_table_size(self.handle))
+
+    def save(self, path):
+        check(library().lp_tuning_table_save(self.handle, os.fsencode(path)))
+
+    def load(self, path):
+        check(library().lp_tuning_table_load(self.handle, os.fsencode(path)))
+
+    def close(self):
+        if self.handle:
+            library().lp_tuning_table_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune(ctx, scans, pipeline=None, seg_configs=None, rings=None, iters=5, table=None, trial_cap=64):
+    """lp_autotune: (best Tuning, report dict with the timed candidates) for these scans; the choice is
+    stored in `table` (a TuningTable) under the scans' bucket when one is given."""
+    pipeline = pipeline or PipelineConfig.default()
+    ins, keep = _scan_inputs(scans, seg_configs, rings)
+    best = Tuning()
+    rep = AutotuneReport()
+    tms = np.zeros(trial_cap, np.float32)
+    tcf = (Tuning * trial_cap)()
+    check(library().lp_autotune(ctx.handle, ctypes.byref(pipeline), ins, len(scans), iters,
+                                table.handle if table is not None else None, ctypes.byref(best), ctypes.byref(rep),
+                                ptr(tms), tcf, trial_cap), ctx)
+    k = min(rep.trials, trial_cap)
+    return best, {"trials": int(rep.trials), "start_ms": float(rep.start_ms), "best_ms": float(rep.best_ms),
+                  "candidates": [(tcf[i].as_dict(), float(tms[i])) for i in range(k)]}
+
+
 class PreparedBatch:
     """Scans uploaded once to HBM; execute() re-runs the pipeline on the device-resident inputs
     (optionally as a captured CUDA graph), download() returns ScanResults, upload() re-copies the
     host inputs (end-to-end measurement)."""
 
-    def __init__(self, ctx, scans, pipeline=None, seg_configs=None, rings=None):
+    def __init__(self, ctx, scans, pipeline=None, seg_configs=None, rings=None, tuning=None):
         self.ctx = ctx
         self.pipeline = pipeline or PipelineConfig.default()
         n = len(scans)
@@ -658,9 +785,19 @@ class PreparedBatch:
                                      len(self._arrs[i]), cfgs[i])
         self._bufs = [ResultBuffers(len(a)) for a in self._arrs]
         h = ctypes.c_void_p()
-        check(library().lp_batch_create(ctx.handle, ctypes.byref(self.pipeline), self._ins, n, ctypes.byref(h)), ctx)
+        if tuning is None:
+            check(library().lp_batch_create(ctx.handle, ctypes.byref(self.pipeline), self._ins, n, ctypes.byref(h)), ctx)
+        else:
+            check(library().lp_batch_create_tuned(ctx.handle, ctypes.byref(self.pipeline), self._ins, n,
+                                                  ctypes.byref(tuning), ctypes.byref(h)), ctx)
         self.handle = h
         self.n = n
+
+    @property
+    def tuning(self):
+        t = Tuning()
+        check(library().lp_batch_get_tuning(self.handle, ctypes.byref(t)), self.ctx)
+        return t
 
     @property
     def points(self):
@@ -730,7 +867,7 @@ class ServerDone(ctypes.Structure):
 
 class ServerStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "batches", "scans_in_batches",
-                                               "max_batch_seen", "pending", "device_bytes")]
+                                               "max_batch_seen", "pending", "device_bytes", "memory_waits")]
 
 
 class Server:

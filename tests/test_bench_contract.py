@@ -21,9 +21,34 @@ class FakeContext:
 
     def __init__(self, device=0):
         self.device = device
+        self.table = None
+
+    def set_tuning_table(self, table):
+        self.table = table
 
     def close(self):
         pass
+
+
+TUNED = {"parts": 2, "balance_parts": 1, "hull_cta_min": 256, "hull_ctas_per_sm": 2, "cell_ctas_per_sm": 8,
+         "jcp_ctas_per_sm": 8}
+
+
+class FakeTuning:
+    def __init__(self, d):
+        self.d = dict(d)
+
+    def as_dict(self):
+        return dict(self.d)
+
+
+class FakeKey:
+    def as_tuple(self):
+        return (1, 1, 1)
+
+
+def fake_autotune(ctx, xs, pipe, cfgs, rings, iters=3, table=None):
+    return FakeTuning(TUNED), {"trials": 14, "start_ms": 2.7, "best_ms": 2.5, "candidates": []}
 
 
 class FakeResult:
@@ -38,6 +63,7 @@ class FakeResult:
 class FakeBatch:
     def __init__(self, ctx, xs, pipe, cfgs, rings):
         self.xs = xs
+        self.tuning = FakeTuning(TUNED if ctx.table is not None else {})
 
     def execute(self):
         pass
@@ -68,6 +94,9 @@ def run_main(monkeypatch, lib, argv):
     monkeypatch.setattr(lp, "library", lambda: lib)
     monkeypatch.setattr(lp, "Context", FakeContext)
     monkeypatch.setattr(lp, "PreparedBatch", FakeBatch)
+    monkeypatch.setattr(lp, "autotune", fake_autotune)
+    monkeypatch.setattr(lp, "TuningTable", lambda: object())
+    monkeypatch.setattr(lp, "tuning_key", lambda xs, cfgs: FakeKey())
     monkeypatch.setattr(sys, "argv", ["bench.py"] + argv)
     for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
         monkeypatch.delenv(k, raising=False)
@@ -88,6 +117,10 @@ def test_bench_line_carries_the_contract(monkeypatch):
     assert abs(line["value"] - 4 * 3 / (3 * 2.5e-3)) < 1e-6  # scans over the summed event time
     assert abs(line["ms_per_step"] - 2.5) < 1e-9
     assert line["config"]["workload"] == "batch4_mixed"
+    # the autotuner ran first and the timed batch took its choice
+    a = line["autotune"]
+    assert a["chosen"] == TUNED and a["bucket"] == [1, 1, 1] and a["trials"] == 14
+    assert a["tuned_ms"] <= a["default_ms"] and line["config"]["tuning"] == TUNED
     e = line["e2e"]
     assert e["unit"] == "scans/s" and e["value"] > 0 and e["h2d_bytes_per_step"] > 0 and e["d2h_bytes_per_step"] > 0
     # the stand-in profile has four of our kernels; k_scan counts three launches (tile sums, look-back, apply)

@@ -77,9 +77,8 @@ def test_large_scan_waits_for_memory_then_completes(ctx):
     assert stats["batches"] >= 2, stats
     d_big, r_big = got[len(data) - 1]
     assert d_big.status == lp.LP_OK
-    # it could only start once a batch ahead of it had finished and returned its memory
-    first_done = min(got[i][0].latency_ms for i in range(len(small)))
-    assert d_big.queue_ms >= 0.5 * first_done, (d_big.queue_ms, first_done)
+    # it did not fit beside the batch ahead of it: the queue's head waited for that batch's memory
+    assert stats["memory_waits"] >= 1, stats
     for i, (x, ring, cfg) in enumerate(data):
         d, r = got[i]
         assert d.status == lp.LP_OK
