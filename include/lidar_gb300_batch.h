@@ -178,6 +178,9 @@ lp_status lp_server_create(int32_t device, const lp_pipeline_config* cfg, const 
 /* Queues one scan. The input buffers and `out` (with its buffers) must stay valid until the scan
  * is reported by lp_server_poll; results are written there exactly as lp_process_scan would. */
 lp_status lp_server_submit(lp_server* server, const lp_scan_input* scan, lp_scan_output* out, uint64_t tag);
+/* hold != 0: submitted scans queue but no new batch starts (running ones finish); 0 resumes. For
+ * a burst to be batched as it would arrive at once (and for the admission tests). */
+lp_status lp_server_hold(lp_server* server, int32_t hold);
 /* Finished scans since the last poll (up to capacity); waits up to wait_us for at least one. */
 lp_status lp_server_poll(lp_server* server, lp_server_done* done, uint32_t capacity, uint32_t* n_done,
                          uint32_t wait_us);

@@ -76,6 +76,7 @@ struct lp_server
     size_t pool_bytes = 0;
     std::map<size_t, size_t> free_regions;
     bool blocked = false; // the queue's head waits for memory: retry after a harvest
+    bool held = false;    // lp_server_hold: scans queue, no batch is admitted
 };
 
 namespace
@@ -321,7 +322,7 @@ void worker_loop(lp_server* sv)
         bool idle_slot = false;
         for (auto& s : sv->slots)
             idle_slot |= !s->busy;
-        if (!any_done && (sv->pending.empty() || !idle_slot || sv->blocked))
+        if (!any_done && (sv->pending.empty() || !idle_slot || sv->blocked || sv->held))
         {
             sv->cv.wait_for(lk, std::chrono::microseconds(500));
             continue;
@@ -334,7 +335,7 @@ void worker_loop(lp_server* sv)
                 lk.lock();
             }
         for (auto& s : sv->slots)
-            if (!s->busy && !sv->pending.empty() && !sv->blocked)
+            if (!s->busy && !sv->pending.empty() && !sv->blocked && !sv->held)
                 admit(sv, *s, lk);
     }
 }
@@ -401,6 +402,18 @@ lp_status lp_server_submit(lp_server* sv, const lp_scan_input* scan, lp_scan_out
             return LP_ERR_BAD_ARG;
         sv->pending.push_back(r);
         sv->stats.submitted += 1;
+    }
+    sv->cv.notify_all();
+    return LP_OK;
+}
+
+lp_status lp_server_hold(lp_server* sv, int32_t hold)
+{
+    if (!sv)
+        return LP_ERR_BAD_ARG;
+    {
+        std::lock_guard<std::mutex> lk(sv->m);
+        sv->held = hold != 0;
     }
     sv->cv.notify_all();
     return LP_OK;

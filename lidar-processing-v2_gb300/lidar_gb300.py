@@ -302,6 +302,7 @@ def _declare(lib):
         "lp_server_poll": (c.c_int32, [P, P, c.c_uint32, c.POINTER(c.c_uint32), c.c_uint32]),
         "lp_server_stats_get": (c.c_int32, [P, P]),
         "lp_server_destroy": (None, [P]),
+        "lp_server_hold": (c.c_int32, [P, c.c_int32]),
         "lp_tuning_default": (None, [P]),
         "lp_tuning_validate": (c.c_int32, [P]),
         "lp_tuning_key_of": (c.c_int32, [P, c.c_uint32, P]),
@@ -901,6 +902,9 @@ class Server:
             _, _, _, buf = self._live.pop(int(d.tag))
             out.append((d, buf.result() if d.status == LP_OK else None))
         return out
+
+    def hold(self, on=True):
+        check(library().lp_server_hold(self.handle, 1 if on else 0))
 
     def stats(self):
         s = ServerStats()

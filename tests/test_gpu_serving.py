@@ -46,7 +46,11 @@ def test_served_results_equal_alone(ctx):
 
 
 def scan_bytes(ctx, x, ring, cfg, pipe):
-    b = lp.PreparedBatch(ctx, [x], pipe, [cfg], [ring])
+    return batch_bytes(ctx, [(x, ring, cfg)], pipe)
+
+
+def batch_bytes(ctx, data, pipe):
+    b = lp.PreparedBatch(ctx, [d[0] for d in data], pipe, [d[2] for d in data], [d[1] for d in data])
     try:
         return b.device_bytes
     finally:
@@ -54,21 +58,23 @@ def scan_bytes(ctx, x, ring, cfg, pipe):
 
 
 def test_large_scan_waits_for_memory_then_completes(ctx):
-    """A pool that holds the largest scan but not that scan beside a running batch: the large scan,
-    submitted right behind a batch of small ones, waits for their memory instead of being refused,
-    then completes; every result equals the oracle."""
+    """A pool that holds the largest scan, and a batch of four small scans, but not both: the large
+    scan, queued right behind the small ones (the server held while the burst is submitted), waits
+    for their memory instead of being refused, then completes; every result equals the oracle."""
     pipe = lp.PipelineConfig.default()
     small = [T.synth_scan(5, i) for i in range(30, 34)]
     sizes = [(len(d[0]), k) for k, d in enumerate(T.synth_scan(5, i) for i in range(34, 48))]
     big = T.synth_scan(5, 34 + max(sizes)[1])
     need_big = scan_bytes(ctx, *big, pipe)
-    need_small = scan_bytes(ctx, *small[0], pipe)
-    budget = need_big + need_small // 2  # the big scan alone fits; beside any small batch it does not
+    need_small = batch_bytes(ctx, small, pipe)
+    budget = max(need_big, need_small) + min(need_big, need_small) // 2  # either alone fits, not both
     server = lp.Server(0, pipe, memory_budget_bytes=budget, max_batch_scans=4, slots=2)
     try:
         data = small + [big]
+        server.hold()  # the burst queues as a whole: the small batch starts first, the big scan is next
         for i, (x, ring, cfg) in enumerate(data):
             server.submit(x, ring, cfg, i)
+        server.hold(False)
         got = drain(server, len(data))
         stats = server.stats()
     finally:
