@@ -1145,72 +1145,65 @@ __device__ __forceinline__ uint8_t pre_view(uint8_t st)
     return (st == PX_GROUND) ? V_G : ((st == PX_OBSTACLE) ? V_O : V_U);
 }
 
-// A queued pixel's vote (segmenter.cpp:585-631) as a 9-state transition map of the in-row chain:
-// for every outcome pair (a, b) of the queued pixels at columns c-1 and c-2 (symbolic where
-// sym_a / sym_b), the label sums g and o are accumulated in slot order exactly like the reference
-// (skipping a slot adds nothing), outcome obstacle iff o > g; then the map (state = 3 x + a) is
-// built for the column gap to the previous queued pixel.
+// A queued pixel's vote (segmenter.cpp:585-631) as a 9-state transition map of the in-row chain.
+// The reference sums, in slot order, the normalised weights of the slots labelled ground into g
+// and of those labelled obstacle into o (a slot with another label adds nothing), and votes
+// obstacle iff o > g. Here both sums run as one pair (a slot adds (w, 0), (0, w) or (0, 0);
+// weights and sums are never negative, so adding +0 is exactly the reference's skip, and each half
+// rounds like its scalar addition in the same order). The labels at slots 10 (column c-2) and 11
+// (c-1) are symbolic where those are queued pixels of the same row (their outcomes, the chain's
+// state; sym_b / sym_a). g after slot 11 is one of four values (whether slot 10, then slot 11, is
+// ground) and so is o, so four chains over slots 12-23 give the final sums for all nine label
+// pairs of slots 10 and 11 (an outcome table of 2 bits per pair); each chain state reads the
+// pair its labels select. The map (state = 3 x + a) is built for the column gap to the previous
+// queued pixel.
 __device__ __forceinline__ unsigned long long vote_map(const float* wn, const uint8_t* lb, bool sym_a, bool sym_b,
                                                        bool live, int32_t gap)
 {
-    uint32_t outc = 0u; // outcome of vote table entry (a, b) in bits 2 (3a + b); V_U when not live
-    if (live)
+    auto gw = [](uint8_t l, float w) { return make_float2(l == V_G ? w : 0.0F, l == V_O ? w : 0.0F); };
+    float2 head = make_float2(0.0F, 0.0F);
+#pragma unroll
+    for (int k = 0; k < 10; ++k)
+        head = __fadd2_rn(head, gw(lb[k], wn[k]));
+    // start i (bit 0: slot 10 adds, bit 1: slot 11 adds): g in .x, o in .y, each slot added in order
+    float2 v[4];
+    v[0] = head;
+    v[1] = __fadd2_rn(head, make_float2(wn[10], wn[10]));
+    v[2] = __fadd2_rn(head, make_float2(wn[11], wn[11]));
+    v[3] = __fadd2_rn(v[1], make_float2(wn[11], wn[11]));
+#pragma unroll
+    for (int k = 12; k < 24; ++k)
     {
-        // (g, o) as one packed pair: a slot adds (w, 0), (0, w) or (0, 0); weights and sums are
-        // never negative, so adding +0 is exactly the reference's skip, and each half rounds like
-        // its scalar addition in the same slot order
-        auto gw = [&](uint8_t l, float w) {
-            return make_float2(l == V_G ? w : 0.0F, l == V_O ? w : 0.0F);
-        };
-        float2 head = make_float2(0.0F, 0.0F);
+        const float2 d = gw(lb[k], wn[k]);
 #pragma unroll
-        for (int k = 0; k < 10; ++k)
-            head = __fadd2_rn(head, gw(lb[k], wn[k]));
-        float2 tail[12];
-#pragma unroll
-        for (int k = 12; k < 24; ++k)
-            tail[k - 12] = gw(lb[k], wn[k]);
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int bb = 0; bb < 3; ++bb)
-            {
-                const uint8_t l10 = sym_b ? static_cast<uint8_t>(bb) : lb[10];
-                const uint8_t l11 = sym_a ? static_cast<uint8_t>(a) : lb[11];
-                float2 v = __fadd2_rn(head, gw(l10, wn[10]));
-                v = __fadd2_rn(v, gw(l11, wn[11]));
-#pragma unroll
-                for (int k = 0; k < 12; ++k)
-                    v = __fadd2_rn(v, tail[k]);
-                outc |= static_cast<uint32_t>((v.y > v.x) ? V_O : V_G) << (2 * (3 * a + bb));
-            }
+        for (int i = 0; i < 4; ++i)
+            v[i] = __fadd2_rn(v[i], d);
     }
+    // outcome of label pair (l10, l11) at bits 2 (3 l10 + l11): the starts it selects are fixed
+    uint32_t otab = 0u;
+#pragma unroll
+    for (int l10 = 0; l10 < 3; ++l10)
+#pragma unroll
+        for (int l11 = 0; l11 < 3; ++l11)
+        {
+            const int ig = (l10 == V_G ? 1 : 0) | (l11 == V_G ? 2 : 0);
+            const int io = (l10 == V_O ? 1 : 0) | (l11 == V_O ? 2 : 0);
+            otab |= static_cast<uint32_t>((v[io].y > v[ig].x) ? V_O : V_G) << (2 * (3 * l10 + l11));
+        }
+    if (!live)
+        otab = 0u; // V_U whatever the labels
+    const int g1 = gap == 1, g2 = gap == 2;
     unsigned long long t = 0ull;
 #pragma unroll
     for (int sidx = 0; sidx < 9; ++sidx)
     {
         const int a = sidx / 3, bb = sidx % 3;
-        int ap, bp, an;
-        if (gap == 1)
-        {
-            ap = a;
-            bp = bb;
-            an = a;
-        }
-        else if (gap == 2)
-        {
-            ap = V_U;
-            bp = a;
-            an = V_U;
-        }
-        else
-        {
-            ap = V_U;
-            bp = V_U;
-            an = V_U;
-        }
-        const int x = static_cast<int>((outc >> (2 * (3 * ap + bp))) & 3u); // V_U when sum ~ 0
-        t |= static_cast<unsigned long long>(3 * x + an) << (4 * sidx);
+        const int ap = g1 ? a : V_U;
+        const int bp = g1 ? bb : (g2 ? a : V_U);
+        const int l10 = sym_b ? bp : lb[10];
+        const int l11 = sym_a ? ap : lb[11];
+        const uint32_t x = (otab >> (2 * (3 * l10 + l11))) & 3u;
+        t |= static_cast<unsigned long long>(3u * x + static_cast<uint32_t>(ap)) << (4 * sidx);
     }
     return t;
 }
@@ -1411,6 +1404,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
     __shared__ float run_w[24];
     __shared__ uint8_t run_l[24];
     __shared__ unsigned long long wmaps[8];
+    __shared__ unsigned long long rmap[256]; // a row's maps by position (rows of at most 256 pixels)
     // final colour (V_U/V_G/V_O) of the queued pixels of the last three rows, by column: the
     // labels a pixel reads from queued pixels above it, without a global load (images up to
     // kFinRingW columns; wider ones read the pixel states)
@@ -1536,6 +1530,10 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
         }
 
         // ---- per queued pixel: vote table -> 9-state transition map --------------------------
+        const int32_t fr2 = (h + 1) % 3, fr1 = (h + 2) % 3; // final-colour rows of h-2 and h-1
+        // Consecutive chunks of pixels per thread (one pixel per thread in rows of at most 256
+        // pixels, whose maps stay in shared memory).
+        const bool spread = m <= blockDim.x;
         const uint32_t chunk = (m + blockDim.x - 1) / blockDim.x;
         const uint32_t j0 = threadIdx.x * chunk;
         const uint32_t j1 = min(m, j0 + chunk);
@@ -1562,6 +1560,37 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                 static_cast<unsigned long long>(__float_as_uint(tail.y)) |
                 (static_cast<unsigned long long>(__float_as_uint(tail.z)) << 32);
             unsigned long long t;
+            if (h >= 2 && h + 2 < H && c >= 2 && c + 2 < W)
+            {
+                // the window lies inside the image: labels from the codes and the final colours
+                // above (no stale slot)
+                const bool live = fabsf(sum) > FLT_EPSILON;
+                uint8_t lb[24];
+                bool sym_a = false, sym_b = false;
+#pragma unroll
+                for (int k = 0; k < 24; ++k)
+                {
+                    const uint32_t code = static_cast<uint32_t>((codes >> (2 * k)) & 3ull);
+                    if (code != 3u)
+                        lb[k] = static_cast<uint8_t>(code);
+                    else if (k < 10)
+                    {
+                        const int32_t hh = h + jcp_dh(k), ww = c + jcp_dw(k);
+                        lb[k] = ring ? fin[k < 5 ? fr2 : fr1][ww] : final_view(st[hh * W + ww]);
+                    }
+                    else
+                    {
+                        lb[k] = V_U; // same row, left of c, queued: the chain's state
+                        if (k == 11)
+                            sym_a = true;
+                        else
+                            sym_b = true;
+                    }
+                }
+                const int32_t gap = (j > 0) ? (c - static_cast<int32_t>(staged ? scols[j - 1] : cols[j - 1])) : 1000;
+                t = vote_map(wn, lb, sym_a, sym_b, live, gap);
+            }
+            else
             {
                 uint8_t nsv[10]; // final colour of the queued pixels above (code 3: inside the image)
 #pragma unroll
@@ -1625,25 +1654,33 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                 }
                 const int32_t gap = (j > 0) ? (c - static_cast<int32_t>(staged ? scols[j - 1] : cols[j - 1])) : 1000;
                 t = vote_map(wn, lb, sym_a, sym_b, live, gap);
-                b.jmap[row_base + j] = t;
             }
+            if (spread)
+                rmap[j] = t;
+            else
+                b.jmap[row_base + j] = t;
             agg = map_compose(t, agg);
         }
 
         // ---- block-wide exclusive scan of the thread aggregates (composition order) -----------
+        // only the warps holding pixels scan (the others' aggregates are the identity)
+        const uint32_t wused = ((m + chunk - 1) / chunk + 31u) / 32u;
         unsigned long long incl = agg;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
+        if (warp < wused)
         {
-            const unsigned long long other = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= static_cast<uint32_t>(o))
-                incl = map_compose(incl, other);
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const unsigned long long other = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= static_cast<uint32_t>(o))
+                    incl = map_compose(incl, other);
+            }
         }
         if (lane == 31)
             wmaps[warp] = incl;
         __syncthreads();
         unsigned long long wpre = map_identity();
-        for (uint32_t w2 = 0; w2 < warp; ++w2)
+        for (uint32_t w2 = 0; w2 < min(warp, wused); ++w2)
             wpre = map_compose(wmaps[w2], wpre);
         unsigned long long excl = __shfl_up_sync(0xffffffffu, incl, 1);
         if (lane == 0)
@@ -1653,7 +1690,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
         uint32_t state = static_cast<uint32_t>(excl & 0xfull);
         for (uint32_t j = j0; j < j1; ++j)
         {
-            state = static_cast<uint32_t>((b.jmap[row_base + j] >> (4 * state)) & 0xfull);
+            state = static_cast<uint32_t>(((spread ? rmap[j] : b.jmap[row_base + j]) >> (4 * state)) & 0xfull);
             const uint32_t x = state / 3;
             if (x != V_U)
                 st[h * W + cols[j]] = (x == V_O) ? PX_RES_O : PX_RES_G;
