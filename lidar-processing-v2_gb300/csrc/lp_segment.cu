@@ -1659,7 +1659,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                 rmap[j] = t;
             else
                 b.jmap[row_base + j] = t;
-            agg = map_compose(t, agg);
+            agg = (j == j0) ? t : map_compose(t, agg);
         }
 
         // ---- block-wide exclusive scan of the thread aggregates (composition order) -----------
@@ -1712,7 +1712,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
             }
             run_l[threadIdx.x] = l;
         }
-        __syncthreads();
+        // no barrier here: the next row's first barrier orders these writes before its readers
         cur ^= 1;
     }
 }
