@@ -100,7 +100,7 @@ lp_status plan(lp_context* ctx, lp_batch& B)
     hb = BatchHost{};
     hb.nscan = static_cast<int>(R.scans.size());
     hb.any_noise = (R.stages & ST_NOISE) != 0;
-    uint64_t pt = 0, pix = 0, row = 0, tile = 0, slice = 0, cell = 0, nearc = 0, hash = 0, cl = 0;
+    uint64_t pt = 0, pix = 0, row = 0, tile = 0, slice = 0, cell = 0, nearc = 0, hash = 0, cl = 0, queue = 0;
     const bool seg = (R.stages & ST_SEG) != 0;
     for (const ScanIn& in : R.scans)
     {
@@ -151,6 +151,8 @@ lp_status plan(lp_context* ctx, lp_batch& B)
             if (sd.compute_ring && sd.first_ring < 0)
                 sd.first_ring = c.image_height - 1;
             pix += static_cast<uint64_t>(sd.H) * static_cast<uint64_t>(sd.W);
+            // a queued pixel of the vote holds a point: at most min(pixels, points) per scan
+            queue += std::min<uint64_t>(static_cast<uint64_t>(sd.H) * static_cast<uint64_t>(sd.W), in.n);
             row += static_cast<uint64_t>(sd.H);
             cell += static_cast<uint64_t>(sd.nslice) * static_cast<uint64_t>(sd.nrad);
             slice += static_cast<uint64_t>(sd.nslice);
@@ -200,6 +202,7 @@ lp_status plan(lp_context* ctx, lp_batch& B)
     b.nrows = static_cast<uint32_t>(row);
     b.nhash = static_cast<uint32_t>(hash);
     b.ncl = static_cast<uint32_t>(cl);
+    b.jq_cap = static_cast<uint32_t>(queue);
     return LP_OK;
 }
 
@@ -303,11 +306,12 @@ size_t carve(lp_batch& B, char* base)
         put(b.pix_state, b.npix);
         put(b.row_cols, b.npix);
         put(b.row_cnt, b.nrows + 1); // [nrows]: queued pixels of the batch
-        put(b.jq, b.npix);
-        put(b.jw, static_cast<size_t>(b.npix) * kJwStride);
-        put(b.jn, static_cast<size_t>(b.npix) * kJwStride);
+        put(b.row_q0, b.nrows);
+        put(b.jq, b.jq_cap + 1);
+        put(b.jw, static_cast<size_t>(b.nrows) * 3u * kJwStride); // the last three queued pixels of each row
+        put(b.jn, (static_cast<size_t>(b.jq_cap) + 1) * kJwStride);
         put(b.jrow, static_cast<size_t>(b.nrows) * kJrowWords);
-        put(b.jmap, b.npix);
+        put(b.jmap, b.jq_cap + 1);
         if (R.stages & ST_IMAGE)
             put(B.d_image, static_cast<size_t>(b.npix) * 3);
     }

@@ -134,8 +134,10 @@ struct BatchDev
     uint16_t* row_cols;        // per pixel slot: intersection columns of the row in order
     uint4* jq;            // flat list of the batch's queued pixels: (image row, position | column << 16, point, scan)
     uint32_t* row_cnt;         // per global row
-    float* jw;                 // per entry: 24 fresh weights + sum (stride kJwStride)
-    float* jn;                 // per entry: 24 normalized weights, sum, slot label codes (stride kJwStride)
+    float* jw;                 // per row, its last three queued pixels: 24 fresh weights + sum (stride kJwStride)
+    float* jn;                 // per queued pixel (flat queue position): 24 normalized weights, sum, slot label codes
+    uint32_t* row_q0;          // per image row: its first position in the flat queue
+    uint32_t jq_cap;           // queue capacity: sum over scans of min(pixels, points)
     uint32_t* jrow;            // per image row: kJrowWords words (lastq, stale-buffer update)
     unsigned long long* jmap;  // per entry: 9-state transition map
 

@@ -1101,8 +1101,16 @@ __global__ void __launch_bounds__(256) k_dilate_rows(BatchDev b)
             run += wcount[k];
         }
         b.row_cnt[r] = run;
-        // the row's segment of the flat list of queued pixels (row_cnt[nrows] counts them)
+        // the row's segment of the flat list of queued pixels (row_cnt[nrows] counts them); the
+        // capacity bound (a queued pixel holds a point) cannot be exceeded, checked all the same
         qbase = run ? atomicAdd(&b.row_cnt[b.nrows], run) : 0u;
+        if (qbase + run > b.jq_cap)
+        {
+            raise_err(&b.state[s], ERR_INTERNAL);
+            b.row_cnt[r] = 0u;
+            qbase = 0u;
+        }
+        b.row_q0[r] = qbase;
     }
     __syncthreads();
     // pass 2: queue entries in column order (this row's states now hold the intersections)
@@ -1117,7 +1125,8 @@ __global__ void __launch_bounds__(256) k_dilate_rows(BatchDev b)
             const uint32_t j = pos + static_cast<uint32_t>(__popc(m & ((1u << lane) - 1u)));
             b.row_cols[row_base + j] = static_cast<uint16_t>(w);
             // (row, position | column << 16, the pixel's point, scan): the weights pass starts here
-            b.jq[qbase + j] = make_uint4(r, j | (static_cast<uint32_t>(w) << 16),
+            if (qbase + j < b.jq_cap)
+                b.jq[qbase + j] = make_uint4(r, j | (static_cast<uint32_t>(w) << 16),
                                          static_cast<uint32_t>(b.pix_map[sd.pix_off + static_cast<uint32_t>(h * W + w)]),
                                          static_cast<uint32_t>(s));
         }
@@ -1223,7 +1232,7 @@ __global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
     // one warp per queued pixel of the batch's flat list (rows of any length spread over the whole
     // grid), lane k = kernel slot k (lanes 24-31 idle); the weights are summed by lane 0 in slot
     // order, as the reference's loop adds them
-    const uint32_t total = b.row_cnt[b.nrows];
+    const uint32_t total = min(b.row_cnt[b.nrows], b.jq_cap);
     const uint32_t lane = lane_id();
     const int k = static_cast<int>(lane);
     const int32_t dh = jcp_dh(k), dw = jcp_dw(k);
@@ -1280,8 +1289,9 @@ __global__ void __launch_bounds__(256) k_jcp_weights(BatchDev b)
         // the raw record is only read for the row's last three queued pixels (the stale-slot
         // sources of later rows and of the row's right border)
         const bool raw = j + 3u >= m;
-        float* out = b.jw + static_cast<size_t>(row_base + j) * kJwStride;
-        float* nrm = b.jn + static_cast<size_t>(row_base + j) * kJwStride;
+        // raw records: the row's last three positions, slot j + 3 - m; normalised: by queue position
+        float* out = raw ? b.jw + (static_cast<size_t>(r) * 3u + (j + 3u - m)) * kJwStride : nullptr;
+        float* nrm = b.jn + static_cast<size_t>(q) * kJwStride;
         if (k < 24)
         {
             if (raw)
@@ -1345,7 +1355,7 @@ __global__ void __launch_bounds__(256) k_jcp_rowrec(BatchDev b)
         const int32_t q = lq[dw > 0 ? dw : 0];
         if (q >= 0 && static_cast<int32_t>(cols[q]) >= (dw < 0 ? -dw : 0))
         {
-            qw = b.jw[static_cast<size_t>(row_base + q) * kJwStride + k];
+            qw = b.jw[(static_cast<size_t>(r) * 3u + static_cast<uint32_t>(q + 3 - static_cast<int32_t>(m))) * kJwStride + k];
             info = V_U;
             if (qw != 0.0F)
             {
@@ -1443,7 +1453,8 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
         const uintptr_t ce = (reinterpret_cast<uintptr_t>(b.row_cols + rb + mm) + 15) & ~static_cast<uintptr_t>(15);
         unsigned char* dst = stage + bf * kStageBytes;
         mbar_expect_tx(&mbar[bf], rec_bytes + static_cast<uint32_t>(ce - ca) + kJrowWords * 4u);
-        bulk_g2s(dst, b.jn + static_cast<size_t>(rb) * kJwStride, rec_bytes, &mbar[bf]);
+        bulk_g2s(dst, b.jn + static_cast<size_t>(b.row_q0[sd.row_off + static_cast<uint32_t>(hh)]) * kJwStride, rec_bytes,
+                 &mbar[bf]);
         bulk_g2s(dst + kStageRecBytes, reinterpret_cast<const void*>(ca), static_cast<uint32_t>(ce - ca), &mbar[bf]);
         bulk_g2s(dst + kStageRecBytes + kStageColBytes,
                  b.jrow + static_cast<size_t>(sd.row_off + static_cast<uint32_t>(hh)) * kJrowWords, kJrowWords * 4u,
@@ -1484,6 +1495,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
             continue;
         const uint32_t row_base = sd.pix_off + static_cast<uint32_t>(h * W);
         const uint16_t* cols = b.row_cols + row_base;
+        const uint32_t q0 = b.row_q0[r]; // the row's first position in the flat queue
         const bool staged = st_row[cur] == h;
         const float4* srec = reinterpret_cast<const float4*>(stage + cur * kStageBytes);
         const uint16_t* scols = reinterpret_cast<const uint16_t*>(stage + cur * kStageBytes + kStageRecBytes) + st_coff[cur];
@@ -1543,7 +1555,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
             // the pixel's queue entry and normalised record: staged in shared memory, or loaded
             const int32_t c = staged ? scols[j] : cols[j];
             const float4* rec = staged ? srec + 7u * j
-                                       : reinterpret_cast<const float4*>(b.jn + static_cast<size_t>(row_base + j) * kJwStride);
+                                       : reinterpret_cast<const float4*>(b.jn + static_cast<size_t>(q0 + j) * kJwStride);
             float wn[24];
 #pragma unroll
             for (int q = 0; q < 6; ++q)
@@ -1620,7 +1632,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
                             const int32_t q = (dw > 0 && hh >= 0 && hh < H) ? lastq[qd] : -1;
                             if (q >= 0)
                             {
-                                const float qw = b.jw[static_cast<size_t>(row_base + q) * kJwStride + k];
+                                const float qw = b.jw[(static_cast<size_t>(r) * 3u + static_cast<uint32_t>(q + 3 - static_cast<int32_t>(m))) * kJwStride + k];
                                 wv = qw;
                                 if (qw != 0.0F)
                                 {
@@ -1658,7 +1670,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
             if (spread)
                 rmap[j] = t;
             else
-                b.jmap[row_base + j] = t;
+                b.jmap[q0 + j] = t;
             agg = (j == j0) ? t : map_compose(t, agg);
         }
 
@@ -1690,7 +1702,7 @@ __global__ void __launch_bounds__(256) k_jcp_rows(BatchDev b)
         uint32_t state = static_cast<uint32_t>(excl & 0xfull);
         for (uint32_t j = j0; j < j1; ++j)
         {
-            state = static_cast<uint32_t>(((spread ? rmap[j] : b.jmap[row_base + j]) >> (4 * state)) & 0xfull);
+            state = static_cast<uint32_t>(((spread ? rmap[j] : b.jmap[q0 + j]) >> (4 * state)) & 0xfull);
             const uint32_t x = state / 3;
             if (x != V_U)
                 st[h * W + cols[j]] = (x == V_O) ? PX_RES_O : PX_RES_G;
