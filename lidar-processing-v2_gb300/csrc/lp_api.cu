@@ -358,6 +358,10 @@ size_t carve(lp_batch& B, char* base)
         put(b.hs_pairs, static_cast<size_t>(4) * N + 16ull * b.ncl + 16);
         put(b.queue, 8);
         put(b.tie_list, b.ncl + 1);
+        put(b.pre_items, N / 4096u + b.ncl + 1);
+        put(b.pre_ext, 16ull * b.ncl + 16);
+        put(b.pre_pk, 16ull * b.ncl + 16);
+        put(b.pre_nact, b.ncl + 1);
     }
     return c.off + 4096;
 }

@@ -185,7 +185,11 @@ struct BatchDev
     double2* hs_pts;      // hull vertices as FP64, at cl_start
     int2* hs_pairs;       // antipodal pairs, at 4 * cl_start + 16 * cluster
     uint32_t* queue;      // [0] clusters in the batch, [1] hull work-queue head, [4] tie clusters
-    uint32_t* tie_list;   // clusters whose hull has a vertex with an identical point (reference tie order)
+    uint32_t* tie_list;
+    uint2* pre_items;          // (cluster, chunk) items of the large clusters' member passes
+    unsigned long long* pre_ext;  // per cluster: its 16 direction extremes (packed keys)
+    unsigned long long* pre_pk;   // per cluster: the farthest member outside each edge of the first polygon
+    uint32_t* pre_nact;        // per cluster: members not inside the first polygon (listed in the chain scratch)   // clusters whose hull has a vertex with an identical point (reference tie order)
 
     // ---- DROR (reference kd-tree replay, lp_kdtree.cu) ------------------------------------------
     float4* kt;                // per input point: tree node record by position (x, y, z, subtree size bits)

@@ -1193,6 +1193,159 @@ struct Extremes16
     }
 };
 
+// Large clusters: the two passes over every member (the 16 direction extremes, the first
+// refinement round against the polygon they span) run grid-wide before the hull kernel, in
+// (cluster, chunk of kPreChunk members) items, so the cluster's CTA starts at the second round.
+// Both reduce exactly (packed-key maxima; the survivors are a set, listed in any order), with
+// the hull kernel's expressions, so the hull kernel continues from the same state.
+constexpr uint32_t kPreMin = 8192;
+constexpr uint32_t kPreChunk = 4096;
+
+__device__ __forceinline__ void hull_dirs(float2* dirs)
+{
+    if (threadIdx.x < kDirs)
+    {
+        const float a = 6.28318530717958647692f * static_cast<float>(threadIdx.x) / kDirs;
+        dirs[threadIdx.x] = make_float2(cosf(a), sinf(a));
+    }
+}
+
+// The first polygon from the extremes' packed keys: extreme members in direction order (counter-
+// clockwise), repeats dropped. Thread 0.
+__device__ int first_polygon(const float2* xy, uint32_t n, const unsigned long long* best, float2* poly)
+{
+    int np = 0;
+    uint32_t prev = 0xffffffffu;
+    for (int d = 0; d < kDirs; ++d)
+    {
+        const uint32_t i = static_cast<uint32_t>(best[d] & 0xffffffffull);
+        if (n > 0 && i != prev)
+        {
+            poly[np++] = xy[i];
+            prev = i;
+        }
+    }
+    if (np > 1 && poly[np - 1].x == poly[0].x && poly[np - 1].y == poly[0].y)
+        --np;
+    return np;
+}
+
+__global__ void __launch_bounds__(256) k_hull_pre_ext(BatchDev b)
+{
+    __shared__ float2 dirs[kDirs];
+    __shared__ unsigned long long ext[kDirs][8];
+    hull_dirs(dirs);
+    __syncthreads();
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    const uint32_t nitems = b.queue[6];
+    for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x)
+    {
+        const uint2 w = b.pre_items[it];
+        const uint32_t g = w.x, start = b.cl_start[g], n = b.cl_cnt[g];
+        const uint32_t i0 = w.y * kPreChunk, i1 = min(n, i0 + kPreChunk);
+        const float2* xy = b.mxy + start;
+        Extremes16 ex;
+        ex.init();
+        for (uint32_t i = i0 + threadIdx.x; i < i1; i += blockDim.x)
+        {
+            const float2 q = xy[i];
+            ex.add(dirs, q.x, q.y, i);
+        }
+#pragma unroll
+        for (int d = 0; d < kDirs; ++d)
+        {
+            const unsigned long long v = warp_max64(ex.key(d));
+            if (lane == 0)
+                ext[d][warp] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < kDirs)
+        {
+            unsigned long long best = ext[threadIdx.x][0];
+            for (uint32_t k = 1; k < (blockDim.x >> 5); ++k)
+                best = ext[threadIdx.x][k] > best ? ext[threadIdx.x][k] : best;
+            atomicMax(&b.pre_ext[16ull * g + threadIdx.x], best);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_hull_pre_ref(BatchDev b)
+{
+    __shared__ float2 poly[kDirs];
+    __shared__ float4 erec[kDirs];
+    __shared__ float2 emar[kDirs];
+    __shared__ unsigned long long pkey[kDirs];
+    __shared__ int npoly;
+    const uint32_t lane = lane_id();
+    const uint32_t nitems = b.queue[6];
+    for (uint32_t it = blockIdx.x; it < nitems; it += gridDim.x)
+    {
+        const uint2 w = b.pre_items[it];
+        const uint32_t g = w.x, start = b.cl_start[g], n = b.cl_cnt[g];
+        const uint32_t i0 = w.y * kPreChunk, i1 = min(n, i0 + kPreChunk);
+        const float2* xy = b.mxy + start;
+        if (threadIdx.x == 0)
+            npoly = first_polygon(xy, n, b.pre_ext + 16ull * g, poly);
+        __syncthreads();
+        const int np = npoly;
+        if (np >= 3)
+        {
+            for (int e = threadIdx.x; e < np; e += blockDim.x)
+            {
+                pkey[e] = 0ull;
+                const float2 a = poly[e], c = poly[(e + 1 == np) ? 0 : e + 1];
+                const float ex = c.x - a.x, ey = c.y - a.y;
+                const float l1 = fabsf(ex) + fabsf(ey);
+                erec[e] = make_float4(a.x, a.y, ex, ey);
+                emar[e] = make_float2(1e-5f * l1, 1e-6f * l1);
+            }
+            __syncthreads();
+            uint32_t* act0 = reinterpret_cast<uint32_t*>(b.hs_stack + 2ull * start + 2ull * g);
+            for (uint32_t base = i0; base < i1; base += blockDim.x)
+            {
+                const uint32_t i = base + threadIdx.x;
+                bool keep = false;
+                if (i < i1)
+                {
+                    // the hull kernel's round-0 test: strictly inside every edge by the margin, and
+                    // the farthest member outside each edge
+                    const float2 q = xy[i];
+                    bool in = true;
+                    for (int e = 0; e < np; ++e)
+                    {
+                        const float4 r = erec[e];
+                        const float2 mg = emar[e];
+                        const float qx = q.x - r.x, qy = q.y - r.y;
+                        const float cr = r.z * qy - r.w * qx;
+                        const float aq = fabsf(qx) + fabsf(qy);
+                        if (!(cr > mg.x * aq))
+                            in = false;
+                        if (cr < -(mg.y * aq))
+                        {
+                            const unsigned long long key = fkey_payload(-cr, i);
+                            if (key > pkey[e])
+                                atomicMax(&pkey[e], key);
+                        }
+                    }
+                    keep = !in;
+                }
+                const uint32_t mask = __ballot_sync(0xffffffffu, keep);
+                uint32_t at = 0;
+                if (lane == 0 && mask)
+                    at = atomicAdd(&b.pre_nact[g], static_cast<uint32_t>(__popc(mask)));
+                at = __shfl_sync(0xffffffffu, at, 0);
+                if (keep)
+                    act0[at + static_cast<uint32_t>(__popc(mask & ((1u << lane) - 1u)))] = i;
+            }
+            __syncthreads();
+            if (threadIdx.x < static_cast<uint32_t>(np) && pkey[threadIdx.x] != 0ull)
+                atomicMax(&b.pre_pk[16ull * g + threadIdx.x], pkey[threadIdx.x]);
+        }
+        __syncthreads();
+    }
+}
+
 // Cluster g of scan s: z range, hull (local indices into hull_tmp at cl_start), boxes.
 __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int compute_obb)
 {
@@ -1215,9 +1368,10 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
     const int32_t a2 = static_cast<int32_t>(start & 1u);
     const float4* xv = reinterpret_cast<const float4*>(b.mxy + (start - static_cast<uint32_t>(a2)));
     const uint32_t npair = (n + static_cast<uint32_t>(a2) + 1u) / 2u;
+    const bool pre = n > kPreMin; // extremes and round 0 came from the grid-wide passes
     Extremes16 ex;
     ex.init();
-    for (uint32_t v0 = threadIdx.x; v0 < npair; v0 += 4u * blockDim.x)
+    for (uint32_t v0 = threadIdx.x; !pre && v0 < npair; v0 += 4u * blockDim.x)
     {
         float4 q[4];
 #pragma unroll
@@ -1236,15 +1390,23 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
                 ex.add(sm.dirs, q[u].z, q[u].w, static_cast<uint32_t>(i + 1));
         }
     }
-    unsigned long long ext[kDirs];
-#pragma unroll
-    for (int d = 0; d < kDirs; ++d)
-        ext[d] = warp_max64(ex.key(d));
-    if (lane == 0)
+    if (!pre)
     {
+        unsigned long long ext[kDirs];
 #pragma unroll
         for (int d = 0; d < kDirs; ++d)
-            sm.ext[d][warp] = ext[d];
+            ext[d] = warp_max64(ex.key(d));
+        if (lane == 0)
+        {
+#pragma unroll
+            for (int d = 0; d < kDirs; ++d)
+                sm.ext[d][warp] = ext[d];
+        }
+    }
+    else if (threadIdx.x < kDirs * (kHullThreads / 32))
+    {
+        const uint32_t d = threadIdx.x / (kHullThreads / 32), w = threadIdx.x % (kHullThreads / 32);
+        sm.ext[d][w] = (w == 0) ? b.pre_ext[16ull * g + d] : 0ull;
     }
     __syncthreads();
     if (threadIdx.x == 0)
@@ -1358,7 +1520,16 @@ __device__ void hull_one(const BatchDev& b, HullSmem& sm, uint32_t g, int s, int
             if (ok1 && !in1)
                 act[nxt][atomicAdd(&sm.ncand, 1)] = i1;
         };
-        if (cur < 0)
+        if (cur < 0 && pre)
+        {
+            // round 0 ran grid-wide against this polygon: its survivors are in act[0], and the
+            // farthest member outside each edge is in the pass's record
+            for (int e = threadIdx.x; e < np; e += blockDim.x)
+                sm.pkey[e] = b.pre_pk[16ull * g + e];
+            if (threadIdx.x == 0)
+                sm.ncand = static_cast<int>(b.pre_nact[g]);
+        }
+        else if (cur < 0)
         {
             // all members: the aligned pairs of step 1, one 16-byte load each
             for (uint32_t v = threadIdx.x; v < npair; v += blockDim.x)
@@ -1979,10 +2150,25 @@ __global__ void k_hull_worklist(BatchDev b, uint32_t* work)
     const int s = find_scan(b.nscan, g, [&](int q) { return b.scans[q].cl_off; });
     if (g - b.scans[s].cl_off >= b.state[s].n_clusters)
         return;
-    if (b.cl_cnt[g] > b.hull_cta_min) // hull_cta_min <= kBigCluster: the warp path's limit
+    const uint32_t n = b.cl_cnt[g];
+    if (n > b.hull_cta_min) // hull_cta_min <= kBigCluster: the warp path's limit
         work[atomicAdd(&b.queue[2], 1u)] = g;
     else
         work[b.ncl - 1u - atomicAdd(&b.queue[3], 1u)] = g;
+    if (n > kPreMin)
+    {
+        // the grid-wide member passes: records cleared, one item per kPreChunk members (queue[6])
+        for (int d = 0; d < 16; ++d)
+        {
+            b.pre_ext[16ull * g + d] = 0ull;
+            b.pre_pk[16ull * g + d] = 0ull;
+        }
+        b.pre_nact[g] = 0u;
+        const uint32_t nch = (n + kPreChunk - 1u) / kPreChunk;
+        const uint32_t at = atomicAdd(&b.queue[6], nch);
+        for (uint32_t c = 0; c < nch; ++c)
+            b.pre_items[at + c] = make_uint2(g, c);
+    }
 }
 
 __device__ __forceinline__ uint32_t work_item(const BatchDev& b, const uint32_t* work, uint32_t w)
@@ -2368,6 +2554,8 @@ void launch_polygons(Launcher& L, const BatchDev& b, const BatchHost& hb, int co
     // the work list reuses the cluster fill counters' scratch (cl_fill, ncl + 1 entries)
     uint32_t* work = b.cl_fill;
     LP_LAUNCH(L, k_hull_worklist, div_up(b.ncl, 256u), 256, b, work);
+    LP_LAUNCH(L, k_hull_pre_ext, static_cast<uint32_t>(sm_count()) * 4u, 256, b);
+    LP_LAUNCH(L, k_hull_pre_ref, static_cast<uint32_t>(sm_count()) * 4u, 256, b);
     const int sms = sm_count();
     LP_LAUNCH_SMEM(L, k_hull, static_cast<uint32_t>(sms) * hb.hull_ctas_per_sm, kHullThreads, kHullDynSmem, b, compute_obb,
                    static_cast<const uint32_t*>(work));
