@@ -319,9 +319,18 @@ __device__ __forceinline__ uint32_t hash_lookup(const BatchDev& b, const ScanDev
     return kEmpty;
 }
 
-// Neighbour offsets (clusterer.hpp:101-105): all 26 (dr, da, de) != (0, 0, 0).
-__device__ __forceinline__ void k_uf_hook_one(const BatchDev& b, uint32_t v)
+// Neighbour offsets (clusterer.hpp:101-105): all 26 (dr, da, de) != (0, 0, 0). Only the 13 after
+// (0, 0, 0) in (de, da, dr) order are probed: every adjacent pair of voxels is then met from one
+// side (or both, where the azimuth wraps onto itself), which yields the same components as probing
+// all 26. One (voxel, offset) pair per thread: the probes are chains of dependent loads, so they
+// run side by side; the components (and the labels, component minima) do not depend on the order
+// of the unions.
+__device__ __forceinline__ void k_uf_hook_pair(const BatchDev& b, uint32_t v, uint32_t o)
 {
+    // offset o: 0 -> (de 0, da 0, dr +1), 1..3 -> (0, +1, -1..+1), 4..12 -> (+1, -1..+1, -1..+1)
+    const int32_t de = (o < 4u) ? 0 : 1;
+    const int32_t da = (o == 0u) ? 0 : ((o < 4u) ? 1 : static_cast<int32_t>((o - 4u) / 3u) - 1);
+    const int32_t dr = (o == 0u) ? 1 : ((o < 4u) ? static_cast<int32_t>(o) - 2 : static_cast<int32_t>((o - 4u) % 3u) - 1);
     const uint32_t slot = b.vslot[v];
     const int s = scan_of_hash(b, slot);
     const ScanDev& sd = b.scans[s];
@@ -331,38 +340,32 @@ __device__ __forceinline__ void k_uf_hook_one(const BatchDev& b, uint32_t v)
     const int32_t r = key % nr;
     const int32_t a = (key / nr) % na;
     const int32_t e = key / (nr * na);
-    int budget = kMaxIters;
-    // Only the 13 offsets after (0, 0, 0) in (de, da, dr) order: every adjacent pair of voxels is
-    // then met from one side (or both, where the azimuth wraps onto itself), which yields the same
-    // components as probing all 26.
-    for (int de = 0; de <= 1; ++de)
-        for (int da = -1; da <= 1; ++da)
-            for (int dr = -1; dr <= 1; ++dr)
-            {
-                if (de == 0 && (da < 0 || (da == 0 && dr <= 0)))
-                    continue;
-                const int32_t rr = r + dr, ee = e + de;
-                if (rr < 0 || rr >= nr || ee < 0 || ee >= ne)
-                    continue;
-                int32_t aa = a + da;
-                if (aa < 0)
-                    aa += na;
-                else if (aa >= na)
-                    aa -= na;
-                const uint32_t nslot = hash_lookup(b, sd, static_cast<uint32_t>(flat_voxel(nr, na, rr, aa, ee)));
-                if (nslot == kEmpty)
-                    continue;
-                const uint32_t u = b.hvid[nslot];
-                if (u != v)
-                    uf_union(b.parent, v, u, st, budget);
-            }
+    const int32_t rr = r + dr, ee = e + de;
+    if (rr < 0 || rr >= nr || ee < 0 || ee >= ne)
+        return;
+    int32_t aa = a + da;
+    if (aa < 0)
+        aa += na;
+    else if (aa >= na)
+        aa -= na;
+    const uint32_t nslot = hash_lookup(b, sd, static_cast<uint32_t>(flat_voxel(nr, na, rr, aa, ee)));
+    if (nslot == kEmpty)
+        return;
+    const uint32_t u = b.hvid[nslot];
+    if (u != v)
+    {
+        int budget = kMaxIters;
+        uf_union(b.parent, v, u, st, budget);
+    }
 }
 
 __global__ void k_uf_hook(BatchDev b)
 {
-    const uint32_t nv = b.hvid[b.nhash]; // occupied voxels: persistent threads stride over them
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x)
-        k_uf_hook_one(b, v);
+    const uint32_t nv = b.hvid[b.nhash]; // occupied voxels; threads stride over (offset, voxel) pairs
+    const unsigned long long total = 13ull * nv;
+    for (unsigned long long t = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; t < total;
+         t += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+        k_uf_hook_pair(b, static_cast<uint32_t>(t % nv), static_cast<uint32_t>(t / nv));
 }
 
 __device__ __forceinline__ void k_uf_flatten_one(const BatchDev& b, uint32_t v)
