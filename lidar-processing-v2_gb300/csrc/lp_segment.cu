@@ -1935,7 +1935,9 @@ void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, ui
     L.scan(b.near_cnt, b.near_start, b.nnear + 1); // near_cnt[nnear] == 0: last entry is the total
     LP_LAUNCH(L, k_near, div_up(b.nnear * 32u, 256u), 256, b, 1);
     LP_LAUNCH(L, k_ransac_draw, static_cast<uint32_t>(b.nscan), 32, b);
-    LP_LAUNCH2D(L, k_ransac_inliers, dim3(16, static_cast<uint32_t>(b.nscan)), 256, b);
+    // chunks per scan: about four CTAs per SM over the batch's scans (the counts add up exactly)
+    const uint32_t rchunks = std::max(16u, div_up(static_cast<uint32_t>(sm_count()) * 4u, static_cast<uint32_t>(b.nscan)));
+    LP_LAUNCH2D(L, k_ransac_inliers, dim3(rchunks, static_cast<uint32_t>(b.nscan)), 256, b);
     LP_LAUNCH(L, k_ransac_select, div_up(static_cast<uint32_t>(b.nscan), 64u), 64, b);
     LP_LAUNCH(L, k_label_depth, div_up(b.npts, T), T, b);
     LP_LAUNCH(L, k_project_key, div_up(b.npts, T), T, b);
