@@ -2,6 +2,8 @@
 // buffers, over the GPU's coherent host link (NVLink-C2C on GB300), one kernel each way instead of
 // one copy per array per scan. Used by lp_process_batch when every buffer of the call was
 // allocated with lp_host_alloc.
+#include <algorithm>
+
 #include "lp_batch.cuh"
 #include "lp_common.cuh"
 #include "lp_stages.hpp"
@@ -10,32 +12,53 @@ namespace lpg
 {
 namespace
 {
-// Input points (and rings) of every scan into the batch arrays.
+// Input points (and rings) of every scan into the batch arrays. A small grid-strided grid (two
+// CTAs per SM) with four host loads in flight per thread: the host link's rate needs far fewer
+// threads than one per point, and the other parts of a split batch keep the remaining SMs for
+// their compute while this part's inputs stream in.
 __global__ void k_io_in(BatchDev b, const IoScan* io)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.nsrc)
-        return;
-    const int s = find_scan(b.nscan, i, [&](int q) { return b.scans[q].src_off; });
-    const ScanDev& sd = b.scans[s];
-    const uint32_t k = i - sd.src_off;
-    if (k >= sd.n_src)
-        return;
-    const IoScan& d = io[s];
-    const_cast<float4*>(b.src)[i] = reinterpret_cast<const float4*>(d.xyzi)[k];
-    if (b.ring_in && d.ring)
-        const_cast<uint16_t*>(b.ring_in)[i] = d.ring[k];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < b.nsrc; i0 += 4u * stride)
+    {
+        float4 v[4];
+        uint16_t rg[4] = {0, 0, 0, 0};
+        uint32_t at[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            const uint32_t i = i0 + static_cast<uint32_t>(u) * stride;
+            at[u] = 0xffffffffu;
+            if (i >= b.nsrc)
+                continue;
+            const int s = find_scan(b.nscan, i, [&](int q) { return b.scans[q].src_off; });
+            const ScanDev& sd = b.scans[s];
+            const uint32_t k = i - sd.src_off;
+            if (k >= sd.n_src)
+                continue;
+            const IoScan& d = io[s];
+            v[u] = reinterpret_cast<const float4*>(d.xyzi)[k];
+            if (b.ring_in && d.ring)
+                rg[u] = d.ring[k];
+            at[u] = i;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (at[u] != 0xffffffffu)
+            {
+                const_cast<float4*>(b.src)[at[u]] = v[u];
+                if (b.ring_in)
+                    const_cast<uint16_t*>(b.ring_in)[at[u]] = rg[u];
+            }
+    }
 }
 
 // Per-point labels of every scan into the caller's buffers, four consecutive points per thread
 // (chunk q of the batch: scan s with io[s].q_off <= q, points 4 (q - q_off) ..): the host link
 // takes whole 16-byte stores (4 B of noise labels, 16 B of segmentation and of cluster labels)
 // where the caller's buffers are aligned for them, and one store per label otherwise.
-__global__ void k_io_out_points(BatchDev b, const IoScan* io, uint32_t nq)
+__device__ __forceinline__ void io_out_chunk(const BatchDev& b, const IoScan* io, uint32_t q)
 {
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nq)
-        return;
     const int s = find_scan(b.nscan, q, [&](int t) { return io[t].q_off; });
     const ScanDev& sd = b.scans[s];
     const IoScan& d = io[s];
@@ -80,6 +103,12 @@ __global__ void k_io_out_points(BatchDev b, const IoScan* io, uint32_t nq)
         if (d.cl)
             d.cl[k0 + u] = cl[u];
     }
+}
+
+__global__ void k_io_out_points(BatchDev b, const IoScan* io, uint32_t nq)
+{
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x)
+        io_out_chunk(b, io, q);
 }
 
 // Per-cluster results: hull offsets (relative to the scan), hull indices, z range, boxes. A scan
@@ -127,13 +156,13 @@ __global__ void k_io_out_clusters(BatchDev b, const IoScan* io, uint32_t* ret, i
 
 void launch_io_in(Launcher& L, const BatchDev& b, const IoScan* io)
 {
-    LP_LAUNCH(L, k_io_in, div_up(b.nsrc, 256u), 256, b, io);
+    LP_LAUNCH(L, k_io_in, std::min(div_up(b.nsrc, 256u), static_cast<uint32_t>(sm_count()) * 2u), 256, b, io);
 }
 
 void launch_io_out(Launcher& L, const BatchDev& b, const IoScan* io, uint32_t* ret, int with_hull, int with_obb,
                    uint32_t nq)
 {
-    LP_LAUNCH(L, k_io_out_points, div_up(nq, 256u), 256, b, io, nq);
+    LP_LAUNCH(L, k_io_out_points, std::min(div_up(nq, 256u), static_cast<uint32_t>(sm_count()) * 2u), 256, b, io, nq);
     if (with_hull)
         LP_LAUNCH(L, k_io_out_clusters, div_up(b.ncl, 256u), 256, b, io, ret, with_obb);
 }
