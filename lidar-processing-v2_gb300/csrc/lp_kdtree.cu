@@ -879,22 +879,20 @@ __device__ uint32_t kt_search(const float4* __restrict__ g, uint32_t n, float qx
 }
 
 // A subtree whose box lies farther than the radius holds no match: the reference's search
-// through it ends without counting anything. The box distance is taken in binary64 against the
-// radius with a relative margin of 1e-5, well above the binary32 rounding of the reference's
-// distance (a few units in 2^-24), so no subtree that could hold a match is skipped.
+// through it ends without counting anything. The box distance is formed in binary32 exactly as
+// kt_search forms a point's distance (per-axis difference, square, d0 + (d1 + d2)). Rounding to
+// nearest is monotone and odd, so for every point p of the box |fl(q - p)| >= fl(gap) on each axis
+// (the gap being the box's bound minus q, or 0 inside the slab), and each square and partial sum of
+// p's distance is at least its counterpart here: when this sum exceeds r2, so does p's, and no
+// subtree that could hold a match is skipped. (Binary32 keeps the test off the binary64 pipe,
+// which runs at a small fraction of the binary32 rate on this GPU.)
 __device__ __forceinline__ bool kt_may_hit(const float4* __restrict__ box, uint32_t m, float qx, float qy, float qz,
                                            float r2)
 {
     const float4 lo = box[2 * m], hi = box[2 * m + 1];
-    auto gap = [](float q, float l, float h) -> double {
-        if (q < l)
-            return static_cast<double>(l) - static_cast<double>(q);
-        if (q > h)
-            return static_cast<double>(q) - static_cast<double>(h);
-        return 0.0;
-    };
-    const double gx = gap(qx, lo.x, hi.x), gy = gap(qy, lo.y, hi.y), gz = gap(qz, lo.z, hi.z);
-    return gx * gx + gy * gy + gz * gz <= static_cast<double>(r2) * (1.0 + 1e-5) + 1e-30;
+    auto gap = [](float q, float l, float h) -> float { return (q < l) ? (l - q) : ((q > h) ? (q - h) : 0.0f); };
+    const float gx = gap(qx, lo.x, hi.x), gy = gap(qy, lo.y, hi.y), gz = gap(qz, lo.z, hi.z);
+    return (gx * gx) + ((gy * gy) + (gz * gz)) <= r2;
 }
 
 __device__ __forceinline__ int kt_scan_of(const BatchDev& b, uint32_t i)
