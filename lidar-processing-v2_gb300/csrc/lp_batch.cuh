@@ -203,7 +203,8 @@ struct BatchDev
     uint32_t* kpool;           // leftover entries as searches produce them (kpool_cap)
     uint32_t* kflat;           // the points' leftovers in point order (kpool_cap)
     uint32_t kpool_cap;
-    uint32_t* kq;              // short points in order
+    uint32_t* kq;              // short points in order (before that, from the build to the own search:
+                               // the input index of the point at each tree position)
     uint4* kc;                 // per short point: count, stop entry, left entries (pool at, count)
     uint32_t* kcflag;          // per short point (+1): 1 if step 3 left it undecided -> exclusive scan
     uint32_t* kcand;           // those candidates (short indices) in order

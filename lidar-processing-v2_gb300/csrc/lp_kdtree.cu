@@ -21,8 +21,8 @@
 //      ranges of at most kKtSmall points finish their whole subtree in shared memory. Node
 //      children follow from the range arithmetic alone, so a node record is its point and its
 //      subtree size; subtree boxes (k_kt_box_level) serve the skip test of steps 3 and 4.
-//   2. Own search (k_kt_own, one thread per point): the point's search from the root, in the
-//      reference's push order, until min_neighbours or exhaustion. A point that reaches the
+//   2. Own search (k_kt_own, one thread per point, taken in tree order): the point's search from
+//      the root, in the reference's push order, until min_neighbours or exhaustion. A point that reaches the
 //      count leaves the rest of its stack behind: those entries go to a pool, then into one
 //      array in point order (k_kt_flat). Points that exhaust their own search ("short" points)
 //      are listed in order (k_kt_short).
@@ -466,8 +466,10 @@ __device__ void kt_select_warp(float4* a, uint32_t first, uint32_t nth, uint32_t
 }
 
 // Subtree of [b0, e0) (at depth d0 of the tree, at most kKtSmall points) built in shared memory;
-// node records get their subtree size in .w; subtree boxes are written bottom-up.
-__device__ void kt_build_small(float4* g, float4* box, uint32_t b0, uint32_t e0, int d0, float4* s, uint16_t* lists)
+// node records get their subtree size in .w (the input index it carried goes to idx); subtree
+// boxes are written bottom-up.
+__device__ void kt_build_small(float4* g, float4* box, uint32_t* idx, uint32_t b0, uint32_t e0, int d0, float4* s,
+                               uint16_t* lists)
 {
     const uint32_t n = e0 - b0;
     const uint32_t warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -507,6 +509,7 @@ __device__ void kt_build_small(float4* g, float4* box, uint32_t b0, uint32_t e0,
                 continue;
             const uint32_t m = b + (e - b) / 2;
             float4 p = s[m];
+            idx[b0 + m] = __float_as_uint(p.w);
             p.w = __uint_as_float(e - b);
             s[m] = p;
             float4 lo = make_float4(p.x, p.y, p.z, 0.0f), hi = lo;
@@ -734,6 +737,7 @@ __global__ void __cluster_dims__(kKtCluster, 1, 1) __launch_bounds__(kKtThreads)
         {
             kt_select_seq(g, first, nth, last, depth, level % 3);
             float4 p = g[nth];
+            b.kq[sd.src_off + nth] = __float_as_uint(p.w);
             p.w = __uint_as_float(len);
             g[nth] = p;
         }
@@ -753,7 +757,9 @@ __global__ void k_kt_load(BatchDev b)
     if (i >= b.nsrc)
         return;
     const float4 p = b.src[i];
-    b.kt[i] = make_float4(p.x, p.y, p.z, 0.0f);
+    // the point's input index rides in .w while the build moves the records (saved in kq when the
+    // record becomes a node and .w takes its subtree size)
+    b.kt[i] = make_float4(p.x, p.y, p.z, __uint_as_float(i));
 }
 
 // One level of the build: CTA (scan, slot j). Ranges above kKtSmall are put in order around their
@@ -784,13 +790,14 @@ __global__ void __launch_bounds__(kKtThreads) k_kt_level(BatchDev b, int level, 
         if (threadIdx.x == 0)
         {
             float4 p = g[nth];
+            b.kq[sd.src_off + nth] = __float_as_uint(p.w);
             p.w = __uint_as_float(len);
             g[nth] = p;
         }
     }
     else if (level == 0 || plen > kKtSmall)
     {
-        kt_build_small(g, box, lb, le, level, kt_smem, reinterpret_cast<uint16_t*>(kt_smem + kKtSmall));
+        kt_build_small(g, box, b.kq + sd.src_off, lb, le, level, kt_smem, reinterpret_cast<uint16_t*>(kt_smem + kKtSmall));
     }
 }
 
@@ -925,15 +932,24 @@ __device__ __forceinline__ uint32_t kt_pool_alloc(uint32_t* head, uint32_t cap, 
     return base + pre;
 }
 
-// Step 2: every point's own search; VALID points' leftovers into the pool.
+// Step 2: every point's own search; VALID points' leftovers into the pool. Thread t takes the
+// point at tree position t (its input index from the build), so the threads of a warp query
+// neighbouring points, whose searches walk largely the same nodes (cache hits, little divergence,
+// where input order may be shuffled); the results go to the point's input index.
 __global__ void k_kt_own(BatchDev b)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.nsrc)
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= b.nsrc)
         return;
-    const int s = kt_scan_of(b, i);
+    const int s = kt_scan_of(b, t);
     const ScanDev& sd = b.scans[s];
-    const float4 q = b.src[i];
+    const float4 q = b.kt[t]; // the point's coordinates, as loaded from the input
+    const uint32_t i = b.kq[t];
+    if (i - sd.src_off >= sd.n_src)
+    {
+        raise_err(&b.state[s], ERR_INTERNAL); // not a point of this scan: reported, never followed
+        return;
+    }
     const float r2 = kt_radius2(sd, q);
     uint32_t stk[kKtStack];
     int sp = 0;
