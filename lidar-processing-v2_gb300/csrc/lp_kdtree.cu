@@ -57,7 +57,7 @@ namespace
 constexpr uint32_t kKtSmall = 2048;    // ranges built in shared memory by one CTA
 constexpr uint32_t kKtHuge = 65536;    // ranges partitioned by a cluster of kKtCluster CTAs
 constexpr int kKtCluster = 8;
-constexpr uint32_t kKtSeqMax = 64;     // ranges built by one thread (introselect as written)
+constexpr uint32_t kKtWarpMin = 16;    // ranges of at most this many points finish on one thread
 constexpr int kKtThreads = 512;        // tree build CTAs
 constexpr int kKtItems = 8;            // elements per thread per tile of the parallel partition
 constexpr int kKtStack = 64;           // search stack entries (>= tree depth + 1 for 2^62 points)
@@ -373,13 +373,17 @@ __device__ uint32_t kt_round_block(float4* a, uint32_t first, uint32_t last, int
     return cut;
 }
 
-// Introselect of nth in [first, last) by a whole CTA; rounds on ranges of at most kKtSeqMax
-// elements (and the depth-limit fallback) run on thread 0.
-__device__ void kt_select_block(float4* a, uint32_t first, uint32_t nth, uint32_t last, int ax, uint32_t* ge,
-                                uint32_t* le, KtShared& sh)
+__device__ void kt_select_warp(float4* a, uint32_t first, uint32_t nth, uint32_t last, int ax, uint16_t* ge,
+                               uint16_t* le, int depth);
+
+// Continues an introselect of nth in [first, last) (global memory) with `depth` rounds left on a
+// whole CTA: parallel rounds while the range exceeds kKtSmall points, then the range is copied to
+// shared memory (srec, with 2 kKtSmall list entries at slist) and warp 0 finishes it there. The
+// depth-limit fallback on a larger range runs on thread 0.
+__device__ void kt_select_block(float4* a, uint32_t first, uint32_t nth, uint32_t last, int depth, int ax,
+                                uint32_t* ge, uint32_t* le, KtShared& sh, float4* srec, uint16_t* slist)
 {
-    int depth = 2 * static_cast<int>(floor_log2_u(last - first));
-    while (last - first > kKtSeqMax && depth > 0)
+    while (last - first > kKtSmall && depth > 0)
     {
         --depth;
         const uint32_t cut = kt_round_block(a, first, last, ax, ge, le, sh);
@@ -388,8 +392,22 @@ __device__ void kt_select_block(float4* a, uint32_t first, uint32_t nth, uint32_
         else
             last = cut;
     }
-    if (threadIdx.x == 0)
-        kt_select_seq(a, first, nth, last, depth, ax);
+    const uint32_t len = last - first;
+    if (len > kKtSmall)
+    {
+        if (threadIdx.x == 0)
+            kt_select_seq(a, first, nth, last, depth, ax);
+        __syncthreads();
+        return;
+    }
+    for (uint32_t k = threadIdx.x; k < len; k += blockDim.x)
+        srec[k] = a[first + k];
+    __syncthreads();
+    if (threadIdx.x < 32)
+        kt_select_warp(srec, 0, nth - first, len, ax, slist, slist + len, depth);
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < len; k += blockDim.x)
+        a[first + k] = srec[k];
     __syncthreads();
 }
 
@@ -447,11 +465,14 @@ __device__ uint32_t kt_round_warp(float4* a, uint32_t first, uint32_t last, int 
     return cut;
 }
 
+// Continues an introselect of nth in [first, last) (shared memory) with `depth` rounds left on one
+// warp: parallel rounds while the range holds more than kKtWarpMin points, then lane 0 as written.
+// (A parallel round replays the sequential partition exactly at any size; a small range on one
+// thread is a chain of dependent shared-memory accesses, and ranges on neighbouring threads diverge.)
 __device__ void kt_select_warp(float4* a, uint32_t first, uint32_t nth, uint32_t last, int ax, uint16_t* ge,
-                               uint16_t* le)
+                               uint16_t* le, int depth)
 {
-    int depth = 2 * static_cast<int>(floor_log2_u(last - first));
-    while (last - first > kKtSeqMax && depth > 0)
+    while (last - first > kKtWarpMin && depth > 0)
     {
         --depth;
         const uint32_t cut = kt_round_warp(a, first, last, ax, ge, le);
@@ -477,23 +498,24 @@ __device__ void kt_build_small(float4* g, float4* box, uint32_t* idx, uint32_t b
         s[k] = g[b0 + k];
     __syncthreads();
     // the longest range at depth d has floor(n / 2^d) points (a range of L splits into floor(L/2)
-    // and ceil(L/2) - 1), so depths 0 .. floor(log2 n) hold ranges. Ranges above kKtSeqMax: one warp
+    // and ceil(L/2) - 1), so depths 0 .. floor(log2 n) hold ranges. Ranges above kKtWarpMin: one warp
     // each (positions of range [b, e) in lists[2b, 2e)); the rest: one thread each.
     const int maxd = static_cast<int>(floor_log2_u(n));
     for (int d = 0; d <= maxd; ++d)
     {
         const uint32_t slots = 1u << d;
-        if ((n >> d) > kKtSeqMax)
+        if ((n >> d) > kKtWarpMin)
             for (uint32_t j = warp; j < slots; j += nwarps)
             {
                 uint32_t b, e;
-                if (kt_range(n, d, j, b, e, nullptr) && e - b > kKtSeqMax)
-                    kt_select_warp(s, b, b + (e - b) / 2, e, (d0 + d) % 3, lists + 2 * b, lists + 2 * b + (e - b));
+                if (kt_range(n, d, j, b, e, nullptr) && e - b > kKtWarpMin)
+                    kt_select_warp(s, b, b + (e - b) / 2, e, (d0 + d) % 3, lists + 2 * b, lists + 2 * b + (e - b),
+                                   2 * static_cast<int>(floor_log2_u(e - b)));
             }
         for (uint32_t j = threadIdx.x; j < slots; j += blockDim.x)
         {
             uint32_t b, e;
-            if (kt_range(n, d, j, b, e, nullptr) && e - b <= kKtSeqMax && e - b > 1)
+            if (kt_range(n, d, j, b, e, nullptr) && e - b <= kKtWarpMin && e - b > 1)
                 kt_select_seq(s, b, b + (e - b) / 2, e, 2 * static_cast<int>(floor_log2_u(e - b)), (d0 + d) % 3);
         }
         __syncthreads();
@@ -695,6 +717,7 @@ __device__ uint32_t kt_round_cluster(float4* a, uint32_t first, uint32_t last, i
 __global__ void __cluster_dims__(kKtCluster, 1, 1) __launch_bounds__(kKtThreads)
     k_kt_level_huge(BatchDev b, int level, uint32_t slots)
 {
+    extern __shared__ float4 kt_smem[];
     __shared__ KtClusterShared csh;
     __shared__ KtShared sh;
     cg::cluster_group cluster = cg::this_cluster();
@@ -723,19 +746,11 @@ __global__ void __cluster_dims__(kKtCluster, 1, 1) __launch_bounds__(kKtThreads)
     }
     if (cluster.block_rank() == 0)
     {
-        // the rest of the introselect on one CTA (the same rounds kt_select_block runs)
-        while (last - first > kKtSeqMax && depth > 0)
-        {
-            --depth;
-            const uint32_t cut = kt_round_block(g, first, last, level % 3, ge, lq, sh);
-            if (cut <= nth)
-                first = cut;
-            else
-                last = cut;
-        }
+        // the rest of the introselect on one CTA
+        kt_select_block(g, first, nth, last, depth, level % 3, ge, lq, sh, kt_smem,
+                        reinterpret_cast<uint16_t*>(kt_smem + kKtSmall));
         if (threadIdx.x == 0)
         {
-            kt_select_seq(g, first, nth, last, depth, level % 3);
             float4 p = g[nth];
             b.kq[sd.src_off + nth] = __float_as_uint(p.w);
             p.w = __uint_as_float(len);
@@ -786,7 +801,8 @@ __global__ void __launch_bounds__(kKtThreads) k_kt_level(BatchDev b, int level, 
     if (len > kKtSmall)
     {
         const uint32_t nth = lb + len / 2;
-        kt_select_block(g, lb, nth, le, level % 3, ge, lq, sh);
+        kt_select_block(g, lb, nth, le, 2 * static_cast<int>(floor_log2_u(len)), level % 3, ge, lq, sh, kt_smem,
+                        reinterpret_cast<uint16_t*>(kt_smem + kKtSmall));
         if (threadIdx.x == 0)
         {
             float4 p = g[nth];
@@ -1452,6 +1468,8 @@ size_t kt_build_smem_bytes()
 void init_kdtree_attributes()
 {
     cudaFuncSetAttribute(k_kt_level, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kt_build_smem_bytes()));
+    cudaFuncSetAttribute(k_kt_level_huge, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(kt_build_smem_bytes()));
 }
 
 void launch_noise(Launcher& L, const BatchDev& b, const BatchHost& hb, const lp_noise_remover_config& cfg)
@@ -1473,7 +1491,7 @@ void launch_noise(Launcher& L, const BatchDev& b, const BatchHost& hb, const lp_
     {
         const uint32_t slots = 1u << l;
         if ((nmax >> l) > kKtHuge)
-            LP_LAUNCH(L, k_kt_level_huge, S * slots * kKtCluster, kKtThreads, b, l, slots);
+            LP_LAUNCH_SMEM(L, k_kt_level_huge, S * slots * kKtCluster, kKtThreads, kt_build_smem_bytes(), b, l, slots);
         LP_LAUNCH_SMEM(L, k_kt_level, S * slots, kKtThreads, kt_build_smem_bytes(), b, l, slots);
     }
     for (int l = levels - 2; l >= 0; --l)
