@@ -194,12 +194,15 @@ struct BatchDev
     // ---- DROR (reference kd-tree replay, lp_kdtree.cu) ------------------------------------------
     float4* kt;                // per input point: tree node record by position (x, y, z, subtree size bits)
     float4* kbb;               // 2 per input point: subtree box (lo, hi) by node position
-    uint32_t* kscr;            // 2 per input point: candidate positions of the parallel partition
-    uint32_t* kown;            // per point: count of its own search (capped at min_neighbours)
+    uint32_t* kscr;            // 2 per input point: candidate positions of the parallel partition (later,
+                               // per candidate: its walk through its predecessor's stop pieces: stop entry, left at)
+    uint32_t* kown;            // per point: count of its own search (capped at min_neighbours); later, per
+                               // candidate: the count after that walk
     uint32_t* kshort;          // per point (+1): 1 if its own search fell short -> exclusive scan
     uint32_t* klo_n;           // per point (+1): entries its search left behind
     uint32_t* klo_off;         // exclusive scan of klo_n: their place in kflat
-    uint32_t* klo_at;          // per point: their place in kpool
+    uint32_t* klo_at;          // per point: their place in kpool; later, per candidate: that walk's status,
+                               // left count and stop piece
     uint32_t* kpool;           // leftover entries as searches produce them (kpool_cap)
     uint32_t* kflat;           // the points' leftovers in point order (kpool_cap)
     uint32_t kpool_cap;

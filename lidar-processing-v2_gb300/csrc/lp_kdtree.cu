@@ -32,14 +32,17 @@
 //      piece from the top; an entry whose subtree box is farther than the radius is consumed
 //      without a match (skipped); the others are searched exactly. Reaching the count there
 //      decides the point (VALID) and records where it stopped and the entries it left.
-//   4. Candidates (short points step 3 did not decide) in two steps. k_kt_spec, one thread per
+//   4. Candidates (short points step 3 did not decide) in three steps. k_kt_spec, one thread per
 //      candidate: the walk through the pieces pushed since the previous candidate, as if nothing
 //      lay below them, which is exact whenever the previous candidate emptied the stack (running
-//      out of entries is NOISE). k_kt_chain, one CTA per scan: the candidates in order with R,
+//      out of entries is NOISE). k_kt_spec_next, one thread per candidate whose walk ran out right
+//      after one whose walk stopped: the walk on through the pieces that stop leaves, which lie
+//      on top of whatever was below. k_kt_chain, one CTA per scan: the candidates in order with R,
 //      what earlier walks left below those pieces; a stopped walk adds its remainder to R, one
-//      that ran out continues into R (the threads searching 256 entries at a time, an ordered
-//      prefix of their counts finding the stop). While R is empty, runs of candidates whose walks ran
-//      out are NOISE at once.
+//      that ran out continues into R: straight after a stop with the walk k_kt_spec_next made,
+//      otherwise (and below those pieces) with the threads searching 256 entries at a time, an
+//      ordered prefix of their counts finding the stop. While R is empty, runs of candidates whose
+//      walks ran out are NOISE at once.
 // The result equals the reference's sequential search bit for bit (same binary32 expressions,
 // same visiting order, same stop points); the tree's node positions equal the reference's.
 #include <cooperative_groups.h>
@@ -1175,6 +1178,109 @@ __global__ void k_kt_spec(BatchDev b)
     b.kspec_n[c] = stop.n;
 }
 
+// Record of a candidate's walk through what its predecessor's stop left (k_kt_spec_next), in
+// arrays free by then (per candidate c): kscr[2c] stop entry, kscr[2c + 1] where the entries that
+// stopping search left start in the pool, kown[c] count, klo_at[c] = status | left count << 2 |
+// piece << 9 (the stop's piece, counted from the top of those pieces).
+constexpr uint32_t kNextNone = 0u, kNextStop = 1u, kNextOut = 2u;
+constexpr uint32_t kNextPieceMax = 1u << 23;
+
+// Step 4a': a candidate whose walk ran out, right after a candidate whose walk stopped, continues
+// into R, and R is then what it was before that stop with the stop's pieces on top: the pieces of
+// the predecessor's pushing points below its stop point u, the rest of u's pieces below the stop,
+// and the entries the stopping search left (the chain pushes exactly these, in this order). Every
+// such candidate walks those pieces here, in parallel, from its count after its own walk. The
+// chain takes the result when the predecessor's stop is the last change to R: a stop in those
+// pieces is exact whatever lies below them; running out of them continues into R below.
+__global__ void k_kt_spec_next(BatchDev b)
+{
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t ncand = b.kcflag[b.kshort[b.nsrc]];
+    if (c >= ncand)
+        return;
+    b.klo_at[c] = kNextNone;
+    const uint32_t t = b.kcand[c];
+    const uint32_t i = b.kq[t];
+    const int s = kt_scan_of(b, i);
+    const ScanDev& sd = b.scans[s];
+    const uint32_t t_first = b.kshort[sd.src_off];
+    const uint32_t c_first = b.kcflag[t_first];
+    if (c == c_first)
+        return; // the scan's first candidate has no predecessor
+    const uint4 own = b.kspec[c], pv = b.kspec[c - 1];
+    if (own.y != kNone || pv.y == kNone)
+        return; // this walk stopped, or the predecessor's ran out
+    const uint32_t tp1 = (c - 1 > c_first) ? b.kcand[c - 2] + 1 : t_first; // the predecessor's first pushing point
+    const uint32_t hu = pv.y, hx = pv.z & 0x7fffffffu, hkind = pv.z >> 31;
+    const float4 q = b.src[i];
+    const float r2 = kt_radius2(sd, q);
+    const float4* g = b.kt + sd.src_off;
+    const float4* box = b.kbb + 2ull * sd.src_off;
+    const uint32_t k = sd.dror_k;
+    uint32_t found = own.x;
+    uint32_t stk[kKtStack];
+    bool overflow = false, pool_full = false;
+    uint32_t piece = 0, sx = 0, sat = 0, sn = 0;
+    // one piece, entries from hi - 1 down; an empty piece is not in R and is not counted
+    auto walk = [&](uint32_t lo, uint32_t hi, bool pool) -> bool {
+        if (hi <= lo)
+            return false;
+        const uint32_t* arr = pool ? b.kpool : b.kflat;
+        for (uint32_t x = hi; x > lo; --x)
+        {
+            const uint32_t e = arr[x - 1];
+            if (!kt_may_hit(box, e >> 2, q.x, q.y, q.z, r2))
+                continue;
+            int sp = 0;
+            stk[sp++] = e;
+            found = kt_search(g, sd.n_src, q.x, q.y, q.z, r2, k, found, stk, sp, overflow);
+            if (found >= k)
+            {
+                uint32_t at = kt_pool_alloc(b.kctr, b.kpool_cap, static_cast<uint32_t>(sp));
+                if (at == kNone)
+                {
+                    pool_full = true;
+                    at = 0;
+                    sp = 0;
+                }
+                for (int v = 0; v < sp; ++v)
+                    b.kpool[at + v] = stk[v];
+                sx = x - 1;
+                sat = at;
+                sn = static_cast<uint32_t>(sp);
+                return true;
+            }
+        }
+        ++piece;
+        return false;
+    };
+    bool stopped = walk(pv.w, pv.w + b.kspec_n[c - 1], true);
+    if (!stopped)
+    {
+        const uint4 cu = b.kc[hu];
+        if (hkind == 1)
+            stopped = walk(cu.z, hx, true) || walk(kt_segment_lo(b, sd, hu), cu.y, false);
+        else
+            stopped = walk(kt_segment_lo(b, sd, hu), hx, false);
+    }
+    for (uint32_t u = hu; !stopped && u > tp1;)
+    {
+        --u;
+        const uint4 cu = b.kc[u];
+        stopped = walk(cu.z, cu.z + cu.w, true) || walk(kt_segment_lo(b, sd, u), cu.y, false);
+    }
+    if (overflow)
+        raise_err(&b.state[s], ERR_INTERNAL);
+    if (pool_full)
+        raise_err(&b.state[s], ERR_HASH_FULL);
+    if (piece >= kNextPieceMax || overflow || pool_full)
+        return; // the chain searches R itself
+    b.kscr[2ull * c] = sx;
+    b.kscr[2ull * c + 1] = sat;
+    b.kown[c] = found;
+    b.klo_at[c] = (stopped ? kNextStop : kNextOut) | (sn << 2) | (piece << 9);
+}
+
 // Step 4b: one CTA per scan applies the candidates' walks in order. R, the stack below the pieces
 // pushed since the previous candidate, is a list of pieces (lo, hi): entries [lo, hi) of the flat
 // array (bit 31 of lo clear) or of the pool (set), consumed from hi - 1 down. A candidate whose
@@ -1198,6 +1304,7 @@ __global__ void __launch_bounds__(kChainThreads) k_kt_chain(BatchDev b)
     __shared__ uint4 w_spec[kChainThreads];
     __shared__ uint32_t w_specn[kChainThreads], w_i[kChainThreads], w_tp1[kChainThreads];
     __shared__ float4 w_q[kChainThreads];
+    __shared__ uint4 w_nx[kChainThreads]; // walk through the predecessor's stop pieces (k_kt_spec_next)
     // the top pieces of R for one round (index 0 = the top) and their entry-count prefix
     __shared__ uint2 r_pc[kChainPieces];
     __shared__ uint32_t r_pre[kChainPieces + 1];
@@ -1215,6 +1322,9 @@ __global__ void __launch_bounds__(kChainThreads) k_kt_chain(BatchDev b)
     const uint32_t t_first = b.kshort[sd.src_off], t_end = b.kshort[sd.src_off + sd.n_src];
     const uint32_t c0 = b.kcflag[t_first], c1 = b.kcflag[t_end];
     uint32_t top = 0; // pieces in R (the same in every thread)
+    // R's top before the last candidate's stop pushed its pieces, while that stop is the last
+    // change to R (kNone otherwise)
+    uint32_t mark = kNone;
     bool overflow = false, pool_full = false, full = false;
     uint32_t stk[kKtStack];
     auto push = [&](uint32_t lo, uint32_t hi) {
@@ -1285,12 +1395,14 @@ __global__ void __launch_bounds__(kChainThreads) k_kt_chain(BatchDev b)
                 w_i[tid] = i;
                 w_tp1[tid] = (cc > c0) ? b.kcand[cc - 1] + 1 : t_first;
                 w_q[tid] = b.src[i];
+                w_nx[tid] = make_uint4(b.kown[cc], b.kscr[2ull * cc], b.kscr[2ull * cc + 1], b.klo_at[cc]);
             }
             __syncthreads();
         }
         if (top == 0)
         {
             // candidates whose walks ran out with R empty are NOISE, up to the first that stopped
+            mark = kNone;
             const uint32_t cc = c + tid;
             const bool live = cc < w1;
             const bool hit = live && w_spec[cc - w0].y != kNone;
@@ -1308,6 +1420,7 @@ __global__ void __launch_bounds__(kChainThreads) k_kt_chain(BatchDev b)
         {
             // the walk stopped at short point u: R gains the pieces of the pushing points below u,
             // then the rest of u's pieces below the stop, then the entries the stopping search left
+            mark = top;
             const uint32_t tp1 = w_tp1[wc];
             const uint32_t hu = sp4.y, hx = sp4.z & 0x7fffffffu, hkind = sp4.z >> 31;
             for (uint32_t u = tp1; u <= hu; ++u)
@@ -1341,6 +1454,28 @@ __global__ void __launch_bounds__(kChainThreads) k_kt_chain(BatchDev b)
         const float r2 = kt_radius2(sd, q);
         uint32_t found = sp4.x;
         bool hit = false;
+        if (mark != kNone)
+        {
+            // the previous candidate stopped and nothing changed R since: its stop's pieces lie on
+            // top of R, and this candidate's walk through them is done
+            const uint4 nx = w_nx[wc];
+            const uint32_t status = nx.w & 3u, nsp = (nx.w >> 2) & 127u, p = nx.w >> 9;
+            if (status == kNextStop && mark + p < top)
+            {
+                const uint2 pc = R[top - 1 - p];
+                top -= p + 1;
+                push(pc.x, nx.y);
+                push(nx.z | 0x80000000u, nx.z + nsp);
+                found = nx.x;
+                hit = true;
+            }
+            else if (status == kNextOut)
+            {
+                found = nx.x;
+                top = mark; // those pieces are used up; R below them follows
+            }
+            mark = kNone;
+        }
         while (top > 0 && !hit)
         {
             // the top pieces (warp 0) and how many entries of them this round covers
@@ -1509,6 +1644,7 @@ void launch_noise(Launcher& L, const BatchDev& b, const BatchHost& hb, const lp_
     L.scan(b.kcflag, b.kcflag, b.nsrc + 1);
     LP_LAUNCH(L, k_kt_cand_list, div_up(b.nsrc, T), T, b);
     LP_LAUNCH(L, k_kt_spec, div_up(b.nsrc, 128u), 128, b);
+    LP_LAUNCH(L, k_kt_spec_next, div_up(b.nsrc, 128u), 128, b);
     LP_LAUNCH(L, k_kt_chain, S, kChainThreads, b);
 }
 } // namespace lpg
