@@ -420,6 +420,7 @@ __global__ void k_keep(BatchDev b)
 // components ordered by smallest point index == the reference's final label.
 __global__ void k_obs_label(BatchDev b)
 {
+    __shared__ BlockAgg agg;
     const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = o < b.obs_flag[b.npts];
     int32_t label = LP_INVALID_CLUSTER;
@@ -439,7 +440,7 @@ __global__ void k_obs_label(BatchDev b)
         b.obs_label[o] = label;
         g = sd.cl_off + static_cast<uint32_t>(label);
     }
-    warp_aggregated_inc(b.cl_cnt, g, in && label >= 0);
+    block_aggregated_inc(b.cl_cnt, g, in && label >= 0, agg);
 }
 
 __global__ void k_cl_state(BatchDev b)
@@ -455,8 +456,9 @@ __global__ void k_cl_state(BatchDev b)
 }
 
 // Members grouped by cluster (slot order within a cluster is free), with their x, y alongside for
-// the hull stage, and each cluster's z range (ordered-key maxima, one atomic pair per cluster
-// and warp).
+// the hull stage, and each cluster's z range (ordered-key maxima: one atomic pair per cluster and
+// warp where a warp's points share few clusters; otherwise per point, skipped when a fresh read
+// of the key shows it cannot rise).
 __device__ __forceinline__ uint32_t z_ord(float f)
 {
     const uint32_t u = __float_as_uint(f);
@@ -465,6 +467,7 @@ __device__ __forceinline__ uint32_t z_ord(float f)
 
 __global__ void k_cl_scatter(BatchDev b)
 {
+    __shared__ BlockAgg agg;
     const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = lane_id();
     const int32_t label = (o < b.obs_flag[b.npts]) ? b.obs_label[o] : -1;
@@ -476,7 +479,7 @@ __global__ void k_cl_scatter(BatchDev b)
         g = b.scans[scan_of_obs(b, o)].cl_off + static_cast<uint32_t>(label);
         p = b.obs_pts[o];
     }
-    const uint32_t rank = warp_aggregated_inc(b.cl_fill, g, in);
+    const uint32_t rank = block_aggregated_inc(b.cl_fill, g, in, agg);
     if (in)
     {
         const uint32_t slot = b.cl_start[g] + rank;
@@ -484,6 +487,19 @@ __global__ void k_cl_scatter(BatchDev b)
         b.mxy[slot] = make_float2(p.x, p.y);
     }
     const uint32_t zo = z_ord(p.z);
+    const uint32_t peers = __match_any_sync(0xffffffffu, in ? g : 0xffffffffu);
+    const uint32_t groups = __popc(__ballot_sync(0xffffffffu, in && lane == static_cast<uint32_t>(__ffs(peers) - 1)));
+    if (groups > 4u)
+    {
+        if (in)
+        {
+            if (~zo > __ldcg(&b.cl_zkey[2u * g]))
+                atomicMax(&b.cl_zkey[2u * g], ~zo);
+            if (zo > __ldcg(&b.cl_zkey[2u * g + 1u]))
+                atomicMax(&b.cl_zkey[2u * g + 1u], zo);
+        }
+        return;
+    }
     for (uint32_t todo = __ballot_sync(0xffffffffu, in); todo != 0u;)
     {
         const int l = __ffs(todo) - 1;

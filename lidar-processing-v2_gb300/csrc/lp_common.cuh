@@ -87,6 +87,64 @@ __device__ __forceinline__ uint32_t warp_aggregated_inc(uint32_t* counters, uint
     return valid ? old + static_cast<uint32_t>(__popc(peers & ((1u << lane) - 1u))) : 0u;
 }
 
+// Block-wide version for counters many threads of a block may share even where the lanes of a
+// warp do not (unordered input): the warps' groups of equal keys meet in a shared-memory table,
+// and one global atomic per key and block reserves the block's total; a key the table cannot take
+// (kBlockAggProbes probes) takes its own global atomic. Every thread of the block calls it (two
+// barriers). Returns the thread's rank among its key's increments (unique, order unspecified).
+constexpr uint32_t kBlockAggSlots = 512;
+constexpr uint32_t kBlockAggProbes = 16;
+static_assert(kBlockAggSlots == 512u, "the slot hash takes the top 9 bits");
+struct BlockAgg
+{
+    uint32_t key[kBlockAggSlots];
+    uint32_t cnt[kBlockAggSlots];
+};
+
+__device__ __forceinline__ uint32_t block_aggregated_inc(uint32_t* counters, uint32_t key, bool valid, BlockAgg& sh)
+{
+    constexpr uint32_t kFree = 0xffffffffu;
+    const uint32_t lane = lane_id();
+    for (uint32_t k = threadIdx.x; k < kBlockAggSlots; k += blockDim.x)
+    {
+        sh.key[k] = kFree;
+        sh.cnt[k] = 0u;
+    }
+    const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? key : kFree) & vmask;
+    const uint32_t leader = peers ? static_cast<uint32_t>(__ffs(peers) - 1) : lane;
+    __syncthreads();
+    uint32_t slot = kFree, loc = 0u;
+    if (valid && lane == leader)
+    {
+        uint32_t h = (key * 2654435761u) >> (32 - 9); // kBlockAggSlots = 2^9
+        for (uint32_t probe = 0; probe < kBlockAggProbes; ++probe)
+        {
+            const uint32_t prev = atomicCAS(&sh.key[h], kFree, key);
+            if (prev == kFree || prev == key)
+            {
+                slot = h;
+                loc = atomicAdd(&sh.cnt[h], static_cast<uint32_t>(__popc(peers)));
+                break;
+            }
+            h = (h + 1u) & (kBlockAggSlots - 1u);
+        }
+        if (slot == kFree)
+            loc = atomicAdd(&counters[key], static_cast<uint32_t>(__popc(peers)));
+    }
+    __syncthreads();
+    // the block's total per key: one global atomic each (the count is replaced by the key's base)
+    for (uint32_t k = threadIdx.x; k < kBlockAggSlots; k += blockDim.x)
+        if (sh.key[k] != kFree)
+            sh.cnt[k] = atomicAdd(&counters[sh.key[k]], sh.cnt[k]);
+    __syncthreads();
+    uint32_t base = 0u;
+    if (valid && lane == leader)
+        base = (slot != kFree) ? sh.cnt[slot] + loc : loc;
+    base = __shfl_sync(0xffffffffu, base, static_cast<int>(leader));
+    return valid ? base + static_cast<uint32_t>(__popc(peers & ((1u << lane) - 1u))) : 0u;
+}
+
 __device__ __forceinline__ uint32_t warp_sum(uint32_t v)
 {
 #pragma unroll
