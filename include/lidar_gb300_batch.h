@@ -16,7 +16,7 @@ extern "C" {
 typedef struct lp_batch lp_batch;
 
 /* Plans the layout, allocates device memory and uploads the scans (host buffers must stay
- * valid for lp_batch_upload). A batch of 16 or more scans is split into up to four parts (one per
+ * valid for lp_batch_upload). A batch of 16 or more scans is split into up to eight parts (one per
  * 8 scans, dealt round-robin) that execute concurrently on their own streams, forked from and
  * joined into the context stream; results and their order are those of the unsplit batch. */
 lp_status lp_batch_create(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans,
@@ -79,7 +79,7 @@ lp_status lp_debug_math_sweep(lp_context* ctx, int32_t kind, uint64_t first, uin
 typedef struct lp_tuning
 {
     uint32_t parts;            /* concurrent parts of a batch of 16 or more scans (1-8; 0: one per 8
-                                  scans, at most 4); never more than the batch has scans */
+                                  scans, at most 8); never more than the batch has scans */
     uint32_t balance_parts;    /* 0: scans dealt round-robin; 1: largest scan first to the part holding
                                   the fewest points */
     uint32_t hull_cta_min;     /* clusters of more members take a whole CTA of the hull kernel, smaller
@@ -132,8 +132,8 @@ typedef struct lp_autotune_report
 } lp_autotune_report;
 
 /* Coordinate descent over the tuning fields on these scans: each candidate is a prepared batch
- * replayed as a CUDA graph, timed with CUDA events over `iters` executions (L2 flushed between
- * them); a candidate replaces the current choice only if at least 1 % faster. Starts from the
+ * replayed as a CUDA graph, timed with CUDA events over `iters` executions back to back (no L2 flush
+ * between them, as batches follow one another in a stream); a candidate replaces the current choice only if at least 1 % faster. Starts from the
  * table's entry for the scans' bucket (else the defaults) and stores the choice there. trial_ms /
  * trial_cfg (trial_cap entries, either may be null) receive every timed candidate in order. */
 lp_status lp_autotune(lp_context* ctx, const lp_pipeline_config* cfg, const lp_scan_input* scans, uint32_t nscans,

@@ -2,7 +2,7 @@
 //
 // A context is one CUDA stream. A batch owns one device allocation holding every array of the
 // launch sequence (inputs stay resident, so a prepared batch can be re-executed or captured as
-// a CUDA graph). A batch of 16 or more scans is split into up to four parts, each its own batch on
+// a CUDA graph). A batch of 16 or more scans is split into up to eight parts, each its own batch on
 // its own stream, forked from and joined into the context stream. A one-shot call (lp_segment,
 // lp_process_batch, ...) reuses batches cached in the context: plan on the host, upload, run the
 // whole sequence without host syncs, read the small per-scan state, then the results. All waits

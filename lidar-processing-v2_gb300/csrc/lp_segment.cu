@@ -864,37 +864,72 @@ __global__ void __launch_bounds__(32) k_ransac_draw(BatchDev b)
 // Inlier counts of every hypothesis plane of a scan (segmenter.cpp:409-430): lane l of every
 // warp holds planes l and l + 32 as a float pair and counts, for the candidates its warp takes,
 // |((n.x p.x + n.y p.y) + n.z p.z) - d| < thr with packed binary32 operations (each half rounds
-// like the scalar operation, in the reference's order).
+// like the scalar operation, in the reference's order). The work is a flat list of tiles of
+// kInlierTile candidates over the batch's scans with usable planes (scan by scan, so a tile
+// belongs to one scan), taken grid-strided: a large scan spreads over the whole grid instead of
+// its own share of it. A CTA's tiles come in increasing order, so it follows the scans with a
+// cursor, loads a scan's planes when it reaches it and adds its counts when it leaves it (integer
+// partial counts add up exactly).
+constexpr uint32_t kInlierTile = 1024;
+
 __global__ void __launch_bounds__(256) k_ransac_inliers(BatchDev b)
 {
     static_assert(kMaxRansacIters <= 64, "two planes per lane");
-    const int s = blockIdx.y;
-    const unsigned long long valid = b.pvalid[s];
-    if (valid == 0ull)
-        return; // uniform over the block
-    const ScanDev& sd = b.scans[s];
-    const ScanState& st = b.state[s];
+    __shared__ float4 tile[kInlierTile];
     const uint32_t lane = lane_id();
     const uint32_t i0 = lane, i1 = lane + 32u;
-    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    const float4 qa = (i0 < static_cast<uint32_t>(kMaxRansacIters)) ? b.planes[s * kMaxRansacIters + i0] : zero;
-    const float4 qb = (i1 < static_cast<uint32_t>(kMaxRansacIters)) ? b.planes[s * kMaxRansacIters + i1] : zero;
-    const float2 qx = make_float2(qa.x, qb.x), qy = make_float2(qa.y, qb.y), qz = make_float2(qa.z, qb.z);
-    const float2 nqw = make_float2(-qa.w, -qb.w); // x - w == x + (-w) exactly
-    const float thr = sd.thr;
-    const uint32_t N = st.n_cand;
-    const float4* cand = b.cand + st.cand_off;
-    uint32_t ca = 0u, cb = 0u;
-    // candidates staged per block in shared memory (coalesced), read by each warp as broadcasts
-    constexpr uint32_t kTile = 1024;
-    __shared__ float4 tile[kTile];
     const uint32_t warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (uint32_t base = blockIdx.x * kTile; base < N; base += gridDim.x * kTile)
+    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    auto tiles_of = [&](int q) -> uint32_t {
+        return (b.pvalid[q] != 0ull) ? div_up(b.state[q].n_cand, kInlierTile) : 0u;
+    };
+    int cs = 0; // the cursor: scan cs owns tiles [cbase, cbase + ctiles)
+    uint32_t cbase = 0u, ctiles = (b.nscan > 0) ? tiles_of(0) : 0u;
+    int s = -1; // the scan whose planes are loaded
+    unsigned long long valid = 0ull;
+    float2 qx = make_float2(0.f, 0.f), qy = qx, qz = qx, nqw = qx;
+    float thr = 0.0f;
+    uint32_t ca = 0u, cb = 0u;
+    auto flush = [&]() {
+        if (s < 0)
+            return;
+        if (i0 < static_cast<uint32_t>(kMaxRansacIters) && ((valid >> i0) & 1ull) && ca)
+            atomicAdd(&b.inliers[s * kMaxRansacIters + i0], ca);
+        if (i1 < static_cast<uint32_t>(kMaxRansacIters) && ((valid >> i1) & 1ull) && cb)
+            atomicAdd(&b.inliers[s * kMaxRansacIters + i1], cb);
+        ca = cb = 0u;
+    };
+    for (uint32_t it = blockIdx.x;; it += gridDim.x)
     {
-        const uint32_t cnt = min(kTile, N - base);
+        while (cs < b.nscan && it >= cbase + ctiles)
+        {
+            cbase += ctiles;
+            ++cs;
+            ctiles = (cs < b.nscan) ? tiles_of(cs) : 0u;
+        }
+        if (cs >= b.nscan)
+            break; // uniform over the block
+        if (cs != s)
+        {
+            flush();
+            s = cs;
+            valid = b.pvalid[s];
+            const float4 qa = (i0 < static_cast<uint32_t>(kMaxRansacIters)) ? b.planes[s * kMaxRansacIters + i0] : zero;
+            const float4 qb = (i1 < static_cast<uint32_t>(kMaxRansacIters)) ? b.planes[s * kMaxRansacIters + i1] : zero;
+            qx = make_float2(qa.x, qb.x);
+            qy = make_float2(qa.y, qb.y);
+            qz = make_float2(qa.z, qb.z);
+            nqw = make_float2(-qa.w, -qb.w); // x - w == x + (-w) exactly
+            thr = b.scans[s].thr;
+        }
+        const ScanState& st = b.state[s];
+        const uint32_t base = (it - cbase) * kInlierTile;
+        const uint32_t cnt = min(kInlierTile, st.n_cand - base);
+        const float4* cand = b.cand + st.cand_off + base;
+        // candidates staged in shared memory (coalesced), read by each warp as broadcasts
         __syncthreads();
         for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x)
-            tile[k] = cand[base + k];
+            tile[k] = cand[k];
         __syncthreads();
 #pragma unroll 4
         for (uint32_t k = warp; k < cnt; k += nwarp)
@@ -908,10 +943,7 @@ __global__ void __launch_bounds__(256) k_ransac_inliers(BatchDev b)
             cb += (fabsf(t.y) < thr) ? 1u : 0u;
         }
     }
-    if (i0 < static_cast<uint32_t>(kMaxRansacIters) && ((valid >> i0) & 1ull) && ca)
-        atomicAdd(&b.inliers[s * kMaxRansacIters + i0], ca);
-    if (i1 < static_cast<uint32_t>(kMaxRansacIters) && ((valid >> i1) & 1ull) && cb)
-        atomicAdd(&b.inliers[s * kMaxRansacIters + i1], cb);
+    flush();
 }
 
 __global__ void k_ransac_select(BatchDev b)
@@ -1935,9 +1967,8 @@ void launch_segmentation(Launcher& L, const BatchDev& b, const BatchHost& hb, ui
     L.scan(b.near_cnt, b.near_start, b.nnear + 1); // near_cnt[nnear] == 0: last entry is the total
     LP_LAUNCH(L, k_near, div_up(b.nnear * 32u, 256u), 256, b, 1);
     LP_LAUNCH(L, k_ransac_draw, static_cast<uint32_t>(b.nscan), 32, b);
-    // chunks per scan: about four CTAs per SM over the batch's scans (the counts add up exactly)
-    const uint32_t rchunks = std::max(16u, div_up(static_cast<uint32_t>(sm_count()) * 4u, static_cast<uint32_t>(b.nscan)));
-    LP_LAUNCH2D(L, k_ransac_inliers, dim3(rchunks, static_cast<uint32_t>(b.nscan)), 256, b);
+    // about four CTAs per SM over the batch's tiles
+    LP_LAUNCH(L, k_ransac_inliers, static_cast<uint32_t>(sm_count()) * 4u, 256, b);
     LP_LAUNCH(L, k_ransac_select, div_up(static_cast<uint32_t>(b.nscan), 64u), 64, b);
     LP_LAUNCH(L, k_label_depth, div_up(b.npts, T), T, b);
     LP_LAUNCH(L, k_project_key, div_up(b.npts, T), T, b);

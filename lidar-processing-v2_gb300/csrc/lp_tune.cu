@@ -82,7 +82,7 @@ uint32_t part_count(const lp_tuning& t, uint32_t nscans)
     if (nscans <= 1u)
         return 1u;
     if (t.parts == 0u)
-        return nscans < 16u ? 1u : std::min(4u, nscans / 8u);
+        return nscans < 16u ? 1u : std::min(8u, nscans / 8u);
     return std::min(t.parts, nscans);
 }
 
@@ -272,6 +272,8 @@ lp_status lp_autotune(lp_context* ctx, const lp_pipeline_config* cfg, const lp_s
         lp_tuning_table_get(table, &key, &cur, nullptr);
     uint32_t trials = 0;
     // one candidate: a prepared batch with this tuning, one warm-up execution, then `iters` timed
+    // back to back (no L2 flush between them: executions follow one another as in a stream of
+    // batches, and as the batch's throughput is measured)
     auto time_it = [&](const lp_tuning& t, float& ms) -> lp_status {
         lp_batch* B = nullptr;
         lp_status st = lprt::create_batch(ctx, cfg, scans, nscans, t, &B);
@@ -283,7 +285,7 @@ lp_status lp_autotune(lp_context* ctx, const lp_pipeline_config* cfg, const lp_s
         if (st == LP_OK)
             st = lp_context_synchronize(ctx);
         if (st == LP_OK)
-            st = lp_batch_time(ctx, B, iters, 1, &ms);
+            st = lp_batch_time(ctx, B, iters, 0, &ms);
         lp_batch_destroy(ctx, B);
         if (st == LP_OK)
         {
