@@ -59,6 +59,7 @@ namespace
 {
 constexpr uint32_t kKtSmall = 2048;    // ranges built in shared memory by one CTA
 constexpr uint32_t kKtHuge = 65536;    // ranges partitioned by a cluster of kKtCluster CTAs
+constexpr uint32_t kKtClusterMin = 8192; // the cluster's rounds run while the range exceeds this
 constexpr int kKtCluster = 8;
 constexpr uint32_t kKtWarpMin = 16;    // ranges of at most this many points finish on one thread
 constexpr int kKtThreads = 512;        // tree build CTAs
@@ -716,7 +717,8 @@ __device__ uint32_t kt_round_cluster(float4* a, uint32_t first, uint32_t last, i
 }
 
 // Levels whose ranges exceed kKtHuge: a cluster per range runs the introselect rounds while the
-// range is above kKtHuge, then its rank 0 finishes it as a single CTA would.
+// range is above kKtClusterMin, then its rank 0 finishes it as a single CTA would (a round on one
+// CTA reads the range at one SM's share of the bandwidth).
 __global__ void __cluster_dims__(kKtCluster, 1, 1) __launch_bounds__(kKtThreads)
     k_kt_level_huge(BatchDev b, int level, uint32_t slots)
 {
@@ -738,7 +740,7 @@ __global__ void __cluster_dims__(kKtCluster, 1, 1) __launch_bounds__(kKtThreads)
     const uint32_t len = le - lb, nth = lb + len / 2;
     uint32_t first = lb, last = le;
     int depth = 2 * static_cast<int>(floor_log2_u(len));
-    while (last - first > kKtHuge && depth > 0)
+    while (last - first > kKtClusterMin && depth > 0)
     {
         --depth;
         const uint32_t cut = kt_round_cluster(g, first, last, level % 3, ge, lq, csh, cluster);
