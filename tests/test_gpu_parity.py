@@ -211,6 +211,26 @@ def test_noise_removal_exact(ctx, cfg):
     assert got.sum() > 0
 
 
+@pytest.mark.parametrize("k", [2, 5, 9])
+def test_noise_removal_grid_ties(ctx, k):
+    """Points on a half-metre grid with duplicates, shuffled, and a fixed radius of 1 m: many
+    neighbours lie at exactly the radius (counted, as d <= r2) and subtree boxes touch the radius
+    exactly, the test the walks use to skip subtrees; larger min_neighbours leave more points short
+    and more candidates for the ordered chain (stops followed by candidates that run out)."""
+    rng = np.random.default_rng(40 + k)
+    g = rng.integers(-24, 25, size=(30000, 3)).astype(np.float32) * 0.5
+    g[:, 2] *= 0.25
+    dup = g[rng.integers(0, len(g), size=6000)]
+    sparse = rng.uniform(-40, 40, size=(4000, 3)).astype(np.float32)
+    pts = np.concatenate([g, dup, sparse])
+    pts = np.ascontiguousarray(pts[rng.permutation(len(pts))])
+    cfg = lp.NoiseRemoverConfig(1e-6, 1.0, k)
+    got = lp.NoiseRemover(ctx, cfg).filter(pts)
+    want = T.o_noise(pts, cfg, T.DROR_KDTREE)
+    assert np.array_equal(got, want)
+    assert 0 < got.sum() < len(pts)
+
+
 def test_polygons(ctx):
     rng = np.random.default_rng(11)
     poly = lp.Polygonizer(ctx)
