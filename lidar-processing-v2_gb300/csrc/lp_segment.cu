@@ -635,22 +635,46 @@ __global__ void k_chain(BatchDev b, uint32_t nslices_total)
     const uint32_t off = sd.cell_off + slice * static_cast<uint32_t>(sd.nrad);
     float prev = -sd.sensor_h + sd.thr;
     b.elev[off] = prev;
-    for (int32_t r = 1; r < sd.nrad; ++r)
+    // the cells' counts and lowest heights do not depend on the chain: 16 cells are loaded before
+    // their links are computed (the loads cannot pass the stores to elev otherwise)
+    constexpr int32_t kAhead = 16;
+    for (int32_t r0 = 1; r0 < sd.nrad; r0 += kAhead)
     {
-        const uint32_t c = off + static_cast<uint32_t>(r);
-        float e;
-        if (b.cell_cnt[c] == 0)
+        uint32_t cnt[kAhead];
+        float zlo[kAhead];
+#pragma unroll
+        for (int32_t u = 0; u < kAhead; ++u)
         {
-            e = prev + sd.delta;
+            const int32_t r = r0 + u;
+            cnt[u] = 0u;
+            zlo[u] = 0.0f;
+            if (r < sd.nrad)
+            {
+                const uint32_t c = off + static_cast<uint32_t>(r);
+                cnt[u] = b.cell_cnt[c];
+                zlo[u] = b.zlow[c];
+            }
         }
-        else
+#pragma unroll
+        for (int32_t u = 0; u < kAhead; ++u)
         {
-            const float lim = prev + sd.delta;
-            const float zl = b.zlow[c];
-            e = (lim < zl) ? lim : zl; // std::min(curr_z_min, prev + delta)
+            const int32_t r = r0 + u;
+            if (r < sd.nrad)
+            {
+                float e;
+                if (cnt[u] == 0)
+                {
+                    e = prev + sd.delta;
+                }
+                else
+                {
+                    const float lim = prev + sd.delta;
+                    e = (lim < zlo[u]) ? lim : zlo[u]; // std::min(curr_z_min, prev + delta)
+                }
+                b.elev[off + static_cast<uint32_t>(r)] = e;
+                prev = e;
+            }
         }
-        b.elev[c] = e;
-        prev = e;
     }
 }
 
@@ -735,16 +759,18 @@ struct Mt19937
 // same for all scans: they are computed once per device on the host (std::mt19937) and read from
 // this table; a scan that needs more (many redraws) runs the generator itself past the table.
 constexpr int kMtTable = 4 * 624;
-__device__ uint32_t g_mt42[kMtTable];
+static_assert(kMtTable % 4 == 0, "copied as 16-byte words");
+__device__ __align__(16) uint32_t g_mt42[kMtTable];
 
 struct Mt42Stream
 {
-    Mt19937 gen; // seeded only past the table
+    const uint32_t* table; // the first kMtTable outputs (a shared-memory copy of g_mt42)
+    Mt19937 gen;           // seeded only past the table
     int idx = 0;
     __device__ uint32_t next()
     {
         if (idx < kMtTable)
-            return g_mt42[idx++];
+            return table[idx++];
         if (idx == kMtTable)
         {
             gen.seed(42u);
@@ -776,6 +802,7 @@ struct Mt42Stream
 __global__ void __launch_bounds__(32) k_ransac_draw(BatchDev b)
 {
     __shared__ uint32_t di2[kMaxRansacIters], di3[kMaxRansacIters];
+    __shared__ __align__(16) uint32_t mt_table[kMtTable]; // lane 0 walks the stream: shared-memory latency per draw
     __shared__ int bad;
     const int s = blockIdx.x;
     const uint32_t lane = lane_id();
@@ -794,9 +821,19 @@ __global__ void __launch_bounds__(32) k_ransac_draw(BatchDev b)
     }
     if (N < 2)
         return; // the reference never ends its p3 draw for N == 1 (segmenter.cpp:382-386)
+    {
+        // 16-byte words, several loads in flight per lane
+        const uint4* src = reinterpret_cast<const uint4*>(g_mt42);
+        uint4* dst = reinterpret_cast<uint4*>(mt_table);
+#pragma unroll 5
+        for (int k = static_cast<int>(lane); k < kMtTable / 4; k += 32)
+            dst[k] = src[k];
+    }
+    __syncwarp();
     if (lane == 0)
     {
         Mt42Stream gen;
+        gen.table = mt_table;
         bad = 0;
         for (int it = 0; it < kMaxRansacIters; ++it)
         {
