@@ -199,7 +199,8 @@ struct BatchDev
     uint32_t* kown;            // per point: count of its own search (capped at min_neighbours); later, per
                                // candidate: the count after that walk
     uint32_t* kshort;          // per point (+1): 1 if its own search fell short -> exclusive scan
-    uint32_t* klo_n;           // per point (+1): entries its search left behind
+    uint32_t* klo_n;           // per point (+1): entries its search left behind; later, per short point:
+                               // the first flat entry of its piece
     uint32_t* klo_off;         // exclusive scan of klo_n: their place in kflat
     uint32_t* klo_at;          // per point: their place in kpool; later, per candidate: that walk's status,
                                // left count and stop piece

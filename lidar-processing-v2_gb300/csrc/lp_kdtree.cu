@@ -1023,6 +1023,13 @@ __global__ void k_kt_short(BatchDev b)
 
 // First entry (flat index) of the piece a short point meets on top of the stack: the leftovers of
 // the points after the previous short point of its scan.
+// The same for short point u once k_kt_segment has run: it records its piece's first entry in
+// klo_n, which holds nothing else by then (one load instead of three dependent ones).
+__device__ __forceinline__ uint32_t kt_piece_lo(const BatchDev& b, uint32_t u)
+{
+    return b.klo_n[u];
+}
+
 __device__ __forceinline__ uint32_t kt_segment_lo(const BatchDev& b, const ScanDev& sd, uint32_t t)
 {
     const uint32_t first = b.kshort[sd.src_off];
@@ -1047,6 +1054,7 @@ __global__ void k_kt_segment(BatchDev b)
     const uint32_t k = sd.dror_k;
     uint32_t found = b.kown[i];
     const uint32_t lo = kt_segment_lo(b, sd, t), hi = b.klo_off[i];
+    b.klo_n[t] = lo; // for the candidate walks and the chain (klo_n is no longer read as counts)
     uint4 res = make_uint4(0u, kNone, 0u, 0u); // found, stop entry, partial leftover at, count
     uint32_t stk[kKtStack];
     bool overflow = false;
@@ -1118,7 +1126,7 @@ __device__ bool kt_walk_pushed(const BatchDev& b, const ScanDev& sd, const float
         const uint4 c = b.kc[u];
         for (int kind = 1; kind >= 0; --kind)
         {
-            const uint32_t lo = kind ? c.z : kt_segment_lo(b, sd, u);
+            const uint32_t lo = kind ? c.z : kt_piece_lo(b, u);
             const uint32_t hi = kind ? c.z + c.w : c.y;
             const uint32_t* arr = kind ? b.kpool : b.kflat;
             for (uint32_t x = hi; x > lo; --x)
@@ -1261,15 +1269,15 @@ __global__ void k_kt_spec_next(BatchDev b)
     {
         const uint4 cu = b.kc[hu];
         if (hkind == 1)
-            stopped = walk(cu.z, hx, true) || walk(kt_segment_lo(b, sd, hu), cu.y, false);
+            stopped = walk(cu.z, hx, true) || walk(kt_piece_lo(b, hu), cu.y, false);
         else
-            stopped = walk(kt_segment_lo(b, sd, hu), hx, false);
+            stopped = walk(kt_piece_lo(b, hu), hx, false);
     }
     for (uint32_t u = hu; !stopped && u > tp1;)
     {
         --u;
         const uint4 cu = b.kc[u];
-        stopped = walk(cu.z, cu.z + cu.w, true) || walk(kt_segment_lo(b, sd, u), cu.y, false);
+        stopped = walk(cu.z, cu.z + cu.w, true) || walk(kt_piece_lo(b, u), cu.y, false);
     }
     if (overflow)
         raise_err(&b.state[s], ERR_INTERNAL);
@@ -1428,7 +1436,7 @@ __global__ void __launch_bounds__(kChainThreads) k_kt_chain(BatchDev b)
             for (uint32_t u = tp1; u <= hu; ++u)
             {
                 const uint4 cu = b.kc[u];
-                const uint32_t lo = kt_segment_lo(b, sd, u);
+                const uint32_t lo = kt_piece_lo(b, u);
                 if (u < hu)
                 {
                     push(lo, cu.y);
